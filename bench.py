@@ -1,0 +1,368 @@
+#!/usr/bin/env python
+"""Benchmark: a 30-qubit layered circuit (40 layers of one random gate from
+{H,X,Y,Z,S,T,RX,RY,RZ} per qubit plus CNOTs on a random matching) followed by a
+30-qubit QFT, on one GB300, through libqgpu.so.
+
+One step = zero-state + the whole circuit (2280 gates) on a device-resident
+2^30-amplitude state. value = gate-amplitudes/s = sum_gates 2^n / step time,
+summed over ranks (replicas: every rank simulates its own state, no collective).
+The state (16 GiB c128 / 8 GiB c64) is larger than L2, so no flush is needed.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+--impl reference times the reference's algorithm (the dense Kronecker mat-vec
+of QClojure's simulator, restated in C in oracle/) on the host cores for the
+same workload: a bounded sample of output amplitudes of one gate per step.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import threading
+import time
+from pathlib import Path
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = "30-qubit layer time & HBM GB/s; serve circuits/s + p50/p99, c64 vs c128"
+UNIT = "gate-amplitudes/s"
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--qubits", type=int, default=30)
+    ap.add_argument("--depth", type=int, default=40)
+    ap.add_argument("--precision", choices=["c128", "c64"], default="c128")
+    ap.add_argument("--fusion", choices=["plain", "tiled", "dense"], default="tiled")
+    ap.add_argument("--no-extras", action="store_true", help="skip the c64 / e2e / cpu-baseline legs")
+    ap.add_argument("--seed", type=int, default=1)
+    return ap.parse_args()
+
+
+# ---------------------------------------------------------------------------
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        fd, self.path = tempfile.mkstemp(suffix=".csv")
+        os.close(fd)
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except FileNotFoundError:
+            self.proc = None
+
+    def stop(self) -> dict:
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        rows = []
+        for line in Path(self.path).read_text().splitlines():
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                rows.append((float(f[1]), float(f[2]), float(f[3]), f[5], f[6], f[7], f[8]))
+            except ValueError:
+                continue
+        os.unlink(self.path)
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+        reasons = set()
+        for r in rows:
+            for name, v in zip(("hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"), r[3:]):
+                if v.lower().startswith("active"):
+                    reasons.add(name)
+        return {"sm_mhz": statistics.median(r[0] for r in rows), "sm_max_mhz": max(r[1] for r in rows),
+                "power_w_max": max(r[2] for r in rows), "samples": len(rows), "reasons": sorted(reasons)}
+
+
+def measured_peaks():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+# ---------------------------------------------------------------------------
+def cpu_reference_rate(n: int, gates_per_step: int, budget_s: float, threads: int | None = None):
+    """Reference algorithm on the host: rows of the dense Kronecker mat-vec of one
+    1-qubit gate (gate.clj:346-395), each row visiting all 2^n columns. Returns
+    (gate-amplitudes/s, description, threads)."""
+    import numpy as np
+
+    from oracle import oracle as O
+
+    O.lib()
+    threads = threads or os.cpu_count() or 1
+    avail_gb = 0.0
+    try:
+        for line in Path("/proc/meminfo").read_text().splitlines():
+            if line.startswith("MemAvailable"):
+                avail_gb = int(line.split()[1]) / 2**20
+    except OSError:
+        pass
+    m = n
+    while m > 20 and (16 << m) / 2**30 > 0.4 * avail_gb:
+        m -= 2
+    rng = np.random.default_rng(0)
+    x = (rng.standard_normal(1 << m) + 1j * rng.standard_normal(1 << m)) / math.sqrt(2 << m)
+    h = [[1 / math.sqrt(2), 1 / math.sqrt(2)], [1 / math.sqrt(2), -1 / math.sqrt(2)]]
+    t0 = time.perf_counter()
+    O.refalgo_rows(x, h, m // 2, 0, 1)
+    one = time.perf_counter() - t0
+    rows_per_thread = max(1, int(budget_s / max(one, 1e-6)))
+    results = [0] * threads
+
+    def work(k):
+        O.refalgo_rows(x, h, m // 2, k * rows_per_thread, rows_per_thread)
+        results[k] = rows_per_thread
+
+    ths = [threading.Thread(target=work, args=(k,)) for k in range(threads)]
+    t0 = time.perf_counter()
+    for t in ths:
+        t.start()
+    for t in ths:
+        t.join()
+    dt = time.perf_counter() - t0
+    rows = sum(results)
+    rate = rows / dt * (2.0 ** (m - n))  # per-row work is 2^m MACs; scale to 2^n columns
+    desc = (f"{rows} output amplitudes of one H gate's dense 2^{m}x2^{m} Kronecker mat-vec"
+            + (f", scaled by 2^{m - n} to {n} qubits (host memory)" if m != n else "")
+            + f", {threads} threads, {dt:.1f} s")
+    return rate, desc, threads
+
+
+# ---------------------------------------------------------------------------
+def run_reference(args):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return 0
+    from qclojure_gb300 import workloads
+
+    gates = len(workloads.large_circuit(args.qubits, args.depth, args.seed)["operations"])
+    vals = []
+    desc = ""
+    threads = os.cpu_count() or 1
+    for _ in range(args.warmup):
+        cpu_reference_rate(args.qubits, gates, 1.0)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        v, desc, threads = cpu_reference_rate(args.qubits, gates, 5.0)
+        vals.append(v)
+    dt = time.perf_counter() - t0
+    value = statistics.mean(vals)
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": dt * 1e3 / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": f"layered-{args.qubits}x{args.depth}+qft{args.qubits}", "n_qubits": args.qubits,
+                   "gates": gates, "precision": "c128"},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port", "sample": desc},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "note": "the reference (Clojure/JVM) cannot run here; this times its algorithm restated in C",
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+# ---------------------------------------------------------------------------
+def main():
+    args = parse()
+    if args.impl == "reference":
+        return run_reference(args)
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    import torch
+
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+
+    import __graft_entry__ as g
+
+    g.build()
+    import ctypes as C
+
+    import numpy as np
+
+    from qclojure_gb300 import _abi as A
+    from qclojure_gb300 import workloads
+    from qclojure_gb300.circuit import encode
+    from qclojure_gb300.state import Context
+
+    n = args.qubits
+    circ = workloads.large_circuit(n, args.depth, args.seed + rank)
+    layers_only = workloads.layered_circuit(n, args.depth, args.seed + rank)
+    gates = len(circ["operations"])
+    N = 1 << n
+    lib = A.load_library()
+    ctx = Context(device=local, workers=1, seed=7)
+    st = ctx.state(n, args.precision)
+    dptr, sptr = st.device_ptr()
+    stream = torch.cuda.ExternalStream(sptr, device=torch.device("cuda", local))
+
+    def step():
+        st.set_basis(0)
+        st.apply(circ, fusion=args.fusion)
+
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
+    clocks = ClockSampler(local)
+    clocks.start()
+    l0 = C.c_uint64()
+    lib.qg_kernel_launches(C.byref(l0))
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(args.steps):
+        step()
+    e1.record(stream)
+    e1.synchronize()
+    l1 = C.c_uint64()
+    lib.qg_kernel_launches(C.byref(l1))
+    ck = clocks.stop()
+    torch.cuda.synchronize()
+    elapsed_ms = e0.elapsed_time(e1)
+    if dist:
+        t = torch.tensor([elapsed_ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        elapsed_ms = float(t.item())
+        dist.barrier()
+    ms_per_step = elapsed_ms / args.steps
+    value = world * gates * N / (ms_per_step / 1e3)
+
+    # per-pass timing (separate, untimed run) for the roofline of the dominant kernel
+    enc = encode(circ)
+    cap = 8192
+    pms = (C.c_float * cap)()
+    pkind = (C.c_int32 * cap)()
+    npass = C.c_int32()
+    st.set_basis(0)
+    from qclojure_gb300.backend import FUSIONS
+
+    rc = lib.qg_state_profile(st.h, enc.ref(), FUSIONS[args.fusion], 0, pms, pkind, cap, C.byref(npass))
+    pass_ms = [pms[i] for i in range(npass.value)] if rc == 0 else []
+    kinds = [pkind[i] for i in range(npass.value)] if rc == 0 else []
+    B = 16 if args.precision == "c128" else 8
+    pass_bytes = 2 * B * N
+    dom_kind = 1 if args.fusion != "plain" else 0
+    dom = [t for t, k in zip(pass_ms, kinds) if k == dom_kind]
+    peak, peak_src = measured_peaks()
+    mean_pass = statistics.mean(dom) if dom else float("nan")
+    achieved = pass_bytes / (mean_pass / 1e3) / 1e9 if dom else float("nan")
+    # time of the 40 random layers alone, per layer
+    st.set_basis(0)
+    tl0 = torch.cuda.Event(enable_timing=True)
+    tl1 = torch.cuda.Event(enable_timing=True)
+    tl0.record(stream)
+    st.apply(layers_only, fusion=args.fusion)
+    tl1.record(stream)
+    tl1.synchronize()
+    layer_ms = tl0.elapsed_time(tl1) / args.depth
+
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64" if args.precision == "c128" else "f32", "data": "synthetic",
+        "config": {"workload": f"layered-{n}x{args.depth}+qft{n}", "n_qubits": n, "depth": args.depth,
+                   "gates": gates, "precision": args.precision, "fusion": args.fusion,
+                   "parallelism": f"replicas{world}", "l2": "state larger than L2 (no flush needed)"},
+        "layer_ms": layer_ms,
+        "hbm_passes_per_step": len(pass_ms),
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": achieved / peak if dom else None, "traffic": None,
+                     "kernel": "k_tile<double>" if args.precision == "c128" else "k_tile<float>",
+                     "peak_source": peak_src, "pass_bytes": pass_bytes, "mean_pass_ms": mean_pass,
+                     "passes": len(dom)},
+        "gpu_launches": int(l1.value - l0.value),
+        "clocks": ck,
+    }
+
+    if rank == 0 and not args.no_extras:
+        # complex64 leg (same circuit)
+        if args.precision == "c128":
+            st64 = ctx.state(n, "c64")
+            _, s64 = st64.device_ptr()
+            stream64 = torch.cuda.ExternalStream(s64, device=torch.device("cuda", local))
+            for _ in range(2):
+                st64.set_basis(0)
+                st64.apply(circ, fusion=args.fusion)
+            a = torch.cuda.Event(enable_timing=True)
+            b = torch.cuda.Event(enable_timing=True)
+            a.record(stream64)
+            for _ in range(args.steps):
+                st64.set_basis(0)
+                st64.apply(circ, fusion=args.fusion)
+            b.record(stream64)
+            b.synchronize()
+            ms64 = a.elapsed_time(b) / args.steps
+            line["c64"] = {"value": gates * N / (ms64 / 1e3), "ms_per_step": ms64}
+            st64.close()
+        # end to end through the job API: circuit in, 1024-shot histogram out (host buffers)
+        from qclojure_gb300.backend import create_simulator, execute_circuit
+
+        st.close()
+        sim = create_simulator({"precision": args.precision, "fusion": args.fusion, "workers": 1, "seed": 5})
+        opts = {"result-specs": {"measurements": {"shots": 1024}}}
+        execute_circuit(sim, circ, opts, timeout_ms=600_000)
+        t0 = time.perf_counter()
+        e2e_steps = max(1, min(args.steps, 2))
+        for _ in range(e2e_steps):
+            r = execute_circuit(sim, circ, opts, timeout_ms=600_000)
+            assert r["job-status"] == "completed", r
+            sim.free_job(r["job-id"])
+        dt = (time.perf_counter() - t0) / e2e_steps
+        h2d = enc.count * C.sizeof(A.QgOp)
+        line["e2e"] = {"value": gates * N / dt, "unit": UNIT, "h2d_bytes_per_step": h2d,
+                       "d2h_bytes_per_step": 1024 * 8 * 2, "ms_per_step": dt * 1e3,
+                       "path": "qg_submit -> qg_wait -> qg_result_counts/shots (1024 shots)"}
+        sim.close()
+        rate, desc, threads = cpu_reference_rate(n, gates, 8.0)
+        line["cpu_baseline"] = {"value": rate, "unit": UNIT, "cores": threads, "kind": "port", "sample": desc}
+    else:
+        st.close()
+    ctx.close()
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if dist:
+        dist.destroy_process_group()
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -1,0 +1,297 @@
+/*
+ * qgpu.h - C ABI of libqgpu.so, a GB300 (sm_103a) state-vector simulator backend.
+ *
+ * The library is a drop-in for QClojure's ideal simulator
+ * (src/org/soulspace/qclojure/adapter/backend/ideal_simulator.clj). The
+ * QuantumBackend protocol methods (src/org/soulspace/qclojure/application/backend.clj:72-115)
+ * map onto the job functions below; a JVM shim calls them through the Foreign
+ * Function & Memory API, a Python host calls them through ctypes. Every entry
+ * point:
+ *   - takes plain pointers and sizes (no C++ or torch types cross the boundary),
+ *   - returns an int status (QG_OK = 0) and never throws, aborts or traps,
+ *   - writes results into caller-owned host buffers; device memory stays owned
+ *     by the library (the amplitude array lives in HBM from the first gate to
+ *     result extraction),
+ *   - is thread-safe on one context.
+ *
+ * Conventions shared with the reference:
+ *   - qubit q of an n-qubit register is bit (n-1-q) of the basis index
+ *     (big-endian, src/org/soulspace/qclojure/domain/state.clj:114-136);
+ *   - SWAP and iSWAP operands are bit positions counted from the least
+ *     significant bit (src/org/soulspace/qclojure/domain/gate.clj:768-778);
+ *   - controlled single-qubit gates apply the transpose of their 2x2 matrix
+ *     (src/org/soulspace/qclojure/domain/gate.clj:473-483);
+ *   - amplitudes cross the boundary as interleaved complex128 (re, im) pairs.
+ */
+#ifndef QGPU_H
+#define QGPU_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define QG_ABI_VERSION 1
+#define QG_MAX_QUBITS 40
+#define QG_MAX_OP_QUBITS 40
+
+/* ---- status codes (returned by every entry point) ---------------------- */
+enum {
+  QG_OK = 0,
+  QG_ERR_INVALID_ARG = 1,      /* null pointer, bad size, bad enum value          */
+  QG_ERR_UNKNOWN_GATE = 2,     /* opcode the reference dispatch rejects           */
+  QG_ERR_QUBIT_RANGE = 3,      /* operand >= num_qubits or repeated operand        */
+  QG_ERR_OOM = 4,              /* state does not fit the HBM budget                */
+  QG_ERR_DEVICE = 5,           /* CUDA error (message via qg_last_error)           */
+  QG_ERR_TIMEOUT = 6,          /* qg_wait ran out of time                          */
+  QG_ERR_CANCELLED = 7,        /* job was cancelled                                */
+  QG_ERR_NOT_FOUND = 8,        /* unknown job / batch id                           */
+  QG_ERR_NOT_COMPLETED = 9,    /* result requested before completion               */
+  QG_ERR_NOT_NORMALIZED = 10,  /* |sum p - 1| > 1e-8 before sampling (state.clj:901) */
+  QG_ERR_BUFFER_TOO_SMALL = 11,/* caller buffer shorter than the result            */
+  QG_ERR_UNSUPPORTED = 12,     /* request the reference also refuses               */
+  QG_ERR_NO_RESULT = 13,       /* result type was not requested in the spec         */
+  QG_ERR_NO_DEVICE = 14        /* no CUDA device visible                           */
+};
+
+/* ---- job status (ideal_simulator.clj:138-141 keywords) ------------------ */
+enum {
+  QG_JOB_QUEUED = 0,
+  QG_JOB_RUNNING = 1,
+  QG_JOB_COMPLETED = 2,
+  QG_JOB_FAILED = 3,
+  QG_JOB_CANCELLED = 4,
+  QG_JOB_NOT_FOUND = 5
+};
+
+/* ---- qg_cancel outcomes (ideal_simulator.clj:154-163) ------------------- */
+enum { QG_CANCEL_CANCELLED = 0, QG_CANCEL_CANNOT = 1, QG_CANCEL_NOT_FOUND = 2 };
+
+/* ---- precision --------------------------------------------------------- */
+enum { QG_C128 = 0, QG_C64 = 1 };
+
+/* ---- fusion modes ------------------------------------------------------ */
+enum {
+  QG_FUSE_PLAIN = 0,   /* one HBM pass per gate (the plain method)                    */
+  QG_FUSE_TILED = 1,   /* gate runs applied in shared-memory tiles, one pass per run  */
+  QG_FUSE_DENSE = 2    /* gate runs merged into dense 2^k x 2^k blocks (k = fuse_k)   */
+};
+
+/* ---- opcodes: the gate set of circuit.clj:933-1072 ---------------------- */
+enum {
+  QG_OP_X = 1, QG_OP_Y = 2, QG_OP_Z = 3, QG_OP_H = 4,
+  QG_OP_S = 5, QG_OP_SDAG = 6, QG_OP_T = 7, QG_OP_TDAG = 8,
+  QG_OP_RX = 9, QG_OP_RY = 10, QG_OP_RZ = 11, QG_OP_PHASE = 12,
+  QG_OP_CNOT = 20, QG_OP_CZ = 21, QG_OP_CRX = 22, QG_OP_CRY = 23, QG_OP_CRZ = 24,
+  QG_OP_CY = 25,              /* reached through :controlled with :target-gate :y   */
+  QG_OP_SWAP = 26, QG_OP_ISWAP = 27, QG_OP_TOFFOLI = 28, QG_OP_FREDKIN = 29,
+  QG_OP_RYDBERG_CZ = 40, QG_OP_RYDBERG_CPHASE = 41, QG_OP_RYDBERG_BLOCKADE = 42,
+  QG_OP_GLOBAL_RX = 50, QG_OP_GLOBAL_RY = 51, QG_OP_GLOBAL_RZ = 52, QG_OP_GLOBAL_H = 53,
+  QG_OP_GLOBAL_X = 54, QG_OP_GLOBAL_Y = 55, QG_OP_GLOBAL_Z = 56,
+  QG_OP_MEASURE = 60,         /* mid-circuit measurement with collapse (circuit.clj:1074) */
+  QG_OP_U = 70,               /* explicit 2x2 matrix m on q[0], applied like a 1-qubit gate */
+  QG_OP_CU = 71,              /* explicit 2x2 matrix m on q[1], control q[0] (transposed, as the reference) */
+  QG_OP_RZZ = 72,             /* exp(-i angle/2 Z(q0) Z(q1)); a diagonal extension for QAOA cost layers */
+  QG_OP_I = 80                /* identity: the reference dispatch has no case for it and fails */
+};
+
+/* One operation. Operand meaning per opcode, in the reference's parameter order:
+ *   1-qubit gates:   q[0] = :target
+ *   CNOT/CZ/CRx/CY:  q[0] = :control, q[1] = :target
+ *   SWAP/iSWAP:      q[0] = :qubit1,  q[1] = :qubit2  (LSB bit positions)
+ *   TOFFOLI:         q[0] = :control1, q[1] = :control2, q[2] = :target
+ *   FREDKIN:         q[0] = :control, q[1] = :target1, q[2] = :target2
+ *   RYDBERG_CZ/CPHASE: q[0] = :control, q[1] = :target
+ *   RYDBERG_BLOCKADE:  q[0..nq) = :qubit-indices
+ *   MEASURE:           q[0..nq) = :measurement-qubits (outcome bit i <-> q[i])
+ *   GLOBAL_*:          no operands
+ *   RZZ:               q[0], q[1]
+ * angle is :angle (radians); m holds a row-major 2x2 complex matrix (re, im) for U/CU. */
+typedef struct qg_op {
+  int32_t opcode;
+  int32_t nq;
+  uint8_t q[QG_MAX_OP_QUBITS];
+  double angle;
+  double m[8];
+} qg_op;
+
+typedef struct qg_circuit {
+  int32_t num_qubits;
+  int32_t num_ops;
+  const qg_op* ops;
+} qg_circuit;
+
+/* Result specification: the keys of result.clj:535-639. A zero flag omits the result. */
+enum {
+  QG_RES_MEASUREMENTS = 1 << 0,   /* :measurements  {:shots}                       */
+  QG_RES_EXPECTATION = 1 << 1,    /* :expectation   {:observables :targets}        */
+  QG_RES_VARIANCE = 1 << 2,       /* :variance      {:observables :targets}        */
+  QG_RES_HAMILTONIAN = 1 << 3,    /* :hamiltonian   [pauli terms]                  */
+  QG_RES_PROBABILITIES = 1 << 4,  /* :probabilities {:targets}                      */
+  QG_RES_AMPLITUDES = 1 << 5,     /* :amplitudes    {:basis-states}                 */
+  QG_RES_STATE_VECTOR = 1 << 6,   /* :state-vector  true                            */
+  QG_RES_DENSITY_MATRIX = 1 << 7, /* :density-matrix true (n <= 14)                 */
+  QG_RES_FIDELITY = 1 << 8        /* :fidelity      {:references}                   */
+};
+
+typedef struct qg_result_spec {
+  uint32_t flags;
+  int32_t reserved;
+  uint64_t shots;                 /* :measurements :shots (default 1)                   */
+  /* :hamiltonian: n_terms coefficients and n_terms strings of num_qubits chars over IXYZ,
+     concatenated; char i of a string acts on qubit i (observables.clj:216-232). */
+  int32_t n_terms;
+  int32_t n_observables;
+  const double* coefficients;
+  const char* pauli_strings;
+  /* :expectation / :variance: n_observables 2x2 Hermitian matrices (8 doubles each,
+     row-major re/im) and one target qubit per observable. */
+  const double* observables;
+  const int32_t* observable_targets;
+  /* :amplitudes :basis-states and :probabilities :targets (basis indices). */
+  int32_t n_basis_states;
+  int32_t n_probability_targets;
+  const uint64_t* basis_states;
+  const uint64_t* probability_targets;
+  /* :fidelity :references: n_references host states of 2^num_qubits complex128 each. */
+  int32_t n_references;
+  int32_t reserved2;
+  const double* references;
+} qg_result_spec;
+
+typedef struct qg_options {
+  const qg_result_spec* spec;     /* may be NULL: no results beyond the final state      */
+  const double* initial_state;    /* host complex128, 2^n amplitudes, or NULL for |0..0> */
+  uint64_t seed;                  /* drives shot sampling and mid-circuit collapse       */
+  int32_t precision;              /* QG_C128 / QG_C64, -1 = context default              */
+  int32_t fusion;                 /* QG_FUSE_*, -1 = context default                     */
+} qg_options;
+
+typedef struct qg_config {
+  int32_t device;                 /* CUDA ordinal                                        */
+  int32_t precision;              /* default precision                                   */
+  int32_t fusion;                 /* default fusion mode                                 */
+  int32_t fuse_k;                 /* dense block width for QG_FUSE_DENSE (1..5)          */
+  int32_t max_qubits;             /* admission limit (0 = derived from HBM)              */
+  int32_t workers;                /* device streams serving jobs concurrently (>=1)      */
+  uint64_t hbm_budget_bytes;      /* 0 = free HBM minus a reserve                        */
+  uint64_t seed;                  /* default seed                                        */
+} qg_config;
+
+typedef struct qg_queue_info {    /* queue-status (ideal_simulator.clj:165-176) + device fields */
+  int64_t total_jobs, queued, running, completed, failed, cancelled;
+  uint64_t hbm_free_bytes, hbm_budget_bytes, hbm_in_use_bytes;
+  int32_t workers, reserved;
+} qg_queue_info;
+
+typedef struct qg_job_info {
+  int32_t status;
+  int32_t num_qubits;
+  int32_t precision;
+  int32_t num_passes;             /* HBM passes the compiled circuit took                */
+  double execution_time_ms;       /* wall time submit-to-completion on the worker         */
+  double device_time_ms;          /* CUDA-event time of the gate passes                   */
+  double queue_time_ms;
+  uint64_t shots;
+  int64_t num_distinct_outcomes;
+  int32_t has_results;            /* QG_RES_* flags that are available                    */
+  int32_t error_code;
+} qg_job_info;
+
+/* ---- context ------------------------------------------------------------ */
+int qg_abi_version(void);
+int qg_device_count(int32_t* count);
+int qg_ctx_create(const qg_config* cfg, void** ctx_out);
+int qg_ctx_destroy(void* ctx);
+/* backend-info / device: capability numbers for the device map (ideal_simulator.clj:34-51). */
+int qg_ctx_capabilities(void* ctx, int32_t* max_qubits_c128, int32_t* max_qubits_c64,
+                        uint64_t* hbm_total_bytes, int32_t* sm_count);
+
+/* ---- jobs: QuantumBackend (backend.clj:72-115) -------------------------- */
+/* submit-circuit (ideal_simulator.clj:120-136): validates, copies the circuit and
+   returns at once; a device worker runs the job. */
+int qg_submit(void* ctx, const qg_circuit* circuit, const qg_options* options, uint64_t* job_out);
+/* job-status (ideal_simulator.clj:138-141). */
+int qg_job_status(void* ctx, uint64_t job, int32_t* status_out);
+/* Blocking wait; replaces the 100 ms poll loop of backend.clj:239-256. */
+int qg_wait(void* ctx, uint64_t job, int64_t timeout_ms, int32_t* status_out);
+/* cancel-job (ideal_simulator.clj:154-163): QG_CANCEL_* in *outcome. */
+int qg_cancel(void* ctx, uint64_t job, int32_t* outcome);
+/* queue-status (ideal_simulator.clj:165-176). */
+int qg_queue_status(void* ctx, qg_queue_info* out);
+int qg_job_details(void* ctx, uint64_t job, qg_job_info* out);
+/* job-result pieces (result.clj:179-497). Buffers are caller-owned. */
+int qg_result_counts(void* ctx, uint64_t job, uint64_t* outcomes, uint64_t* counts, int64_t cap, int64_t* n_out);
+int qg_result_shots(void* ctx, uint64_t job, uint64_t* outcomes, int64_t cap);
+int qg_result_probabilities(void* ctx, uint64_t job, double* out, int64_t cap);
+int qg_result_target_probabilities(void* ctx, uint64_t job, double* out, int64_t cap);
+int qg_result_state(void* ctx, uint64_t job, double* out_c128, int64_t cap_amplitudes);
+int qg_result_amplitudes(void* ctx, uint64_t job, double* out_c128, int64_t cap_amplitudes);
+int qg_result_expectations(void* ctx, uint64_t job, double* expectation, double* variance, int64_t cap);
+int qg_result_hamiltonian(void* ctx, uint64_t job, double* energy, double* term_values, int64_t cap);
+int qg_result_fidelities(void* ctx, uint64_t job, double* out, int64_t cap);
+int qg_result_density_matrix(void* ctx, uint64_t job, double* out_c128, int64_t cap_entries);
+int qg_last_error(void* ctx, uint64_t job, char* buf, int64_t len);
+/* Releases a job and its device state (cleanup-completed-jobs!, ideal_simulator.clj:243-264). */
+int qg_job_free(void* ctx, uint64_t job);
+int qg_cleanup_completed(void* ctx, int64_t max_age_ms, int64_t* removed);
+
+/* ---- batches: BatchJobBackend (backend.clj:136-168) --------------------- */
+/* batch-submit: all circuits share the options; jobs_out receives one job id per circuit.
+   Queued jobs of equal qubit count are run together by the batched pass kernel. */
+int qg_batch_submit(void* ctx, const qg_circuit* circuits, int32_t count, const qg_options* options,
+                    uint64_t* batch_out, uint64_t* jobs_out);
+/* batch-status: one QG_JOB_* per job, in submission order. */
+int qg_batch_status(void* ctx, uint64_t batch, int32_t* statuses, int32_t cap, int32_t* n_out);
+int qg_batch_jobs(void* ctx, uint64_t batch, uint64_t* jobs, int32_t cap, int32_t* n_out);
+
+/* ---- device-resident state (state.clj, gate.clj, result.clj on one state) ----
+   These bypass the job queue: the state stays in HBM between calls, which is
+   how the QAOA/VQE loop and the benchmarks drive the kernels. */
+int qg_state_create(void* ctx, int32_t num_qubits, int32_t precision, void** state_out);
+int qg_state_destroy(void* state);
+int qg_state_num_qubits(void* state, int32_t* n, int32_t* precision);
+/* zero-state (state.clj:251-284) or basis state |index>. */
+int qg_state_set_basis(void* state, uint64_t index);
+int qg_state_upload(void* state, const double* host_c128);
+int qg_state_download(void* state, double* host_c128);
+/* Apply a circuit in place with the given fusion mode; mid-circuit measurements draw
+   from seed. passes_out (may be NULL) receives the number of HBM passes. */
+int qg_state_apply(void* state, const qg_circuit* circuit, int32_t fusion, uint64_t seed, int32_t* passes_out);
+/* probabilities (state.clj:658-682) into a host buffer of 2^n doubles. */
+int qg_state_probabilities(void* state, double* host_out);
+/* Shot sampling (state.clj:869-913 rule: first outcome whose cumulative probability
+   reaches the uniform draw) with Philox uniforms from seed; outcomes in shot order. */
+int qg_state_sample(void* state, uint64_t shots, uint64_t seed, uint64_t* host_outcomes);
+/* <psi|P|psi> for a Pauli string of num_qubits chars (hamiltonian.clj:82-94). */
+int qg_state_pauli_expectation(void* state, const char* pauli, double* out);
+/* sum_j c_j <P_j> (hamiltonian.clj:96-114), strings concatenated. */
+int qg_state_hamiltonian(void* state, int32_t n_terms, const double* coeffs, const char* paulis, double* out);
+/* <psi|O_t|psi> for a 2x2 observable on one target qubit (result.clj:254-288). */
+int qg_state_expectation_1q(void* state, const double* obs8, int32_t target, double* out);
+/* Sum of |a|^2 and <a|b> (complex_linear_algebra.clj:318,435), FP64 compensated. */
+int qg_state_norm2(void* state, double* out);
+int qg_state_inner(void* a, void* b, double* re, double* im);
+/* Partial measurement with collapse (state.clj:915-1014); outcome bit i <-> qubits[i]. */
+int qg_state_measure(void* state, const int32_t* qubits, int32_t count, uint64_t seed,
+                     uint64_t* outcome_out, double* probability_out);
+/* Device pointer of the amplitude array (interleaved re/im, fp64 for c128, fp32 for c64)
+   and its CUDA stream, for callers that hand the state to other CUDA code. */
+int qg_state_device_ptr(void* state, void** dptr, void** stream);
+int qg_state_synchronize(void* state);
+
+/* ---- measurement (no counterpart in the reference) ----------------------------
+   qg_state_profile applies a circuit like qg_state_apply and records a CUDA event
+   pair around every HBM pass on the state's stream: pass_ms[i] is the duration of
+   pass i and pass_kind[i] its kind (0 plain gate, 1 tiled pass, 2 measurement).
+   qg_kernel_launches reports how many kernels this library has launched in the
+   process so far. */
+int qg_state_profile(void* state, const qg_circuit* circuit, int32_t fusion, uint64_t seed, float* pass_ms,
+                     int32_t* pass_kind, int32_t cap, int32_t* n_passes);
+int qg_kernel_launches(uint64_t* count);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* QGPU_H */

@@ -1,0 +1,1014 @@
+// sm_103a kernels of libqgpu.so.
+//
+// State layout in HBM: 2^n interleaved complex amplitudes (double2 for c128,
+// float2 for c64), basis index i, qubit q <-> bit (n-1-q) of i.
+//
+// Arithmetic: every 2x2 class, phase and collapse multiplies with the same
+// rounded products and sums the reference's complex multiply and dense row sum
+// form (src/org/soulspace/qclojure/domain/gate.clj:384-395,
+// src/org/soulspace/qclojure/domain/math/fastmath/complex_linear_algebra.clj:408-431),
+// written with explicit __dmul_rn/__dadd_rn so nothing is contracted into an FMA.
+// The complex128 path therefore reproduces the CPU restatement bit for bit, and
+// the plain (one pass per gate) and tiled (many gates per pass) executors give
+// identical amplitudes. Dense fused blocks use FMA and are checked to tolerance.
+#include <atomic>
+#include <cstdio>
+
+#include "qgpu_internal.h"
+
+namespace qg {
+
+namespace {
+
+constexpr int kSMs = 152;
+
+std::atomic<unsigned long long> g_launches{0};
+inline void counted(int k = 1) { g_launches.fetch_add((unsigned long long)k, std::memory_order_relaxed); }
+
+template <typename R> struct C2;
+template <> struct C2<double> { using T = double2; };
+template <> struct C2<float> { using T = float2; };
+
+__device__ __forceinline__ double mul_(double a, double b) { return __dmul_rn(a, b); }
+__device__ __forceinline__ double add_(double a, double b) { return __dadd_rn(a, b); }
+__device__ __forceinline__ double sub_(double a, double b) { return __dsub_rn(a, b); }
+__device__ __forceinline__ float mul_(float a, float b) { return __fmul_rn(a, b); }
+__device__ __forceinline__ float add_(float a, float b) { return __fadd_rn(a, b); }
+__device__ __forceinline__ float sub_(float a, float b) { return __fsub_rn(a, b); }
+
+// reference complex multiply g*x: (g.re x.re - g.im x.im, g.re x.im + g.im x.re)
+template <typename V, typename R>
+__device__ __forceinline__ V cmul(R gr, R gi, V x) {
+  V r;
+  r.x = sub_(mul_(gr, x.x), mul_(gi, x.y));
+  r.y = add_(mul_(gr, x.y), mul_(gi, x.x));
+  return r;
+}
+template <typename V>
+__device__ __forceinline__ V cadd(V a, V b) {
+  V r;
+  r.x = add_(a.x, b.x);
+  r.y = add_(a.y, b.y);
+  return r;
+}
+
+template <typename R>
+struct Mat {
+  R m[8];
+};
+
+template <typename R>
+Mat<R> to_mat(const double* m) {
+  Mat<R> r;
+  for (int k = 0; k < 8; ++k) r.m[k] = (R)m[k];
+  return r;
+}
+
+// 2x2 application per class; y0,y1 from x0,x1.
+template <int CLS, typename V, typename R>
+__device__ __forceinline__ void u2_apply(const R* m, V x0, V x1, V& y0, V& y1) {
+  if (CLS == U2_GENERAL) {
+    y0 = cadd(cmul(m[0], m[1], x0), cmul(m[2], m[3], x1));
+    y1 = cadd(cmul(m[4], m[5], x0), cmul(m[6], m[7], x1));
+  } else if (CLS == U2_REAL) {
+    y0.x = add_(mul_(m[0], x0.x), mul_(m[2], x1.x));
+    y0.y = add_(mul_(m[0], x0.y), mul_(m[2], x1.y));
+    y1.x = add_(mul_(m[4], x0.x), mul_(m[6], x1.x));
+    y1.y = add_(mul_(m[4], x0.y), mul_(m[6], x1.y));
+  } else if (CLS == U2_RXLIKE) {
+    // m0=(a,0) m1=(0,b) m2=(0,c) m3=(d,0)
+    y0.x = sub_(mul_(m[0], x0.x), mul_(m[3], x1.y));
+    y0.y = add_(mul_(m[0], x0.y), mul_(m[3], x1.x));
+    y1.x = sub_(mul_(m[6], x1.x), mul_(m[5], x0.y));
+    y1.y = add_(mul_(m[5], x0.x), mul_(m[6], x1.y));
+  } else if (CLS == U2_DIAG) {
+    y0 = cmul(m[0], m[1], x0);
+    y1 = cmul(m[6], m[7], x1);
+  } else if (CLS == U2_ANTIDIAG) {
+    y0 = cmul(m[2], m[3], x1);
+    y1 = cmul(m[4], m[5], x0);
+  } else if (CLS == U2_X) {
+    y0 = x1;
+    y1 = x0;
+  } else {  // U2_IMAG_ANTI: m1=(0,s1), m2=(0,s2), s=+-1: (0,s)*x = (-s x.im, s x.re)
+    if (m[3] > 0) { y0.x = -x1.y; y0.y = x1.x; } else { y0.x = x1.y; y0.y = -x1.x; }
+    if (m[5] > 0) { y1.x = -x0.y; y1.y = x0.x; } else { y1.x = x0.y; y1.y = -x0.x; }
+  }
+}
+
+template <int CLS, typename V, typename R>
+__device__ __forceinline__ V phase_apply(const R* m, V x) {
+  if (CLS == PH_GENERAL) return cmul(m[0], m[1], x);
+  V r;
+  if (CLS == PH_NEG) { r.x = -x.x; r.y = -x.y; }
+  else if (CLS == PH_I) { r.x = -x.y; r.y = x.x; }
+  else { r.x = x.y; r.y = -x.x; }
+  return r;
+}
+
+// Insert bits: positions ascending; bits in setmask become 1, the others 0.
+struct Fixed {
+  int n;
+  int pos[8];
+  uint64_t setmask;
+};
+__device__ __forceinline__ uint64_t expand(uint64_t j, const Fixed& f) {
+#pragma unroll 1
+  for (int i = 0; i < f.n; ++i) {
+    int b = f.pos[i];
+    uint64_t lo = j & ((1ULL << b) - 1);
+    j = ((j >> b) << (b + 1)) | lo;
+  }
+  return j | f.setmask;
+}
+
+Fixed make_fixed(uint64_t zero_bits, uint64_t one_bits) {
+  Fixed f;
+  f.n = 0;
+  f.setmask = one_bits;
+  uint64_t all = zero_bits | one_bits;
+  for (int b = 0; b < 64 && f.n < 8; ++b)
+    if (all & (1ULL << b)) f.pos[f.n++] = b;
+  return f;
+}
+
+inline int grid_for(uint64_t work, int threads) {
+  uint64_t g = (work + threads - 1) / threads;
+  uint64_t cap = (uint64_t)kSMs * 8;
+  if (g > cap) g = cap;
+  if (g < 1) g = 1;
+  return (int)g;
+}
+
+// ---------------------------------------------------------------------------
+// Plain kernels: one gate, one HBM pass, grid-stride.
+// ---------------------------------------------------------------------------
+template <int CLS, typename R>
+__global__ void __launch_bounds__(256) k_u2(typename C2<R>::T* __restrict__ s, uint64_t work, int t, Fixed f,
+                                            Mat<R> m) {
+  using V = typename C2<R>::T;
+  const uint64_t tb = 1ULL << t;
+  for (uint64_t j = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; j < work; j += (uint64_t)gridDim.x * blockDim.x) {
+    uint64_t i0 = expand(j, f);
+    V x0 = s[i0], x1 = s[i0 | tb], y0, y1;
+    u2_apply<CLS, V, R>(m.m, x0, x1, y0, y1);
+    s[i0] = y0;
+    s[i0 | tb] = y1;
+  }
+}
+
+template <int CLS, typename R>
+__global__ void __launch_bounds__(256) k_phase(typename C2<R>::T* __restrict__ s, uint64_t work, Fixed f, Mat<R> m) {
+  for (uint64_t j = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; j < work; j += (uint64_t)gridDim.x * blockDim.x) {
+    uint64_t i = expand(j, f);
+    s[i] = phase_apply<CLS>(m.m, s[i]);
+  }
+}
+
+template <typename R>
+__global__ void __launch_bounds__(256) k_swap(typename C2<R>::T* __restrict__ s, uint64_t work, uint64_t flip, Fixed f,
+                                              int iswap) {
+  using V = typename C2<R>::T;
+  for (uint64_t j = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; j < work; j += (uint64_t)gridDim.x * blockDim.x) {
+    uint64_t i = expand(j, f), p = i ^ flip;
+    V a = s[i], b = s[p];
+    if (iswap) {
+      V ra, rb;
+      ra.x = -b.y; ra.y = b.x;   // i * b
+      rb.x = -a.y; rb.y = a.x;   // i * a
+      a = ra;
+      b = rb;
+      s[i] = a;
+      s[p] = b;
+    } else {
+      s[i] = b;
+      s[p] = a;
+    }
+  }
+}
+
+// kind: 0 blockade (popcount==1 -> ph), 1 parity (ph0/ph1), 2 collapse (match -> scale, else 0)
+template <int KIND, typename R>
+__global__ void __launch_bounds__(256) k_diag_all(typename C2<R>::T* __restrict__ s, uint64_t N, uint64_t mask,
+                                                  uint64_t val, Mat<R> m) {
+  using V = typename C2<R>::T;
+  for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < N; i += (uint64_t)gridDim.x * blockDim.x) {
+    V x = s[i];
+    if (KIND == 0) {
+      if (__popcll(i & mask) == 1) s[i] = cmul(m.m[0], m.m[1], x);
+    } else if (KIND == 1) {
+      if (__popcll(i & mask) & 1) s[i] = cmul(m.m[2], m.m[3], x);
+      else s[i] = cmul(m.m[0], m.m[1], x);
+    } else {
+      V r;
+      if ((i & mask) == val) { r.x = mul_(x.x, m.m[0]); r.y = mul_(x.y, m.m[0]); }
+      else { r.x = 0; r.y = 0; }
+      s[i] = r;
+    }
+  }
+}
+
+template <typename R>
+cudaError_t plain_op_t(void* sv, int n, const GOp& op, cudaStream_t st) {
+  using V = typename C2<R>::T;
+  V* s = (V*)sv;
+  const int T = 256;
+  const uint64_t N = 1ULL << n;
+  switch (op.kind) {
+    case OK_U2: {
+      Fixed f = make_fixed(1ULL << op.t, op.cmask);
+      uint64_t work = N >> f.n;
+      Mat<R> m = to_mat<R>(op.m);
+      int g = grid_for(work, T);
+      switch (op.cls) {
+        case U2_GENERAL: k_u2<U2_GENERAL, R><<<g, T, 0, st>>>(s, work, op.t, f, m); break;
+        case U2_REAL: k_u2<U2_REAL, R><<<g, T, 0, st>>>(s, work, op.t, f, m); break;
+        case U2_RXLIKE: k_u2<U2_RXLIKE, R><<<g, T, 0, st>>>(s, work, op.t, f, m); break;
+        case U2_DIAG: k_u2<U2_DIAG, R><<<g, T, 0, st>>>(s, work, op.t, f, m); break;
+        case U2_ANTIDIAG: k_u2<U2_ANTIDIAG, R><<<g, T, 0, st>>>(s, work, op.t, f, m); break;
+        case U2_X: k_u2<U2_X, R><<<g, T, 0, st>>>(s, work, op.t, f, m); break;
+        default: k_u2<U2_IMAG_ANTI, R><<<g, T, 0, st>>>(s, work, op.t, f, m); break;
+      }
+    } break;
+    case OK_PHASE: {
+      Fixed f = make_fixed(0, op.mask);
+      uint64_t work = N >> f.n;
+      Mat<R> m = to_mat<R>(op.m);
+      int g = grid_for(work, T);
+      switch (op.cls) {
+        case PH_GENERAL: k_phase<PH_GENERAL, R><<<g, T, 0, st>>>(s, work, f, m); break;
+        case PH_NEG: k_phase<PH_NEG, R><<<g, T, 0, st>>>(s, work, f, m); break;
+        case PH_I: k_phase<PH_I, R><<<g, T, 0, st>>>(s, work, f, m); break;
+        default: k_phase<PH_MINUS_I, R><<<g, T, 0, st>>>(s, work, f, m); break;
+      }
+    } break;
+    case OK_SWAP: {
+      Fixed f = make_fixed(1ULL << op.t2, (1ULL << op.t) | op.cmask);
+      uint64_t work = N >> f.n;
+      k_swap<R><<<grid_for(work, T), T, 0, st>>>(s, work, (1ULL << op.t) | (1ULL << op.t2), f, op.flags & 1);
+    } break;
+    case OK_BLOCKADE:
+      k_diag_all<0, R><<<grid_for(N, T), T, 0, st>>>(s, N, op.mask, 0, to_mat<R>(op.m));
+      break;
+    case OK_PARITY:
+      k_diag_all<1, R><<<grid_for(N, T), T, 0, st>>>(s, N, op.mask, 0, to_mat<R>(op.m));
+      break;
+    case OK_COLLAPSE:
+      k_diag_all<2, R><<<grid_for(N, T), T, 0, st>>>(s, N, op.mask, op.val, to_mat<R>(op.m));
+      break;
+    default:
+      return cudaErrorInvalidValue;
+  }
+  counted();
+  return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------
+// Tiled executor: one CTA holds 2^k amplitudes (local bits pd.lbits) in shared
+// memory and applies the pass's op run to them before writing back.
+// ---------------------------------------------------------------------------
+constexpr int kTileThreads = 512;
+constexpr int kMaxItems = 16;  // dense-block outputs per thread (2^13 / 512)
+
+template <typename R>
+__global__ void __launch_bounds__(kTileThreads) k_tile(typename C2<R>::T* __restrict__ s, PassDesc pd,
+                                                      const TOp* __restrict__ ops, const double* __restrict__ dense,
+                                                      uint64_t ntiles) {
+  using V = typename C2<R>::T;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int k = pd.k, K = 1 << k, klow = pd.klow;
+  V* tile = reinterpret_cast<V*>(smem_raw);
+  uint64_t* hioff = reinterpret_cast<uint64_t*>(smem_raw + sizeof(V) * K);
+  const int nhi = 1 << (k - klow);
+  for (int h = threadIdx.x; h < nhi; h += blockDim.x) {
+    uint64_t off = 0;
+    for (int j = klow; j < k; ++j)
+      if ((h >> (j - klow)) & 1) off |= 1ULL << pd.lbits[j];
+    hioff[h] = off;
+  }
+  __syncthreads();
+  const uint32_t lowmask = (1u << klow) - 1;
+  for (uint64_t tid = blockIdx.x; tid < ntiles; tid += gridDim.x) {
+    uint64_t base = 0;
+    for (int r = 0; r < pd.nruns; ++r)
+      base |= ((tid >> pd.run_src[r]) & ((1ULL << pd.run_len[r]) - 1)) << pd.run_dst[r];
+    for (int l = threadIdx.x; l < K; l += blockDim.x) tile[l] = s[base | (l & lowmask) | hioff[l >> klow]];
+    __syncthreads();
+    for (int64_t o = pd.op_begin; o < pd.op_end; ++o) {
+      const TOp* op = ops + o;
+      const int kind = op->kind;
+      if (kind == OK_U2) {
+        if ((base & op->gcmask) != op->gcmask) continue;
+        const int t = op->t, cls = op->cls;
+        const uint32_t lc = op->lcmask, tb = 1u << t;
+        R m[8];
+#pragma unroll
+        for (int q = 0; q < 8; ++q) m[q] = (R)op->m[q];
+        for (int p = threadIdx.x; p < (K >> 1); p += blockDim.x) {
+          uint32_t l0 = ((p >> t) << (t + 1)) | (p & (tb - 1));
+          if ((l0 & lc) != lc) continue;
+          V x0 = tile[l0], x1 = tile[l0 | tb], y0, y1;
+          switch (cls) {
+            case U2_GENERAL: u2_apply<U2_GENERAL>(m, x0, x1, y0, y1); break;
+            case U2_REAL: u2_apply<U2_REAL>(m, x0, x1, y0, y1); break;
+            case U2_RXLIKE: u2_apply<U2_RXLIKE>(m, x0, x1, y0, y1); break;
+            case U2_DIAG: u2_apply<U2_DIAG>(m, x0, x1, y0, y1); break;
+            case U2_ANTIDIAG: u2_apply<U2_ANTIDIAG>(m, x0, x1, y0, y1); break;
+            case U2_X: u2_apply<U2_X>(m, x0, x1, y0, y1); break;
+            default: u2_apply<U2_IMAG_ANTI>(m, x0, x1, y0, y1); break;
+          }
+          tile[l0] = y0;
+          tile[l0 | tb] = y1;
+        }
+      } else if (kind == OK_PHASE) {
+        if ((base & op->gmask) != op->gmask) continue;
+        const uint32_t lm = op->lmask;
+        const int cls = op->cls;
+        const R pr = (R)op->m[0], pi = (R)op->m[1];
+        R m2[2] = {pr, pi};
+        for (int l = threadIdx.x; l < K; l += blockDim.x) {
+          if ((l & lm) != lm) continue;
+          V x = tile[l];
+          switch (cls) {
+            case PH_GENERAL: x = phase_apply<PH_GENERAL>(m2, x); break;
+            case PH_NEG: x = phase_apply<PH_NEG>(m2, x); break;
+            case PH_I: x = phase_apply<PH_I>(m2, x); break;
+            default: x = phase_apply<PH_MINUS_I>(m2, x); break;
+          }
+          tile[l] = x;
+        }
+      } else if (kind == OK_SWAP) {
+        if ((base & op->gcmask) != op->gcmask) continue;
+        const uint32_t lc = op->lcmask, ta = 1u << op->t, tb2 = 1u << op->t2;
+        const int iswap = op->flags & 1;
+        for (int l = threadIdx.x; l < K; l += blockDim.x) {
+          if (!(l & ta) || (l & tb2) || (l & lc) != lc) continue;
+          uint32_t p = l ^ ta ^ tb2;
+          V a = tile[l], b = tile[p];
+          if (iswap) {
+            V ra, rb;
+            ra.x = -b.y; ra.y = b.x;
+            rb.x = -a.y; rb.y = a.x;
+            tile[l] = ra;
+            tile[p] = rb;
+          } else {
+            tile[l] = b;
+            tile[p] = a;
+          }
+        }
+      } else if (kind == OK_BLOCKADE) {
+        const int gc = __popcll(base & op->gmask);
+        if (gc > 1) continue;
+        const uint32_t lm = op->lmask;
+        const R pr = (R)op->m[0], pi = (R)op->m[1];
+        for (int l = threadIdx.x; l < K; l += blockDim.x)
+          if (gc + __popc(l & lm) == 1) tile[l] = cmul(pr, pi, tile[l]);
+      } else if (kind == OK_PARITY) {
+        const int gp = __popcll(base & op->gmask) & 1;
+        const uint32_t lm = op->lmask;
+        const R p0r = (R)op->m[0], p0i = (R)op->m[1], p1r = (R)op->m[2], p1i = (R)op->m[3];
+        for (int l = threadIdx.x; l < K; l += blockDim.x) {
+          int par = gp ^ (__popc(l & lm) & 1);
+          tile[l] = par ? cmul(p1r, p1i, tile[l]) : cmul(p0r, p0i, tile[l]);
+        }
+      } else if (kind == OK_COLLAPSE) {
+        const bool gok = (base & op->gmask) == op->gval;
+        const uint32_t lm = op->lmask, lv = op->lval;
+        const R sc = (R)op->m[0];
+        for (int l = threadIdx.x; l < K; l += blockDim.x) {
+          V x = tile[l], r;
+          if (gok && (l & lm) == lv) { r.x = mul_(x.x, sc); r.y = mul_(x.y, sc); }
+          else { r.x = 0; r.y = 0; }
+          tile[l] = r;
+        }
+      } else if (kind == OK_DENSE) {
+        const int dk = op->dk, D = 1 << dk;
+        const double* M = dense + 2 * op->doff;
+        V out[kMaxItems];
+        int cnt = 0;
+        for (int idx = threadIdx.x; idx < K; idx += blockDim.x, ++cnt) {
+          int g = idx >> dk, r = idx & (D - 1);
+          // deposit group bits around the block bits, block bits from r / c
+          uint32_t lg = g;
+          for (int j = 0; j < dk; ++j) {
+            int b = op->dbits[j];
+            lg = ((lg >> b) << (b + 1)) | (lg & ((1u << b) - 1));
+          }
+          R ar = 0, ai = 0;
+          for (int c = 0; c < D; ++c) {
+            uint32_t lc = lg;
+            for (int j = 0; j < dk; ++j)
+              if ((c >> j) & 1) lc |= 1u << op->dbits[j];
+            V x = tile[lc];
+            R mr = (R)M[2 * (r * D + c)], mi = (R)M[2 * (r * D + c) + 1];
+            ar = fma(mr, x.x, fma(-mi, x.y, ar));
+            ai = fma(mr, x.y, fma(mi, x.x, ai));
+          }
+          V y;
+          y.x = ar;
+          y.y = ai;
+          out[cnt] = y;
+        }
+        __syncthreads();
+        cnt = 0;
+        for (int idx = threadIdx.x; idx < K; idx += blockDim.x, ++cnt) {
+          int g = idx >> dk, r = idx & (D - 1);
+          uint32_t lg = g;
+          for (int j = 0; j < dk; ++j) {
+            int b = op->dbits[j];
+            lg = ((lg >> b) << (b + 1)) | (lg & ((1u << b) - 1));
+          }
+          for (int j = 0; j < dk; ++j)
+            if ((r >> j) & 1) lg |= 1u << op->dbits[j];
+          tile[lg] = out[cnt];
+        }
+      }
+      __syncthreads();
+    }
+    for (int l = threadIdx.x; l < K; l += blockDim.x) s[base | (l & lowmask) | hioff[l >> klow]] = tile[l];
+    __syncthreads();
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Reductions. Per-thread TwoSum accumulation, warp/block combination of
+// (sum, compensation) pairs, one pair per block written to d_part.
+// ---------------------------------------------------------------------------
+struct DD {
+  double s, c;
+};
+__device__ __forceinline__ void two_sum_acc(DD& a, double x) {
+  double t = __dadd_rn(a.s, x);
+  double bp = __dsub_rn(t, a.s);
+  double e = __dadd_rn(__dsub_rn(a.s, __dsub_rn(t, bp)), __dsub_rn(x, bp));
+  a.s = t;
+  a.c = __dadd_rn(a.c, e);
+}
+__device__ __forceinline__ DD dd_add(DD a, DD b) {
+  DD r = a;
+  two_sum_acc(r, b.s);
+  r.c = __dadd_rn(r.c, b.c);
+  return r;
+}
+template <int NT>
+__device__ __forceinline__ void block_reduce_store(DD v, double* d_part, int slot) {
+  __shared__ DD red[NT / 32];
+  for (int o = 16; o > 0; o >>= 1) {
+    DD w;
+    w.s = __shfl_down_sync(0xffffffffu, v.s, o);
+    w.c = __shfl_down_sync(0xffffffffu, v.c, o);
+    v = dd_add(v, w);
+  }
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = v;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    DD a = red[0];
+    for (int w = 1; w < NT / 32; ++w) a = dd_add(a, red[w]);
+    d_part[2 * slot] = a.s;
+    d_part[2 * slot + 1] = a.c;
+  }
+}
+
+template <typename R>
+__device__ __forceinline__ double p_of(typename C2<R>::T a) {
+  double re = (double)a.x, im = (double)a.y;
+  return __dadd_rn(__dmul_rn(re, re), __dmul_rn(im, im));
+}
+
+template <typename R>
+__global__ void __launch_bounds__(256) k_probs(const typename C2<R>::T* __restrict__ s, uint64_t N,
+                                               double* __restrict__ p) {
+  for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < N; i += (uint64_t)gridDim.x * blockDim.x)
+    p[i] = p_of<R>(s[i]);
+}
+
+template <typename R>
+__global__ void __launch_bounds__(256) k_norm2(const typename C2<R>::T* __restrict__ s, uint64_t N, double* d_part) {
+  DD a{0, 0};
+  for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < N; i += (uint64_t)gridDim.x * blockDim.x)
+    two_sum_acc(a, p_of<R>(s[i]));
+  block_reduce_store<256>(a, d_part, blockIdx.x);
+}
+
+// Re(w * conj(a) b), w in {1, -i, -1, i} indexed by wk (0..3): conj(a)b = R + iI
+__device__ __forceinline__ double re_wab(int wk, double ar, double ai, double br, double bi) {
+  double R = ar * br + ai * bi, I = ar * bi - ai * br;
+  switch (wk & 3) {
+    case 0: return R;
+    case 1: return I;   // -i*(R+iI) = I - iR
+    case 2: return -R;
+    default: return -I; //  i*(R+iI) = -I + iR
+  }
+}
+
+// <psi|P|psi>, (P psi)_i = (-i)^ny (-1)^popc(i&z) psi_{i^x}
+template <typename R>
+__global__ void __launch_bounds__(256) k_pauli(const typename C2<R>::T* __restrict__ s, uint64_t N, uint64_t xm,
+                                               uint64_t zm, int ny, double* d_part) {
+  DD acc{0, 0};
+  const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+  if (xm == 0) {
+    // diagonal: (-1)^popc(i & z) p_i   (ny = 0 when x = 0)
+    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < N; i += stride) {
+      double p = p_of<R>(s[i]);
+      two_sum_acc(acc, (__popcll(i & zm) & 1) ? -p : p);
+    }
+  } else {
+    const int hb = 63 - __clzll(xm);
+    const uint64_t half = N >> 1;
+    for (uint64_t q = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; q < half; q += stride) {
+      uint64_t i = ((q >> hb) << (hb + 1)) | (q & ((1ULL << hb) - 1));
+      uint64_t j = i ^ xm;
+      auto a = s[i];
+      auto b = s[j];
+      // term i: Re(conj(a_i) w_i a_j), term j: Re(conj(a_j) w_j a_i)
+      int wi = ny + ((__popcll(i & zm) & 1) ? 2 : 0);
+      int wj = ny + ((__popcll(j & zm) & 1) ? 2 : 0);
+      double v = re_wab(wi, a.x, a.y, b.x, b.y) + re_wab(wj, b.x, b.y, a.x, a.y);
+      two_sum_acc(acc, v);
+    }
+  }
+  block_reduce_store<256>(acc, d_part, blockIdx.x);
+}
+
+template <typename R>
+__global__ void __launch_bounds__(256) k_expect1q(const typename C2<R>::T* __restrict__ s, uint64_t N, int bit,
+                                                  Mat<double> o, double* d_part) {
+  DD acc{0, 0};
+  const uint64_t half = N >> 1, tb = 1ULL << bit;
+  for (uint64_t q = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; q < half; q += (uint64_t)gridDim.x * blockDim.x) {
+    uint64_t i0 = ((q >> bit) << (bit + 1)) | (q & (tb - 1));
+    auto a = s[i0];
+    auto b = s[i0 | tb];
+    double x0r = a.x, x0i = a.y, x1r = b.x, x1i = b.y;
+    double y0r = o.m[0] * x0r - o.m[1] * x0i + o.m[2] * x1r - o.m[3] * x1i;
+    double y0i = o.m[0] * x0i + o.m[1] * x0r + o.m[2] * x1i + o.m[3] * x1r;
+    double y1r = o.m[4] * x0r - o.m[5] * x0i + o.m[6] * x1r - o.m[7] * x1i;
+    double y1i = o.m[4] * x0i + o.m[5] * x0r + o.m[6] * x1i + o.m[7] * x1r;
+    two_sum_acc(acc, x0r * y0r + x0i * y0i + x1r * y1r + x1i * y1i);
+  }
+  block_reduce_store<256>(acc, d_part, blockIdx.x);
+}
+
+template <typename R>
+__global__ void __launch_bounds__(256) k_inner(const typename C2<R>::T* __restrict__ a,
+                                               const typename C2<R>::T* __restrict__ b, uint64_t N, double* d_part) {
+  DD re{0, 0}, im{0, 0};
+  for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < N; i += (uint64_t)gridDim.x * blockDim.x) {
+    auto x = a[i];
+    auto y = b[i];
+    two_sum_acc(re, (double)x.x * y.x + (double)x.y * y.y);
+    two_sum_acc(im, (double)x.x * y.y - (double)x.y * y.x);
+  }
+  block_reduce_store<256>(re, d_part, blockIdx.x);
+  __syncthreads();
+  block_reduce_store<256>(im, d_part, gridDim.x + blockIdx.x);
+}
+
+// Marginal over fixed-bit outcomes: blockIdx.y = outcome over the unique measured bits.
+template <typename R>
+__global__ void __launch_bounds__(256) k_marginal(const typename C2<R>::T* __restrict__ s, uint64_t work, Fixed f0,
+                                                  int m, const int* __restrict__ bits, double* d_pm,
+                                                  unsigned long long* d_qm) {
+  const int o = blockIdx.y;
+  Fixed f = f0;
+  uint64_t set = 0;
+  for (int k = 0; k < m; ++k)
+    if ((o >> k) & 1) set |= 1ULL << bits[k];
+  f.setmask = set;
+  DD acc{0, 0};
+  unsigned long long qs = 0;
+  for (uint64_t j = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; j < work; j += (uint64_t)gridDim.x * blockDim.x) {
+    double p = p_of<R>(s[expand(j, f)]);
+    two_sum_acc(acc, p);
+    double v = p * 4611686018427387904.0;
+    qs += (v > 0) ? (unsigned long long)v : 0ULL;
+  }
+  const int slot = o * gridDim.x + blockIdx.x;
+  block_reduce_store<256>(acc, d_pm, slot);
+  __shared__ unsigned long long qred[8];
+  for (int off = 16; off > 0; off >>= 1) qs += __shfl_down_sync(0xffffffffu, qs, off);
+  if ((threadIdx.x & 31) == 0) qred[threadIdx.x >> 5] = qs;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    unsigned long long t = 0;
+    for (int w = 0; w < 8; ++w) t += qred[w];
+    d_qm[slot] = t;
+  }
+}
+
+template <typename R>
+__global__ void k_gather(const typename C2<R>::T* __restrict__ s, const uint64_t* __restrict__ idx, int64_t count,
+                         double* __restrict__ out) {
+  for (int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; j < count; j += (int64_t)gridDim.x * blockDim.x) {
+    auto a = s[idx[j]];
+    out[2 * j] = a.x;
+    out[2 * j + 1] = a.y;
+  }
+}
+
+template <typename R>
+__global__ void k_density(const typename C2<R>::T* __restrict__ s, uint64_t N, double* __restrict__ rho) {
+  for (uint64_t e = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; e < N * N; e += (uint64_t)gridDim.x * blockDim.x) {
+    uint64_t i = e / N, j = e % N;
+    auto a = s[i];
+    auto b = s[j];
+    // a_i conj(a_j)
+    rho[2 * e] = (double)a.x * b.x + (double)a.y * b.y;
+    rho[2 * e + 1] = (double)a.y * b.x - (double)a.x * b.y;
+  }
+}
+
+__global__ void k_set_one(void* s, int prec, uint64_t idx) {
+  if (prec == QG_C64) reinterpret_cast<float2*>(s)[idx] = make_float2(1.f, 0.f);
+  else reinterpret_cast<double2*>(s)[idx] = make_double2(1.0, 0.0);
+}
+
+__global__ void k_c128_to_c64(const double2* __restrict__ a, float2* __restrict__ b, uint64_t n) {
+  for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
+    double2 v = a[i];
+    b[i] = make_float2((float)v.x, (float)v.y);
+  }
+}
+__global__ void k_c64_to_c128(const float2* __restrict__ a, double2* __restrict__ b, uint64_t n) {
+  for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
+    float2 v = a[i];
+    b[i] = make_double2(v.x, v.y);
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Hierarchical sampler. Probabilities are quantised q_i = floor(p_i 2^62);
+// chunk (32 amplitudes) and block (256 chunks) sums are exact integers, so the
+// cumulative distribution does not depend on launch shape. A shot draws
+// u = floor(r64 * T / 2^64) from Philox and takes the first i whose cumulative
+// sum exceeds u: block by binary search of the block prefix, chunk by a warp
+// scan of the block's chunk sums, amplitude by a warp scan inside the chunk.
+// ---------------------------------------------------------------------------
+struct SampleGeom {
+  uint64_t N;
+  int ch;       // amplitudes per chunk (<= 32)
+  int cpb;      // chunks per block (<= 256)
+  uint64_t nb;  // blocks
+  uint64_t nchunks;
+};
+SampleGeom sample_geom(int n) {
+  SampleGeom g;
+  g.N = 1ULL << n;
+  g.ch = (int)(g.N < 32 ? g.N : 32);
+  uint64_t nch = g.N / g.ch;
+  g.cpb = (int)(nch < 256 ? nch : 256);
+  g.nchunks = nch;
+  g.nb = nch / g.cpb;
+  return g;
+}
+
+__device__ __forceinline__ unsigned long long quant(double p) {
+  double v = p * 4611686018427387904.0;
+  return v > 0 ? (unsigned long long)v : 0ULL;
+}
+
+// one CTA (256 threads = 8 warps) per sample block; each warp handles cpb/8 chunks
+template <typename R>
+__global__ void __launch_bounds__(256) k_samp_sums(const typename C2<R>::T* __restrict__ s, SampleGeom g,
+                                                   unsigned long long* __restrict__ csum,
+                                                   unsigned long long* __restrict__ bsum, double* __restrict__ bsumf) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  __shared__ unsigned long long wq[8];
+  __shared__ DD wf[8];
+  for (uint64_t b = blockIdx.x; b < g.nb; b += gridDim.x) {
+    unsigned long long bq = 0;
+    DD bf{0, 0};
+    for (int c = warp; c < g.cpb; c += 8) {
+      uint64_t chunk = b * g.cpb + c;
+      unsigned long long q = 0;
+      double p = 0;
+      if (lane < g.ch) {
+        p = p_of<R>(s[chunk * g.ch + lane]);
+        q = quant(p);
+      }
+      for (int o = 16; o > 0; o >>= 1) q += __shfl_down_sync(0xffffffffu, q, o);
+      DD pf{p, 0};
+      for (int o = 16; o > 0; o >>= 1) {
+        DD w;
+        w.s = __shfl_down_sync(0xffffffffu, pf.s, o);
+        w.c = __shfl_down_sync(0xffffffffu, pf.c, o);
+        pf = dd_add(pf, w);
+      }
+      if (lane == 0) {
+        csum[chunk] = q;
+        bq += q;
+        bf = dd_add(bf, pf);
+      }
+    }
+    if (lane == 0) {
+      wq[warp] = bq;
+      wf[warp] = bf;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      unsigned long long t = 0;
+      DD f{0, 0};
+      for (int w = 0; w < 8; ++w) {
+        t += wq[w];
+        f = dd_add(f, wf[w]);
+      }
+      bsum[b] = t;
+      bsumf[b] = f.s + f.c;
+    }
+    __syncthreads();
+  }
+}
+
+// single CTA: exclusive prefix of block sums (bpre[nb] = T) and compensated FP64 total
+__global__ void __launch_bounds__(1024) k_samp_scan(const unsigned long long* __restrict__ bsum,
+                                                    const double* __restrict__ bsumf, uint64_t nb,
+                                                    unsigned long long* __restrict__ bpre, double* __restrict__ total) {
+  __shared__ unsigned long long sh[1024];
+  __shared__ unsigned long long carry;
+  __shared__ DD fred[32];
+  if (threadIdx.x == 0) carry = 0;
+  DD f{0, 0};
+  __syncthreads();
+  for (uint64_t base = 0; base < nb; base += 1024) {
+    uint64_t i = base + threadIdx.x;
+    unsigned long long v = i < nb ? bsum[i] : 0ULL;
+    if (i < nb) two_sum_acc(f, bsumf[i]);
+    sh[threadIdx.x] = v;
+    __syncthreads();
+    for (int o = 1; o < 1024; o <<= 1) {  // Hillis-Steele inclusive scan
+      unsigned long long add = threadIdx.x >= (unsigned)o ? sh[threadIdx.x - o] : 0ULL;
+      __syncthreads();
+      sh[threadIdx.x] += add;
+      __syncthreads();
+    }
+    if (i < nb) bpre[i] = carry + sh[threadIdx.x] - v;
+    __syncthreads();
+    if (threadIdx.x == 1023) carry += sh[1023];
+    __syncthreads();
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    DD w;
+    w.s = __shfl_down_sync(0xffffffffu, f.s, o);
+    w.c = __shfl_down_sync(0xffffffffu, f.c, o);
+    f = dd_add(f, w);
+  }
+  if ((threadIdx.x & 31) == 0) fred[threadIdx.x >> 5] = f;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    DD a = fred[0];
+    for (int w = 1; w < 32; ++w) a = dd_add(a, fred[w]);
+    total[0] = a.s + a.c;
+    bpre[nb] = carry;
+  }
+}
+
+// one warp per shot
+template <typename R>
+__global__ void __launch_bounds__(256) k_samp_resolve(const typename C2<R>::T* __restrict__ s, SampleGeom g,
+                                                      const unsigned long long* __restrict__ csum,
+                                                      const unsigned long long* __restrict__ bpre, uint64_t shots,
+                                                      uint64_t seed, uint64_t* __restrict__ out) {
+  const int lane = threadIdx.x & 31;
+  const uint64_t warps = ((uint64_t)gridDim.x * blockDim.x) >> 5;
+  const unsigned long long T = bpre[g.nb];
+  for (uint64_t shot = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; shot < shots; shot += warps) {
+    if (T == 0) {
+      if (lane == 0) out[shot] = 0;
+      continue;
+    }
+    unsigned long long u = __umul64hi(draw64(seed, shot, 0u), T);
+    // block: first b with bpre[b+1] > u
+    uint64_t lo = 0, hi = g.nb - 1;
+    while (lo < hi) {
+      uint64_t mid = (lo + hi) >> 1;
+      if (bpre[mid + 1] > u) hi = mid; else lo = mid + 1;
+    }
+    const uint64_t b = lo;
+    unsigned long long r = u - bpre[b];
+    // chunk within block: cpb <= 256 chunk sums, 8 per lane
+    const int per = (g.cpb + 31) / 32;
+    unsigned long long loc[8];
+    unsigned long long mine = 0;
+    for (int k = 0; k < per; ++k) {
+      int c = lane * per + k;
+      loc[k] = c < g.cpb ? csum[b * g.cpb + c] : 0ULL;
+      mine += loc[k];
+    }
+    unsigned long long incl = mine;
+    for (int o = 1; o < 32; o <<= 1) {
+      unsigned long long v = __shfl_up_sync(0xffffffffu, incl, o);
+      if (lane >= o) incl += v;
+    }
+    unsigned long long excl = incl - mine;
+    unsigned ballot = __ballot_sync(0xffffffffu, incl > r);
+    int owner = ballot ? __ffs(ballot) - 1 : 31;
+    int chunk_in_block = 0;
+    unsigned long long before = 0;
+    if (lane == owner) {
+      unsigned long long c = excl;
+      int kk = 0;
+      for (; kk < per; ++kk) {
+        if (c + loc[kk] > r) break;
+        c += loc[kk];
+      }
+      if (kk >= per) kk = per - 1;
+      chunk_in_block = lane * per + kk;
+      before = c;
+      if (chunk_in_block >= g.cpb) chunk_in_block = g.cpb - 1;
+    }
+    chunk_in_block = __shfl_sync(0xffffffffu, chunk_in_block, owner);
+    before = __shfl_sync(0xffffffffu, before, owner);
+    unsigned long long r2 = r - before;
+    const uint64_t chunk = b * g.cpb + chunk_in_block;
+    unsigned long long q = lane < g.ch ? quant(p_of<R>(s[chunk * g.ch + lane])) : 0ULL;
+    unsigned long long qi = q;
+    for (int o = 1; o < 32; o <<= 1) {
+      unsigned long long v = __shfl_up_sync(0xffffffffu, qi, o);
+      if (lane >= o) qi += v;
+    }
+    unsigned bl = __ballot_sync(0xffffffffu, (lane < g.ch) && qi > r2);
+    int pick = bl ? __ffs(bl) - 1 : g.ch - 1;
+    if (lane == 0) out[shot] = chunk * g.ch + pick;
+  }
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------------------
+// launchers
+// ---------------------------------------------------------------------------
+unsigned long long kernel_launch_count() { return g_launches.load(); }
+
+int reduce_blocks_for(int n) {
+  uint64_t N = 1ULL << n;
+  uint64_t b = (N + 255) / 256;
+  if (b > (uint64_t)kSMs * 4) b = (uint64_t)kSMs * 4;
+  return (int)(b < 1 ? 1 : b);
+}
+
+cudaError_t launch_set_basis(void* s, int precision, int n, uint64_t idx, cudaStream_t st) {
+  size_t bytes = (precision == QG_C64 ? 8ULL : 16ULL) << n;
+  cudaError_t e = cudaMemsetAsync(s, 0, bytes, st);
+  if (e != cudaSuccess) return e;
+  k_set_one<<<1, 1, 0, st>>>(s, precision, idx);
+  counted();
+  return cudaGetLastError();
+}
+
+cudaError_t launch_plain_op(void* s, int precision, int n, const GOp& op, cudaStream_t st) {
+  return precision == QG_C64 ? plain_op_t<float>(s, n, op, st) : plain_op_t<double>(s, n, op, st);
+}
+
+cudaError_t launch_tile_pass(void* s, int precision, int n, const PassDesc& pd, const TOp* d_tops,
+                             const double* d_dense, cudaStream_t st) {
+  const int K = 1 << pd.k;
+  const size_t amp = precision == QG_C64 ? 8 : 16;
+  const size_t smem = amp * K + sizeof(uint64_t) * (1u << (pd.k - pd.klow));
+  const uint64_t ntiles = 1ULL << (n - pd.k);
+  int threads = K >= 2 * kTileThreads ? kTileThreads : (K / 2 < 32 ? 32 : K / 2);
+  if (K / threads > kMaxItems) return cudaErrorInvalidValue;
+  int per_sm = (int)((200 * 1024) / smem);
+  if (per_sm > 4) per_sm = 4;
+  if (per_sm < 1) per_sm = 1;
+  uint64_t grid = (uint64_t)kSMs * per_sm;
+  if (grid > ntiles) grid = ntiles;
+  cudaError_t e;
+  if (precision == QG_C64) {
+    e = cudaFuncSetAttribute(k_tile<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    k_tile<float><<<(unsigned)grid, threads, smem, st>>>((float2*)s, pd, d_tops, d_dense, ntiles);
+  } else {
+    e = cudaFuncSetAttribute(k_tile<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    k_tile<double><<<(unsigned)grid, threads, smem, st>>>((double2*)s, pd, d_tops, d_dense, ntiles);
+  }
+  counted();
+  return cudaGetLastError();
+}
+
+cudaError_t launch_c128_to_c64(const double* src, float* dst, uint64_t count, cudaStream_t st) {
+  k_c128_to_c64<<<grid_for(count, 256), 256, 0, st>>>((const double2*)src, (float2*)dst, count);
+  counted();
+  return cudaGetLastError();
+}
+cudaError_t launch_c64_to_c128(const float* src, double* dst, uint64_t count, cudaStream_t st) {
+  k_c64_to_c128<<<grid_for(count, 256), 256, 0, st>>>((const float2*)src, (double2*)dst, count);
+  counted();
+  return cudaGetLastError();
+}
+
+cudaError_t launch_probabilities(const void* s, int precision, int n, double* d_p, cudaStream_t st) {
+  uint64_t N = 1ULL << n;
+  if (precision == QG_C64) k_probs<float><<<grid_for(N, 256), 256, 0, st>>>((const float2*)s, N, d_p);
+  else k_probs<double><<<grid_for(N, 256), 256, 0, st>>>((const double2*)s, N, d_p);
+  counted();
+  return cudaGetLastError();
+}
+
+cudaError_t launch_norm2(const void* s, int precision, int n, double* d_part, int nblocks, cudaStream_t st) {
+  uint64_t N = 1ULL << n;
+  if (precision == QG_C64) k_norm2<float><<<nblocks, 256, 0, st>>>((const float2*)s, N, d_part);
+  else k_norm2<double><<<nblocks, 256, 0, st>>>((const double2*)s, N, d_part);
+  counted();
+  return cudaGetLastError();
+}
+
+cudaError_t launch_pauli_expect(const void* s, int precision, int n, uint64_t xmask, uint64_t zmask, int ny,
+                                double* d_part, int nblocks, cudaStream_t st) {
+  uint64_t N = 1ULL << n;
+  if (precision == QG_C64) k_pauli<float><<<nblocks, 256, 0, st>>>((const float2*)s, N, xmask, zmask, ny, d_part);
+  else k_pauli<double><<<nblocks, 256, 0, st>>>((const double2*)s, N, xmask, zmask, ny, d_part);
+  counted();
+  return cudaGetLastError();
+}
+
+cudaError_t launch_expect_1q(const void* s, int precision, int n, int bit, const double* o8, double* d_part,
+                             int nblocks, cudaStream_t st) {
+  uint64_t N = 1ULL << n;
+  Mat<double> o = to_mat<double>(o8);
+  if (precision == QG_C64) k_expect1q<float><<<nblocks, 256, 0, st>>>((const float2*)s, N, bit, o, d_part);
+  else k_expect1q<double><<<nblocks, 256, 0, st>>>((const double2*)s, N, bit, o, d_part);
+  counted();
+  return cudaGetLastError();
+}
+
+cudaError_t launch_inner(const void* a, const void* b, int precision, int n, double* d_part, int nblocks,
+                         cudaStream_t st) {
+  uint64_t N = 1ULL << n;
+  if (precision == QG_C64) k_inner<float><<<nblocks, 256, 0, st>>>((const float2*)a, (const float2*)b, N, d_part);
+  else k_inner<double><<<nblocks, 256, 0, st>>>((const double2*)a, (const double2*)b, N, d_part);
+  counted();
+  return cudaGetLastError();
+}
+
+cudaError_t launch_marginal_host(const void* s, int precision, int n, const int* h_bits, const int* d_bits, int m,
+                                 int nbx, double* d_pm, unsigned long long* d_qm, cudaStream_t st) {
+  uint64_t zero = 0;
+  for (int k = 0; k < m; ++k) zero |= 1ULL << h_bits[k];
+  Fixed f = make_fixed(zero, 0);
+  uint64_t work = (1ULL << n) >> m;
+  dim3 grid(nbx, 1u << m);
+  if (precision == QG_C64)
+    k_marginal<float><<<grid, 256, 0, st>>>((const float2*)s, work, f, m, d_bits, d_pm, d_qm);
+  else
+    k_marginal<double><<<grid, 256, 0, st>>>((const double2*)s, work, f, m, d_bits, d_pm, d_qm);
+  counted();
+  return cudaGetLastError();
+}
+
+cudaError_t launch_gather(const void* s, int precision, const uint64_t* d_idx, int64_t count, double* d_out,
+                          cudaStream_t st) {
+  int g = grid_for((uint64_t)count, 256);
+  if (precision == QG_C64) k_gather<float><<<g, 256, 0, st>>>((const float2*)s, d_idx, count, d_out);
+  else k_gather<double><<<g, 256, 0, st>>>((const double2*)s, d_idx, count, d_out);
+  counted();
+  return cudaGetLastError();
+}
+
+cudaError_t launch_density(const void* s, int precision, int n, double* d_rho, cudaStream_t st) {
+  uint64_t N = 1ULL << n;
+  int g = grid_for(N * N, 256);
+  if (precision == QG_C64) k_density<float><<<g, 256, 0, st>>>((const float2*)s, N, d_rho);
+  else k_density<double><<<g, 256, 0, st>>>((const double2*)s, N, d_rho);
+  counted();
+  return cudaGetLastError();
+}
+
+size_t sampler_scratch_bytes(int n, uint64_t shots) {
+  (void)shots;
+  SampleGeom g = sample_geom(n);
+  return sizeof(unsigned long long) * (g.nchunks + g.nb + (g.nb + 1)) + sizeof(double) * (g.nb + 2) + 256;
+}
+
+cudaError_t launch_sample(const void* s, int precision, int n, uint64_t shots, uint64_t seed, void* d_scratch,
+                          uint64_t* d_outcomes, double* d_total, cudaStream_t st) {
+  SampleGeom g = sample_geom(n);
+  unsigned long long* csum = (unsigned long long*)d_scratch;
+  unsigned long long* bsum = csum + g.nchunks;
+  unsigned long long* bpre = bsum + g.nb;
+  double* bsumf = (double*)(bpre + g.nb + 1);
+  int grid = (int)(g.nb < (uint64_t)kSMs * 8 ? g.nb : (uint64_t)kSMs * 8);
+  if (precision == QG_C64)
+    k_samp_sums<float><<<grid, 256, 0, st>>>((const float2*)s, g, csum, bsum, bsumf);
+  else
+    k_samp_sums<double><<<grid, 256, 0, st>>>((const double2*)s, g, csum, bsum, bsumf);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return e;
+  k_samp_scan<<<1, 1024, 0, st>>>(bsum, bsumf, g.nb, bpre, d_total);
+  e = cudaGetLastError();
+  counted(2);
+  if (e != cudaSuccess || shots == 0) return e;
+  uint64_t warps_needed = shots;
+  uint64_t blocks = (warps_needed * 32 + 255) / 256;
+  if (blocks > (uint64_t)kSMs * 16) blocks = (uint64_t)kSMs * 16;
+  if (precision == QG_C64)
+    k_samp_resolve<float><<<(unsigned)blocks, 256, 0, st>>>((const float2*)s, g, csum, bpre, shots, seed, d_outcomes);
+  else
+    k_samp_resolve<double><<<(unsigned)blocks, 256, 0, st>>>((const double2*)s, g, csum, bpre, shots, seed,
+                                                             d_outcomes);
+  counted();
+  return cudaGetLastError();
+}
+
+}  // namespace qg

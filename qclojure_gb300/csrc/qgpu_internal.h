@@ -1,0 +1,203 @@
+// Internal types shared by the circuit compiler (compile.cpp), the kernels
+// (kernels.cu) and the runtime (runtime.cpp) of libqgpu.so.
+#pragma once
+
+#include <cstdint>
+#include <string>
+#include <vector>
+
+#include <cuda_runtime.h>
+
+#include "../../include/qgpu.h"
+
+namespace qg {
+
+// ---------------------------------------------------------------------------
+// Device operation ("gate op") in amplitude-index space. Bit b of the basis
+// index is qubit (n-1-b). All controlled forms are already transposed the way
+// the reference's apply-controlled-gate applies them.
+// ---------------------------------------------------------------------------
+enum OpKind : int32_t {
+  OK_U2 = 0,        // 2x2 on bit t where (idx & cmask) == cmask; class in cls
+  OK_PHASE = 1,     // amp *= ph where (idx & mask) == mask; class in cls
+  OK_SWAP = 2,      // exchange bits t,t2 where (idx & cmask) == cmask; flags&1: iSWAP phase i
+  OK_BLOCKADE = 3,  // amp *= ph where popcount(idx & mask) == 1
+  OK_PARITY = 4,    // amp *= (parity(idx & mask) ? ph1 : ph0)
+  OK_COLLAPSE = 5,  // amp = ((idx & mask) == val) ? amp * scale : 0
+  OK_DENSE = 6      // dense 2^dk x 2^dk block on bits dbits[0..dk) (dbits[0] = least significant)
+};
+
+// Matrix classes of OK_U2 (picked on the host from exact zero / unit entries).
+enum U2Class : int32_t {
+  U2_GENERAL = 0,   // y0 = m0 x0 + m1 x1, y1 = m2 x0 + m3 x1
+  U2_REAL = 1,      // all four entries real
+  U2_RXLIKE = 2,    // real diagonal, imaginary off-diagonal
+  U2_DIAG = 3,      // off-diagonal exactly zero
+  U2_ANTIDIAG = 4,  // diagonal exactly zero
+  U2_X = 5,         // [[0,1],[1,0]] exactly: a pure swap
+  U2_IMAG_ANTI = 6  // diagonal zero, off-diagonal = +-i exactly: swap with (re,im) rotation
+};
+
+// Phase classes of OK_PHASE.
+enum PhaseClass : int32_t {
+  PH_GENERAL = 0,   // multiply by (m[0], m[1])
+  PH_NEG = 1,       // multiply by -1 (exact)
+  PH_I = 2,         // multiply by +i (exact)
+  PH_MINUS_I = 3    // multiply by -i (exact)
+};
+
+struct GOp {
+  int32_t kind;
+  int32_t cls;
+  int32_t t, t2;
+  int32_t flags;
+  int32_t dk;
+  uint64_t cmask;
+  uint64_t mask;
+  uint64_t val;
+  double m[8];
+  int32_t dbits[5];
+  int32_t pad;
+  int64_t doff;     // offset (in complex entries) of a dense block in the pass's matrix buffer
+};
+
+// ---------------------------------------------------------------------------
+// Tile-local operation: a GOp rewritten for one pass of the tiled executor.
+// l* fields are masks / bit positions in tile-local index space (0..k-1),
+// g* fields are the parts of the masks on non-local bits, tested once per tile.
+// ---------------------------------------------------------------------------
+struct TOp {
+  int32_t kind;
+  int32_t cls;
+  int32_t t, t2;     // local bit positions
+  int32_t flags;
+  int32_t dk;
+  uint32_t lcmask;   // local control mask
+  uint32_t lmask;    // local part of mask
+  uint32_t lval;     // local part of val
+  uint32_t pad0;
+  uint64_t gcmask;   // non-local control bits (absolute)
+  uint64_t gmask;    // non-local part of mask (absolute)
+  uint64_t gval;     // non-local part of val (absolute)
+  double m[8];
+  int32_t dbits[5];  // local bit positions of a dense block
+  int32_t pad1;
+  int64_t doff;
+};
+
+constexpr int kMaxTileBits = 13;     // 2^13 amplitudes per tile at most
+constexpr int kMaxLocal = kMaxTileBits;
+
+// One HBM pass of the tiled executor.
+struct PassDesc {
+  int32_t k;                 // local bits per tile
+  int32_t klow;              // bits 0..klow-1 are always local (contiguous runs)
+  int32_t lbits[kMaxLocal];  // absolute bit position of local bit j (ascending)
+  int32_t nruns;             // runs of non-local bits for the tile-index deposit
+  int32_t run_src[kMaxLocal + 1];
+  int32_t run_dst[kMaxLocal + 1];
+  int32_t run_len[kMaxLocal + 1];
+  int64_t op_begin, op_end;  // range in the TOp array
+};
+
+// A compiled step sequence.
+struct Step {
+  enum Kind { PLAIN_OP, TILE_PASS, MEASURE } kind;
+  GOp op;                  // PLAIN_OP
+  PassDesc pass;           // TILE_PASS
+  std::vector<int> mqubits;// MEASURE (qubit indices, outcome bit i <-> mqubits[i])
+};
+
+struct Program {
+  int n = 0;
+  std::vector<Step> steps;
+  std::vector<TOp> tops;             // all tile ops, referenced by PassDesc ranges
+  std::vector<double> dense;         // dense block matrices (re, im interleaved)
+  int hbm_passes = 0;
+};
+
+// Compile a reference-level circuit into GOps (returns QG_OK or an error code;
+// err receives a message in the reference's words).
+int lower_circuit(const qg_circuit* c, std::vector<GOp>* gops, std::vector<std::vector<int>>* measures,
+                  std::vector<int>* measure_at, std::string* err);
+// Schedule GOps into passes for the given fusion mode.
+int schedule(int n, int precision, int fusion, int fuse_k, const std::vector<GOp>& gops,
+             const std::vector<std::vector<int>>& measures, const std::vector<int>& measure_at,
+             Program* prog, std::string* err);
+
+// ---------------------------------------------------------------------------
+// Kernel launchers (kernels.cu). All return cudaError_t from the launch.
+// ---------------------------------------------------------------------------
+int tile_bits_for(int n, int precision);
+
+cudaError_t launch_set_basis(void* s, int precision, int n, uint64_t idx, cudaStream_t st);
+cudaError_t launch_plain_op(void* s, int precision, int n, const GOp& op, cudaStream_t st);
+cudaError_t launch_tile_pass(void* s, int precision, int n, const PassDesc& pd, const TOp* d_tops,
+                             const double* d_dense, cudaStream_t st);
+cudaError_t launch_c128_to_c64(const double* src, float* dst, uint64_t count, cudaStream_t st);
+cudaError_t launch_c64_to_c128(const float* src, double* dst, uint64_t count, cudaStream_t st);
+
+// Reductions (results written to device scratch, copied by the caller).
+// partial sums per block are (sum, compensation) pairs of doubles.
+struct ReduceScratch {
+  double* d_part = nullptr;     // 2 * nblocks doubles
+  int nblocks = 0;
+};
+cudaError_t launch_probabilities(const void* s, int precision, int n, double* d_p, cudaStream_t st);
+cudaError_t launch_norm2(const void* s, int precision, int n, double* d_part, int nblocks, cudaStream_t st);
+cudaError_t launch_pauli_expect(const void* s, int precision, int n, uint64_t xmask, uint64_t zmask, int ny,
+                                double* d_part, int nblocks, cudaStream_t st);
+cudaError_t launch_expect_1q(const void* s, int precision, int n, int bit, const double* o8, double* d_part,
+                             int nblocks, cudaStream_t st);
+cudaError_t launch_inner(const void* a, const void* b, int precision, int n, double* d_part, int nblocks,
+                         cudaStream_t st);
+// Marginal probabilities over measured bits: per outcome FP64 (sum, comp) and u64 quantised totals.
+cudaError_t launch_marginal_host(const void* s, int precision, int n, const int* h_bits, const int* d_bits, int m,
+                                 int nbx, double* d_pm, unsigned long long* d_qm, cudaStream_t st);
+cudaError_t launch_gather(const void* s, int precision, const uint64_t* d_idx, int64_t count, double* d_out,
+                          cudaStream_t st);
+cudaError_t launch_density(const void* s, int precision, int n, double* d_rho, cudaStream_t st);
+
+// Hierarchical shot sampler. Scratch sized by sampler_scratch_bytes().
+size_t sampler_scratch_bytes(int n, uint64_t shots);
+cudaError_t launch_sample(const void* s, int precision, int n, uint64_t shots, uint64_t seed, void* d_scratch,
+                          uint64_t* d_outcomes, double* d_total, cudaStream_t st);
+
+int reduce_blocks_for(int n);
+unsigned long long kernel_launch_count();
+
+// Philox4x32-10 (Salmon et al., SC'11), shared by host and device code.
+#if defined(__CUDACC__)
+#define QG_HD __host__ __device__ __forceinline__
+#else
+#define QG_HD inline
+#endif
+QG_HD void philox4x32_10(uint32_t c0, uint32_t c1, uint32_t c2, uint32_t c3, uint32_t k0, uint32_t k1,
+                         uint32_t out[4]) {
+  for (int r = 0; r < 10; ++r) {
+    if (r) {
+      k0 += 0x9E3779B9u;
+      k1 += 0xBB67AE85u;
+    }
+    uint64_t p0 = (uint64_t)0xD2511F53u * c0, p1 = (uint64_t)0xCD9E8D57u * c2;
+    uint32_t hi0 = (uint32_t)(p0 >> 32), lo0 = (uint32_t)p0;
+    uint32_t hi1 = (uint32_t)(p1 >> 32), lo1 = (uint32_t)p1;
+    uint32_t n0 = hi1 ^ c1 ^ k0, n2 = hi0 ^ c3 ^ k1;
+    c0 = n0;
+    c1 = lo1;
+    c2 = n2;
+    c3 = lo0;
+  }
+  out[0] = c0;
+  out[1] = c1;
+  out[2] = c2;
+  out[3] = c3;
+}
+// 64 uniform bits for (seed, index, stream): stream 0 = shots, 1 = mid-circuit measurements.
+QG_HD uint64_t draw64(uint64_t seed, uint64_t index, uint32_t stream) {
+  uint32_t o[4];
+  philox4x32_10((uint32_t)index, (uint32_t)(index >> 32), stream, 0u, (uint32_t)seed, (uint32_t)(seed >> 32), o);
+  return ((uint64_t)o[1] << 32) | o[0];
+}
+
+}  // namespace qg

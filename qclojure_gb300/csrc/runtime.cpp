@@ -1,0 +1,1600 @@
+// Runtime of libqgpu.so: contexts, device-resident states, the job queue and
+// every extern "C" entry point declared in include/qgpu.h.
+//
+// Job semantics follow src/org/soulspace/qclojure/adapter/backend/ideal_simulator.clj:
+// submit returns at once (:120-136), status goes :queued -> :running ->
+// :completed | :failed | :cancelled (:138-141), failures carry a message
+// (:93-96), cancel answers :cancelled / :cannot-cancel / :not-found
+// (:154-163), queue-status counts jobs by status (:165-176). Worker threads
+// (one CUDA stream each) run jobs; a job is admitted only when its state fits
+// the HBM budget, so several jobs overlap on the device.
+#include <algorithm>
+#include <atomic>
+#include <chrono>
+#include <cmath>
+#include <condition_variable>
+#include <cstring>
+#include <deque>
+#include <map>
+#include <memory>
+#include <mutex>
+#include <string>
+#include <thread>
+#include <vector>
+
+#include "qgpu_internal.h"
+
+namespace qg {
+
+using Clock = std::chrono::steady_clock;
+
+static double ms_since(Clock::time_point t0) {
+  return std::chrono::duration<double, std::milli>(Clock::now() - t0).count();
+}
+
+struct Ctx;
+
+// ---------------------------------------------------------------------------
+// Device state
+// ---------------------------------------------------------------------------
+struct State {
+  Ctx* ctx = nullptr;
+  int n = 0;
+  int prec = QG_C128;
+  void* d = nullptr;
+  size_t bytes = 0;
+  cudaStream_t stream = nullptr;
+  bool own_stream = false;
+  double* d_part = nullptr;  // reduction partials: 4 * reduce_blocks doubles
+  int nblocks = 0;
+  std::string err;
+};
+
+static size_t amp_bytes(int prec) { return prec == QG_C64 ? 8 : 16; }
+
+static int cuda_fail(std::string* err, cudaError_t e, const char* what) {
+  if (err) *err = std::string(what) + ": " + cudaGetErrorString(e);
+  return QG_ERR_DEVICE;
+}
+#define CK(expr, what)                                   \
+  do {                                                   \
+    cudaError_t e_ = (expr);                             \
+    if (e_ != cudaSuccess) return cuda_fail(err, e_, what); \
+  } while (0)
+
+static int state_alloc(State* s, int n, int prec, cudaStream_t stream, std::string* err) {
+  s->n = n;
+  s->prec = prec;
+  s->bytes = amp_bytes(prec) << n;
+  s->stream = stream;
+  s->nblocks = reduce_blocks_for(n);
+  CK(cudaMallocAsync(&s->d, s->bytes, stream), "cudaMallocAsync(state)");
+  CK(cudaMallocAsync((void**)&s->d_part, sizeof(double) * 4 * s->nblocks, stream), "cudaMallocAsync(partials)");
+  return QG_OK;
+}
+
+static void state_release(State* s) {
+  if (s->d) cudaFreeAsync(s->d, s->stream);
+  if (s->d_part) cudaFreeAsync(s->d_part, s->stream);
+  s->d = nullptr;
+  s->d_part = nullptr;
+}
+
+// Sum (sum, comp) pairs from the device in a fixed order.
+static int fetch_dd(State* s, const double* d_part, int count, double* out, std::string* err) {
+  std::vector<double> h(2 * (size_t)count);
+  CK(cudaMemcpyAsync(h.data(), d_part, sizeof(double) * 2 * count, cudaMemcpyDeviceToHost, s->stream), "D2H partials");
+  CK(cudaStreamSynchronize(s->stream), "sync");
+  long double acc = 0;
+  double hi = 0, lo = 0;
+  for (int i = 0; i < count; ++i) {
+    // TwoSum in double keeps the compensation; long double only for the final fold
+    double x = h[2 * i];
+    double t = hi + x, bp = t - hi;
+    lo += (hi - (t - bp)) + (x - bp);
+    hi = t;
+    lo += h[2 * i + 1];
+  }
+  acc = (long double)hi + (long double)lo;
+  *out = (double)acc;
+  return QG_OK;
+}
+
+static int upload_c128(State* s, const double* host, std::string* err) {
+  const uint64_t N = 1ULL << s->n;
+  if (s->prec == QG_C128) {
+    CK(cudaMemcpyAsync(s->d, host, s->bytes, cudaMemcpyHostToDevice, s->stream), "H2D state");
+    return QG_OK;
+  }
+  // complex64: stage complex128 chunks through a device buffer
+  const uint64_t chunk = std::min<uint64_t>(N, 1ULL << 24);
+  double* tmp = nullptr;
+  CK(cudaMallocAsync((void**)&tmp, chunk * 16, s->stream), "cudaMallocAsync(stage)");
+  for (uint64_t off = 0; off < N; off += chunk) {
+    uint64_t c = std::min(chunk, N - off);
+    CK(cudaMemcpyAsync(tmp, host + 2 * off, c * 16, cudaMemcpyHostToDevice, s->stream), "H2D stage");
+    CK(launch_c128_to_c64(tmp, (float*)s->d + 2 * off, c, s->stream), "convert");
+  }
+  CK(cudaFreeAsync(tmp, s->stream), "cudaFreeAsync");
+  return QG_OK;
+}
+
+static int download_c128(State* s, double* host, std::string* err) {
+  const uint64_t N = 1ULL << s->n;
+  if (s->prec == QG_C128) {
+    CK(cudaMemcpyAsync(host, s->d, s->bytes, cudaMemcpyDeviceToHost, s->stream), "D2H state");
+    CK(cudaStreamSynchronize(s->stream), "sync");
+    return QG_OK;
+  }
+  const uint64_t chunk = std::min<uint64_t>(N, 1ULL << 24);
+  double* tmp = nullptr;
+  CK(cudaMallocAsync((void**)&tmp, chunk * 16, s->stream), "cudaMallocAsync(stage)");
+  for (uint64_t off = 0; off < N; off += chunk) {
+    uint64_t c = std::min(chunk, N - off);
+    CK(launch_c64_to_c128((const float*)s->d + 2 * off, tmp, c, s->stream), "convert");
+    CK(cudaMemcpyAsync(host + 2 * off, tmp, c * 16, cudaMemcpyDeviceToHost, s->stream), "D2H stage");
+  }
+  CK(cudaFreeAsync(tmp, s->stream), "cudaFreeAsync");
+  CK(cudaStreamSynchronize(s->stream), "sync");
+  return QG_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Program execution (shared by jobs and qg_state_apply)
+// ---------------------------------------------------------------------------
+struct ExecStats {
+  double device_ms = 0;
+  int passes = 0;
+  std::vector<float>* pass_ms = nullptr;  // per-step CUDA-event times when profiling
+  std::vector<int>* pass_kind = nullptr;
+};
+
+static int do_measure(State* s, const std::vector<int>& qubits, uint64_t seed, uint64_t draw_index,
+                      uint64_t* outcome_out, double* prob_out, std::string* err) {
+  const int n = s->n;
+  const int m_orig = (int)qubits.size();
+  // unique bits in order of first appearance
+  std::vector<int> ubits;
+  std::vector<int> orig_to_u(m_orig);
+  for (int k = 0; k < m_orig; ++k) {
+    int b = n - 1 - qubits[k];
+    auto it = std::find(ubits.begin(), ubits.end(), b);
+    if (it == ubits.end()) {
+      orig_to_u[k] = (int)ubits.size();
+      ubits.push_back(b);
+    } else {
+      orig_to_u[k] = (int)(it - ubits.begin());
+    }
+  }
+  const int m = (int)ubits.size();
+  if (m > 15) {
+    *err = "measurement of more than 15 distinct qubits is not supported";
+    return QG_ERR_UNSUPPORTED;
+  }
+  const int nout = 1 << m;
+  int nbx = std::max(1, 1024 / nout);
+  uint64_t work = (1ULL << n) >> m;
+  if ((uint64_t)nbx * 256 > work) nbx = (int)std::max<uint64_t>(1, (work + 255) / 256);
+  int* d_bits = nullptr;
+  double* d_pm = nullptr;
+  unsigned long long* d_qm = nullptr;
+  CK(cudaMallocAsync((void**)&d_bits, sizeof(int) * 16, s->stream), "alloc");
+  CK(cudaMallocAsync((void**)&d_pm, sizeof(double) * 2 * nout * nbx, s->stream), "alloc");
+  CK(cudaMallocAsync((void**)&d_qm, sizeof(unsigned long long) * nout * nbx, s->stream), "alloc");
+  CK(cudaMemcpyAsync(d_bits, ubits.data(), sizeof(int) * m, cudaMemcpyHostToDevice, s->stream), "H2D bits");
+  CK(launch_marginal_host(s->d, s->prec, n, ubits.data(), d_bits, m, nbx, d_pm, d_qm, s->stream), "marginal");
+  std::vector<double> hpm(2 * (size_t)nout * nbx);
+  std::vector<unsigned long long> hqm((size_t)nout * nbx);
+  CK(cudaMemcpyAsync(hpm.data(), d_pm, sizeof(double) * hpm.size(), cudaMemcpyDeviceToHost, s->stream), "D2H");
+  CK(cudaMemcpyAsync(hqm.data(), d_qm, sizeof(unsigned long long) * hqm.size(), cudaMemcpyDeviceToHost, s->stream),
+     "D2H");
+  CK(cudaStreamSynchronize(s->stream), "sync");
+  cudaFreeAsync(d_bits, s->stream);
+  cudaFreeAsync(d_pm, s->stream);
+  cudaFreeAsync(d_qm, s->stream);
+  std::vector<double> Pu(nout);
+  std::vector<uint64_t> Qu(nout);
+  for (int o = 0; o < nout; ++o) {
+    double hi = 0, lo = 0;
+    uint64_t q = 0;
+    for (int b = 0; b < nbx; ++b) {
+      size_t slot = (size_t)o * nbx + b;
+      double x = hpm[2 * slot];
+      double t = hi + x, bp = t - hi;
+      lo += (hi - (t - bp)) + (x - bp);
+      hi = t;
+      lo += hpm[2 * slot + 1];
+      q += hqm[slot];
+    }
+    Pu[o] = hi + lo;
+    Qu[o] = q;
+  }
+  // outcomes in the reference's index order (bit k <-> qubits[k])
+  const uint64_t norig = 1ULL << m_orig;
+  auto to_u = [&](uint64_t o, bool* ok) {
+    uint64_t u = 0;
+    uint64_t seen = 0, val = 0;
+    for (int k = 0; k < m_orig; ++k) {
+      int ui = orig_to_u[k];
+      uint64_t bit = (o >> k) & 1;
+      if (seen & (1ULL << ui)) {
+        if (((val >> ui) & 1) != bit) { *ok = false; return (uint64_t)0; }
+      } else {
+        seen |= 1ULL << ui;
+        val |= bit << ui;
+      }
+    }
+    u = val;
+    *ok = true;
+    return u;
+  };
+  uint64_t T = 0;
+  for (int o = 0; o < nout; ++o) T += Qu[o];
+  uint64_t sel = norig - 1;
+  if (T > 0) {
+    unsigned __int128 prod = (unsigned __int128)draw64(seed, draw_index, 1u) * T;
+    uint64_t u = (uint64_t)(prod >> 64), c = 0;
+    for (uint64_t o = 0; o < norig; ++o) {
+      bool ok;
+      uint64_t ui = to_u(o, &ok);
+      if (!ok) continue;
+      c += Qu[ui];
+      if (c > u) { sel = o; break; }
+    }
+  }
+  bool ok;
+  uint64_t usel = to_u(sel, &ok);
+  double ps = ok ? Pu[usel] : 0.0;
+  double nf = ps > 0 ? 1.0 / std::sqrt(ps) : 1.0;
+  GOp g;
+  std::memset(&g, 0, sizeof(g));
+  g.kind = OK_COLLAPSE;
+  for (int k = 0; k < m; ++k) {
+    g.mask |= 1ULL << ubits[k];
+    if (ok && ((usel >> k) & 1)) g.val |= 1ULL << ubits[k];
+  }
+  if (!ok) g.val = ~0ULL;  // impossible outcome: everything collapses to zero (never chosen with T > 0)
+  g.m[0] = nf;
+  CK(launch_plain_op(s->d, s->prec, n, g, s->stream), "collapse");
+  if (outcome_out) *outcome_out = sel;
+  if (prob_out) *prob_out = ps;
+  return QG_OK;
+}
+
+static int exec_program(State* s, const Program& prog, uint64_t seed, const std::atomic<bool>* cancel,
+                        ExecStats* stats, std::string* err) {
+  TOp* d_tops = nullptr;
+  double* d_dense = nullptr;
+  if (!prog.tops.empty()) {
+    CK(cudaMallocAsync((void**)&d_tops, sizeof(TOp) * prog.tops.size(), s->stream), "alloc tops");
+    CK(cudaMemcpyAsync(d_tops, prog.tops.data(), sizeof(TOp) * prog.tops.size(), cudaMemcpyHostToDevice, s->stream),
+       "H2D tops");
+  }
+  if (!prog.dense.empty()) {
+    CK(cudaMallocAsync((void**)&d_dense, sizeof(double) * prog.dense.size(), s->stream), "alloc dense");
+    CK(cudaMemcpyAsync(d_dense, prog.dense.data(), sizeof(double) * prog.dense.size(), cudaMemcpyHostToDevice,
+                       s->stream),
+       "H2D dense");
+  }
+  cudaEvent_t e0, e1;
+  CK(cudaEventCreate(&e0), "event");
+  CK(cudaEventCreate(&e1), "event");
+  CK(cudaEventRecord(e0, s->stream), "event");
+  uint64_t measure_index = 0;
+  int rc = QG_OK;
+  const bool profile = stats && stats->pass_ms;
+  std::vector<cudaEvent_t> evs;
+  if (profile) {
+    evs.resize(prog.steps.size() + 1);
+    for (auto& ev : evs) CK(cudaEventCreate(&ev), "event");
+  }
+  for (size_t i = 0; i < prog.steps.size() && rc == QG_OK; ++i) {
+    if (cancel && cancel->load()) {
+      rc = QG_ERR_CANCELLED;
+      break;
+    }
+    const Step& st = prog.steps[i];
+    if (profile) cudaEventRecord(evs[i], s->stream);
+    cudaError_t e = cudaSuccess;
+    if (st.kind == Step::PLAIN_OP) {
+      e = launch_plain_op(s->d, s->prec, s->n, st.op, s->stream);
+    } else if (st.kind == Step::TILE_PASS) {
+      e = launch_tile_pass(s->d, s->prec, s->n, st.pass, d_tops, d_dense, s->stream);
+    } else {
+      rc = do_measure(s, st.mqubits, seed, measure_index++, nullptr, nullptr, err);
+    }
+    if (e != cudaSuccess) rc = cuda_fail(err, e, "gate pass");
+    if (profile) cudaEventRecord(evs[i + 1], s->stream);
+  }
+  cudaEventRecord(e1, s->stream);
+  cudaError_t se = cudaEventSynchronize(e1);
+  if (se != cudaSuccess && rc == QG_OK) rc = cuda_fail(err, se, "gate passes");
+  float ms = 0;
+  cudaEventElapsedTime(&ms, e0, e1);
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  if (profile) {
+    stats->pass_ms->clear();
+    stats->pass_kind->clear();
+    for (size_t i = 0; i < prog.steps.size(); ++i) {
+      float t = 0;
+      if (rc == QG_OK) cudaEventElapsedTime(&t, evs[i], evs[i + 1]);
+      stats->pass_ms->push_back(t);
+      stats->pass_kind->push_back(prog.steps[i].kind == Step::PLAIN_OP ? 0 : prog.steps[i].kind == Step::TILE_PASS ? 1 : 2);
+    }
+    for (auto& ev : evs) cudaEventDestroy(ev);
+  }
+  if (d_tops) cudaFreeAsync(d_tops, s->stream);
+  if (d_dense) cudaFreeAsync(d_dense, s->stream);
+  if (stats) {
+    stats->device_ms = ms;
+    stats->passes = prog.hbm_passes;
+  }
+  return rc;
+}
+
+static int compile_program(const qg_circuit* c, int precision, int fusion, int fuse_k, Program* prog,
+                           std::string* err) {
+  std::vector<GOp> gops;
+  std::vector<std::vector<int>> measures;
+  std::vector<int> measure_at;
+  int rc = lower_circuit(c, &gops, &measures, &measure_at, err);
+  if (rc != QG_OK) return rc;
+  return schedule(c->num_qubits, precision, fusion, fuse_k, gops, measures, measure_at, prog, err);
+}
+
+// ---------------------------------------------------------------------------
+// Result extraction on a device state
+// ---------------------------------------------------------------------------
+static int st_norm2(State* s, double* out, std::string* err) {
+  CK(launch_norm2(s->d, s->prec, s->n, s->d_part, s->nblocks, s->stream), "norm2");
+  return fetch_dd(s, s->d_part, s->nblocks, out, err);
+}
+
+static int st_pauli(State* s, const char* pauli, double* out, std::string* err) {
+  uint64_t xm = 0, zm = 0;
+  int ny = 0;
+  for (int q = 0; q < s->n; ++q) {
+    uint64_t b = 1ULL << (s->n - 1 - q);
+    char ch = pauli[q];
+    if (ch == 'X') xm |= b;
+    else if (ch == 'Y') { xm |= b; zm |= b; ++ny; }
+    else if (ch == 'Z') zm |= b;
+    else if (ch != 'I') {
+      *err = "Pauli strings use the characters I, X, Y, Z";
+      return QG_ERR_INVALID_ARG;
+    }
+  }
+  CK(launch_pauli_expect(s->d, s->prec, s->n, xm, zm, ny & 3, s->d_part, s->nblocks, s->stream), "pauli");
+  return fetch_dd(s, s->d_part, s->nblocks, out, err);
+}
+
+static int st_expect1q(State* s, const double* o8, int target, double* out, std::string* err) {
+  if (target < 0 || target >= s->n) {
+    *err = "observable target out of range";
+    return QG_ERR_QUBIT_RANGE;
+  }
+  CK(launch_expect_1q(s->d, s->prec, s->n, s->n - 1 - target, o8, s->d_part, s->nblocks, s->stream), "expect");
+  return fetch_dd(s, s->d_part, s->nblocks, out, err);
+}
+
+static int st_inner(State* a, State* b, double* re, double* im, std::string* err) {
+  if (a->n != b->n || a->prec != b->prec) {
+    *err = "states differ in size or precision";
+    return QG_ERR_INVALID_ARG;
+  }
+  CK(cudaStreamSynchronize(b->stream), "sync");
+  CK(launch_inner(a->d, b->d, a->prec, a->n, a->d_part, a->nblocks, a->stream), "inner");
+  int rc = fetch_dd(a, a->d_part, a->nblocks, re, err);
+  if (rc != QG_OK) return rc;
+  return fetch_dd(a, a->d_part + 2 * a->nblocks, a->nblocks, im, err);
+}
+
+static int st_sample(State* s, uint64_t shots, uint64_t seed, std::vector<uint64_t>* outcomes, std::string* err) {
+  size_t scratch = sampler_scratch_bytes(s->n, shots);
+  void* d_scratch = nullptr;
+  uint64_t* d_out = nullptr;
+  double* d_total = nullptr;
+  CK(cudaMallocAsync(&d_scratch, scratch, s->stream), "alloc sampler");
+  CK(cudaMallocAsync((void**)&d_out, sizeof(uint64_t) * std::max<uint64_t>(shots, 1), s->stream), "alloc outcomes");
+  CK(cudaMallocAsync((void**)&d_total, sizeof(double) * 2, s->stream), "alloc total");
+  CK(launch_sample(s->d, s->prec, s->n, shots, seed, d_scratch, d_out, d_total, s->stream), "sample");
+  double total = 0;
+  outcomes->resize(shots);
+  CK(cudaMemcpyAsync(&total, d_total, sizeof(double), cudaMemcpyDeviceToHost, s->stream), "D2H total");
+  if (shots) {
+    CK(cudaMemcpyAsync(outcomes->data(), d_out, sizeof(uint64_t) * shots, cudaMemcpyDeviceToHost, s->stream),
+       "D2H outcomes");
+  }
+  CK(cudaStreamSynchronize(s->stream), "sync");
+  cudaFreeAsync(d_scratch, s->stream);
+  cudaFreeAsync(d_out, s->stream);
+  cudaFreeAsync(d_total, s->stream);
+  // state.clj:901-903 rejects |sum p - 1| > 1e-8; a complex64 state carries FP32
+  // rounding (about 1e-7 per gate), so its check allows 1e-4 instead.
+  const double norm_tol = s->prec == QG_C64 ? 1e-4 : 1e-8;
+  if (std::fabs(total - 1.0) > norm_tol) {
+    *err = "State is not properly normalized (total probability " + std::to_string(total) + ")";
+    outcomes->clear();
+    return QG_ERR_NOT_NORMALIZED;
+  }
+  return QG_OK;
+}
+
+static int st_probs(State* s, double* host, std::string* err) {
+  const uint64_t N = 1ULL << s->n;
+  const uint64_t chunk = std::min<uint64_t>(N, 1ULL << 25);
+  double* d_p = nullptr;
+  CK(cudaMallocAsync((void**)&d_p, sizeof(double) * N, s->stream), "alloc probs");
+  CK(launch_probabilities(s->d, s->prec, s->n, d_p, s->stream), "probabilities");
+  for (uint64_t off = 0; off < N; off += chunk) {
+    uint64_t c = std::min(chunk, N - off);
+    CK(cudaMemcpyAsync(host + off, d_p + off, sizeof(double) * c, cudaMemcpyDeviceToHost, s->stream), "D2H probs");
+  }
+  CK(cudaStreamSynchronize(s->stream), "sync");
+  cudaFreeAsync(d_p, s->stream);
+  return QG_OK;
+}
+
+static int st_gather(State* s, const std::vector<uint64_t>& idx, std::vector<double>* out, std::string* err) {
+  out->assign(2 * idx.size(), 0.0);
+  if (idx.empty()) return QG_OK;
+  const uint64_t N = 1ULL << s->n;
+  for (uint64_t i : idx)
+    if (i >= N) {
+      *err = "basis state index out of range";
+      return QG_ERR_INVALID_ARG;
+    }
+  uint64_t* d_idx = nullptr;
+  double* d_out = nullptr;
+  CK(cudaMallocAsync((void**)&d_idx, sizeof(uint64_t) * idx.size(), s->stream), "alloc");
+  CK(cudaMallocAsync((void**)&d_out, sizeof(double) * 2 * idx.size(), s->stream), "alloc");
+  CK(cudaMemcpyAsync(d_idx, idx.data(), sizeof(uint64_t) * idx.size(), cudaMemcpyHostToDevice, s->stream), "H2D");
+  CK(launch_gather(s->d, s->prec, d_idx, (int64_t)idx.size(), d_out, s->stream), "gather");
+  CK(cudaMemcpyAsync(out->data(), d_out, sizeof(double) * out->size(), cudaMemcpyDeviceToHost, s->stream), "D2H");
+  CK(cudaStreamSynchronize(s->stream), "sync");
+  cudaFreeAsync(d_idx, s->stream);
+  cudaFreeAsync(d_out, s->stream);
+  return QG_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Jobs
+// ---------------------------------------------------------------------------
+struct SpecCopy {
+  uint32_t flags = 0;
+  uint64_t shots = 1;
+  std::vector<double> coeffs;
+  std::string paulis;
+  std::vector<double> observables;
+  std::vector<int32_t> obs_targets;
+  std::vector<uint64_t> basis_states;
+  std::vector<uint64_t> prob_targets;
+  std::vector<double> references;
+  int n_terms = 0, n_obs = 0, n_refs = 0;
+};
+
+struct Job {
+  uint64_t id = 0;
+  int n = 0;
+  std::vector<qg_op> ops;
+  SpecCopy spec;
+  std::vector<double> initial;
+  uint64_t seed = 0;
+  int precision = QG_C128, fusion = QG_FUSE_TILED;
+  std::atomic<int> status{QG_JOB_QUEUED};
+  std::atomic<bool> cancel{false};
+  int error_code = QG_OK;
+  std::string error;
+  Clock::time_point submitted, started, finished;
+  double exec_ms = 0, device_ms = 0, queue_ms = 0;
+  int passes = 0;
+  // results
+  std::vector<uint64_t> shots;
+  std::vector<std::pair<uint64_t, uint64_t>> counts;
+  std::vector<double> probs;          // full probability vector (when small or requested)
+  std::vector<double> target_probs;
+  std::vector<double> amplitudes;
+  std::vector<double> expectations, variances;
+  std::vector<double> term_values;
+  double energy = 0;
+  std::vector<double> fidelities;
+  std::vector<double> density;
+  int has = 0;
+  std::unique_ptr<State> state;       // final state kept on the device
+  bool state_pinned = false;          // requested by :state-vector; never evicted
+  uint64_t batch = 0;
+};
+
+struct Ctx {
+  int device = 0;
+  qg_config cfg{};
+  std::mutex mu;
+  std::condition_variable cv;       // queue / admission
+  std::condition_variable done_cv;  // job completion
+  std::map<uint64_t, std::shared_ptr<Job>> jobs;
+  std::deque<uint64_t> queue;
+  std::map<uint64_t, std::vector<uint64_t>> batches;
+  std::vector<std::thread> workers;
+  bool stop = false;
+  uint64_t next_id = 1;
+  uint64_t hbm_budget = 0, hbm_in_use = 0, hbm_total = 0;
+  int sm_count = 0;
+  std::string last_error;
+  std::mutex err_mu;
+};
+
+static void set_ctx_error(Ctx* c, const std::string& e) {
+  std::lock_guard<std::mutex> g(c->err_mu);
+  c->last_error = e;
+}
+
+static size_t job_bytes(int n, int prec) {
+  size_t st = amp_bytes(prec) << n;
+  return st + st / 4 + (64ULL << 20);  // state + sampler/probability scratch headroom
+}
+
+static void finish_job(Ctx* c, Job* j, int status) {
+  j->finished = Clock::now();
+  j->exec_ms = std::chrono::duration<double, std::milli>(j->finished - j->started).count();
+  {
+    std::lock_guard<std::mutex> g(c->mu);
+    j->status.store(status);
+  }
+  c->done_cv.notify_all();
+}
+
+// Evict final states of completed jobs (oldest first) until `need` bytes fit. Caller holds mu.
+static bool make_room(Ctx* c, size_t need) {
+  if (c->hbm_in_use + need <= c->hbm_budget) return true;
+  std::vector<std::shared_ptr<Job>> cands;
+  for (auto& kv : c->jobs) {
+    Job* j = kv.second.get();
+    if (j->state && !j->state_pinned && j->status.load() == QG_JOB_COMPLETED) cands.push_back(kv.second);
+  }
+  std::sort(cands.begin(), cands.end(), [](auto& a, auto& b) { return a->finished < b->finished; });
+  for (auto& j : cands) {
+    if (c->hbm_in_use + need <= c->hbm_budget) break;
+    cudaStreamSynchronize(j->state->stream);
+    size_t b = job_bytes(j->n, j->state->prec);
+    state_release(j->state.get());
+    cudaStreamSynchronize(j->state->stream);
+    if (j->state->own_stream) cudaStreamDestroy(j->state->stream);
+    j->state.reset();
+    c->hbm_in_use -= std::min(c->hbm_in_use, b);
+  }
+  return c->hbm_in_use + need <= c->hbm_budget;
+}
+
+static int run_job(Ctx* c, Job* j, cudaStream_t stream) {
+  std::string err;
+  int rc;
+  Program prog;
+  qg_circuit circ{j->n, (int32_t)j->ops.size(), j->ops.data()};
+  rc = compile_program(&circ, j->precision, j->fusion, c->cfg.fuse_k, &prog, &err);
+  if (rc != QG_OK) {
+    j->error_code = rc;
+    j->error = err;
+    return rc;
+  }
+  auto st = std::make_unique<State>();
+  st->ctx = c;
+  rc = state_alloc(st.get(), j->n, j->precision, stream, &err);
+  if (rc == QG_OK) {
+    if (!j->initial.empty()) rc = upload_c128(st.get(), j->initial.data(), &err);
+    else {
+      cudaError_t e = launch_set_basis(st->d, st->prec, st->n, 0, stream);
+      if (e != cudaSuccess) rc = cuda_fail(&err, e, "zero-state");
+    }
+  }
+  ExecStats stats;
+  if (rc == QG_OK) rc = exec_program(st.get(), prog, j->seed, &j->cancel, &stats, &err);
+  j->device_ms = stats.device_ms;
+  j->passes = stats.passes;
+  const SpecCopy& sp = j->spec;
+  const uint64_t N = 1ULL << j->n;
+  if (rc == QG_OK && (sp.flags & QG_RES_MEASUREMENTS)) {
+    rc = st_sample(st.get(), sp.shots, j->seed, &j->shots, &err);
+    if (rc == QG_OK) {
+      std::vector<uint64_t> sorted = j->shots;
+      std::sort(sorted.begin(), sorted.end());
+      j->counts.clear();
+      for (size_t i = 0; i < sorted.size();) {
+        size_t k = i;
+        while (k < sorted.size() && sorted[k] == sorted[i]) ++k;
+        j->counts.emplace_back(sorted[i], (uint64_t)(k - i));
+        i = k;
+      }
+      j->has |= QG_RES_MEASUREMENTS;
+    }
+  }
+  if (rc == QG_OK && (sp.flags & QG_RES_PROBABILITIES)) {
+    if (!sp.prob_targets.empty()) {
+      std::vector<double> amps;
+      rc = st_gather(st.get(), sp.prob_targets, &amps, &err);
+      j->target_probs.resize(sp.prob_targets.size());
+      for (size_t i = 0; rc == QG_OK && i < sp.prob_targets.size(); ++i) {
+        double re = amps[2 * i], im = amps[2 * i + 1];
+        j->target_probs[i] = re * re + im * im;
+      }
+    } else if (j->n <= 26) {
+      j->probs.resize(N);
+      rc = st_probs(st.get(), j->probs.data(), &err);
+    }
+    if (rc == QG_OK) j->has |= QG_RES_PROBABILITIES;
+  }
+  if (rc == QG_OK && (sp.flags & QG_RES_AMPLITUDES)) {
+    rc = st_gather(st.get(), sp.basis_states, &j->amplitudes, &err);
+    if (rc == QG_OK) j->has |= QG_RES_AMPLITUDES;
+  }
+  if (rc == QG_OK && (sp.flags & (QG_RES_EXPECTATION | QG_RES_VARIANCE))) {
+    j->expectations.assign(sp.n_obs, 0.0);
+    j->variances.assign(sp.n_obs, 0.0);
+    for (int k = 0; rc == QG_OK && k < sp.n_obs; ++k) {
+      const double* o = &sp.observables[8 * k];
+      int t = sp.obs_targets.empty() ? -1 : sp.obs_targets[k];
+      if (t < 0) {
+        if (j->n == 1) t = 0;
+        else {
+          err = "observables without a target qubit must match the register size; pass a target";
+          rc = QG_ERR_UNSUPPORTED;
+          break;
+        }
+      }
+      double e;
+      rc = st_expect1q(st.get(), o, t, &e, &err);
+      if (rc != QG_OK) break;
+      // O^2 (observables.clj:305-320 squares the full observable)
+      double o2[8];
+      for (int r = 0; r < 2; ++r)
+        for (int cc = 0; cc < 2; ++cc) {
+          double re = 0, im = 0;
+          for (int q = 0; q < 2; ++q) {
+            double ar = o[2 * (2 * r + q)], ai = o[2 * (2 * r + q) + 1];
+            double br = o[2 * (2 * q + cc)], bi = o[2 * (2 * q + cc) + 1];
+            re += ar * br - ai * bi;
+            im += ar * bi + ai * br;
+          }
+          o2[2 * (2 * r + cc)] = re;
+          o2[2 * (2 * r + cc) + 1] = im;
+        }
+      double e2;
+      rc = st_expect1q(st.get(), o2, t, &e2, &err);
+      j->expectations[k] = e;
+      j->variances[k] = e2 - e * e;
+    }
+    if (rc == QG_OK) j->has |= (sp.flags & (QG_RES_EXPECTATION | QG_RES_VARIANCE));
+  }
+  if (rc == QG_OK && (sp.flags & QG_RES_HAMILTONIAN)) {
+    j->term_values.assign(sp.n_terms, 0.0);
+    double energy = 0;
+    for (int k = 0; rc == QG_OK && k < sp.n_terms; ++k) {
+      double v;
+      rc = st_pauli(st.get(), sp.paulis.data() + (size_t)k * j->n, &v, &err);
+      j->term_values[k] = v;
+      double term = sp.coeffs[k] * v;
+      energy = (k == 0) ? term : energy + term;  // (reduce + ...) in term order
+    }
+    j->energy = energy;
+    if (rc == QG_OK) j->has |= QG_RES_HAMILTONIAN;
+  }
+  if (rc == QG_OK && (sp.flags & QG_RES_FIDELITY)) {
+    j->fidelities.assign(sp.n_refs, 0.0);
+    for (int k = 0; rc == QG_OK && k < sp.n_refs; ++k) {
+      State ref;
+      ref.ctx = c;
+      rc = state_alloc(&ref, j->n, j->precision, stream, &err);
+      if (rc == QG_OK) rc = upload_c128(&ref, sp.references.data() + 2 * N * (size_t)k, &err);
+      double re = 0, im = 0;
+      if (rc == QG_OK) rc = st_inner(st.get(), &ref, &re, &im, &err);
+      cudaStreamSynchronize(stream);
+      state_release(&ref);
+      j->fidelities[k] = std::sqrt(re * re + im * im);
+    }
+    if (rc == QG_OK) j->has |= QG_RES_FIDELITY;
+  }
+  if (rc == QG_OK && (sp.flags & QG_RES_DENSITY_MATRIX)) {
+    if (j->n > 12) {
+      err = "density matrix limited to 12 qubits (4^n entries)";
+      rc = QG_ERR_UNSUPPORTED;
+    } else {
+      double* d_rho = nullptr;
+      cudaError_t e = cudaMallocAsync((void**)&d_rho, sizeof(double) * 2 * N * N, stream);
+      if (e == cudaSuccess) e = launch_density(st->d, st->prec, st->n, d_rho, stream);
+      j->density.resize(2 * N * N);
+      if (e == cudaSuccess)
+        e = cudaMemcpyAsync(j->density.data(), d_rho, sizeof(double) * 2 * N * N, cudaMemcpyDeviceToHost, stream);
+      if (e == cudaSuccess) e = cudaStreamSynchronize(stream);
+      if (d_rho) cudaFreeAsync(d_rho, stream);
+      if (e != cudaSuccess) rc = cuda_fail(&err, e, "density matrix");
+      else j->has |= QG_RES_DENSITY_MATRIX;
+    }
+  }
+  cudaError_t se = cudaStreamSynchronize(stream);
+  if (se != cudaSuccess && rc == QG_OK) rc = cuda_fail(&err, se, "job");
+  if (rc == QG_OK) {
+    j->has |= QG_RES_STATE_VECTOR;  // final state available while kept
+    j->state_pinned = (sp.flags & QG_RES_STATE_VECTOR) != 0;
+    // the kept state gets its own stream so it outlives this worker's queue
+    cudaStream_t own;
+    if (cudaStreamCreateWithFlags(&own, cudaStreamNonBlocking) == cudaSuccess) {
+      st->stream = own;
+      st->own_stream = true;
+    }
+    j->state = std::move(st);
+  } else {
+    state_release(st.get());
+    cudaStreamSynchronize(stream);
+    j->error_code = rc;
+    j->error = err;
+  }
+  return rc;
+}
+
+static void worker_loop(Ctx* c) {
+  cudaSetDevice(c->device);
+  cudaStream_t stream;
+  cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking);
+  for (;;) {
+    std::shared_ptr<Job> j;
+    {
+      std::unique_lock<std::mutex> lk(c->mu);
+      for (;;) {
+        if (c->stop) break;
+        // first queued job that fits (jobs that can never fit fail at once)
+        bool picked = false;
+        for (auto it = c->queue.begin(); it != c->queue.end(); ++it) {
+          auto jj = c->jobs.find(*it);
+          if (jj == c->jobs.end() || jj->second->status.load() != QG_JOB_QUEUED) {
+            c->queue.erase(it);
+            picked = true;  // rescan
+            break;
+          }
+          size_t need = job_bytes(jj->second->n, jj->second->precision);
+          if (need > c->hbm_budget) {
+            j = jj->second;
+            c->queue.erase(it);
+            picked = true;
+            break;
+          }
+          if (make_room(c, need)) {
+            c->hbm_in_use += need;
+            j = jj->second;
+            c->queue.erase(it);
+            picked = true;
+            break;
+          }
+        }
+        if (j) break;
+        if (!picked) c->cv.wait(lk);
+      }
+      if (!j) break;
+      j->started = Clock::now();
+      j->queue_ms = std::chrono::duration<double, std::milli>(j->started - j->submitted).count();
+      if (j->cancel.load()) {
+        j->status.store(QG_JOB_CANCELLED);
+      } else {
+        j->status.store(QG_JOB_RUNNING);
+      }
+    }
+    if (j->status.load() == QG_JOB_CANCELLED) {
+      c->done_cv.notify_all();
+      continue;
+    }
+    const size_t need = job_bytes(j->n, j->precision);
+    int rc;
+    if (need > c->hbm_budget) {
+      j->error_code = QG_ERR_OOM;
+      j->error = "state of " + std::to_string(j->n) + " qubits does not fit the HBM budget";
+      rc = QG_ERR_OOM;
+    } else {
+      rc = run_job(c, j.get(), stream);
+    }
+    {
+      std::lock_guard<std::mutex> g(c->mu);
+      if (need <= c->hbm_budget && !j->state) c->hbm_in_use -= std::min(c->hbm_in_use, need);
+    }
+    c->cv.notify_all();
+    if (rc == QG_OK) finish_job(c, j.get(), QG_JOB_COMPLETED);
+    else if (rc == QG_ERR_CANCELLED) finish_job(c, j.get(), QG_JOB_CANCELLED);
+    else finish_job(c, j.get(), QG_JOB_FAILED);
+  }
+  cudaStreamSynchronize(stream);
+  cudaStreamDestroy(stream);
+}
+
+static std::shared_ptr<Job> find_job(Ctx* c, uint64_t id) {
+  std::lock_guard<std::mutex> g(c->mu);
+  auto it = c->jobs.find(id);
+  return it == c->jobs.end() ? nullptr : it->second;
+}
+
+static int copy_spec(const qg_result_spec* in, int n, SpecCopy* out, std::string* err) {
+  if (!in) return QG_OK;
+  out->flags = in->flags;
+  out->shots = in->shots ? in->shots : 1;
+  if (in->flags & QG_RES_HAMILTONIAN) {
+    if (in->n_terms < 0 || (in->n_terms > 0 && (!in->coefficients || !in->pauli_strings))) {
+      *err = "hamiltonian terms need coefficients and pauli strings";
+      return QG_ERR_INVALID_ARG;
+    }
+    out->n_terms = in->n_terms;
+    out->coeffs.assign(in->coefficients, in->coefficients + in->n_terms);
+    out->paulis.assign(in->pauli_strings, (size_t)in->n_terms * n);
+    for (char ch : out->paulis)
+      if (ch != 'I' && ch != 'X' && ch != 'Y' && ch != 'Z') {
+        *err = "Pauli strings use the characters I, X, Y, Z and have num-qubits characters";
+        return QG_ERR_INVALID_ARG;
+      }
+  }
+  if (in->flags & (QG_RES_EXPECTATION | QG_RES_VARIANCE)) {
+    if (in->n_observables < 0 || (in->n_observables > 0 && !in->observables)) {
+      *err = "expectation needs observables";
+      return QG_ERR_INVALID_ARG;
+    }
+    out->n_obs = in->n_observables;
+    out->observables.assign(in->observables, in->observables + 8 * (size_t)in->n_observables);
+    if (in->observable_targets)
+      out->obs_targets.assign(in->observable_targets, in->observable_targets + in->n_observables);
+  }
+  if (in->flags & QG_RES_AMPLITUDES) {
+    if (in->n_basis_states < 0 || (in->n_basis_states > 0 && !in->basis_states)) {
+      *err = "amplitudes need basis-states";
+      return QG_ERR_INVALID_ARG;
+    }
+    out->basis_states.assign(in->basis_states, in->basis_states + in->n_basis_states);
+  }
+  if ((in->flags & QG_RES_PROBABILITIES) && in->n_probability_targets > 0) {
+    if (!in->probability_targets) {
+      *err = "probability targets missing";
+      return QG_ERR_INVALID_ARG;
+    }
+    out->prob_targets.assign(in->probability_targets, in->probability_targets + in->n_probability_targets);
+    for (uint64_t t : out->prob_targets)
+      if (t >= (1ULL << n)) {
+        *err = "probability target out of range";
+        return QG_ERR_INVALID_ARG;
+      }
+  }
+  if (in->flags & QG_RES_FIDELITY) {
+    if (in->n_references < 0 || (in->n_references > 0 && !in->references)) {
+      *err = "fidelity needs reference states";
+      return QG_ERR_INVALID_ARG;
+    }
+    if (n > 28) {
+      *err = "fidelity references limited to 28 qubits";
+      return QG_ERR_UNSUPPORTED;
+    }
+    out->n_refs = in->n_references;
+    out->references.assign(in->references, in->references + 2 * ((size_t)in->n_references << n));
+  }
+  return QG_OK;
+}
+
+static int submit_one(Ctx* c, const qg_circuit* circ, const qg_options* opt, uint64_t batch, uint64_t* id_out) {
+  if (!circ || !id_out) return QG_ERR_INVALID_ARG;
+  std::string err;
+  // validate now (ideal_simulator.clj relies on :pre checks in backend.clj:228-230)
+  {
+    std::vector<GOp> g;
+    std::vector<std::vector<int>> m;
+    std::vector<int> at;
+    int rc = lower_circuit(circ, &g, &m, &at, &err);
+    if (rc != QG_OK) {
+      set_ctx_error(c, err);
+      return rc;
+    }
+  }
+  auto j = std::make_shared<Job>();
+  j->n = circ->num_qubits;
+  j->ops.assign(circ->ops, circ->ops + circ->num_ops);
+  j->seed = c->cfg.seed;
+  j->precision = c->cfg.precision;
+  j->fusion = c->cfg.fusion;
+  if (opt) {
+    int rc = copy_spec(opt->spec, j->n, &j->spec, &err);
+    if (rc != QG_OK) {
+      set_ctx_error(c, err);
+      return rc;
+    }
+    if (opt->initial_state) j->initial.assign(opt->initial_state, opt->initial_state + 2 * (1ULL << j->n));
+    if (opt->seed) j->seed = opt->seed;
+    if (opt->precision == QG_C128 || opt->precision == QG_C64) j->precision = opt->precision;
+    if (opt->fusion >= QG_FUSE_PLAIN && opt->fusion <= QG_FUSE_DENSE) j->fusion = opt->fusion;
+  }
+  if (c->cfg.max_qubits > 0 && j->n > c->cfg.max_qubits) {
+    set_ctx_error(c, "circuit exceeds max-qubits of this backend");
+    return QG_ERR_OOM;
+  }
+  j->submitted = Clock::now();
+  j->batch = batch;
+  {
+    std::lock_guard<std::mutex> g(c->mu);
+    j->id = c->next_id++;
+    c->jobs[j->id] = j;
+    c->queue.push_back(j->id);
+    if (batch) c->batches[batch].push_back(j->id);
+  }
+  c->cv.notify_all();
+  *id_out = j->id;
+  return QG_OK;
+}
+
+}  // namespace qg
+
+using namespace qg;
+
+// ===========================================================================
+// extern "C" entry points
+// ===========================================================================
+extern "C" {
+
+int qg_abi_version(void) { return QG_ABI_VERSION; }
+
+int qg_device_count(int32_t* count) {
+  if (!count) return QG_ERR_INVALID_ARG;
+  int c = 0;
+  cudaError_t e = cudaGetDeviceCount(&c);
+  *count = e == cudaSuccess ? c : 0;
+  return QG_OK;
+}
+
+int qg_ctx_create(const qg_config* cfg, void** ctx_out) {
+  if (!ctx_out) return QG_ERR_INVALID_ARG;
+  *ctx_out = nullptr;
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return QG_ERR_NO_DEVICE;
+  auto* c = new Ctx();
+  if (cfg) c->cfg = *cfg;
+  if (c->cfg.workers < 1) c->cfg.workers = 2;
+  if (c->cfg.fuse_k < 1 || c->cfg.fuse_k > 5) c->cfg.fuse_k = 4;
+  if (c->cfg.precision != QG_C64) c->cfg.precision = QG_C128;
+  if (c->cfg.fusion < QG_FUSE_PLAIN || c->cfg.fusion > QG_FUSE_DENSE) c->cfg.fusion = QG_FUSE_TILED;
+  if (c->cfg.seed == 0) c->cfg.seed = 0x5eed5eedULL;
+  c->device = c->cfg.device;
+  if (c->device < 0 || c->device >= ndev) {
+    delete c;
+    return QG_ERR_INVALID_ARG;
+  }
+  cudaSetDevice(c->device);
+  size_t fr = 0, tot = 0;
+  if (cudaMemGetInfo(&fr, &tot) != cudaSuccess) {
+    delete c;
+    return QG_ERR_DEVICE;
+  }
+  c->hbm_total = tot;
+  const size_t reserve = 4ULL << 30;
+  c->hbm_budget = c->cfg.hbm_budget_bytes ? c->cfg.hbm_budget_bytes : (fr > reserve ? fr - reserve : fr / 2);
+  cudaDeviceGetAttribute(&c->sm_count, cudaDevAttrMultiProcessorCount, c->device);
+  // keep freed blocks in the stream-ordered pool for reuse
+  cudaMemPool_t pool;
+  if (cudaDeviceGetDefaultMemPool(&pool, c->device) == cudaSuccess) {
+    uint64_t thr = UINT64_MAX;
+    cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &thr);
+  }
+  for (int w = 0; w < c->cfg.workers; ++w) c->workers.emplace_back(worker_loop, c);
+  *ctx_out = c;
+  return QG_OK;
+}
+
+int qg_ctx_destroy(void* ctx) {
+  if (!ctx) return QG_ERR_INVALID_ARG;
+  Ctx* c = (Ctx*)ctx;
+  {
+    std::lock_guard<std::mutex> g(c->mu);
+    c->stop = true;
+    for (auto& kv : c->jobs) kv.second->cancel.store(true);
+  }
+  c->cv.notify_all();
+  for (auto& t : c->workers) t.join();
+  cudaSetDevice(c->device);
+  for (auto& kv : c->jobs)
+    if (kv.second->state) {
+      State* s = kv.second->state.get();
+      state_release(s);
+      cudaStreamSynchronize(s->stream);
+      if (s->own_stream) cudaStreamDestroy(s->stream);
+    }
+  cudaDeviceSynchronize();
+  delete c;
+  return QG_OK;
+}
+
+int qg_ctx_capabilities(void* ctx, int32_t* mq128, int32_t* mq64, uint64_t* hbm_total, int32_t* sms) {
+  if (!ctx) return QG_ERR_INVALID_ARG;
+  Ctx* c = (Ctx*)ctx;
+  auto maxq = [&](int prec) {
+    int q = 1;
+    while (q < QG_MAX_QUBITS && job_bytes(q + 1, prec) <= c->hbm_budget) ++q;
+    return q;
+  };
+  if (mq128) *mq128 = maxq(QG_C128);
+  if (mq64) *mq64 = maxq(QG_C64);
+  if (hbm_total) *hbm_total = c->hbm_total;
+  if (sms) *sms = c->sm_count;
+  return QG_OK;
+}
+
+int qg_submit(void* ctx, const qg_circuit* circuit, const qg_options* options, uint64_t* job_out) {
+  if (!ctx) return QG_ERR_INVALID_ARG;
+  return submit_one((Ctx*)ctx, circuit, options, 0, job_out);
+}
+
+int qg_job_status(void* ctx, uint64_t job, int32_t* status_out) {
+  if (!ctx || !status_out) return QG_ERR_INVALID_ARG;
+  auto j = find_job((Ctx*)ctx, job);
+  *status_out = j ? j->status.load() : QG_JOB_NOT_FOUND;
+  return QG_OK;
+}
+
+int qg_wait(void* ctx, uint64_t job, int64_t timeout_ms, int32_t* status_out) {
+  if (!ctx) return QG_ERR_INVALID_ARG;
+  Ctx* c = (Ctx*)ctx;
+  auto j = find_job(c, job);
+  if (!j) {
+    if (status_out) *status_out = QG_JOB_NOT_FOUND;
+    return QG_ERR_NOT_FOUND;
+  }
+  std::unique_lock<std::mutex> lk(c->mu);
+  auto pred = [&] {
+    int s = j->status.load();
+    return s == QG_JOB_COMPLETED || s == QG_JOB_FAILED || s == QG_JOB_CANCELLED;
+  };
+  bool ok = true;
+  if (timeout_ms < 0) c->done_cv.wait(lk, pred);
+  else ok = c->done_cv.wait_for(lk, std::chrono::milliseconds(timeout_ms), pred);
+  if (status_out) *status_out = j->status.load();
+  return ok ? QG_OK : QG_ERR_TIMEOUT;
+}
+
+int qg_cancel(void* ctx, uint64_t job, int32_t* outcome) {
+  if (!ctx || !outcome) return QG_ERR_INVALID_ARG;
+  Ctx* c = (Ctx*)ctx;
+  std::lock_guard<std::mutex> g(c->mu);
+  auto it = c->jobs.find(job);
+  if (it == c->jobs.end()) {
+    *outcome = QG_CANCEL_NOT_FOUND;
+    return QG_OK;
+  }
+  Job* j = it->second.get();
+  int s = j->status.load();
+  if (s == QG_JOB_QUEUED) {
+    j->cancel.store(true);
+    j->status.store(QG_JOB_CANCELLED);
+    j->finished = Clock::now();
+    *outcome = QG_CANCEL_CANCELLED;
+    c->done_cv.notify_all();
+  } else if (s == QG_JOB_RUNNING) {
+    j->cancel.store(true);  // the worker stops between passes
+    *outcome = QG_CANCEL_CANCELLED;
+  } else {
+    *outcome = QG_CANCEL_CANNOT;
+  }
+  return QG_OK;
+}
+
+int qg_queue_status(void* ctx, qg_queue_info* out) {
+  if (!ctx || !out) return QG_ERR_INVALID_ARG;
+  Ctx* c = (Ctx*)ctx;
+  std::memset(out, 0, sizeof(*out));
+  std::lock_guard<std::mutex> g(c->mu);
+  for (auto& kv : c->jobs) {
+    ++out->total_jobs;
+    switch (kv.second->status.load()) {
+      case QG_JOB_QUEUED: ++out->queued; break;
+      case QG_JOB_RUNNING: ++out->running; break;
+      case QG_JOB_COMPLETED: ++out->completed; break;
+      case QG_JOB_FAILED: ++out->failed; break;
+      default: ++out->cancelled; break;
+    }
+  }
+  size_t fr = 0, tot = 0;
+  cudaSetDevice(c->device);
+  cudaMemGetInfo(&fr, &tot);
+  out->hbm_free_bytes = fr;
+  out->hbm_budget_bytes = c->hbm_budget;
+  out->hbm_in_use_bytes = c->hbm_in_use;
+  out->workers = (int32_t)c->workers.size();
+  return QG_OK;
+}
+
+int qg_job_details(void* ctx, uint64_t job, qg_job_info* out) {
+  if (!ctx || !out) return QG_ERR_INVALID_ARG;
+  auto j = find_job((Ctx*)ctx, job);
+  if (!j) return QG_ERR_NOT_FOUND;
+  std::memset(out, 0, sizeof(*out));
+  out->status = j->status.load();
+  out->num_qubits = j->n;
+  out->precision = j->precision;
+  out->num_passes = j->passes;
+  out->execution_time_ms = j->exec_ms;
+  out->device_time_ms = j->device_ms;
+  out->queue_time_ms = j->queue_ms;
+  out->shots = j->shots.size();
+  out->num_distinct_outcomes = (int64_t)j->counts.size();
+  out->has_results = j->has & (j->state ? ~0 : ~QG_RES_STATE_VECTOR);
+  out->error_code = j->error_code;
+  return QG_OK;
+}
+
+// common guard for result getters
+static int completed_job(void* ctx, uint64_t job, std::shared_ptr<Job>* out) {
+  if (!ctx) return QG_ERR_INVALID_ARG;
+  auto j = find_job((Ctx*)ctx, job);
+  if (!j) return QG_ERR_NOT_FOUND;
+  int s = j->status.load();
+  if (s == QG_JOB_CANCELLED) return QG_ERR_CANCELLED;
+  if (s != QG_JOB_COMPLETED) return QG_ERR_NOT_COMPLETED;
+  *out = j;
+  return QG_OK;
+}
+
+int qg_result_counts(void* ctx, uint64_t job, uint64_t* outcomes, uint64_t* counts, int64_t cap, int64_t* n_out) {
+  std::shared_ptr<Job> j;
+  int rc = completed_job(ctx, job, &j);
+  if (rc != QG_OK) return rc;
+  if (!(j->has & QG_RES_MEASUREMENTS)) return QG_ERR_NO_RESULT;
+  if (n_out) *n_out = (int64_t)j->counts.size();
+  if (cap < (int64_t)j->counts.size()) return QG_ERR_BUFFER_TOO_SMALL;
+  for (size_t i = 0; i < j->counts.size(); ++i) {
+    if (outcomes) outcomes[i] = j->counts[i].first;
+    if (counts) counts[i] = j->counts[i].second;
+  }
+  return QG_OK;
+}
+
+int qg_result_shots(void* ctx, uint64_t job, uint64_t* outcomes, int64_t cap) {
+  std::shared_ptr<Job> j;
+  int rc = completed_job(ctx, job, &j);
+  if (rc != QG_OK) return rc;
+  if (!(j->has & QG_RES_MEASUREMENTS)) return QG_ERR_NO_RESULT;
+  if (cap < (int64_t)j->shots.size()) return QG_ERR_BUFFER_TOO_SMALL;
+  if (!outcomes) return QG_ERR_INVALID_ARG;
+  std::memcpy(outcomes, j->shots.data(), sizeof(uint64_t) * j->shots.size());
+  return QG_OK;
+}
+
+int qg_result_probabilities(void* ctx, uint64_t job, double* out, int64_t cap) {
+  std::shared_ptr<Job> j;
+  int rc = completed_job(ctx, job, &j);
+  if (rc != QG_OK) return rc;
+  const uint64_t N = 1ULL << j->n;
+  if (!out) return QG_ERR_INVALID_ARG;
+  if (cap < (int64_t)N) return QG_ERR_BUFFER_TOO_SMALL;
+  if (!j->probs.empty()) {
+    std::memcpy(out, j->probs.data(), sizeof(double) * N);
+    return QG_OK;
+  }
+  if (!j->state) return QG_ERR_NO_RESULT;
+  std::string err;
+  cudaSetDevice(((Ctx*)ctx)->device);
+  rc = st_probs(j->state.get(), out, &err);
+  if (rc != QG_OK) set_ctx_error((Ctx*)ctx, err);
+  return rc;
+}
+
+int qg_result_target_probabilities(void* ctx, uint64_t job, double* out, int64_t cap) {
+  std::shared_ptr<Job> j;
+  int rc = completed_job(ctx, job, &j);
+  if (rc != QG_OK) return rc;
+  if (j->target_probs.empty() && !(j->has & QG_RES_PROBABILITIES)) return QG_ERR_NO_RESULT;
+  if (cap < (int64_t)j->target_probs.size()) return QG_ERR_BUFFER_TOO_SMALL;
+  if (!j->target_probs.empty()) std::memcpy(out, j->target_probs.data(), sizeof(double) * j->target_probs.size());
+  return QG_OK;
+}
+
+int qg_result_state(void* ctx, uint64_t job, double* out, int64_t cap) {
+  std::shared_ptr<Job> j;
+  int rc = completed_job(ctx, job, &j);
+  if (rc != QG_OK) return rc;
+  if (!out) return QG_ERR_INVALID_ARG;
+  if (!j->state) {
+    set_ctx_error((Ctx*)ctx, "final state evicted; request :state-vector in the result spec to retain it");
+    return QG_ERR_NO_RESULT;
+  }
+  if (cap < (int64_t)(1ULL << j->n)) return QG_ERR_BUFFER_TOO_SMALL;
+  std::string err;
+  cudaSetDevice(((Ctx*)ctx)->device);
+  rc = download_c128(j->state.get(), out, &err);
+  if (rc != QG_OK) set_ctx_error((Ctx*)ctx, err);
+  return rc;
+}
+
+int qg_result_amplitudes(void* ctx, uint64_t job, double* out, int64_t cap) {
+  std::shared_ptr<Job> j;
+  int rc = completed_job(ctx, job, &j);
+  if (rc != QG_OK) return rc;
+  if (!(j->has & QG_RES_AMPLITUDES)) return QG_ERR_NO_RESULT;
+  if (cap < (int64_t)(j->amplitudes.size() / 2)) return QG_ERR_BUFFER_TOO_SMALL;
+  if (!j->amplitudes.empty()) std::memcpy(out, j->amplitudes.data(), sizeof(double) * j->amplitudes.size());
+  return QG_OK;
+}
+
+int qg_result_expectations(void* ctx, uint64_t job, double* expectation, double* variance, int64_t cap) {
+  std::shared_ptr<Job> j;
+  int rc = completed_job(ctx, job, &j);
+  if (rc != QG_OK) return rc;
+  if (!(j->has & (QG_RES_EXPECTATION | QG_RES_VARIANCE))) return QG_ERR_NO_RESULT;
+  if (cap < (int64_t)j->expectations.size()) return QG_ERR_BUFFER_TOO_SMALL;
+  for (size_t i = 0; i < j->expectations.size(); ++i) {
+    if (expectation) expectation[i] = j->expectations[i];
+    if (variance) variance[i] = j->variances[i];
+  }
+  return QG_OK;
+}
+
+int qg_result_hamiltonian(void* ctx, uint64_t job, double* energy, double* term_values, int64_t cap) {
+  std::shared_ptr<Job> j;
+  int rc = completed_job(ctx, job, &j);
+  if (rc != QG_OK) return rc;
+  if (!(j->has & QG_RES_HAMILTONIAN)) return QG_ERR_NO_RESULT;
+  if (energy) *energy = j->energy;
+  if (term_values) {
+    if (cap < (int64_t)j->term_values.size()) return QG_ERR_BUFFER_TOO_SMALL;
+    std::memcpy(term_values, j->term_values.data(), sizeof(double) * j->term_values.size());
+  }
+  return QG_OK;
+}
+
+int qg_result_fidelities(void* ctx, uint64_t job, double* out, int64_t cap) {
+  std::shared_ptr<Job> j;
+  int rc = completed_job(ctx, job, &j);
+  if (rc != QG_OK) return rc;
+  if (!(j->has & QG_RES_FIDELITY)) return QG_ERR_NO_RESULT;
+  if (cap < (int64_t)j->fidelities.size()) return QG_ERR_BUFFER_TOO_SMALL;
+  if (!j->fidelities.empty()) std::memcpy(out, j->fidelities.data(), sizeof(double) * j->fidelities.size());
+  return QG_OK;
+}
+
+int qg_result_density_matrix(void* ctx, uint64_t job, double* out, int64_t cap) {
+  std::shared_ptr<Job> j;
+  int rc = completed_job(ctx, job, &j);
+  if (rc != QG_OK) return rc;
+  if (!(j->has & QG_RES_DENSITY_MATRIX)) return QG_ERR_NO_RESULT;
+  if (cap < (int64_t)(j->density.size() / 2)) return QG_ERR_BUFFER_TOO_SMALL;
+  std::memcpy(out, j->density.data(), sizeof(double) * j->density.size());
+  return QG_OK;
+}
+
+int qg_last_error(void* ctx, uint64_t job, char* buf, int64_t len) {
+  if (!ctx || !buf || len <= 0) return QG_ERR_INVALID_ARG;
+  Ctx* c = (Ctx*)ctx;
+  std::string msg;
+  if (job) {
+    auto j = find_job(c, job);
+    if (!j) return QG_ERR_NOT_FOUND;
+    msg = j->error;
+  } else {
+    std::lock_guard<std::mutex> g(c->err_mu);
+    msg = c->last_error;
+  }
+  std::snprintf(buf, (size_t)len, "%s", msg.c_str());
+  return QG_OK;
+}
+
+int qg_job_free(void* ctx, uint64_t job) {
+  if (!ctx) return QG_ERR_INVALID_ARG;
+  Ctx* c = (Ctx*)ctx;
+  std::shared_ptr<Job> j;
+  {
+    std::lock_guard<std::mutex> g(c->mu);
+    auto it = c->jobs.find(job);
+    if (it == c->jobs.end()) return QG_ERR_NOT_FOUND;
+    int s = it->second->status.load();
+    if (s == QG_JOB_RUNNING || s == QG_JOB_QUEUED) return QG_ERR_NOT_COMPLETED;
+    j = it->second;
+    c->jobs.erase(it);
+    if (j->state) {
+      c->hbm_in_use -= std::min(c->hbm_in_use, job_bytes(j->n, j->state->prec));
+    }
+  }
+  if (j->state) {
+    cudaSetDevice(c->device);
+    cudaStream_t st = j->state->stream;
+    state_release(j->state.get());
+    cudaStreamSynchronize(st);
+    if (j->state->own_stream) cudaStreamDestroy(st);
+    j->state.reset();
+  }
+  c->cv.notify_all();
+  return QG_OK;
+}
+
+int qg_cleanup_completed(void* ctx, int64_t max_age_ms, int64_t* removed) {
+  if (!ctx) return QG_ERR_INVALID_ARG;
+  Ctx* c = (Ctx*)ctx;
+  std::vector<uint64_t> old;
+  {
+    std::lock_guard<std::mutex> g(c->mu);
+    auto now = Clock::now();
+    for (auto& kv : c->jobs) {
+      Job* j = kv.second.get();
+      if (j->status.load() != QG_JOB_COMPLETED) continue;
+      double age = std::chrono::duration<double, std::milli>(now - j->finished).count();
+      if (age > (double)max_age_ms) old.push_back(kv.first);
+    }
+  }
+  for (uint64_t id : old) qg_job_free(ctx, id);
+  if (removed) *removed = (int64_t)old.size();
+  return QG_OK;
+}
+
+int qg_batch_submit(void* ctx, const qg_circuit* circuits, int32_t count, const qg_options* options,
+                    uint64_t* batch_out, uint64_t* jobs_out) {
+  if (!ctx || !circuits || count < 0 || !batch_out) return QG_ERR_INVALID_ARG;
+  Ctx* c = (Ctx*)ctx;
+  uint64_t bid;
+  {
+    std::lock_guard<std::mutex> g(c->mu);
+    bid = c->next_id++;
+    c->batches[bid];
+  }
+  for (int i = 0; i < count; ++i) {
+    uint64_t id = 0;
+    int rc = submit_one(c, &circuits[i], options, bid, &id);
+    if (rc != QG_OK) return rc;
+    if (jobs_out) jobs_out[i] = id;
+  }
+  *batch_out = bid;
+  return QG_OK;
+}
+
+int qg_batch_status(void* ctx, uint64_t batch, int32_t* statuses, int32_t cap, int32_t* n_out) {
+  if (!ctx) return QG_ERR_INVALID_ARG;
+  Ctx* c = (Ctx*)ctx;
+  std::lock_guard<std::mutex> g(c->mu);
+  auto it = c->batches.find(batch);
+  if (it == c->batches.end()) return QG_ERR_NOT_FOUND;
+  if (n_out) *n_out = (int32_t)it->second.size();
+  if (cap < (int32_t)it->second.size()) return QG_ERR_BUFFER_TOO_SMALL;
+  for (size_t i = 0; i < it->second.size(); ++i) {
+    auto jt = c->jobs.find(it->second[i]);
+    statuses[i] = jt == c->jobs.end() ? QG_JOB_NOT_FOUND : jt->second->status.load();
+  }
+  return QG_OK;
+}
+
+int qg_batch_jobs(void* ctx, uint64_t batch, uint64_t* jobs, int32_t cap, int32_t* n_out) {
+  if (!ctx) return QG_ERR_INVALID_ARG;
+  Ctx* c = (Ctx*)ctx;
+  std::lock_guard<std::mutex> g(c->mu);
+  auto it = c->batches.find(batch);
+  if (it == c->batches.end()) return QG_ERR_NOT_FOUND;
+  if (n_out) *n_out = (int32_t)it->second.size();
+  if (cap < (int32_t)it->second.size()) return QG_ERR_BUFFER_TOO_SMALL;
+  for (size_t i = 0; i < it->second.size(); ++i) jobs[i] = it->second[i];
+  return QG_OK;
+}
+
+// ---- device-resident state ---------------------------------------------------
+int qg_state_create(void* ctx, int32_t n, int32_t precision, void** state_out) {
+  if (!ctx || !state_out || n < 1 || n > QG_MAX_QUBITS) return QG_ERR_INVALID_ARG;
+  if (precision != QG_C128 && precision != QG_C64) return QG_ERR_INVALID_ARG;
+  Ctx* c = (Ctx*)ctx;
+  cudaSetDevice(c->device);
+  auto* s = new State();
+  s->ctx = c;
+  s->own_stream = true;
+  if (cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking) != cudaSuccess) {
+    delete s;
+    return QG_ERR_DEVICE;
+  }
+  std::string err;
+  int rc = state_alloc(s, n, precision, s->stream, &err);
+  if (rc == QG_OK) {
+    cudaError_t e = launch_set_basis(s->d, precision, n, 0, s->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s->stream);
+    if (e != cudaSuccess) rc = cuda_fail(&err, e, "zero-state");
+  }
+  if (rc != QG_OK) {
+    set_ctx_error(c, err);
+    state_release(s);
+    cudaStreamSynchronize(s->stream);
+    cudaStreamDestroy(s->stream);
+    delete s;
+    return rc == QG_ERR_DEVICE ? QG_ERR_OOM : rc;
+  }
+  *state_out = s;
+  return QG_OK;
+}
+
+int qg_state_destroy(void* state) {
+  if (!state) return QG_ERR_INVALID_ARG;
+  State* s = (State*)state;
+  cudaSetDevice(s->ctx->device);
+  state_release(s);
+  cudaStreamSynchronize(s->stream);
+  if (s->own_stream) cudaStreamDestroy(s->stream);
+  delete s;
+  return QG_OK;
+}
+
+int qg_state_num_qubits(void* state, int32_t* n, int32_t* precision) {
+  if (!state) return QG_ERR_INVALID_ARG;
+  State* s = (State*)state;
+  if (n) *n = s->n;
+  if (precision) *precision = s->prec;
+  return QG_OK;
+}
+
+static int state_err(State* s, int rc, const std::string& err) {
+  if (rc != QG_OK) set_ctx_error(s->ctx, err);
+  return rc;
+}
+
+int qg_state_set_basis(void* state, uint64_t index) {
+  if (!state) return QG_ERR_INVALID_ARG;
+  State* s = (State*)state;
+  if (index >= (1ULL << s->n)) return QG_ERR_INVALID_ARG;
+  cudaSetDevice(s->ctx->device);
+  cudaError_t e = launch_set_basis(s->d, s->prec, s->n, index, s->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s->stream);
+  std::string err;
+  return state_err(s, e == cudaSuccess ? QG_OK : cuda_fail(&err, e, "set_basis"), err);
+}
+
+int qg_state_upload(void* state, const double* host) {
+  if (!state || !host) return QG_ERR_INVALID_ARG;
+  State* s = (State*)state;
+  cudaSetDevice(s->ctx->device);
+  std::string err;
+  int rc = upload_c128(s, host, &err);
+  if (rc == QG_OK && cudaStreamSynchronize(s->stream) != cudaSuccess) rc = QG_ERR_DEVICE;
+  return state_err(s, rc, err);
+}
+
+int qg_state_download(void* state, double* host) {
+  if (!state || !host) return QG_ERR_INVALID_ARG;
+  State* s = (State*)state;
+  cudaSetDevice(s->ctx->device);
+  std::string err;
+  return state_err(s, download_c128(s, host, &err), err);
+}
+
+int qg_state_apply(void* state, const qg_circuit* circuit, int32_t fusion, uint64_t seed, int32_t* passes_out) {
+  if (!state || !circuit) return QG_ERR_INVALID_ARG;
+  State* s = (State*)state;
+  if (circuit->num_qubits != s->n) {
+    set_ctx_error(s->ctx, "circuit and state have mismatched number of qubits");
+    return QG_ERR_INVALID_ARG;
+  }
+  cudaSetDevice(s->ctx->device);
+  std::string err;
+  Program prog;
+  int rc = compile_program(circuit, s->prec, fusion, s->ctx->cfg.fuse_k, &prog, &err);
+  if (rc != QG_OK) return state_err(s, rc, err);
+  ExecStats st;
+  rc = exec_program(s, prog, seed, nullptr, &st, &err);
+  if (passes_out) *passes_out = st.passes;
+  return state_err(s, rc, err);
+}
+
+int qg_state_probabilities(void* state, double* host_out) {
+  if (!state || !host_out) return QG_ERR_INVALID_ARG;
+  State* s = (State*)state;
+  cudaSetDevice(s->ctx->device);
+  std::string err;
+  return state_err(s, st_probs(s, host_out, &err), err);
+}
+
+int qg_state_sample(void* state, uint64_t shots, uint64_t seed, uint64_t* host_outcomes) {
+  if (!state || (shots && !host_outcomes)) return QG_ERR_INVALID_ARG;
+  State* s = (State*)state;
+  cudaSetDevice(s->ctx->device);
+  std::string err;
+  std::vector<uint64_t> out;
+  int rc = st_sample(s, shots, seed, &out, &err);
+  if (rc == QG_OK && shots) std::memcpy(host_outcomes, out.data(), sizeof(uint64_t) * shots);
+  return state_err(s, rc, err);
+}
+
+int qg_state_pauli_expectation(void* state, const char* pauli, double* out) {
+  if (!state || !pauli || !out) return QG_ERR_INVALID_ARG;
+  State* s = (State*)state;
+  cudaSetDevice(s->ctx->device);
+  std::string err;
+  return state_err(s, st_pauli(s, pauli, out, &err), err);
+}
+
+int qg_state_hamiltonian(void* state, int32_t n_terms, const double* coeffs, const char* paulis, double* out) {
+  if (!state || !out || n_terms < 0 || (n_terms && (!coeffs || !paulis))) return QG_ERR_INVALID_ARG;
+  State* s = (State*)state;
+  cudaSetDevice(s->ctx->device);
+  std::string err;
+  double energy = 0;
+  for (int k = 0; k < n_terms; ++k) {
+    double v;
+    int rc = st_pauli(s, paulis + (size_t)k * s->n, &v, &err);
+    if (rc != QG_OK) return state_err(s, rc, err);
+    double term = coeffs[k] * v;
+    energy = k == 0 ? term : energy + term;
+  }
+  *out = energy;
+  return QG_OK;
+}
+
+int qg_state_expectation_1q(void* state, const double* obs8, int32_t target, double* out) {
+  if (!state || !obs8 || !out) return QG_ERR_INVALID_ARG;
+  State* s = (State*)state;
+  cudaSetDevice(s->ctx->device);
+  std::string err;
+  return state_err(s, st_expect1q(s, obs8, target, out, &err), err);
+}
+
+int qg_state_norm2(void* state, double* out) {
+  if (!state || !out) return QG_ERR_INVALID_ARG;
+  State* s = (State*)state;
+  cudaSetDevice(s->ctx->device);
+  std::string err;
+  return state_err(s, st_norm2(s, out, &err), err);
+}
+
+int qg_state_inner(void* a, void* b, double* re, double* im) {
+  if (!a || !b || !re || !im) return QG_ERR_INVALID_ARG;
+  State* s = (State*)a;
+  cudaSetDevice(s->ctx->device);
+  std::string err;
+  return state_err(s, st_inner(s, (State*)b, re, im, &err), err);
+}
+
+int qg_state_measure(void* state, const int32_t* qubits, int32_t count, uint64_t seed, uint64_t* outcome_out,
+                     double* probability_out) {
+  if (!state || !qubits || count < 1 || count > 20) return QG_ERR_INVALID_ARG;
+  State* s = (State*)state;
+  std::vector<int> qs(qubits, qubits + count);
+  for (int q : qs)
+    if (q < 0 || q >= s->n) return QG_ERR_QUBIT_RANGE;
+  cudaSetDevice(s->ctx->device);
+  std::string err;
+  int rc = do_measure(s, qs, seed, 0, outcome_out, probability_out, &err);
+  if (rc == QG_OK && cudaStreamSynchronize(s->stream) != cudaSuccess) rc = QG_ERR_DEVICE;
+  return state_err(s, rc, err);
+}
+
+int qg_state_device_ptr(void* state, void** dptr, void** stream) {
+  if (!state) return QG_ERR_INVALID_ARG;
+  State* s = (State*)state;
+  if (dptr) *dptr = s->d;
+  if (stream) *stream = (void*)s->stream;
+  return QG_OK;
+}
+
+int qg_state_synchronize(void* state) {
+  if (!state) return QG_ERR_INVALID_ARG;
+  State* s = (State*)state;
+  return cudaStreamSynchronize(s->stream) == cudaSuccess ? QG_OK : QG_ERR_DEVICE;
+}
+
+int qg_state_profile(void* state, const qg_circuit* circuit, int32_t fusion, uint64_t seed, float* pass_ms,
+                     int32_t* pass_kind, int32_t cap, int32_t* n_passes) {
+  if (!state || !circuit || cap < 0) return QG_ERR_INVALID_ARG;
+  State* s = (State*)state;
+  if (circuit->num_qubits != s->n) return QG_ERR_INVALID_ARG;
+  cudaSetDevice(s->ctx->device);
+  std::string err;
+  Program prog;
+  int rc = compile_program(circuit, s->prec, fusion, s->ctx->cfg.fuse_k, &prog, &err);
+  if (rc != QG_OK) return state_err(s, rc, err);
+  std::vector<float> ms;
+  std::vector<int> kinds;
+  ExecStats st;
+  st.pass_ms = &ms;
+  st.pass_kind = &kinds;
+  rc = exec_program(s, prog, seed, nullptr, &st, &err);
+  if (n_passes) *n_passes = (int32_t)ms.size();
+  if (rc != QG_OK) return state_err(s, rc, err);
+  if ((int32_t)ms.size() > cap) return QG_ERR_BUFFER_TOO_SMALL;
+  for (size_t i = 0; i < ms.size(); ++i) {
+    if (pass_ms) pass_ms[i] = ms[i];
+    if (pass_kind) pass_kind[i] = kinds[i];
+  }
+  return QG_OK;
+}
+
+int qg_kernel_launches(uint64_t* count) {
+  if (!count) return QG_ERR_INVALID_ARG;
+  *count = kernel_launch_count();
+  return QG_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,147 @@
+"""DeviceState: an amplitude array resident in HBM, driven through the C ABI.
+
+This is the state-level surface of the backend (state.clj, gate.clj and the
+result extractors on one state) for callers that keep a state on the GPU
+across many circuits, such as variational loops and the benchmarks.
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from . import _abi as A
+from .backend import PRECISIONS, FUSIONS, _check
+from .circuit import encode
+
+
+class Context:
+    """A library context on one GPU (no job workers are needed for direct state use)."""
+
+    def __init__(self, device: int = 0, precision: str = "c128", fusion: str = "tiled", fusion_width: int = 4,
+                 workers: int = 1, seed: int = 0):
+        self.lib = A.load_library()
+        cfg = A.QgConfig()
+        cfg.device = device
+        cfg.precision = PRECISIONS[precision]
+        cfg.fusion = FUSIONS[fusion]
+        cfg.fuse_k = fusion_width
+        cfg.workers = workers
+        cfg.seed = seed
+        ctx = C.c_void_p()
+        _check(self.lib.qg_ctx_create(C.byref(cfg), C.byref(ctx)))
+        self.ctx = ctx
+
+    def close(self):
+        if self.ctx:
+            self.lib.qg_ctx_destroy(self.ctx)
+            self.ctx = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def state(self, num_qubits: int, precision: str = "c128") -> "DeviceState":
+        return DeviceState(self, num_qubits, precision)
+
+
+class DeviceState:
+    def __init__(self, ctx: Context, num_qubits: int, precision: str = "c128"):
+        self.ctx, self.lib = ctx, ctx.lib
+        self.n = num_qubits
+        self.precision = precision
+        h = C.c_void_p()
+        _check(self.lib.qg_state_create(ctx.ctx, num_qubits, PRECISIONS[precision], C.byref(h)), self.lib, ctx.ctx)
+        self.h = h
+
+    def close(self):
+        if self.h:
+            self.lib.qg_state_destroy(self.h)
+            self.h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def _ck(self, rc):
+        _check(rc, self.lib, self.ctx.ctx)
+
+    def set_basis(self, index: int = 0):
+        self._ck(self.lib.qg_state_set_basis(self.h, C.c_uint64(index)))
+
+    def upload(self, sv: np.ndarray):
+        sv = np.ascontiguousarray(sv, dtype=np.complex128)
+        assert sv.size == 1 << self.n
+        self._ck(self.lib.qg_state_upload(self.h, sv.ctypes.data_as(A.DP)))
+
+    def download(self) -> np.ndarray:
+        out = np.empty(1 << self.n, np.complex128)
+        self._ck(self.lib.qg_state_download(self.h, out.ctypes.data_as(A.DP)))
+        return out
+
+    def apply(self, circuit: dict, fusion: str = "tiled", seed: int = 0) -> int:
+        enc = encode(circuit)
+        passes = C.c_int32()
+        self._ck(self.lib.qg_state_apply(self.h, enc.ref(), FUSIONS[fusion], C.c_uint64(seed), C.byref(passes)))
+        return passes.value
+
+    def probabilities(self) -> np.ndarray:
+        out = np.empty(1 << self.n, np.float64)
+        self._ck(self.lib.qg_state_probabilities(self.h, out.ctypes.data_as(A.DP)))
+        return out
+
+    def sample(self, shots: int, seed: int) -> np.ndarray:
+        out = np.empty(max(1, shots), np.uint64)
+        self._ck(self.lib.qg_state_sample(self.h, C.c_uint64(shots), C.c_uint64(seed), out.ctypes.data_as(A.U64P)))
+        return out[:shots]
+
+    def pauli_expectation(self, pauli: str) -> float:
+        out = C.c_double()
+        self._ck(self.lib.qg_state_pauli_expectation(self.h, pauli.encode(), C.byref(out)))
+        return out.value
+
+    def hamiltonian(self, terms: list[tuple[float, str]]) -> float:
+        coeffs = (C.c_double * max(1, len(terms)))(*[c for c, _ in terms])
+        strs = "".join(s for _, s in terms).encode()
+        out = C.c_double()
+        self._ck(self.lib.qg_state_hamiltonian(self.h, len(terms), coeffs, strs, C.byref(out)))
+        return out.value
+
+    def expectation_1q(self, obs, target: int) -> float:
+        flat = []
+        for row in obs:
+            for z in row:
+                z = complex(z)
+                flat += [z.real, z.imag]
+        arr = (C.c_double * 8)(*flat)
+        out = C.c_double()
+        self._ck(self.lib.qg_state_expectation_1q(self.h, arr, target, C.byref(out)))
+        return out.value
+
+    def norm2(self) -> float:
+        out = C.c_double()
+        self._ck(self.lib.qg_state_norm2(self.h, C.byref(out)))
+        return out.value
+
+    def inner(self, other: "DeviceState") -> complex:
+        re, im = C.c_double(), C.c_double()
+        self._ck(self.lib.qg_state_inner(self.h, other.h, C.byref(re), C.byref(im)))
+        return complex(re.value, im.value)
+
+    def measure(self, qubits: list[int], seed: int) -> tuple[int, float]:
+        arr = (C.c_int32 * len(qubits))(*qubits)
+        o, p = C.c_uint64(), C.c_double()
+        self._ck(self.lib.qg_state_measure(self.h, arr, len(qubits), C.c_uint64(seed), C.byref(o), C.byref(p)))
+        return o.value, p.value
+
+    def device_ptr(self):
+        d, s = C.c_void_p(), C.c_void_p()
+        self._ck(self.lib.qg_state_device_ptr(self.h, C.byref(d), C.byref(s)))
+        return d.value, s.value
+
+    def synchronize(self):
+        self._ck(self.lib.qg_state_synchronize(self.h))
