@@ -71,6 +71,12 @@ enum { QG_CANCEL_CANCELLED = 0, QG_CANCEL_CANNOT = 1, QG_CANCEL_NOT_FOUND = 2 };
 /* ---- precision --------------------------------------------------------- */
 enum { QG_C128 = 0, QG_C64 = 1 };
 
+/* ---- complex128 arithmetic in tiled passes ---------------------------- */
+enum {
+  QG_ARITH_EXACT = 0,        /* FP64, same rounded products and sums as the reference (bit-identical) */
+  QG_ARITH_DOUBLE_FLOAT = 1  /* float pairs on the FP32 pipes (about 48 bits), doubles in HBM          */
+};
+
 /* ---- fusion modes ------------------------------------------------------ */
 enum {
   QG_FUSE_PLAIN = 0,   /* one HBM pass per gate (the plain method)                    */
@@ -166,6 +172,8 @@ typedef struct qg_options {
   uint64_t seed;                  /* drives shot sampling and mid-circuit collapse       */
   int32_t precision;              /* QG_C128 / QG_C64, -1 = context default              */
   int32_t fusion;                 /* QG_FUSE_*, -1 = context default                     */
+  int32_t arithmetic;             /* QG_ARITH_*, -1 = context default                    */
+  int32_t reserved;
 } qg_options;
 
 typedef struct qg_config {
@@ -177,6 +185,8 @@ typedef struct qg_config {
   int32_t workers;                /* device streams serving jobs concurrently (>=1)      */
   uint64_t hbm_budget_bytes;      /* 0 = free HBM minus a reserve                        */
   uint64_t seed;                  /* default seed                                        */
+  int32_t arithmetic;             /* QG_ARITH_* for complex128 tiled passes              */
+  int32_t reserved;
 } qg_config;
 
 typedef struct qg_queue_info {    /* queue-status (ideal_simulator.clj:165-176) + device fields */

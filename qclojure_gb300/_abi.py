@@ -49,6 +49,7 @@ CANCEL_OUTCOME = {0: "cancelled", 1: "cannot-cancel", 2: "not-found"}
 
 QG_C128, QG_C64 = 0, 1
 QG_FUSE_PLAIN, QG_FUSE_TILED, QG_FUSE_DENSE = 0, 1, 2
+QG_ARITH_EXACT, QG_ARITH_DOUBLE_FLOAT = 0, 1
 
 # opcodes
 OP = dict(
@@ -94,13 +95,14 @@ class QgResultSpec(C.Structure):
 
 class QgOptions(C.Structure):
     _fields_ = [("spec", C.POINTER(QgResultSpec)), ("initial_state", C.POINTER(C.c_double)),
-                ("seed", C.c_uint64), ("precision", C.c_int32), ("fusion", C.c_int32)]
+                ("seed", C.c_uint64), ("precision", C.c_int32), ("fusion", C.c_int32),
+                ("arithmetic", C.c_int32), ("reserved", C.c_int32)]
 
 
 class QgConfig(C.Structure):
     _fields_ = [("device", C.c_int32), ("precision", C.c_int32), ("fusion", C.c_int32), ("fuse_k", C.c_int32),
                 ("max_qubits", C.c_int32), ("workers", C.c_int32), ("hbm_budget_bytes", C.c_uint64),
-                ("seed", C.c_uint64)]
+                ("seed", C.c_uint64), ("arithmetic", C.c_int32), ("reserved", C.c_int32)]
 
 
 class QgQueueInfo(C.Structure):

@@ -26,6 +26,7 @@ from .circuit import (CircuitError, NATIVE_SIMULATOR_GATE_SET, circuit_metadata,
 
 PRECISIONS = {"c128": A.QG_C128, "c64": A.QG_C64, "complex128": A.QG_C128, "complex64": A.QG_C64}
 FUSIONS = {"plain": A.QG_FUSE_PLAIN, "tiled": A.QG_FUSE_TILED, "dense": A.QG_FUSE_DENSE}
+ARITHMETIC = {"exact": A.QG_ARITH_EXACT, "double-float": A.QG_ARITH_DOUBLE_FLOAT}
 
 PAULI = {
     "I": [[1, 0], [0, 1]], "X": [[0, 1], [1, 0]], "Y": [[0, -1j], [1j, 0]], "Z": [[1, 0], [0, -1]],
@@ -124,6 +125,7 @@ class GpuStateVectorSimulator:
         cfg.workers = int(self.config.get("workers", 2))
         cfg.hbm_budget_bytes = int(self.config.get("hbm-budget", 0))
         cfg.seed = int(self.config.get("seed", 0) or 0) & (2**64 - 1)
+        cfg.arithmetic = ARITHMETIC[self.config.get("arithmetic", "double-float")]
         ctx = C.c_void_p()
         _check(self._lib.qg_ctx_create(C.byref(cfg), C.byref(ctx)))
         self._ctx = ctx
@@ -288,6 +290,7 @@ class GpuStateVectorSimulator:
         opts.seed = int(options.get("seed", 0) or 0) & (2**64 - 1)
         opts.precision = PRECISIONS.get(options.get("precision"), -1) if options.get("precision") else -1
         opts.fusion = FUSIONS.get(options.get("fusion"), -1) if options.get("fusion") else -1
+        opts.arithmetic = ARITHMETIC.get(options.get("arithmetic"), -1) if options.get("arithmetic") else -1
         return opts, keep, meta
 
     def _submit(self, circuit: dict, options: dict) -> int:

@@ -435,9 +435,70 @@ void host_apply(std::vector<cd>& v, int kb, const int* pos, const GOp& g) {
 }  // namespace
 
 int tile_bits_for(int n, int precision) {
-  int kmax = precision == QG_C64 ? 13 : 12;
+  (void)precision;
+  const int kmax = 12;  // 4096 amplitudes: 512 threads x 8 registers
   return n < kmax ? n : kmax;
 }
+
+namespace {
+
+// Split the 2x2 coefficients into float pairs for the double-float policy.
+void split_coeffs(TOp* t) {
+  for (int q = 0; q < 8; ++q) {
+    const float hi = (float)t->m[q];
+    t->mf[q] = hi;
+    t->mf[8 + q] = (float)(t->m[q] - (double)hi);
+  }
+}
+
+// Insert OK_LAYOUT ops: consecutive ops whose non-diagonal bits fit in three
+// register bits form a group; the register positions are written into the ops.
+void plan_register_groups(std::vector<TOp>& ops, int k) {
+  std::vector<TOp> out;
+  size_t i = 0;
+  while (i < ops.size()) {
+    if (ops[i].kind == OK_DENSE) {
+      out.push_back(ops[i++]);
+      continue;
+    }
+    uint32_t rb = 0;
+    size_t j = i;
+    while (j < ops.size() && ops[j].kind != OK_DENSE) {
+      uint32_t req = 0;
+      if (ops[j].kind == OK_U2) req = 1u << ops[j].t;
+      else if (ops[j].kind == OK_SWAP) req = (1u << ops[j].t) | (1u << ops[j].t2);
+      if (__builtin_popcount(rb | req) > 3) break;
+      rb |= req;
+      ++j;
+    }
+    // pad with the highest free local bits so the thread bits stay low (coalesced shared memory)
+    for (int b = k - 1; b >= 0 && __builtin_popcount(rb) < 3; --b) rb |= 1u << b;
+    int pos[3], np = 0;
+    for (int b = 0; b < k && np < 3; ++b)
+      if (rb & (1u << b)) pos[np++] = b;
+    TOp lay;
+    std::memset(&lay, 0, sizeof(lay));
+    lay.kind = OK_LAYOUT;
+    for (int q = 0; q < 3; ++q) lay.dbits[q] = pos[q];
+    out.push_back(lay);
+    auto rpos = [&](int b) { return b == pos[0] ? 0 : b == pos[1] ? 1 : 2; };
+    for (size_t q = i; q < j; ++q) {
+      TOp t = ops[q];
+      if (t.kind == OK_U2) {
+        t.t2 = rpos(t.t);
+      } else if (t.kind == OK_SWAP) {
+        int a = rpos(t.t), b = rpos(t.t2);
+        t.dbits[0] = a < b ? a : b;
+        t.dbits[1] = a < b ? b : a;
+      }
+      out.push_back(t);
+    }
+    i = j;
+  }
+  ops.swap(out);
+}
+
+}  // namespace
 
 int schedule(int n, int precision, int fusion, int fuse_k, const std::vector<GOp>& gops,
              const std::vector<std::vector<int>>& measures, const std::vector<int>& measure_at, Program* prog,
@@ -459,7 +520,7 @@ int schedule(int n, int precision, int fusion, int fuse_k, const std::vector<GOp
     }
   };
 
-  if (fusion == QG_FUSE_PLAIN) {
+  if (fusion == QG_FUSE_PLAIN || n < 5) {  // registers need at least 2^5 amplitudes per tile
     for (size_t gi = 0; gi < gops.size(); ++gi) {
       emit_measures_at(gi);
       Step s;
@@ -572,8 +633,14 @@ int schedule(int n, int precision, int fusion, int fuse_k, const std::vector<GOp
     int lpos[64];
     for (int b = 0; b < 64; ++b) lpos[b] = -1;
     for (int j = 0; j < s.pass.k; ++j) lpos[s.pass.lbits[j]] = j;
+    std::vector<TOp> pass_ops;
+    for (size_t j = begin; j < oi; ++j) pass_ops.push_back(localize(ops[j], lpos, n));
+    plan_register_groups(pass_ops, s.pass.k);
     s.pass.op_begin = (int64_t)prog->tops.size();
-    for (size_t j = begin; j < oi; ++j) prog->tops.push_back(localize(ops[j], lpos, n));
+    for (TOp& t : pass_ops) {
+      split_coeffs(&t);
+      prog->tops.push_back(t);
+    }
     s.pass.op_end = (int64_t)prog->tops.size();
     prog->steps.push_back(s);
     prog->hbm_passes += 1;

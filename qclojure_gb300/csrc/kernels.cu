@@ -264,173 +264,6 @@ cudaError_t plain_op_t(void* sv, int n, const GOp& op, cudaStream_t st) {
 }
 
 // ---------------------------------------------------------------------------
-// Tiled executor: one CTA holds 2^k amplitudes (local bits pd.lbits) in shared
-// memory and applies the pass's op run to them before writing back.
-// ---------------------------------------------------------------------------
-constexpr int kTileThreads = 512;
-constexpr int kMaxItems = 16;  // dense-block outputs per thread (2^13 / 512)
-
-template <typename R>
-__global__ void __launch_bounds__(kTileThreads) k_tile(typename C2<R>::T* __restrict__ s, PassDesc pd,
-                                                      const TOp* __restrict__ ops, const double* __restrict__ dense,
-                                                      uint64_t ntiles) {
-  using V = typename C2<R>::T;
-  extern __shared__ __align__(16) unsigned char smem_raw[];
-  const int k = pd.k, K = 1 << k, klow = pd.klow;
-  V* tile = reinterpret_cast<V*>(smem_raw);
-  uint64_t* hioff = reinterpret_cast<uint64_t*>(smem_raw + sizeof(V) * K);
-  const int nhi = 1 << (k - klow);
-  for (int h = threadIdx.x; h < nhi; h += blockDim.x) {
-    uint64_t off = 0;
-    for (int j = klow; j < k; ++j)
-      if ((h >> (j - klow)) & 1) off |= 1ULL << pd.lbits[j];
-    hioff[h] = off;
-  }
-  __syncthreads();
-  const uint32_t lowmask = (1u << klow) - 1;
-  for (uint64_t tid = blockIdx.x; tid < ntiles; tid += gridDim.x) {
-    uint64_t base = 0;
-    for (int r = 0; r < pd.nruns; ++r)
-      base |= ((tid >> pd.run_src[r]) & ((1ULL << pd.run_len[r]) - 1)) << pd.run_dst[r];
-    for (int l = threadIdx.x; l < K; l += blockDim.x) tile[l] = s[base | (l & lowmask) | hioff[l >> klow]];
-    __syncthreads();
-    for (int64_t o = pd.op_begin; o < pd.op_end; ++o) {
-      const TOp* op = ops + o;
-      const int kind = op->kind;
-      if (kind == OK_U2) {
-        if ((base & op->gcmask) != op->gcmask) continue;
-        const int t = op->t, cls = op->cls;
-        const uint32_t lc = op->lcmask, tb = 1u << t;
-        R m[8];
-#pragma unroll
-        for (int q = 0; q < 8; ++q) m[q] = (R)op->m[q];
-        for (int p = threadIdx.x; p < (K >> 1); p += blockDim.x) {
-          uint32_t l0 = ((p >> t) << (t + 1)) | (p & (tb - 1));
-          if ((l0 & lc) != lc) continue;
-          V x0 = tile[l0], x1 = tile[l0 | tb], y0, y1;
-          switch (cls) {
-            case U2_GENERAL: u2_apply<U2_GENERAL>(m, x0, x1, y0, y1); break;
-            case U2_REAL: u2_apply<U2_REAL>(m, x0, x1, y0, y1); break;
-            case U2_RXLIKE: u2_apply<U2_RXLIKE>(m, x0, x1, y0, y1); break;
-            case U2_DIAG: u2_apply<U2_DIAG>(m, x0, x1, y0, y1); break;
-            case U2_ANTIDIAG: u2_apply<U2_ANTIDIAG>(m, x0, x1, y0, y1); break;
-            case U2_X: u2_apply<U2_X>(m, x0, x1, y0, y1); break;
-            default: u2_apply<U2_IMAG_ANTI>(m, x0, x1, y0, y1); break;
-          }
-          tile[l0] = y0;
-          tile[l0 | tb] = y1;
-        }
-      } else if (kind == OK_PHASE) {
-        if ((base & op->gmask) != op->gmask) continue;
-        const uint32_t lm = op->lmask;
-        const int cls = op->cls;
-        const R pr = (R)op->m[0], pi = (R)op->m[1];
-        R m2[2] = {pr, pi};
-        for (int l = threadIdx.x; l < K; l += blockDim.x) {
-          if ((l & lm) != lm) continue;
-          V x = tile[l];
-          switch (cls) {
-            case PH_GENERAL: x = phase_apply<PH_GENERAL>(m2, x); break;
-            case PH_NEG: x = phase_apply<PH_NEG>(m2, x); break;
-            case PH_I: x = phase_apply<PH_I>(m2, x); break;
-            default: x = phase_apply<PH_MINUS_I>(m2, x); break;
-          }
-          tile[l] = x;
-        }
-      } else if (kind == OK_SWAP) {
-        if ((base & op->gcmask) != op->gcmask) continue;
-        const uint32_t lc = op->lcmask, ta = 1u << op->t, tb2 = 1u << op->t2;
-        const int iswap = op->flags & 1;
-        for (int l = threadIdx.x; l < K; l += blockDim.x) {
-          if (!(l & ta) || (l & tb2) || (l & lc) != lc) continue;
-          uint32_t p = l ^ ta ^ tb2;
-          V a = tile[l], b = tile[p];
-          if (iswap) {
-            V ra, rb;
-            ra.x = -b.y; ra.y = b.x;
-            rb.x = -a.y; rb.y = a.x;
-            tile[l] = ra;
-            tile[p] = rb;
-          } else {
-            tile[l] = b;
-            tile[p] = a;
-          }
-        }
-      } else if (kind == OK_BLOCKADE) {
-        const int gc = __popcll(base & op->gmask);
-        if (gc > 1) continue;
-        const uint32_t lm = op->lmask;
-        const R pr = (R)op->m[0], pi = (R)op->m[1];
-        for (int l = threadIdx.x; l < K; l += blockDim.x)
-          if (gc + __popc(l & lm) == 1) tile[l] = cmul(pr, pi, tile[l]);
-      } else if (kind == OK_PARITY) {
-        const int gp = __popcll(base & op->gmask) & 1;
-        const uint32_t lm = op->lmask;
-        const R p0r = (R)op->m[0], p0i = (R)op->m[1], p1r = (R)op->m[2], p1i = (R)op->m[3];
-        for (int l = threadIdx.x; l < K; l += blockDim.x) {
-          int par = gp ^ (__popc(l & lm) & 1);
-          tile[l] = par ? cmul(p1r, p1i, tile[l]) : cmul(p0r, p0i, tile[l]);
-        }
-      } else if (kind == OK_COLLAPSE) {
-        const bool gok = (base & op->gmask) == op->gval;
-        const uint32_t lm = op->lmask, lv = op->lval;
-        const R sc = (R)op->m[0];
-        for (int l = threadIdx.x; l < K; l += blockDim.x) {
-          V x = tile[l], r;
-          if (gok && (l & lm) == lv) { r.x = mul_(x.x, sc); r.y = mul_(x.y, sc); }
-          else { r.x = 0; r.y = 0; }
-          tile[l] = r;
-        }
-      } else if (kind == OK_DENSE) {
-        const int dk = op->dk, D = 1 << dk;
-        const double* M = dense + 2 * op->doff;
-        V out[kMaxItems];
-        int cnt = 0;
-        for (int idx = threadIdx.x; idx < K; idx += blockDim.x, ++cnt) {
-          int g = idx >> dk, r = idx & (D - 1);
-          // deposit group bits around the block bits, block bits from r / c
-          uint32_t lg = g;
-          for (int j = 0; j < dk; ++j) {
-            int b = op->dbits[j];
-            lg = ((lg >> b) << (b + 1)) | (lg & ((1u << b) - 1));
-          }
-          R ar = 0, ai = 0;
-          for (int c = 0; c < D; ++c) {
-            uint32_t lc = lg;
-            for (int j = 0; j < dk; ++j)
-              if ((c >> j) & 1) lc |= 1u << op->dbits[j];
-            V x = tile[lc];
-            R mr = (R)M[2 * (r * D + c)], mi = (R)M[2 * (r * D + c) + 1];
-            ar = fma(mr, x.x, fma(-mi, x.y, ar));
-            ai = fma(mr, x.y, fma(mi, x.x, ai));
-          }
-          V y;
-          y.x = ar;
-          y.y = ai;
-          out[cnt] = y;
-        }
-        __syncthreads();
-        cnt = 0;
-        for (int idx = threadIdx.x; idx < K; idx += blockDim.x, ++cnt) {
-          int g = idx >> dk, r = idx & (D - 1);
-          uint32_t lg = g;
-          for (int j = 0; j < dk; ++j) {
-            int b = op->dbits[j];
-            lg = ((lg >> b) << (b + 1)) | (lg & ((1u << b) - 1));
-          }
-          for (int j = 0; j < dk; ++j)
-            if ((r >> j) & 1) lg |= 1u << op->dbits[j];
-          tile[lg] = out[cnt];
-        }
-      }
-      __syncthreads();
-    }
-    for (int l = threadIdx.x; l < K; l += blockDim.x) s[base | (l & lowmask) | hioff[l >> klow]] = tile[l];
-    __syncthreads();
-  }
-}
-
-// ---------------------------------------------------------------------------
 // Reductions. Per-thread TwoSum accumulation, warp/block combination of
 // (sum, compensation) pairs, one pair per block written to d_part.
 // ---------------------------------------------------------------------------
@@ -839,6 +672,7 @@ __global__ void __launch_bounds__(256) k_samp_resolve(const typename C2<R>::T* _
 // launchers
 // ---------------------------------------------------------------------------
 unsigned long long kernel_launch_count() { return g_launches.load(); }
+void count_launch(int k) { counted(k); }
 
 int reduce_blocks_for(int n) {
   uint64_t N = 1ULL << n;
@@ -858,33 +692,6 @@ cudaError_t launch_set_basis(void* s, int precision, int n, uint64_t idx, cudaSt
 
 cudaError_t launch_plain_op(void* s, int precision, int n, const GOp& op, cudaStream_t st) {
   return precision == QG_C64 ? plain_op_t<float>(s, n, op, st) : plain_op_t<double>(s, n, op, st);
-}
-
-cudaError_t launch_tile_pass(void* s, int precision, int n, const PassDesc& pd, const TOp* d_tops,
-                             const double* d_dense, cudaStream_t st) {
-  const int K = 1 << pd.k;
-  const size_t amp = precision == QG_C64 ? 8 : 16;
-  const size_t smem = amp * K + sizeof(uint64_t) * (1u << (pd.k - pd.klow));
-  const uint64_t ntiles = 1ULL << (n - pd.k);
-  int threads = K >= 2 * kTileThreads ? kTileThreads : (K / 2 < 32 ? 32 : K / 2);
-  if (K / threads > kMaxItems) return cudaErrorInvalidValue;
-  int per_sm = (int)((200 * 1024) / smem);
-  if (per_sm > 4) per_sm = 4;
-  if (per_sm < 1) per_sm = 1;
-  uint64_t grid = (uint64_t)kSMs * per_sm;
-  if (grid > ntiles) grid = ntiles;
-  cudaError_t e;
-  if (precision == QG_C64) {
-    e = cudaFuncSetAttribute(k_tile<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    if (e != cudaSuccess) return e;
-    k_tile<float><<<(unsigned)grid, threads, smem, st>>>((float2*)s, pd, d_tops, d_dense, ntiles);
-  } else {
-    e = cudaFuncSetAttribute(k_tile<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    if (e != cudaSuccess) return e;
-    k_tile<double><<<(unsigned)grid, threads, smem, st>>>((double2*)s, pd, d_tops, d_dense, ntiles);
-  }
-  counted();
-  return cudaGetLastError();
 }
 
 cudaError_t launch_c128_to_c64(const double* src, float* dst, uint64_t count, cudaStream_t st) {

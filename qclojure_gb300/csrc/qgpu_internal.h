@@ -24,7 +24,8 @@ enum OpKind : int32_t {
   OK_BLOCKADE = 3,  // amp *= ph where popcount(idx & mask) == 1
   OK_PARITY = 4,    // amp *= (parity(idx & mask) ? ph1 : ph0)
   OK_COLLAPSE = 5,  // amp = ((idx & mask) == val) ? amp * scale : 0
-  OK_DENSE = 6      // dense 2^dk x 2^dk block on bits dbits[0..dk) (dbits[0] = least significant)
+  OK_DENSE = 6,     // dense 2^dk x 2^dk block on bits dbits[0..dk) (dbits[0] = least significant)
+  OK_LAYOUT = 7     // tiled executor only: registers hold the local bits dbits[0..3) from here on
 };
 
 // Matrix classes of OK_U2 (picked on the host from exact zero / unit entries).
@@ -69,7 +70,7 @@ struct GOp {
 struct TOp {
   int32_t kind;
   int32_t cls;
-  int32_t t, t2;     // local bit positions
+  int32_t t, t2;     // local bit positions; for OK_U2 in the tiled executor t2 = register position
   int32_t flags;
   int32_t dk;
   uint32_t lcmask;   // local control mask
@@ -80,9 +81,11 @@ struct TOp {
   uint64_t gmask;    // non-local part of mask (absolute)
   uint64_t gval;     // non-local part of val (absolute)
   double m[8];
-  int32_t dbits[5];  // local bit positions of a dense block
+  int32_t dbits[5];  // local bit positions of a dense block; register bits of OK_LAYOUT;
+                     // register positions (a < b) of OK_SWAP
   int32_t pad1;
   int64_t doff;
+  float mf[16];      // m split into float pairs: hi in mf[0..8), lo in mf[8..16)
 };
 
 constexpr int kMaxTileBits = 13;     // 2^13 amplitudes per tile at most
@@ -114,6 +117,7 @@ struct Program {
   std::vector<TOp> tops;             // all tile ops, referenced by PassDesc ranges
   std::vector<double> dense;         // dense block matrices (re, im interleaved)
   int hbm_passes = 0;
+  int arith = QG_ARITH_EXACT;        // complex128 arithmetic of the tiled passes
 };
 
 // Compile a reference-level circuit into GOps (returns QG_OK or an error code;
@@ -132,8 +136,9 @@ int tile_bits_for(int n, int precision);
 
 cudaError_t launch_set_basis(void* s, int precision, int n, uint64_t idx, cudaStream_t st);
 cudaError_t launch_plain_op(void* s, int precision, int n, const GOp& op, cudaStream_t st);
-cudaError_t launch_tile_pass(void* s, int precision, int n, const PassDesc& pd, const TOp* d_tops,
+cudaError_t launch_tile_pass(void* s, int precision, int arithmetic, int n, const PassDesc& pd, const TOp* d_tops,
                              const double* d_dense, cudaStream_t st);
+void count_launch(int k);
 cudaError_t launch_c128_to_c64(const double* src, float* dst, uint64_t count, cudaStream_t st);
 cudaError_t launch_c64_to_c128(const float* src, double* dst, uint64_t count, cudaStream_t st);
 

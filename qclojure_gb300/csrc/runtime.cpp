@@ -299,7 +299,7 @@ static int exec_program(State* s, const Program& prog, uint64_t seed, const std:
     if (st.kind == Step::PLAIN_OP) {
       e = launch_plain_op(s->d, s->prec, s->n, st.op, s->stream);
     } else if (st.kind == Step::TILE_PASS) {
-      e = launch_tile_pass(s->d, s->prec, s->n, st.pass, d_tops, d_dense, s->stream);
+      e = launch_tile_pass(s->d, s->prec, prog.arith, s->n, st.pass, d_tops, d_dense, s->stream);
     } else {
       rc = do_measure(s, st.mqubits, seed, measure_index++, nullptr, nullptr, err);
     }
@@ -333,8 +333,10 @@ static int exec_program(State* s, const Program& prog, uint64_t seed, const std:
   return rc;
 }
 
-static int compile_program(const qg_circuit* c, int precision, int fusion, int fuse_k, Program* prog,
+static int compile_program(const qg_circuit* c, int precision, int fusion, int fuse_k, int arith, Program* prog,
                            std::string* err) {
+  // dense fused blocks are evaluated in FP64 (FMA) whatever the arithmetic setting
+  prog->arith = (fusion == QG_FUSE_DENSE || arith != QG_ARITH_DOUBLE_FLOAT) ? QG_ARITH_EXACT : QG_ARITH_DOUBLE_FLOAT;
   std::vector<GOp> gops;
   std::vector<std::vector<int>> measures;
   std::vector<int> measure_at;
@@ -481,7 +483,7 @@ struct Job {
   SpecCopy spec;
   std::vector<double> initial;
   uint64_t seed = 0;
-  int precision = QG_C128, fusion = QG_FUSE_TILED;
+  int precision = QG_C128, fusion = QG_FUSE_TILED, arith = QG_ARITH_EXACT;
   std::atomic<int> status{QG_JOB_QUEUED};
   std::atomic<bool> cancel{false};
   int error_code = QG_OK;
@@ -571,7 +573,7 @@ static int run_job(Ctx* c, Job* j, cudaStream_t stream) {
   int rc;
   Program prog;
   qg_circuit circ{j->n, (int32_t)j->ops.size(), j->ops.data()};
-  rc = compile_program(&circ, j->precision, j->fusion, c->cfg.fuse_k, &prog, &err);
+  rc = compile_program(&circ, j->precision, j->fusion, c->cfg.fuse_k, j->arith, &prog, &err);
   if (rc != QG_OK) {
     j->error_code = rc;
     j->error = err;
@@ -891,6 +893,7 @@ static int submit_one(Ctx* c, const qg_circuit* circ, const qg_options* opt, uin
   j->seed = c->cfg.seed;
   j->precision = c->cfg.precision;
   j->fusion = c->cfg.fusion;
+  j->arith = c->cfg.arithmetic;
   if (opt) {
     int rc = copy_spec(opt->spec, j->n, &j->spec, &err);
     if (rc != QG_OK) {
@@ -901,6 +904,7 @@ static int submit_one(Ctx* c, const qg_circuit* circ, const qg_options* opt, uin
     if (opt->seed) j->seed = opt->seed;
     if (opt->precision == QG_C128 || opt->precision == QG_C64) j->precision = opt->precision;
     if (opt->fusion >= QG_FUSE_PLAIN && opt->fusion <= QG_FUSE_DENSE) j->fusion = opt->fusion;
+    if (opt->arithmetic == QG_ARITH_EXACT || opt->arithmetic == QG_ARITH_DOUBLE_FLOAT) j->arith = opt->arithmetic;
   }
   if (c->cfg.max_qubits > 0 && j->n > c->cfg.max_qubits) {
     set_ctx_error(c, "circuit exceeds max-qubits of this backend");
@@ -950,6 +954,7 @@ int qg_ctx_create(const qg_config* cfg, void** ctx_out) {
   if (c->cfg.fuse_k < 1 || c->cfg.fuse_k > 5) c->cfg.fuse_k = 4;
   if (c->cfg.precision != QG_C64) c->cfg.precision = QG_C128;
   if (c->cfg.fusion < QG_FUSE_PLAIN || c->cfg.fusion > QG_FUSE_DENSE) c->cfg.fusion = QG_FUSE_TILED;
+  if (c->cfg.arithmetic != QG_ARITH_DOUBLE_FLOAT) c->cfg.arithmetic = QG_ARITH_EXACT;
   if (c->cfg.seed == 0) c->cfg.seed = 0x5eed5eedULL;
   c->device = c->cfg.device;
   if (c->device < 0 || c->device >= ndev) {
@@ -1461,7 +1466,7 @@ int qg_state_apply(void* state, const qg_circuit* circuit, int32_t fusion, uint6
   cudaSetDevice(s->ctx->device);
   std::string err;
   Program prog;
-  int rc = compile_program(circuit, s->prec, fusion, s->ctx->cfg.fuse_k, &prog, &err);
+  int rc = compile_program(circuit, s->prec, fusion, s->ctx->cfg.fuse_k, s->ctx->cfg.arithmetic, &prog, &err);
   if (rc != QG_OK) return state_err(s, rc, err);
   ExecStats st;
   rc = exec_program(s, prog, seed, nullptr, &st, &err);
@@ -1573,7 +1578,7 @@ int qg_state_profile(void* state, const qg_circuit* circuit, int32_t fusion, uin
   cudaSetDevice(s->ctx->device);
   std::string err;
   Program prog;
-  int rc = compile_program(circuit, s->prec, fusion, s->ctx->cfg.fuse_k, &prog, &err);
+  int rc = compile_program(circuit, s->prec, fusion, s->ctx->cfg.fuse_k, s->ctx->cfg.arithmetic, &prog, &err);
   if (rc != QG_OK) return state_err(s, rc, err);
   std::vector<float> ms;
   std::vector<int> kinds;

@@ -11,7 +11,7 @@ import ctypes as C
 import numpy as np
 
 from . import _abi as A
-from .backend import PRECISIONS, FUSIONS, _check
+from .backend import ARITHMETIC, PRECISIONS, FUSIONS, _check
 from .circuit import encode
 
 
@@ -19,7 +19,7 @@ class Context:
     """A library context on one GPU (no job workers are needed for direct state use)."""
 
     def __init__(self, device: int = 0, precision: str = "c128", fusion: str = "tiled", fusion_width: int = 4,
-                 workers: int = 1, seed: int = 0):
+                 workers: int = 1, seed: int = 0, arithmetic: str = "double-float"):
         self.lib = A.load_library()
         cfg = A.QgConfig()
         cfg.device = device
@@ -28,6 +28,7 @@ class Context:
         cfg.fuse_k = fusion_width
         cfg.workers = workers
         cfg.seed = seed
+        cfg.arithmetic = ARITHMETIC[arithmetic]
         ctx = C.c_void_p()
         _check(self.lib.qg_ctx_create(C.byref(cfg), C.byref(ctx)))
         self.ctx = ctx

@@ -34,7 +34,16 @@ def oracle(built):
 def gpu_ctx(built):
     from qclojure_gb300.state import Context
 
-    ctx = Context(seed=1)
+    ctx = Context(seed=1, arithmetic="exact")
+    yield ctx
+    ctx.close()
+
+
+@pytest.fixture(scope="session")
+def gpu_ctx_df(built):
+    from qclojure_gb300.state import Context
+
+    ctx = Context(seed=1, arithmetic="double-float")
     yield ctx
     ctx.close()
 
@@ -43,6 +52,15 @@ def gpu_ctx(built):
 def sim(built):
     from qclojure_gb300.backend import create_simulator
 
-    s = create_simulator({"precision": "c128", "fusion": "tiled", "seed": 3})
+    s = create_simulator({"precision": "c128", "fusion": "tiled", "seed": 3, "arithmetic": "exact"})
+    yield s
+    s.close()
+
+
+@pytest.fixture(scope="session")
+def sim_df(built):
+    from qclojure_gb300.backend import create_simulator
+
+    s = create_simulator({"precision": "c128", "fusion": "tiled", "seed": 3, "arithmetic": "double-float"})
     yield s
     s.close()

@@ -322,6 +322,55 @@ def test_plain_equals_tiled_at_24_qubits(gpu_ctx):
 
 
 # ---------------------------------------------------------------------------
+# complex128 in double-float arithmetic (float pairs on the FP32 pipes):
+# tolerance max |d amp| <= 1e-12 against the FP64 oracle
+@pytest.mark.parametrize("n", [5, 8, 12, 13, 14, 17, 20])
+def test_layered_c128_double_float(gpu_ctx_df, oracle, n):
+    from qclojure_gb300 import workloads
+
+    c = workloads.layered_circuit(n, 20 if n <= 14 else 8, seed=n)
+    ref = oracle.run(c)
+    with gpu_ctx_df.state(n) as st:
+        st.apply(c, fusion="tiled")
+        got = st.download()
+        assert np.max(np.abs(got - ref)) <= 1e-12
+        assert np.array_equal(st.sample(2000, 3), oracle.sample(ref, 2000, 3))
+
+
+@pytest.mark.parametrize("n", [9, 16])
+def test_every_gate_c128_double_float(gpu_ctx_df, oracle, n):
+    c = every_gate_circuit(n, seed=200 + n)
+    ref = oracle.run(c)
+    with gpu_ctx_df.state(n) as st:
+        st.apply(c, fusion="tiled")
+        assert np.max(np.abs(st.download() - ref)) <= 1e-12
+
+
+def test_double_float_deep_circuit_error(gpu_ctx_df, oracle):
+    """300 layers (4500 gates) on 10 qubits: accumulated error stays below 1e-12."""
+    from qclojure_gb300 import workloads
+
+    c = workloads.layered_circuit(10, 300, seed=77)
+    ref = oracle.run(c)
+    with gpu_ctx_df.state(10) as st:
+        st.apply(c, fusion="tiled")
+        err = np.max(np.abs(st.download() - ref))
+    assert err <= 1e-12, err
+
+
+def test_double_float_inverse_at_26_qubits(gpu_ctx_df):
+    from qclojure_gb300 import workloads
+
+    n = 26
+    c = workloads.large_circuit(n, 6, seed=3)
+    with gpu_ctx_df.state(n) as st:
+        st.apply(c, fusion="tiled")
+        st.apply(_inverse(c), fusion="tiled")
+        assert abs(st.pauli_expectation("Z" * n) - 1.0) <= 1e-12
+        assert np.all(st.sample(500, 1) == 0)
+
+
+# ---------------------------------------------------------------------------
 class GpuEngine:
     def __init__(self, sim):
         self.sim = sim
