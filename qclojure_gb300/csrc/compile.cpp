@@ -480,17 +480,42 @@ void plan_register_groups(std::vector<TOp>& ops, int k) {
     std::memset(&lay, 0, sizeof(lay));
     lay.kind = OK_LAYOUT;
     for (int q = 0; q < 3; ++q) lay.dbits[q] = pos[q];
+    for (int s = 0; s < 8; ++s)
+      lay.lj[s] = ((uint32_t)(s & 1) << pos[0]) | ((uint32_t)((s >> 1) & 1) << pos[1]) |
+                  ((uint32_t)((s >> 2) & 1) << pos[2]);
     out.push_back(lay);
     auto rpos = [&](int b) { return b == pos[0] ? 0 : b == pos[1] ? 1 : 2; };
+    const uint32_t rbm = (1u << pos[0]) | (1u << pos[1]) | (1u << pos[2]);
+    auto reg_part = [&](uint32_t m) {
+      uint32_t r = 0;
+      for (int q = 0; q < 3; ++q)
+        if (m & (1u << pos[q])) r |= 1u << q;
+      return r;
+    };
     for (size_t q = i; q < j; ++q) {
       TOp t = ops[q];
+      uint32_t m = 0, v = 0;
       if (t.kind == OK_U2) {
         t.t2 = rpos(t.t);
+        m = v = t.lcmask;
       } else if (t.kind == OK_SWAP) {
         int a = rpos(t.t), b = rpos(t.t2);
         t.dbits[0] = a < b ? a : b;
         t.dbits[1] = a < b ? b : a;
+        m = v = t.lcmask;
+      } else if (t.kind == OK_PHASE) {
+        m = v = t.lmask;
+      } else if (t.kind == OK_COLLAPSE) {
+        m = t.lmask;
+        v = t.lval;
+      } else {  // BLOCKADE, PARITY: the mask selects the bits to count
+        m = t.lmask;
+        v = 0;
       }
+      t.rmask = reg_part(m);
+      t.rval = reg_part(v);
+      t.tmask = m & ~rbm;
+      t.tval = v & ~rbm;
       out.push_back(t);
     }
     i = j;
@@ -615,7 +640,9 @@ int schedule(int n, int precision, int fusion, int fuse_k, const std::vector<GOp
       // ops before the next measurement only
       while (limit > begin && orig_index[limit - 1] >= (size_t)measure_at[mi]) --limit;
     }
-    while (oi < limit) {
+    // at most half the kernel-parameter op records: every gate may need a layout op before it
+    const size_t max_ops = (size_t)max_ops_per_tile_pass() / 2;
+    while (oi < limit && oi - begin < max_ops) {
       uint64_t r = required_local(ops[oi]);
       if (__builtin_popcountll(L | r) > k) break;
       L |= r;

@@ -86,6 +86,11 @@ struct TOp {
   int32_t pad1;
   int64_t doff;
   float mf[16];      // m split into float pairs: hi in mf[0..8), lo in mf[8..16)
+  // Tiled executor: the local mask of the op (controls of U2/SWAP, mask of the
+  // diagonal kinds) split into its register positions (3-bit rmask/rval) and its
+  // thread bits (tmask/tval), so each thread tests one word per op.
+  uint32_t rmask, rval, tmask, tval;
+  uint32_t lj[8];    // OK_LAYOUT: local offset of register slot j
 };
 
 constexpr int kMaxTileBits = 13;     // 2^13 amplitudes per tile at most
@@ -136,8 +141,12 @@ int tile_bits_for(int n, int precision);
 
 cudaError_t launch_set_basis(void* s, int precision, int n, uint64_t idx, cudaStream_t st);
 cudaError_t launch_plain_op(void* s, int precision, int n, const GOp& op, cudaStream_t st);
-cudaError_t launch_tile_pass(void* s, int precision, int arithmetic, int n, const PassDesc& pd, const TOp* d_tops,
+// d_kops: the program's compact op records on the device (encode_kops), indexed by the pass's op range.
+cudaError_t launch_tile_pass(void* s, int precision, int arithmetic, int n, const PassDesc& pd, const void* d_kops,
                              const double* d_dense, cudaStream_t st);
+int max_ops_per_tile_pass();
+size_t kop_record_bytes();
+void encode_kops(int precision, int arithmetic, const TOp* tops, int64_t count, void* out);
 void count_launch(int k);
 cudaError_t launch_c128_to_c64(const double* src, float* dst, uint64_t count, cudaStream_t st);
 cudaError_t launch_c64_to_c128(const float* src, double* dst, uint64_t count, cudaStream_t st);

@@ -263,12 +263,14 @@ static int do_measure(State* s, const std::vector<int>& qubits, uint64_t seed, u
 
 static int exec_program(State* s, const Program& prog, uint64_t seed, const std::atomic<bool>* cancel,
                         ExecStats* stats, std::string* err) {
-  TOp* d_tops = nullptr;
   double* d_dense = nullptr;
+  void* d_kops = nullptr;
   if (!prog.tops.empty()) {
-    CK(cudaMallocAsync((void**)&d_tops, sizeof(TOp) * prog.tops.size(), s->stream), "alloc tops");
-    CK(cudaMemcpyAsync(d_tops, prog.tops.data(), sizeof(TOp) * prog.tops.size(), cudaMemcpyHostToDevice, s->stream),
-       "H2D tops");
+    std::vector<unsigned char> kops(kop_record_bytes() * prog.tops.size());
+    encode_kops(s->prec, prog.arith, prog.tops.data(), (int64_t)prog.tops.size(), kops.data());
+    CK(cudaMallocAsync(&d_kops, kops.size(), s->stream), "alloc ops");
+    CK(cudaMemcpyAsync(d_kops, kops.data(), kops.size(), cudaMemcpyHostToDevice, s->stream), "H2D ops");
+    CK(cudaStreamSynchronize(s->stream), "sync");  // the host buffer dies at scope end
   }
   if (!prog.dense.empty()) {
     CK(cudaMallocAsync((void**)&d_dense, sizeof(double) * prog.dense.size(), s->stream), "alloc dense");
@@ -299,7 +301,7 @@ static int exec_program(State* s, const Program& prog, uint64_t seed, const std:
     if (st.kind == Step::PLAIN_OP) {
       e = launch_plain_op(s->d, s->prec, s->n, st.op, s->stream);
     } else if (st.kind == Step::TILE_PASS) {
-      e = launch_tile_pass(s->d, s->prec, prog.arith, s->n, st.pass, d_tops, d_dense, s->stream);
+      e = launch_tile_pass(s->d, s->prec, prog.arith, s->n, st.pass, d_kops, d_dense, s->stream);
     } else {
       rc = do_measure(s, st.mqubits, seed, measure_index++, nullptr, nullptr, err);
     }
@@ -324,8 +326,8 @@ static int exec_program(State* s, const Program& prog, uint64_t seed, const std:
     }
     for (auto& ev : evs) cudaEventDestroy(ev);
   }
-  if (d_tops) cudaFreeAsync(d_tops, s->stream);
   if (d_dense) cudaFreeAsync(d_dense, s->stream);
+  if (d_kops) cudaFreeAsync(d_kops, s->stream);
   if (stats) {
     stats->device_ms = ms;
     stats->passes = prog.hbm_passes;

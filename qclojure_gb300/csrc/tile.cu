@@ -22,6 +22,8 @@
 //   PolDF  complex128 stored as IEEE doubles in HBM, computed as double-float
 //          pairs on the FP32 pipes (df64.cuh); within 1e-14 per pass.
 #include <cstdio>
+#include <cstring>
+#include <type_traits>
 
 #include "df64.cuh"
 #include "qgpu_internal.h"
@@ -53,19 +55,6 @@ struct PolExact {
   struct Cst {
     R m[8];
   };
-  __device__ static Cst cst(const TOp& op) {
-    Cst c;
-    if constexpr (sizeof(R) == 4) {
-      // FP32 coefficients were rounded on the host: a double->float conversion
-      // here would run on the FP64 pipe, once per op and thread
-#pragma unroll
-      for (int q = 0; q < 8; ++q) c.m[q] = op.mf[q];
-    } else {
-#pragma unroll
-      for (int q = 0; q < 8; ++q) c.m[q] = op.m[q];
-    }
-    return c;
-  }
   __device__ static V load_raw(const unsigned char* sm, int pos) { return reinterpret_cast<const V*>(sm)[pos]; }
   __device__ static V load_work(const unsigned char* sm, int pos) { return load_raw(sm, pos); }
   __device__ static void store_raw(unsigned char* sm, int pos, const V& v) { reinterpret_cast<V*>(sm)[pos] = v; }
@@ -120,7 +109,10 @@ struct PolExact {
     return r;
   }
   __device__ static V times_i(V x) { V r; r.x = -x.y; r.y = x.x; return r; }
-  __device__ static V cmul_idx(const Cst& c, int which, V x) { return cm(c.m[2 * which], c.m[2 * which + 1], x); }
+  // entry 0 or 1 of a phase pair (selected without indexing the constant array)
+  __device__ static V cmul_idx(const Cst& c, int which, V x) {
+    return which ? cm(c.m[2], c.m[3], x) : cm(c.m[0], c.m[1], x);
+  }
   __device__ static V scale(const Cst& c, V x) { V r; r.x = mulD(x.x, c.m[0]); r.y = mulD(x.y, c.m[0]); return r; }
   __device__ static V zero() { V r; r.x = 0; r.y = 0; return r; }
 };
@@ -139,15 +131,6 @@ struct PolDF {
   struct Cst {
     float h[8], l[8];
   };
-  __device__ static Cst cst(const TOp& op) {
-    Cst c;
-#pragma unroll
-    for (int q = 0; q < 8; ++q) {
-      c.h[q] = op.mf[q];
-      c.l[q] = op.mf[8 + q];
-    }
-    return c;
-  }
   __device__ static dfc load_raw(const unsigned char* sm, int pos) {
     return load_dfc(reinterpret_cast<const double2*>(sm)[pos]);
   }
@@ -214,7 +197,10 @@ struct PolDF {
     return dfc{x.ih, x.il, -x.rh, -x.rl};
   }
   __device__ static dfc times_i(const dfc& x) { return dfc{-x.ih, -x.il, x.rh, x.rl}; }
-  __device__ static dfc cmul_idx(const Cst& c, int which, const dfc& x) { return cmk(c, which, x); }
+  __device__ static dfc cmul_idx(const Cst& c, int which, const dfc& x) {
+    const bool w = which != 0;
+    return cmul_df(w ? c.h[2] : c.h[0], w ? c.l[2] : c.l[0], w ? c.h[3] : c.h[1], w ? c.l[3] : c.l[1], x);
+  }
   __device__ static dfc scale(const Cst& c, const dfc& x) {
     dfc r;
     mul1(c.h[0], c.l[0], x.rh, x.rl, r.rh, r.rl);
@@ -279,55 +265,88 @@ __device__ __forceinline__ void store_tile(const unsigned char* buf, unsigned ch
 }
 
 // ---- register-level op application ----------------------------------------
-template <class P, int CLS, int RP>
-__device__ __forceinline__ void u2_regs(typename P::Reg (&r)[kRegs], const typename P::Cst& c, uint32_t lt,
-                                        const uint32_t (&lj)[kRegs], uint32_t lc) {
+// ---------------------------------------------------------------------------
+// Compact op records passed by value in kernel-parameter (constant-bank) space:
+// every thread reads the same record, so the loads are uniform and cheap.
+// ---------------------------------------------------------------------------
+enum KCode : int32_t {
+  KC_LAYOUT = 0,   // tmask/tval/rmr = register bits rb0/rb1/rb2, c[0..8) = lj (bit patterns)
+  KC_DENSE = 1,    // tmask = dk, tval = doff, rmr = dbits (4 bits each)
+  KC_U2 = 16,      // + cls * 4 + register position
+  KC_PHASE = 48,   // + phase class
+  KC_SWAP = 56,    // + register pair (0: {0,1}, 1: {0,2}, 2: {1,2}) + 3 * iswap
+  KC_BLOCKADE = 62,
+  KC_PARITY = 63,
+  KC_COLLAPSE = 64,
+  KF_COND = 0x100  // the op has control / mask conditions to evaluate
+};
+
+struct __align__(16) KOp {
+  int32_t code;
+  uint32_t tmask, tval, rmr;  // thread-bit mask/value, register mask | register value << 8
+  uint64_t gmask, gval;       // non-local mask/value (controls of U2/SWAP: gval = gmask)
+  float c[16];                // coefficients: float pairs (hi[8], lo[8]) or 8 doubles (FP64 policy)
+};
+
+constexpr int kMaxKOps = 320;
+
+static_assert(sizeof(KOp) == 96, "KOp layout");
+
+template <class P>
+__device__ __forceinline__ typename P::Cst kcst(const KOp& op);
+template <>
+__device__ __forceinline__ PolD::Cst kcst<PolD>(const KOp& op) {
+  PolD::Cst c;
+  const double* d = reinterpret_cast<const double*>(op.c);
+#pragma unroll
+  for (int q = 0; q < 8; ++q) c.m[q] = d[q];
+  return c;
+}
+template <>
+__device__ __forceinline__ PolF::Cst kcst<PolF>(const KOp& op) {
+  PolF::Cst c;
+#pragma unroll
+  for (int q = 0; q < 8; ++q) c.m[q] = op.c[q];
+  return c;
+}
+template <>
+__device__ __forceinline__ PolDF::Cst kcst<PolDF>(const KOp& op) {
+  PolDF::Cst c;
+#pragma unroll
+  for (int q = 0; q < 8; ++q) {
+    c.h[q] = op.c[q];
+    c.l[q] = op.c[8 + q];
+  }
+  return c;
+}
+
+// Register slot j holds local index lt | lj[j]; bit q of j is register position q.
+// A conditional op tests its thread bits once per thread and its register
+// positions (cr, uniform) per slot with compile-time slot numbers.
+template <class P, int CLS, int RP, bool COND>
+__device__ __forceinline__ void u2_regs(typename P::Reg (&r)[kRegs], const typename P::Cst& c, uint32_t cr) {
 #pragma unroll
   for (int q = 0; q < 4; ++q) {
     const int j0 = ((q >> RP) << (RP + 1)) | (q & ((1 << RP) - 1));
     const int j1 = j0 | (1 << RP);
-    if (((lt | lj[j0]) & lc) == lc) P::template u2<CLS>(c, r[j0], r[j1]);
+    if (!COND || (j0 & cr) == cr) P::template u2<CLS>(c, r[j0], r[j1]);
   }
 }
 
-template <class P, int CLS>
-__device__ __forceinline__ void u2_dispatch_rp(int rp, typename P::Reg (&r)[kRegs], const typename P::Cst& c,
-                                               uint32_t lt, const uint32_t (&lj)[kRegs], uint32_t lc) {
-  if (rp == 0) u2_regs<P, CLS, 0>(r, c, lt, lj, lc);
-  else if (rp == 1) u2_regs<P, CLS, 1>(r, c, lt, lj, lc);
-  else u2_regs<P, CLS, 2>(r, c, lt, lj, lc);
-}
-
-template <class P>
-__device__ __forceinline__ void u2_dispatch(int cls, int rp, typename P::Reg (&r)[kRegs], const typename P::Cst& c,
-                                            uint32_t lt, const uint32_t (&lj)[kRegs], uint32_t lc) {
-  switch (cls) {
-    case U2_GENERAL: u2_dispatch_rp<P, U2_GENERAL>(rp, r, c, lt, lj, lc); break;
-    case U2_REAL: u2_dispatch_rp<P, U2_REAL>(rp, r, c, lt, lj, lc); break;
-    case U2_RXLIKE: u2_dispatch_rp<P, U2_RXLIKE>(rp, r, c, lt, lj, lc); break;
-    case U2_DIAG: u2_dispatch_rp<P, U2_DIAG>(rp, r, c, lt, lj, lc); break;
-    case U2_ANTIDIAG: u2_dispatch_rp<P, U2_ANTIDIAG>(rp, r, c, lt, lj, lc); break;
-    case U2_X: u2_dispatch_rp<P, U2_X>(rp, r, c, lt, lj, lc); break;
-    default: u2_dispatch_rp<P, U2_IMAG_ANTI>(rp, r, c, lt, lj, lc); break;
-  }
-}
-
-template <class P, int CLS>
-__device__ __forceinline__ void phase_regs(typename P::Reg (&r)[kRegs], const typename P::Cst& c, uint32_t lt,
-                                           const uint32_t (&lj)[kRegs], uint32_t lm) {
+template <class P, int CLS, bool COND>
+__device__ __forceinline__ void phase_regs(typename P::Reg (&r)[kRegs], const typename P::Cst& c, uint32_t cr) {
 #pragma unroll
   for (int j = 0; j < kRegs; ++j)
-    if (((lt | lj[j]) & lm) == lm) r[j] = P::template phase<CLS>(c, r[j]);
+    if (!COND || (j & cr) == cr) r[j] = P::template phase<CLS>(c, r[j]);
 }
 
 template <class P, int A, int B>  // swap register bits A < B: pairs with bit A = 1, bit B = 0
-__device__ __forceinline__ void swap_regs(typename P::Reg (&r)[kRegs], uint32_t lt, const uint32_t (&lj)[kRegs],
-                                          uint32_t lc, bool iswap) {
+__device__ __forceinline__ void swap_regs(typename P::Reg (&r)[kRegs], uint32_t cr, bool iswap) {
 #pragma unroll
   for (int j = 0; j < kRegs; ++j) {
     if (((j >> A) & 1) && !((j >> B) & 1)) {
       const int p = j ^ (1 << A) ^ (1 << B);
-      if (((lt | lj[j]) & lc) == lc) {
+      if ((j & cr) == cr) {
         typename P::Reg a = r[j], b = r[p];
         if (iswap) {
           r[j] = P::times_i(b);
@@ -343,11 +362,14 @@ __device__ __forceinline__ void swap_regs(typename P::Reg (&r)[kRegs], uint32_t 
 
 // dense 2^dk block applied in shared memory (exact policies only)
 template <class P>
-__device__ void dense_smem(unsigned char* buf, const TOp& op, const double* dense, const TileGeo& g) {
+__device__ void dense_smem(unsigned char* buf, const KOp& op, const double* dense, const TileGeo& g) {
   using V = typename P::Reg;
   constexpr int E = P::kElem;
-  const int dk = op.dk, D = 1 << dk;
-  const double* M = dense + 2 * op.doff;
+  const int dk = (int)op.tmask, D = 1 << dk;
+  const double* M = dense + 2 * (int64_t)op.tval;
+  int dbits[5];
+#pragma unroll
+  for (int j = 0; j < 5; ++j) dbits[j] = (op.rmr >> (4 * j)) & 15;
   constexpr int kMaxItems = 16;
   V out[kMaxItems];
   int cnt = 0;
@@ -355,14 +377,14 @@ __device__ void dense_smem(unsigned char* buf, const TOp& op, const double* dens
     const int grp = idx >> dk, row = idx & (D - 1);
     uint32_t lg = grp;
     for (int j = 0; j < dk; ++j) {
-      const int b = op.dbits[j];
+      const int b = dbits[j];
       lg = ((lg >> b) << (b + 1)) | (lg & ((1u << b) - 1));
     }
     double ar = 0, ai = 0;
     for (int col = 0; col < D; ++col) {
       uint32_t lc = lg;
       for (int j = 0; j < dk; ++j)
-        if ((col >> j) & 1) lc |= 1u << op.dbits[j];
+        if ((col >> j) & 1) lc |= 1u << dbits[j];
       const V x = P::load_work(buf, swz<E>(lc));
       const double mr = M[2 * (row * D + col)], mi = M[2 * (row * D + col) + 1];
       ar = fma(mr, (double)x.x, fma(-mi, (double)x.y, ar));
@@ -379,62 +401,69 @@ __device__ void dense_smem(unsigned char* buf, const TOp& op, const double* dens
     const int grp = idx >> dk, row = idx & (D - 1);
     uint32_t lg = grp;
     for (int j = 0; j < dk; ++j) {
-      const int b = op.dbits[j];
+      const int b = dbits[j];
       lg = ((lg >> b) << (b + 1)) | (lg & ((1u << b) - 1));
     }
     for (int j = 0; j < dk; ++j)
-      if ((row >> j) & 1) lg |= 1u << op.dbits[j];
+      if ((row >> j) & 1) lg |= 1u << dbits[j];
     P::store_work(buf, swz<E>(lg), out[cnt]);
   }
   __syncthreads();
 }
 
+#define QG_U2_CASES(CLS)                                                                              \
+  case KC_U2 + CLS * 4 + 0: u2_regs<P, CLS, 0, false>(r, kcst<P>(op), 0); break;                      \
+  case KC_U2 + CLS * 4 + 1: u2_regs<P, CLS, 1, false>(r, kcst<P>(op), 0); break;                      \
+  case KC_U2 + CLS * 4 + 2: u2_regs<P, CLS, 2, false>(r, kcst<P>(op), 0); break;                      \
+  case KF_COND | (KC_U2 + CLS * 4 + 0): if (tc) u2_regs<P, CLS, 0, true>(r, kcst<P>(op), cr); break; \
+  case KF_COND | (KC_U2 + CLS * 4 + 1): if (tc) u2_regs<P, CLS, 1, true>(r, kcst<P>(op), cr); break; \
+  case KF_COND | (KC_U2 + CLS * 4 + 2): if (tc) u2_regs<P, CLS, 2, true>(r, kcst<P>(op), cr); break;
+
+#define QG_PHASE_CASES(CLS)                                                                         \
+  case KC_PHASE + CLS: phase_regs<P, CLS, false>(r, kcst<P>(op), 0); break;                         \
+  case KF_COND | (KC_PHASE + CLS): if (tc) phase_regs<P, CLS, true>(r, kcst<P>(op), cr); break;
+
 // Apply the pass's ops to the tile in buf. Returns with the tile in raw format.
 template <class P>
-__device__ void run_ops(unsigned char* buf, const PassDesc& pd, const TOp* __restrict__ ops,
-                        const double* __restrict__ dense, uint64_t base, const TileGeo& g) {
+__device__ void run_ops(unsigned char* buf, const KOp* __restrict__ sops, int nops, const double* __restrict__ dense,
+                        uint64_t base, const TileGeo& g) {
   using Reg = typename P::Reg;
   constexpr int E = P::kElem;
   Reg r[kRegs];
-  uint32_t lj[kRegs];
+  int pos[kRegs];  // swizzled shared-memory slot of register j in the current layout
   uint32_t lt = 0;
   bool in_regs = false, raw = true;
-  for (int64_t o = pd.op_begin; o < pd.op_end; ++o) {
-    const TOp& op = ops[o];
-    const int kind = op.kind;
-    if (kind == OK_LAYOUT) {
+  for (int o = 0; o < nops; ++o) {
+    const KOp& op = sops[o];  // shared memory: a broadcast read
+    const int code = op.code;
+    if (code == KC_LAYOUT) {
       if (in_regs) {
 #pragma unroll
-        for (int j = 0; j < kRegs; ++j) P::store_work(buf, swz<E>(lt | lj[j]), r[j]);
+        for (int j = 0; j < kRegs; ++j) P::store_work(buf, pos[j], r[j]);
         raw = false;
         __syncthreads();
       }
-      // thread bits: local positions not in the register set, ascending
-      const uint32_t rbmask = (1u << op.dbits[0]) | (1u << op.dbits[1]) | (1u << op.dbits[2]);
-      lt = 0;
-      int tb = 0;
-      for (int b = 0; b < g.k; ++b) {
-        if (rbmask & (1u << b)) continue;
-        lt |= ((threadIdx.x >> tb) & 1u) << b;
-        ++tb;
-      }
+      // thread bits: insert zeros at the three register positions (ascending)
+      lt = threadIdx.x;
+      const uint32_t rb[3] = {op.tmask, op.tval, op.rmr};
 #pragma unroll
-      for (int j = 0; j < kRegs; ++j)
-        lj[j] = ((j & 1) << op.dbits[0]) | (((j >> 1) & 1) << op.dbits[1]) | (((j >> 2) & 1) << op.dbits[2]);
+      for (int q = 0; q < 3; ++q) lt = ((lt >> rb[q]) << (rb[q] + 1)) | (lt & ((1u << rb[q]) - 1));
+#pragma unroll
+      for (int j = 0; j < kRegs; ++j) pos[j] = swz<E>(lt | __float_as_uint(op.c[j]));
       if (raw) {
 #pragma unroll
-        for (int j = 0; j < kRegs; ++j) r[j] = P::load_raw(buf, swz<E>(lt | lj[j]));
+        for (int j = 0; j < kRegs; ++j) r[j] = P::load_raw(buf, pos[j]);
       } else {
 #pragma unroll
-        for (int j = 0; j < kRegs; ++j) r[j] = P::load_work(buf, swz<E>(lt | lj[j]));
+        for (int j = 0; j < kRegs; ++j) r[j] = P::load_work(buf, pos[j]);
       }
       in_regs = true;
       continue;
     }
-    if (kind == OK_DENSE) {
+    if (code == KC_DENSE) {
       if (in_regs) {
 #pragma unroll
-        for (int j = 0; j < kRegs; ++j) P::store_work(buf, swz<E>(lt | lj[j]), r[j]);
+        for (int j = 0; j < kRegs; ++j) P::store_work(buf, pos[j], r[j]);
         in_regs = false;
         raw = false;
         __syncthreads();
@@ -442,65 +471,70 @@ __device__ void run_ops(unsigned char* buf, const PassDesc& pd, const TOp* __res
       if constexpr (P::kDense) dense_smem<P>(buf, op, dense, g);
       continue;
     }
-    const typename P::Cst c = P::cst(op);
-    switch (kind) {
-      case OK_U2:
-        if ((base & op.gcmask) == op.gcmask) u2_dispatch<P>(op.cls, op.t2, r, c, lt, lj, op.lcmask);
-        break;
-      case OK_PHASE:
-        if ((base & op.gmask) == op.gmask) {
-          switch (op.cls) {
-            case PH_GENERAL: phase_regs<P, PH_GENERAL>(r, c, lt, lj, op.lmask); break;
-            case PH_NEG: phase_regs<P, PH_NEG>(r, c, lt, lj, op.lmask); break;
-            case PH_I: phase_regs<P, PH_I>(r, c, lt, lj, op.lmask); break;
-            default: phase_regs<P, PH_MINUS_I>(r, c, lt, lj, op.lmask); break;
+    bool tc = true;
+    uint32_t cr = 0;
+    if (code & KF_COND) {
+      tc = ((base & op.gmask) == op.gval) && ((lt & op.tmask) == op.tval);
+      cr = op.rmr & 0xFFu;
+    }
+    switch (code) {
+      QG_U2_CASES(U2_GENERAL)
+      QG_U2_CASES(U2_REAL)
+      QG_U2_CASES(U2_RXLIKE)
+      QG_U2_CASES(U2_DIAG)
+      QG_U2_CASES(U2_ANTIDIAG)
+      QG_U2_CASES(U2_X)
+      QG_U2_CASES(U2_IMAG_ANTI)
+      QG_PHASE_CASES(PH_GENERAL)
+      QG_PHASE_CASES(PH_NEG)
+      QG_PHASE_CASES(PH_I)
+      QG_PHASE_CASES(PH_MINUS_I)
+      default: {
+        const int k = code & 0xFF;
+        if (k >= KC_SWAP && k < KC_SWAP + 6) {
+          if (tc) {
+            const int pr = (k - KC_SWAP) % 3;
+            const bool isw = (k - KC_SWAP) >= 3;
+            if (pr == 0) swap_regs<P, 0, 1>(r, cr, isw);
+            else if (pr == 1) swap_regs<P, 0, 2>(r, cr, isw);
+            else swap_regs<P, 1, 2>(r, cr, isw);
           }
-        }
-        break;
-      case OK_SWAP:
-        if ((base & op.gcmask) == op.gcmask) {
-          const int a = op.dbits[0], b = op.dbits[1];  // register positions, a < b
-          const bool isw = op.flags & 1;
-          if (a == 0 && b == 1) swap_regs<P, 0, 1>(r, lt, lj, op.lcmask, isw);
-          else if (a == 0) swap_regs<P, 0, 2>(r, lt, lj, op.lcmask, isw);
-          else swap_regs<P, 1, 2>(r, lt, lj, op.lcmask, isw);
-        }
-        break;
-      case OK_BLOCKADE: {
-        const int gc = __popcll(base & op.gmask);
-        if (gc <= 1) {
+        } else if (k == KC_BLOCKADE) {
+          const int cnt = __popcll(base & op.gmask) + __popc(lt & op.tmask);
+          if (cnt <= 1) {
+            const typename P::Cst c = kcst<P>(op);
 #pragma unroll
-          for (int j = 0; j < kRegs; ++j)
-            if (gc + __popc((lt | lj[j]) & op.lmask) == 1) r[j] = P::cmul_idx(c, 0, r[j]);
+            for (int j = 0; j < kRegs; ++j)
+              if (cnt + __popc(j & cr) == 1) r[j] = P::cmul_idx(c, 0, r[j]);
+          }
+        } else if (k == KC_PARITY) {
+          const int par = (__popcll(base & op.gmask) + __popc(lt & op.tmask)) & 1;
+          const typename P::Cst c = kcst<P>(op);
+#pragma unroll
+          for (int j = 0; j < kRegs; ++j) r[j] = P::cmul_idx(c, par ^ (__popc(j & cr) & 1), r[j]);
+        } else if (k == KC_COLLAPSE) {
+          const typename P::Cst c = kcst<P>(op);
+          const uint32_t rv = (op.rmr >> 8) & 0xFFu;
+#pragma unroll
+          for (int j = 0; j < kRegs; ++j) r[j] = (tc && (j & cr) == rv) ? P::scale(c, r[j]) : P::zero();
         }
       } break;
-      case OK_PARITY: {
-        const int gp = __popcll(base & op.gmask) & 1;
-#pragma unroll
-        for (int j = 0; j < kRegs; ++j)
-          r[j] = P::cmul_idx(c, gp ^ (__popc((lt | lj[j]) & op.lmask) & 1), r[j]);
-      } break;
-      case OK_COLLAPSE: {
-        const bool gok = (base & op.gmask) == op.gval;
-#pragma unroll
-        for (int j = 0; j < kRegs; ++j)
-          r[j] = (gok && (((lt | lj[j]) & op.lmask) == op.lval)) ? P::scale(c, r[j]) : P::zero();
-      } break;
-      default:
-        break;
     }
   }
   if (in_regs) {
 #pragma unroll
-    for (int j = 0; j < kRegs; ++j) P::store_raw(buf, swz<E>(lt | lj[j]), r[j]);
+    for (int j = 0; j < kRegs; ++j) P::store_raw(buf, pos[j], r[j]);
   }
   __syncthreads();
 }
 
+#undef QG_U2_CASES
+#undef QG_PHASE_CASES
+
 template <class P>
-__global__ void __launch_bounds__(512, 1) k_tile2(unsigned char* __restrict__ state, PassDesc pd,
-                                                   const TOp* __restrict__ ops, const double* __restrict__ dense,
-                                                   uint64_t ntiles) {
+__global__ void __launch_bounds__(512, 1) k_tile2(unsigned char* __restrict__ state, const PassDesc pd,
+                                                  const KOp* __restrict__ kops, int nops,
+                                                  const double* __restrict__ dense, uint64_t ntiles) {
   constexpr int E = P::kElem;
   extern __shared__ __align__(128) unsigned char smem[];
   TileGeo g;
@@ -509,8 +543,15 @@ __global__ void __launch_bounds__(512, 1) k_tile2(unsigned char* __restrict__ st
   g.klow = pd.klow;
   g.T = blockDim.x;
   const size_t tile_bytes = (size_t)g.K * E;
-  uint64_t* hioff = reinterpret_cast<uint64_t*>(smem + 2 * tile_bytes);
   const int nhi = 1 << (g.k - g.klow);
+  KOp* sops = reinterpret_cast<KOp*>(smem + 2 * tile_bytes);  // 16-byte aligned: tile_bytes % 16 == 0
+  uint64_t* hioff = reinterpret_cast<uint64_t*>(sops + nops);
+  {  // stage the pass's op records (96 bytes each) in shared memory
+    const uint4* src = reinterpret_cast<const uint4*>(kops);
+    uint4* dst = reinterpret_cast<uint4*>(sops);
+    const int words = nops * (int)(sizeof(KOp) / 16);
+    for (int w = threadIdx.x; w < words; w += g.T) dst[w] = src[w];
+  }
   for (int h = threadIdx.x; h < nhi; h += g.T) {
     uint64_t off = 0;
     for (int j = g.klow; j < g.k; ++j)
@@ -534,41 +575,129 @@ __global__ void __launch_bounds__(512, 1) k_tile2(unsigned char* __restrict__ st
     }
     __syncthreads();
     const uint64_t base = tile_base(pd, tile);
-    run_ops<P>(cur, pd, ops, dense, base, g);
+    run_ops<P>(cur, sops, nops, dense, base, g);
     store_tile<E>(cur, state, base, hioff, g);
     __syncthreads();  // the buffer is refilled two tiles later
   }
 }
 
+// Host: translate TOps into the compact records of policy P.
 template <class P>
-cudaError_t launch_t(void* s, int n, const PassDesc& pd, const TOp* d_tops, const double* d_dense,
-                     cudaStream_t st) {
+void build_kops(KOp* out, const TOp* ops, int64_t nops) {
+  std::memset(out, 0, sizeof(KOp) * (size_t)nops);
+  for (int64_t o = 0; o < nops; ++o) {
+    const TOp& t = ops[o];
+    KOp& k = out[o];
+    if (t.kind == OK_LAYOUT) {
+      k.code = KC_LAYOUT;
+      k.tmask = t.dbits[0];
+      k.tval = t.dbits[1];
+      k.rmr = t.dbits[2];
+      for (int j = 0; j < 8; ++j) std::memcpy(&k.c[j], &t.lj[j], 4);
+      continue;
+    }
+    if (t.kind == OK_DENSE) {
+      k.code = KC_DENSE;
+      k.tmask = t.dk;
+      k.tval = (uint32_t)t.doff;
+      for (int j = 0; j < t.dk; ++j) k.rmr |= (uint32_t)t.dbits[j] << (4 * j);
+      continue;
+    }
+    if (std::is_same<P, PolD>::value) {
+      std::memcpy(k.c, t.m, sizeof(double) * 8);
+    } else {
+      std::memcpy(k.c, t.mf, sizeof(float) * 16);
+    }
+    k.tmask = t.tmask;
+    k.tval = t.tval;
+    k.rmr = t.rmask | (t.rval << 8);
+    bool cond = t.tmask != 0 || t.rmask != 0;
+    switch (t.kind) {
+      case OK_U2:
+        k.code = KC_U2 + t.cls * 4 + t.t2;
+        k.gmask = k.gval = t.gcmask;
+        cond = cond || t.gcmask != 0;
+        break;
+      case OK_PHASE:
+        k.code = KC_PHASE + t.cls;
+        k.gmask = k.gval = t.gmask;
+        cond = cond || t.gmask != 0;
+        break;
+      case OK_SWAP: {
+        const int a = t.dbits[0], b = t.dbits[1];
+        const int pr = (a == 0 && b == 1) ? 0 : (a == 0 ? 1 : 2);
+        k.code = KC_SWAP + pr + 3 * (t.flags & 1);
+        k.gmask = k.gval = t.gcmask;
+        cond = true;
+      } break;
+      case OK_BLOCKADE:
+        k.code = KC_BLOCKADE;
+        k.gmask = t.gmask;
+        cond = true;
+        break;
+      case OK_PARITY:
+        k.code = KC_PARITY;
+        k.gmask = t.gmask;
+        cond = true;
+        break;
+      default:  // OK_COLLAPSE
+        k.code = KC_COLLAPSE;
+        k.gmask = t.gmask;
+        k.gval = t.gval;
+        cond = true;
+        break;
+    }
+    if (cond) k.code |= KF_COND;
+  }
+}
+
+template <class P>
+cudaError_t launch_t(void* s, int n, const PassDesc& pd, const void* d_kops, const double* d_dense, cudaStream_t st) {
   constexpr int E = P::kElem;
   const int K = 1 << pd.k;
   const int threads = K / kRegs;
-  if (threads < 1 || threads > 512 || (K * E) % 16 != 0 || K * E < 16 * threads) return cudaErrorInvalidValue;
-  const size_t smem = 2 * (size_t)K * E + sizeof(uint64_t) * (1u << (pd.k - pd.klow));
+  const int nops = (int)(pd.op_end - pd.op_begin);
+  if (threads < 1 || threads > 512 || (K * E) % 16 != 0 || K * E < 16 * threads || nops > kMaxKOps)
+    return cudaErrorInvalidValue;
+  const size_t smem = 2 * (size_t)K * E + sizeof(KOp) * (size_t)nops + sizeof(uint64_t) * (1u << (pd.k - pd.klow));
   const uint64_t ntiles = 1ULL << (n - pd.k);
   int per_sm = (int)((220 * 1024) / smem);
   if (per_sm > 2048 / threads) per_sm = 2048 / threads;
   if (per_sm < 1) per_sm = 1;
   uint64_t grid = (uint64_t)kSMs * per_sm;
   if (grid > ntiles) grid = ntiles;
-  cudaError_t e = cudaFuncSetAttribute(k_tile2<P>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  // One fixed limit for every launch: worker threads launch passes of different
+  // sizes concurrently, and a per-launch value could undercut another thread's launch.
+  // two 64 KiB tile buffers, the largest op list, the chunk-offset table
+  constexpr size_t kSmemLimit = 2 * (size_t(64) << 10) + sizeof(KOp) * kMaxKOps + 8 * 256;
+  static_assert(kSmemLimit <= 227 * 1024, "shared memory");
+  if (smem > kSmemLimit) return cudaErrorInvalidValue;
+  cudaError_t e = cudaFuncSetAttribute(k_tile2<P>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmemLimit);
   if (e != cudaSuccess) return e;
-  k_tile2<P><<<(unsigned)grid, threads, smem, st>>>((unsigned char*)s, pd, d_tops, d_dense, ntiles);
+  const KOp* ops = reinterpret_cast<const KOp*>(d_kops) + pd.op_begin;
+  k_tile2<P><<<(unsigned)grid, threads, smem, st>>>((unsigned char*)s, pd, ops, nops, d_dense, ntiles);
   count_launch(1);
   return cudaGetLastError();
 }
 
 }  // namespace
 
-cudaError_t launch_tile_pass(void* s, int precision, int arithmetic, int n, const PassDesc& pd, const TOp* d_tops,
+int max_ops_per_tile_pass() { return kMaxKOps; }
+size_t kop_record_bytes() { return sizeof(KOp); }
+
+void encode_kops(int precision, int arithmetic, const TOp* tops, int64_t count, void* out) {
+  KOp* k = reinterpret_cast<KOp*>(out);
+  if (precision == QG_C64) build_kops<PolF>(k, tops, count);
+  else if (arithmetic == QG_ARITH_DOUBLE_FLOAT) build_kops<PolDF>(k, tops, count);
+  else build_kops<PolD>(k, tops, count);
+}
+
+cudaError_t launch_tile_pass(void* s, int precision, int arithmetic, int n, const PassDesc& pd, const void* d_kops,
                              const double* d_dense, cudaStream_t st) {
   if (pd.k < 3 || pd.k > kMaxTileBits) return cudaErrorInvalidValue;
-  if (precision == QG_C64) return launch_t<PolF>(s, n, pd, d_tops, d_dense, st);
-  if (arithmetic == QG_ARITH_DOUBLE_FLOAT) return launch_t<PolDF>(s, n, pd, d_tops, d_dense, st);
-  return launch_t<PolD>(s, n, pd, d_tops, d_dense, st);
+  if (precision == QG_C64) return launch_t<PolF>(s, n, pd, d_kops, d_dense, st);
+  if (arithmetic == QG_ARITH_DOUBLE_FLOAT) return launch_t<PolDF>(s, n, pd, d_kops, d_dense, st);
+  return launch_t<PolD>(s, n, pd, d_kops, d_dense, st);
 }
 
 }  // namespace qg
