@@ -333,6 +333,39 @@ def main():
             ms64 = a.elapsed_time(b) / args.steps
             line["c64"] = {"value": gates * N / (ms64 / 1e3), "ms_per_step": ms64}
             st64.close()
+        # batched parameter sweep: 1024 QAOA MaxCut circuits (p=3, n uniform over 12..24 even),
+        # one launch per pass over all states of a size, replayed from CUDA graphs
+        from qclojure_gb300.sweep import Sweep
+
+        st.close()
+        qc_list = workloads.qaoa_sweep(1024, 3, seed=7)
+        hams = [c["hamiltonian"] for c in qc_list]
+        qaoa = {}
+        for prec, arith in (("c64", "exact"), ("c128", "double-float")):
+            with Sweep(ctx, qc_list, precision=prec, arithmetic=arith) as sw:
+                for _ in range(2):
+                    sw.run(hams)
+                t0 = time.perf_counter()
+                reps = 3
+                for _ in range(reps):
+                    en, sst = sw.run(hams)
+                dt = (time.perf_counter() - t0) / reps
+                qaoa[prec] = {"circuits_per_s": len(qc_list) / dt, "ms_per_sweep": dt * 1e3,
+                              "device_ms": sst["device-ms"], "energy_ms": sst["expect-ms"],
+                              "launches": sst["launches"], "graphs": sst["graphs"],
+                              "state_gib": sst["state-bytes"] / 2**30}
+        # plain per-circuit complex128 (one HBM pass per gate, one job at a time) on a sample
+        sample = qc_list[:48]
+        t0 = time.perf_counter()
+        for c in sample:
+            with ctx.state(c["num-qubits"], "c128") as s1:
+                s1.apply(c, fusion="plain")
+                s1.hamiltonian([(t["coefficient"], t["pauli-string"]) for t in c["hamiltonian"]])
+        dt = time.perf_counter() - t0
+        qaoa["plain_c128_per_circuit"] = {"circuits_per_s": len(sample) / dt, "sample": len(sample)}
+        qaoa["workload"] = "1024 QAOA MaxCut p=3, random 3-regular graphs, n uniform in {12,...,24}"
+        line["qaoa_sweep"] = qaoa
+
         # end to end through the job API: circuit in, 1024-shot histogram out (host buffers)
         from qclojure_gb300.backend import create_simulator, execute_circuit
 

@@ -291,6 +291,39 @@ int qg_state_measure(void* state, const int32_t* qubits, int32_t count, uint64_t
 int qg_state_device_ptr(void* state, void** dptr, void** stream);
 int qg_state_synchronize(void* state);
 
+/* ---- parameter sweeps: many circuits of one structure, replayed -------------
+   The variational loop of the reference (application/algorithm/variational_algorithm.clj:310-363,
+   qaoa.clj:1087-1115) executes the same circuit structure with new angles, one
+   execute-circuit per parameter vector. A sweep holds one device state per circuit;
+   circuits of equal qubit count and equal pass structure run together, one kernel
+   launch per HBM pass over all of their states, captured once into a CUDA graph and
+   replayed. Every run starts from |0...0>. */
+typedef struct qg_sweep_stats {
+  double device_ms;       /* CUDA-event time of the gate passes (graph replays)   */
+  double expect_ms;       /* CUDA-event time of the energy kernels                */
+  int32_t groups;         /* batches of equal structure                           */
+  int32_t launches;       /* kernel launches per run (inside the graphs)          */
+  int32_t graphs;         /* groups replayed from a CUDA graph                    */
+  int32_t reserved;
+  uint64_t state_bytes;   /* HBM held by the sweep's states                       */
+} qg_sweep_stats;
+
+/* Compile circuits (no mid-circuit measurement), allocate their states, capture graphs. */
+int qg_sweep_create(void* ctx, const qg_circuit* circuits, int32_t count, int32_t precision, int32_t arithmetic,
+                    void** sweep_out);
+/* New parameters for the same circuits: op records are rewritten in place; a circuit
+   whose pass structure changed makes this return QG_ERR_INVALID_ARG. */
+int qg_sweep_update(void* sweep, const qg_circuit* circuits, int32_t count);
+/* Run every circuit and evaluate one Hamiltonian per circuit: circuit c owns terms
+   [term_offsets[c], term_offsets[c+1]) of coefficients / pauli_strings (strings of
+   that circuit's num_qubits chars, concatenated in term order). energies[c] =
+   sum_j c_j <P_j> (hamiltonian.clj:96-114). term_offsets may be NULL (no energies). */
+int qg_sweep_run(void* sweep, const int32_t* term_offsets, const double* coefficients, const char* pauli_strings,
+                 double* energies, qg_sweep_stats* stats);
+/* Copy circuit c's final state (complex128) to the host. */
+int qg_sweep_state(void* sweep, int32_t c, double* host_c128);
+int qg_sweep_destroy(void* sweep);
+
 /* ---- measurement (no counterpart in the reference) ----------------------------
    qg_state_profile applies a circuit like qg_state_apply and records a CUDA event
    pair around every HBM pass on the state's stream: pass_ms[i] is the duration of

@@ -119,6 +119,12 @@ class QgJobInfo(C.Structure):
                 ("has_results", C.c_int32), ("error_code", C.c_int32)]
 
 
+class QgSweepStats(C.Structure):
+    _fields_ = [("device_ms", C.c_double), ("expect_ms", C.c_double), ("groups", C.c_int32),
+                ("launches", C.c_int32), ("graphs", C.c_int32), ("reserved", C.c_int32),
+                ("state_bytes", C.c_uint64)]
+
+
 P = C.c_void_p
 U64 = C.c_uint64
 I32 = C.c_int32
@@ -174,6 +180,11 @@ SIGNATURES = {
     "qg_state_synchronize": ([P], C.c_int),
     "qg_state_profile": ([P, C.POINTER(QgCircuit), I32, U64, C.POINTER(C.c_float), I32P, I32, I32P], C.c_int),
     "qg_kernel_launches": ([U64P], C.c_int),
+    "qg_sweep_create": ([P, C.POINTER(QgCircuit), I32, I32, I32, C.POINTER(P)], C.c_int),
+    "qg_sweep_update": ([P, C.POINTER(QgCircuit), I32], C.c_int),
+    "qg_sweep_run": ([P, I32P, DP, C.c_char_p, DP, C.POINTER(QgSweepStats)], C.c_int),
+    "qg_sweep_state": ([P, I32, DP], C.c_int),
+    "qg_sweep_destroy": ([P], C.c_int),
 }
 
 

@@ -141,11 +141,23 @@ int tile_bits_for(int n, int precision);
 
 cudaError_t launch_set_basis(void* s, int precision, int n, uint64_t idx, cudaStream_t st);
 cudaError_t launch_plain_op(void* s, int precision, int n, const GOp& op, cudaStream_t st);
-// d_kops: the program's compact op records on the device (encode_kops), indexed by the pass's op range.
-cudaError_t launch_tile_pass(void* s, int precision, int arithmetic, int n, const PassDesc& pd, const void* d_kops,
-                             const double* d_dense, cudaStream_t st);
+// One tiled pass over nstates states of n qubits sharing the pass structure pd.
+// d_states: device array of amplitude pointers; d_kops: compact op records on the
+// device (encode_kops) for state 0, indexed by pd's op range; state s uses the
+// records ops_stride further on (0: all states share one list).
+cudaError_t launch_tile_pass(int precision, int arithmetic, int n, const PassDesc& pd, void* const* d_states,
+                             int nstates, const void* d_kops, int64_t ops_stride, const double* d_dense,
+                             cudaStream_t st);
 int max_ops_per_tile_pass();
 size_t kop_record_bytes();
+// batched sweep kernels (sweep.cu)
+int diag_max_groups();
+size_t diag_state_bytes();
+void fill_diag_state(void* out, uint64_t zoff, int ngroups, const int* gcount);
+cudaError_t launch_batch_zero(void* slab, int precision, int n, int nstates, cudaStream_t st);
+cudaError_t launch_diag_expect(void* const* d_states, int precision, int n, const void* d_diag, const uint64_t* d_z,
+                               int nstates, double* d_partial, const double* d_gcoef, double* d_energies,
+                               cudaStream_t st);
 void encode_kops(int precision, int arithmetic, const TOp* tops, int64_t count, void* out);
 void count_launch(int k);
 cudaError_t launch_c128_to_c64(const double* src, float* dst, uint64_t count, cudaStream_t st);

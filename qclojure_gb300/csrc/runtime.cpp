@@ -46,6 +46,7 @@ struct State {
   cudaStream_t stream = nullptr;
   bool own_stream = false;
   double* d_part = nullptr;  // reduction partials: 4 * reduce_blocks doubles
+  void** d_self = nullptr;   // device copy of d (the tiled kernel takes an array of states)
   int nblocks = 0;
   std::string err;
 };
@@ -70,12 +71,16 @@ static int state_alloc(State* s, int n, int prec, cudaStream_t stream, std::stri
   s->nblocks = reduce_blocks_for(n);
   CK(cudaMallocAsync(&s->d, s->bytes, stream), "cudaMallocAsync(state)");
   CK(cudaMallocAsync((void**)&s->d_part, sizeof(double) * 4 * s->nblocks, stream), "cudaMallocAsync(partials)");
+  CK(cudaMallocAsync((void**)&s->d_self, sizeof(void*), stream), "cudaMallocAsync(self)");
+  CK(cudaMemcpyAsync(s->d_self, &s->d, sizeof(void*), cudaMemcpyHostToDevice, stream), "H2D self");
   return QG_OK;
 }
 
 static void state_release(State* s) {
   if (s->d) cudaFreeAsync(s->d, s->stream);
   if (s->d_part) cudaFreeAsync(s->d_part, s->stream);
+  if (s->d_self) cudaFreeAsync(s->d_self, s->stream);
+  s->d_self = nullptr;
   s->d = nullptr;
   s->d_part = nullptr;
 }
@@ -301,7 +306,7 @@ static int exec_program(State* s, const Program& prog, uint64_t seed, const std:
     if (st.kind == Step::PLAIN_OP) {
       e = launch_plain_op(s->d, s->prec, s->n, st.op, s->stream);
     } else if (st.kind == Step::TILE_PASS) {
-      e = launch_tile_pass(s->d, s->prec, prog.arith, s->n, st.pass, d_kops, d_dense, s->stream);
+      e = launch_tile_pass(s->prec, prog.arith, s->n, st.pass, s->d_self, 1, d_kops, 0, d_dense, s->stream);
     } else {
       rc = do_measure(s, st.mqubits, seed, measure_index++, nullptr, nullptr, err);
     }
@@ -1601,6 +1606,434 @@ int qg_state_profile(void* state, const qg_circuit* circuit, int32_t fusion, uin
 int qg_kernel_launches(uint64_t* count) {
   if (!count) return QG_ERR_INVALID_ARG;
   *count = kernel_launch_count();
+  return QG_OK;
+}
+
+}  // extern "C"
+
+// ===========================================================================
+// Parameter sweeps (batched states of one structure, CUDA-graph replays)
+// ===========================================================================
+namespace qg {
+
+struct SweepGroup {
+  int n = 0;
+  std::vector<int> members;              // circuit indices
+  std::vector<Program> progs;            // one per member; equal pass structure
+  std::vector<int> pass_steps;           // TILE_PASS step indices
+  std::vector<int64_t> pass_off;         // first op record of each pass in d_kops
+  std::vector<int> pass_nops;
+  bool batched = true;                   // false: members run one by one (small or measured circuits)
+  void* slab = nullptr;
+  void** d_states = nullptr;
+  void* d_kops = nullptr;
+  std::vector<unsigned char> kops_host;
+  std::vector<std::unique_ptr<State>> views;
+  cudaGraphExec_t exec = nullptr;
+  int launches = 0;
+};
+
+struct Sweep {
+  Ctx* ctx = nullptr;
+  int prec = QG_C128, arith = QG_ARITH_EXACT;
+  cudaStream_t stream = nullptr;
+  int count = 0;
+  std::vector<SweepGroup> groups;
+  std::vector<std::pair<int, int>> where;  // circuit -> (group, member)
+  uint64_t bytes = 0;
+};
+
+static std::vector<int64_t> pass_signature(const Program& p) {
+  std::vector<int64_t> sig{p.n};
+  for (const Step& s : p.steps) {
+    if (s.kind != Step::TILE_PASS) {
+      sig.push_back(-1 - (int)s.kind);
+      continue;
+    }
+    sig.push_back(s.pass.k);
+    sig.push_back(s.pass.klow);
+    for (int j = 0; j < s.pass.k; ++j) sig.push_back(s.pass.lbits[j]);
+    sig.push_back(s.pass.op_end - s.pass.op_begin);
+  }
+  return sig;
+}
+
+static int view_init(State* v, Ctx* c, void* d, int n, int prec, cudaStream_t st, std::string* err) {
+  v->ctx = c;
+  v->n = n;
+  v->prec = prec;
+  v->d = d;
+  v->bytes = amp_bytes(prec) << n;
+  v->stream = st;
+  v->nblocks = reduce_blocks_for(n);
+  CK(cudaMallocAsync((void**)&v->d_part, sizeof(double) * 4 * v->nblocks, st), "alloc partials");
+  CK(cudaMallocAsync((void**)&v->d_self, sizeof(void*), st), "alloc self");
+  CK(cudaMemcpyAsync(v->d_self, &v->d, sizeof(void*), cudaMemcpyHostToDevice, st), "H2D self");
+  return QG_OK;
+}
+
+static void encode_group_kops(Sweep* sw, SweepGroup& g) {
+  const size_t rec = kop_record_bytes();
+  for (size_t p = 0; p < g.pass_steps.size(); ++p)
+    for (size_t m = 0; m < g.members.size(); ++m) {
+      const Program& pr = g.progs[m];
+      const PassDesc& pd = pr.steps[g.pass_steps[p]].pass;
+      encode_kops(sw->prec, pr.arith, pr.tops.data() + pd.op_begin, pd.op_end - pd.op_begin,
+                  g.kops_host.data() + rec * (size_t)(g.pass_off[p] + (int64_t)m * g.pass_nops[p]));
+    }
+}
+
+static cudaError_t launch_group_passes(Sweep* sw, SweepGroup& g) {
+  const size_t rec = kop_record_bytes();
+  cudaError_t e = launch_batch_zero(g.slab, sw->prec, g.n, (int)g.members.size(), sw->stream);
+  for (size_t p = 0; p < g.pass_steps.size() && e == cudaSuccess; ++p) {
+    PassDesc pd = g.progs[0].steps[g.pass_steps[p]].pass;
+    pd.op_begin = 0;
+    pd.op_end = g.pass_nops[p];
+    e = launch_tile_pass(sw->prec, g.progs[0].arith, g.n, pd, g.d_states, (int)g.members.size(),
+                         (const unsigned char*)g.d_kops + rec * (size_t)g.pass_off[p], g.pass_nops[p], nullptr,
+                         sw->stream);
+  }
+  return e;
+}
+
+static void sweep_free(Sweep* sw) {
+  for (auto& g : sw->groups) {
+    if (g.exec) cudaGraphExecDestroy(g.exec);
+    for (auto& v : g.views) {
+      if (v->d_part) cudaFreeAsync(v->d_part, sw->stream);
+      if (v->d_self) cudaFreeAsync(v->d_self, sw->stream);
+    }
+    if (g.slab) cudaFreeAsync(g.slab, sw->stream);
+    if (g.d_states) cudaFreeAsync(g.d_states, sw->stream);
+    if (g.d_kops) cudaFreeAsync(g.d_kops, sw->stream);
+  }
+  if (sw->stream) {
+    cudaStreamSynchronize(sw->stream);
+    cudaStreamDestroy(sw->stream);
+  }
+  delete sw;
+}
+
+}  // namespace qg
+
+extern "C" {
+
+int qg_sweep_create(void* ctx, const qg_circuit* circuits, int32_t count, int32_t precision, int32_t arithmetic,
+                    void** sweep_out) {
+  if (!ctx || !circuits || count < 1 || !sweep_out) return QG_ERR_INVALID_ARG;
+  if (precision != QG_C128 && precision != QG_C64) return QG_ERR_INVALID_ARG;
+  Ctx* c = (Ctx*)ctx;
+  cudaSetDevice(c->device);
+  auto* sw = new Sweep();
+  sw->ctx = c;
+  sw->prec = precision;
+  sw->arith = arithmetic == QG_ARITH_DOUBLE_FLOAT ? QG_ARITH_DOUBLE_FLOAT : QG_ARITH_EXACT;
+  sw->count = count;
+  sw->where.resize(count);
+  std::string err;
+  if (cudaStreamCreateWithFlags(&sw->stream, cudaStreamNonBlocking) != cudaSuccess) {
+    delete sw;
+    return QG_ERR_DEVICE;
+  }
+  std::map<std::vector<int64_t>, int> by_sig;
+  for (int i = 0; i < count; ++i) {
+    Program prog;
+    int rc = compile_program(&circuits[i], precision, QG_FUSE_TILED, c->cfg.fuse_k, sw->arith, &prog, &err);
+    if (rc != QG_OK) {
+      set_ctx_error(c, "circuit " + std::to_string(i) + ": " + err);
+      sweep_free(sw);
+      return rc;
+    }
+    std::vector<int64_t> sig = pass_signature(prog);
+    auto it = by_sig.find(sig);
+    int gi;
+    if (it == by_sig.end()) {
+      gi = (int)sw->groups.size();
+      by_sig[sig] = gi;
+      sw->groups.emplace_back();
+      sw->groups.back().n = prog.n;
+    } else {
+      gi = it->second;
+    }
+    SweepGroup& g = sw->groups[gi];
+    sw->where[i] = {gi, (int)g.members.size()};
+    g.members.push_back(i);
+    g.progs.push_back(std::move(prog));
+  }
+  const size_t rec = kop_record_bytes();
+  for (auto& g : sw->groups) {
+    const Program& p0 = g.progs[0];
+    for (size_t s = 0; s < p0.steps.size(); ++s) {
+      if (p0.steps[s].kind != Step::TILE_PASS) g.batched = false;
+      else g.pass_steps.push_back((int)s);
+    }
+    if (!p0.dense.empty()) g.batched = false;
+    const size_t S = g.members.size();
+    const size_t per = amp_bytes(precision) << g.n;
+    cudaError_t e = cudaMallocAsync(&g.slab, per * S, sw->stream);
+    if (e != cudaSuccess) {
+      set_ctx_error(c, "sweep states do not fit in HBM");
+      sweep_free(sw);
+      return QG_ERR_OOM;
+    }
+    sw->bytes += per * S;
+    std::vector<void*> ptrs(S);
+    for (size_t m = 0; m < S; ++m) {
+      ptrs[m] = (unsigned char*)g.slab + per * m;
+      g.views.push_back(std::make_unique<State>());
+      int rc = view_init(g.views.back().get(), c, ptrs[m], g.n, precision, sw->stream, &err);
+      if (rc != QG_OK) {
+        set_ctx_error(c, err);
+        sweep_free(sw);
+        return rc;
+      }
+    }
+    if (cudaMallocAsync((void**)&g.d_states, sizeof(void*) * S, sw->stream) != cudaSuccess ||
+        cudaMemcpyAsync(g.d_states, ptrs.data(), sizeof(void*) * S, cudaMemcpyHostToDevice, sw->stream) !=
+            cudaSuccess) {
+      sweep_free(sw);
+      return QG_ERR_DEVICE;
+    }
+    if (!g.batched) continue;
+    int64_t off = 0;
+    for (int ps : g.pass_steps) {
+      const PassDesc& pd = p0.steps[ps].pass;
+      g.pass_off.push_back(off);
+      g.pass_nops.push_back((int)(pd.op_end - pd.op_begin));
+      off += (int64_t)(pd.op_end - pd.op_begin) * (int64_t)S;
+    }
+    g.kops_host.assign(rec * (size_t)std::max<int64_t>(off, 1), 0);
+    encode_group_kops(sw, g);
+    if (cudaMallocAsync(&g.d_kops, g.kops_host.size(), sw->stream) != cudaSuccess ||
+        cudaMemcpyAsync(g.d_kops, g.kops_host.data(), g.kops_host.size(), cudaMemcpyHostToDevice, sw->stream) !=
+            cudaSuccess) {
+      sweep_free(sw);
+      return QG_ERR_DEVICE;
+    }
+    cudaStreamSynchronize(sw->stream);
+    g.launches = 1 + (int)g.pass_steps.size();
+    // capture the group's passes once; runs replay the graph
+    cudaGraph_t graph = nullptr;
+    if (cudaStreamBeginCapture(sw->stream, cudaStreamCaptureModeThreadLocal) == cudaSuccess) {
+      cudaError_t le = launch_group_passes(sw, g);
+      cudaError_t ce = cudaStreamEndCapture(sw->stream, &graph);
+      if (le == cudaSuccess && ce == cudaSuccess && graph) {
+        if (cudaGraphInstantiate(&g.exec, graph, 0) != cudaSuccess) g.exec = nullptr;
+      }
+      if (graph) cudaGraphDestroy(graph);
+      cudaGetLastError();
+      count_launch(-g.launches);  // captured launches do not run here; replays count them
+    }
+  }
+  if (cudaStreamSynchronize(sw->stream) != cudaSuccess) {
+    sweep_free(sw);
+    return QG_ERR_DEVICE;
+  }
+  *sweep_out = sw;
+  return QG_OK;
+}
+
+int qg_sweep_update(void* sweep, const qg_circuit* circuits, int32_t count) {
+  if (!sweep || !circuits) return QG_ERR_INVALID_ARG;
+  Sweep* sw = (Sweep*)sweep;
+  if (count != sw->count) return QG_ERR_INVALID_ARG;
+  cudaSetDevice(sw->ctx->device);
+  std::string err;
+  for (int i = 0; i < count; ++i) {
+    Program prog;
+    int rc = compile_program(&circuits[i], sw->prec, QG_FUSE_TILED, sw->ctx->cfg.fuse_k, sw->arith, &prog, &err);
+    if (rc != QG_OK) {
+      set_ctx_error(sw->ctx, err);
+      return rc;
+    }
+    SweepGroup& g = sw->groups[sw->where[i].first];
+    Program& old = g.progs[sw->where[i].second];
+    if (pass_signature(prog) != pass_signature(old)) {
+      set_ctx_error(sw->ctx, "circuit " + std::to_string(i) + " changed its structure; create a new sweep");
+      return QG_ERR_INVALID_ARG;
+    }
+    old = std::move(prog);
+  }
+  for (auto& g : sw->groups) {
+    if (!g.batched) continue;
+    encode_group_kops(sw, g);
+    if (cudaMemcpyAsync(g.d_kops, g.kops_host.data(), g.kops_host.size(), cudaMemcpyHostToDevice, sw->stream) !=
+        cudaSuccess)
+      return QG_ERR_DEVICE;
+  }
+  return cudaStreamSynchronize(sw->stream) == cudaSuccess ? QG_OK : QG_ERR_DEVICE;
+}
+
+int qg_sweep_run(void* sweep, const int32_t* term_offsets, const double* coefficients, const char* pauli_strings,
+                 double* energies, qg_sweep_stats* stats) {
+  if (!sweep) return QG_ERR_INVALID_ARG;
+  Sweep* sw = (Sweep*)sweep;
+  cudaSetDevice(sw->ctx->device);
+  std::string err;
+  cudaEvent_t e0, e1, e2;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  cudaEventCreate(&e2);
+  cudaEventRecord(e0, sw->stream);
+  int launches = 0, graphs = 0;
+  int rc = QG_OK;
+  for (auto& g : sw->groups) {
+    if (g.batched) {
+      cudaError_t e = g.exec ? cudaGraphLaunch(g.exec, sw->stream) : launch_group_passes(sw, g);
+      if (e != cudaSuccess) {
+        rc = cuda_fail(&err, e, "sweep passes");
+        break;
+      }
+      launches += g.launches;
+      graphs += g.exec ? 1 : 0;
+      if (g.exec) count_launch(g.launches);
+    } else {
+      for (size_t m = 0; m < g.members.size() && rc == QG_OK; ++m) {
+        State* v = g.views[m].get();
+        cudaError_t e = launch_set_basis(v->d, v->prec, v->n, 0, sw->stream);
+        if (e != cudaSuccess) rc = cuda_fail(&err, e, "zero-state");
+        ExecStats st;
+        if (rc == QG_OK) rc = exec_program(v, g.progs[m], 0, nullptr, &st, &err);
+        launches += st.passes + 1;
+      }
+    }
+  }
+  cudaEventRecord(e1, sw->stream);
+  // energies
+  if (rc == QG_OK && term_offsets && energies) {
+    std::vector<int64_t> char_off(sw->count + 1, 0);
+    for (int i = 0; i < sw->count; ++i) {
+      const int n = sw->groups[sw->where[i].first].n;
+      char_off[i + 1] = char_off[i] + (int64_t)(term_offsets[i + 1] - term_offsets[i]) * n;
+    }
+    const int G = diag_max_groups();
+    for (auto& g : sw->groups) {
+      const size_t S = g.members.size();
+      // batched path: every member's terms are I/Z strings with at most G distinct coefficients
+      bool diag = g.n >= 12;
+      std::vector<unsigned char> dstate(diag_state_bytes() * S);
+      std::vector<uint64_t> zs;
+      std::vector<double> gcoef(S * G, 0.0);
+      for (size_t m = 0; m < S && diag; ++m) {
+        const int ci = g.members[m];
+        std::vector<double> vals;
+        std::vector<std::vector<uint64_t>> per(G);
+        for (int t = term_offsets[ci]; t < term_offsets[ci + 1] && diag; ++t) {
+          const char* ps = pauli_strings + char_off[ci] + (int64_t)(t - term_offsets[ci]) * g.n;
+          uint64_t z = 0;
+          for (int q = 0; q < g.n; ++q) {
+            if (ps[q] == 'Z') z |= 1ULL << (g.n - 1 - q);
+            else if (ps[q] != 'I') diag = false;
+          }
+          int gi = -1;
+          for (size_t k = 0; k < vals.size(); ++k)
+            if (vals[k] == coefficients[t]) gi = (int)k;
+          if (gi < 0) {
+            if ((int)vals.size() == G) {
+              diag = false;
+              break;
+            }
+            gi = (int)vals.size();
+            vals.push_back(coefficients[t]);
+          }
+          per[gi].push_back(z);
+        }
+        if (!diag) break;
+        int gcount[8] = {0};
+        const uint64_t zoff = zs.size();
+        for (int k = 0; k < (int)vals.size(); ++k) {
+          gcount[k] = (int)per[k].size();
+          zs.insert(zs.end(), per[k].begin(), per[k].end());
+          gcoef[m * G + k] = vals[k];
+        }
+        fill_diag_state(dstate.data() + diag_state_bytes() * m, zoff, (int)vals.size(), gcount);
+      }
+      if (diag) {
+        const uint64_t chunks = 1ULL << (g.n - 12);
+        void* d_diag = nullptr;
+        uint64_t* d_z = nullptr;
+        double *d_gcoef = nullptr, *d_part = nullptr, *d_en = nullptr;
+        cudaError_t e = cudaMallocAsync(&d_diag, dstate.size(), sw->stream);
+        if (e == cudaSuccess) e = cudaMallocAsync((void**)&d_z, sizeof(uint64_t) * std::max<size_t>(zs.size(), 1), sw->stream);
+        if (e == cudaSuccess) e = cudaMallocAsync((void**)&d_gcoef, sizeof(double) * gcoef.size(), sw->stream);
+        if (e == cudaSuccess) e = cudaMallocAsync((void**)&d_part, sizeof(double) * G * chunks * S, sw->stream);
+        if (e == cudaSuccess) e = cudaMallocAsync((void**)&d_en, sizeof(double) * S, sw->stream);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(d_diag, dstate.data(), dstate.size(), cudaMemcpyHostToDevice, sw->stream);
+        if (e == cudaSuccess && !zs.empty())
+          e = cudaMemcpyAsync(d_z, zs.data(), sizeof(uint64_t) * zs.size(), cudaMemcpyHostToDevice, sw->stream);
+        if (e == cudaSuccess)
+          e = cudaMemcpyAsync(d_gcoef, gcoef.data(), sizeof(double) * gcoef.size(), cudaMemcpyHostToDevice, sw->stream);
+        if (e == cudaSuccess)
+          e = launch_diag_expect(g.d_states, sw->prec, g.n, d_diag, d_z, (int)S, d_part, d_gcoef, d_en, sw->stream);
+        std::vector<double> en(S);
+        if (e == cudaSuccess)
+          e = cudaMemcpyAsync(en.data(), d_en, sizeof(double) * S, cudaMemcpyDeviceToHost, sw->stream);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(sw->stream);
+        for (void* p : {(void*)d_diag, (void*)d_z, (void*)d_gcoef, (void*)d_part, (void*)d_en})
+          if (p) cudaFreeAsync(p, sw->stream);
+        if (e != cudaSuccess) {
+          rc = cuda_fail(&err, e, "sweep energies");
+          break;
+        }
+        launches += 2;
+        for (size_t m = 0; m < S; ++m) energies[g.members[m]] = en[m];
+      } else {
+        for (size_t m = 0; m < S && rc == QG_OK; ++m) {
+          const int ci = g.members[m];
+          double energy = 0;
+          for (int t = term_offsets[ci]; t < term_offsets[ci + 1] && rc == QG_OK; ++t) {
+            double v;
+            rc = st_pauli(g.views[m].get(), pauli_strings + char_off[ci] + (int64_t)(t - term_offsets[ci]) * g.n,
+                          &v, &err);
+            const double term = coefficients[t] * v;
+            energy = (t == term_offsets[ci]) ? term : energy + term;
+            ++launches;
+          }
+          energies[ci] = energy;
+        }
+      }
+    }
+  }
+  cudaEventRecord(e2, sw->stream);
+  cudaError_t se = cudaEventSynchronize(e2);
+  if (se != cudaSuccess && rc == QG_OK) rc = cuda_fail(&err, se, "sweep");
+  if (stats) {
+    std::memset(stats, 0, sizeof(*stats));
+    float a = 0, b = 0;
+    cudaEventElapsedTime(&a, e0, e1);
+    cudaEventElapsedTime(&b, e1, e2);
+    stats->device_ms = a;
+    stats->expect_ms = b;
+    stats->groups = (int32_t)sw->groups.size();
+    stats->launches = launches;
+    stats->graphs = graphs;
+    stats->state_bytes = sw->bytes;
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  cudaEventDestroy(e2);
+  if (rc != QG_OK) set_ctx_error(sw->ctx, err);
+  return rc;
+}
+
+int qg_sweep_state(void* sweep, int32_t c, double* host) {
+  if (!sweep || !host) return QG_ERR_INVALID_ARG;
+  Sweep* sw = (Sweep*)sweep;
+  if (c < 0 || c >= sw->count) return QG_ERR_INVALID_ARG;
+  cudaSetDevice(sw->ctx->device);
+  std::string err;
+  State* v = sw->groups[sw->where[c].first].views[sw->where[c].second].get();
+  int rc = download_c128(v, host, &err);
+  if (rc != QG_OK) set_ctx_error(sw->ctx, err);
+  return rc;
+}
+
+int qg_sweep_destroy(void* sweep) {
+  if (!sweep) return QG_ERR_INVALID_ARG;
+  Sweep* sw = (Sweep*)sweep;
+  cudaSetDevice(sw->ctx->device);
+  sweep_free(sw);
   return QG_OK;
 }
 

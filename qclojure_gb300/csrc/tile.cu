@@ -531,9 +531,17 @@ __device__ void run_ops(unsigned char* buf, const KOp* __restrict__ sops, int no
 #undef QG_U2_CASES
 #undef QG_PHASE_CASES
 
+// States processed by one launch: all share the pass structure (PassDesc, op
+// kinds and count); op records may differ per state (ops_stride records apart).
+struct BatchArgs {
+  unsigned char* const* states;  // device array of nstates amplitude arrays
+  const KOp* kops;               // op records of state 0
+  int64_t ops_stride;            // records between consecutive states' lists (0: one shared list)
+  int nstates;
+};
+
 template <class P>
-__global__ void __launch_bounds__(512, 1) k_tile2(unsigned char* __restrict__ state, const PassDesc pd,
-                                                  const KOp* __restrict__ kops, int nops,
+__global__ void __launch_bounds__(512, 1) k_tile2(const PassDesc pd, const BatchArgs ba, int nops,
                                                   const double* __restrict__ dense, uint64_t ntiles) {
   constexpr int E = P::kElem;
   extern __shared__ __align__(128) unsigned char smem[];
@@ -546,38 +554,49 @@ __global__ void __launch_bounds__(512, 1) k_tile2(unsigned char* __restrict__ st
   const int nhi = 1 << (g.k - g.klow);
   KOp* sops = reinterpret_cast<KOp*>(smem + 2 * tile_bytes);  // 16-byte aligned: tile_bytes % 16 == 0
   uint64_t* hioff = reinterpret_cast<uint64_t*>(sops + nops);
-  {  // stage the pass's op records (96 bytes each) in shared memory
-    const uint4* src = reinterpret_cast<const uint4*>(kops);
-    uint4* dst = reinterpret_cast<uint4*>(sops);
-    const int words = nops * (int)(sizeof(KOp) / 16);
-    for (int w = threadIdx.x; w < words; w += g.T) dst[w] = src[w];
-  }
   for (int h = threadIdx.x; h < nhi; h += g.T) {
     uint64_t off = 0;
     for (int j = g.klow; j < g.k; ++j)
       if ((h >> (j - g.klow)) & 1) off |= 1ULL << pd.lbits[j];
     hioff[h] = off;
   }
-  __syncthreads();
-  uint64_t tile = blockIdx.x;
-  if (tile >= ntiles) return;
-  load_tile<E>(smem, state, tile_base(pd, tile), hioff, g);
-  cp_commit();
-  for (int i = 0; tile < ntiles; ++i, tile += gridDim.x) {
-    const uint64_t next = tile + gridDim.x;
-    unsigned char* cur = smem + (i & 1) * tile_bytes;
-    if (next < ntiles) {
-      load_tile<E>(smem + ((i + 1) & 1) * tile_bytes, state, tile_base(pd, next), hioff, g);
-      cp_commit();
-      cp_wait<1>();
-    } else {
-      cp_wait<0>();
+  // contiguous range of (state, tile) work items for this CTA
+  const uint64_t W = ntiles * (uint64_t)ba.nstates;
+  const uint64_t w0 = W * blockIdx.x / gridDim.x, w1 = W * (blockIdx.x + 1) / gridDim.x;
+  int staged = -1;
+  for (uint64_t w = w0; w < w1;) {
+    const int si = (int)(w / ntiles);
+    const uint64_t t0 = w - (uint64_t)si * ntiles;
+    const uint64_t t1 = (ntiles - t0 < w1 - w) ? ntiles : t0 + (w1 - w);
+    unsigned char* state = ba.states[si];
+    if (staged < 0 || (si != staged && ba.ops_stride != 0)) {
+      __syncthreads();  // previous segment's readers of sops are done
+      const uint4* src = reinterpret_cast<const uint4*>(ba.kops + (int64_t)si * ba.ops_stride);
+      uint4* dst = reinterpret_cast<uint4*>(sops);
+      const int words = nops * (int)(sizeof(KOp) / 16);
+      for (int q = threadIdx.x; q < words; q += g.T) dst[q] = src[q];
     }
+    staged = si;
     __syncthreads();
-    const uint64_t base = tile_base(pd, tile);
-    run_ops<P>(cur, sops, nops, dense, base, g);
-    store_tile<E>(cur, state, base, hioff, g);
-    __syncthreads();  // the buffer is refilled two tiles later
+    load_tile<E>(smem, state, tile_base(pd, t0), hioff, g);
+    cp_commit();
+    int i = 0;
+    for (uint64_t tile = t0; tile < t1; ++tile, ++i) {
+      unsigned char* cur = smem + (i & 1) * tile_bytes;
+      if (tile + 1 < t1) {
+        load_tile<E>(smem + ((i + 1) & 1) * tile_bytes, state, tile_base(pd, tile + 1), hioff, g);
+        cp_commit();
+        cp_wait<1>();
+      } else {
+        cp_wait<0>();
+      }
+      __syncthreads();
+      const uint64_t base = tile_base(pd, tile);
+      run_ops<P>(cur, sops, nops, dense, base, g);
+      store_tile<E>(cur, state, base, hioff, g);
+      __syncthreads();  // the buffer is refilled two tiles later
+    }
+    w += t1 - t0;
   }
 }
 
@@ -652,20 +671,22 @@ void build_kops(KOp* out, const TOp* ops, int64_t nops) {
 }
 
 template <class P>
-cudaError_t launch_t(void* s, int n, const PassDesc& pd, const void* d_kops, const double* d_dense, cudaStream_t st) {
+cudaError_t launch_t(int n, const PassDesc& pd, const BatchArgs& ba, const double* d_dense, cudaStream_t st) {
   constexpr int E = P::kElem;
   const int K = 1 << pd.k;
   const int threads = K / kRegs;
   const int nops = (int)(pd.op_end - pd.op_begin);
-  if (threads < 1 || threads > 512 || (K * E) % 16 != 0 || K * E < 16 * threads || nops > kMaxKOps)
+  if (threads < 1 || threads > 512 || (K * E) % 16 != 0 || K * E < 16 * threads || nops > kMaxKOps ||
+      ba.nstates < 1)
     return cudaErrorInvalidValue;
   const size_t smem = 2 * (size_t)K * E + sizeof(KOp) * (size_t)nops + sizeof(uint64_t) * (1u << (pd.k - pd.klow));
   const uint64_t ntiles = 1ULL << (n - pd.k);
+  const uint64_t work = ntiles * (uint64_t)ba.nstates;
   int per_sm = (int)((220 * 1024) / smem);
   if (per_sm > 2048 / threads) per_sm = 2048 / threads;
   if (per_sm < 1) per_sm = 1;
   uint64_t grid = (uint64_t)kSMs * per_sm;
-  if (grid > ntiles) grid = ntiles;
+  if (grid > work) grid = work;
   // One fixed limit for every launch: worker threads launch passes of different
   // sizes concurrently, and a per-launch value could undercut another thread's launch.
   // two 64 KiB tile buffers, the largest op list, the chunk-offset table
@@ -674,8 +695,7 @@ cudaError_t launch_t(void* s, int n, const PassDesc& pd, const void* d_kops, con
   if (smem > kSmemLimit) return cudaErrorInvalidValue;
   cudaError_t e = cudaFuncSetAttribute(k_tile2<P>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmemLimit);
   if (e != cudaSuccess) return e;
-  const KOp* ops = reinterpret_cast<const KOp*>(d_kops) + pd.op_begin;
-  k_tile2<P><<<(unsigned)grid, threads, smem, st>>>((unsigned char*)s, pd, ops, nops, d_dense, ntiles);
+  k_tile2<P><<<(unsigned)grid, threads, smem, st>>>(pd, ba, nops, d_dense, ntiles);
   count_launch(1);
   return cudaGetLastError();
 }
@@ -692,12 +712,18 @@ void encode_kops(int precision, int arithmetic, const TOp* tops, int64_t count, 
   else build_kops<PolD>(k, tops, count);
 }
 
-cudaError_t launch_tile_pass(void* s, int precision, int arithmetic, int n, const PassDesc& pd, const void* d_kops,
-                             const double* d_dense, cudaStream_t st) {
+cudaError_t launch_tile_pass(int precision, int arithmetic, int n, const PassDesc& pd, void* const* d_states,
+                             int nstates, const void* d_kops, int64_t ops_stride, const double* d_dense,
+                             cudaStream_t st) {
   if (pd.k < 3 || pd.k > kMaxTileBits) return cudaErrorInvalidValue;
-  if (precision == QG_C64) return launch_t<PolF>(s, n, pd, d_kops, d_dense, st);
-  if (arithmetic == QG_ARITH_DOUBLE_FLOAT) return launch_t<PolDF>(s, n, pd, d_kops, d_dense, st);
-  return launch_t<PolD>(s, n, pd, d_kops, d_dense, st);
+  BatchArgs ba;
+  ba.states = reinterpret_cast<unsigned char* const*>(d_states);
+  ba.kops = reinterpret_cast<const KOp*>(d_kops) + pd.op_begin;
+  ba.ops_stride = ops_stride;
+  ba.nstates = nstates;
+  if (precision == QG_C64) return launch_t<PolF>(n, pd, ba, d_dense, st);
+  if (arithmetic == QG_ARITH_DOUBLE_FLOAT) return launch_t<PolDF>(n, pd, ba, d_dense, st);
+  return launch_t<PolD>(n, pd, ba, d_dense, st);
 }
 
 }  // namespace qg

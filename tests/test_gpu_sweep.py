@@ -1,0 +1,90 @@
+"""Batched parameter sweeps (QAOA MaxCut, uneven sizes) against the oracle.
+
+Tolerances: complex128 exact arithmetic  energies |d| <= 1e-10 (grouped FP64 sums),
+            complex128 double-float      energies |d| <= 1e-10, states <= 1e-12,
+            complex64                    energies |d| <= 1e-4 * max(1, |E|).
+"""
+import math
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def _qaoa_set(count, seed, ns=(12, 14, 16)):
+    from qclojure_gb300 import workloads
+
+    rng = np.random.default_rng(seed)
+    return [workloads.qaoa_maxcut(int(rng.choice(ns)), 3, seed * 1000 + i) for i in range(count)]
+
+
+def _energy(oracle, c):
+    return oracle.hamiltonian_expectation(oracle.run(c), c["hamiltonian"])
+
+
+@pytest.mark.parametrize("precision,arith,tol", [("c128", "exact", 1e-10), ("c128", "double-float", 1e-10),
+                                                 ("c64", "exact", 1e-4)])
+def test_qaoa_sweep_energies(gpu_ctx, oracle, precision, arith, tol):
+    from qclojure_gb300.sweep import Sweep
+
+    circs = _qaoa_set(12, seed=5)
+    with Sweep(gpu_ctx, circs, precision=precision, arithmetic=arith) as sw:
+        en, st = sw.run([c["hamiltonian"] for c in circs])
+        distinct = len({c["num-qubits"] for c in circs})
+        assert st["groups"] == distinct and st["graphs"] == distinct
+        for c, e in zip(circs, en):
+            ref = _energy(oracle, c)
+            assert abs(e - ref) <= tol * max(1.0, abs(ref)), (e, ref)
+        if precision == "c128":
+            for k in (0, 5):
+                assert np.max(np.abs(sw.state(k) - oracle.run(circs[k]))) <= 1e-12
+
+
+def test_sweep_update_new_angles(gpu_ctx, oracle):
+    from qclojure_gb300 import workloads
+    from qclojure_gb300.sweep import Sweep
+
+    circs = _qaoa_set(6, seed=9, ns=(12, 14))
+    with Sweep(gpu_ctx, circs, precision="c128", arithmetic="exact") as sw:
+        e1, _ = sw.run([c["hamiltonian"] for c in circs])
+        # same graphs, new angles
+        new = []
+        for c in circs:
+            d = {**c, "operations": [dict(op, **({"operation-params": {**op["operation-params"],
+                                                                    "angle": op["operation-params"]["angle"] * 0.5}}
+                                                 if "angle" in op.get("operation-params", {}) else {}))
+                                     for op in c["operations"]]}
+            new.append(d)
+        sw.update(new)
+        e2, _ = sw.run([c["hamiltonian"] for c in new])
+        for c, e in zip(new, e2):
+            assert abs(e - _energy(oracle, c)) <= 1e-10
+        assert np.max(np.abs(e1 - e2)) > 1e-6
+
+
+def test_sweep_matches_single_state_runs(gpu_ctx):
+    """Batched states equal the same circuits run one at a time (bit-exact, exact arithmetic)."""
+    from qclojure_gb300.sweep import Sweep
+
+    circs = _qaoa_set(5, seed=2, ns=(18, 20))
+    with Sweep(gpu_ctx, circs, precision="c128", arithmetic="exact") as sw:
+        sw.run()
+        for k, c in enumerate(circs):
+            with gpu_ctx.state(c["num-qubits"]) as st:
+                st.apply(c, fusion="tiled")
+                assert np.array_equal(sw.state(k), st.download())
+
+
+def test_sweep_general_hamiltonian_fallback(gpu_ctx, oracle):
+    from qclojure_gb300 import workloads
+    from qclojure_gb300.sweep import Sweep
+
+    circs = [workloads.layered_circuit(n, 4, seed=n) for n in (6, 12, 12)]
+    rng = np.random.default_rng(0)
+    hams = [[{"coefficient": float(rng.normal()), "pauli-string": "".join("IXYZ"[k] for k in rng.integers(0, 4, c["num-qubits"]))}
+             for _ in range(4)] for c in circs]
+    with Sweep(gpu_ctx, circs, precision="c128", arithmetic="exact") as sw:
+        en, _ = sw.run(hams)
+    for c, h, e in zip(circs, hams, en):
+        assert abs(e - oracle.hamiltonian_expectation(oracle.run(c), h)) <= 1e-12
