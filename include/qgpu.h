@@ -274,6 +274,20 @@ int qg_state_probabilities(void* state, double* host_out);
 /* Shot sampling (state.clj:869-913 rule: first outcome whose cumulative probability
    reaches the uniform draw) with Philox uniforms from seed; outcomes in shot order. */
 int qg_state_sample(void* state, uint64_t shots, uint64_t seed, uint64_t* host_outcomes);
+/* qg_state_sample_noalloc has no counterpart in the reference. It draws the same
+   outcomes as qg_state_sample (same seed, same shots) but allocates no device memory:
+   for callers that cannot allocate while sampling, such as a host runtime that has
+   handed every free byte of HBM to its own pool, or a loop that must not take the
+   allocator's locks and possible synchronisation on each call. Its scratch is one fixed
+   array per device inside this library (about 4.3 MB), which limits the state to
+   24 qubits; larger states return QG_ERR_INVALID_ARG. device_outcomes is caller-owned
+   device memory of the state's device holding at least `shots` values; the call
+   returns after the outcomes are written (it synchronises the state's stream).
+   The first call on a device looks up the array's device address once (with that
+   device current); make that first call before any stream capture begins. Calls that
+   overlap on one device (from several host threads) share the array and race:
+   serialise them. */
+int qg_state_sample_noalloc(void* state, uint64_t shots, uint64_t seed, uint64_t* device_outcomes);
 /* <psi|P|psi> for a Pauli string of num_qubits chars (hamiltonian.clj:82-94). */
 int qg_state_pauli_expectation(void* state, const char* pauli, double* out);
 /* sum_j c_j <P_j> (hamiltonian.clj:96-114), strings concatenated. */

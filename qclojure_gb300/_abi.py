@@ -170,6 +170,7 @@ SIGNATURES = {
     "qg_state_apply": ([P, C.POINTER(QgCircuit), I32, U64, I32P], C.c_int),
     "qg_state_probabilities": ([P, DP], C.c_int),
     "qg_state_sample": ([P, U64, U64, U64P], C.c_int),
+    "qg_state_sample_noalloc": ([P, U64, U64, P], C.c_int),
     "qg_state_pauli_expectation": ([P, C.c_char_p, DP], C.c_int),
     "qg_state_hamiltonian": ([P, I32, DP, C.c_char_p, DP], C.c_int),
     "qg_state_expectation_1q": ([P, DP, I32, DP], C.c_int),

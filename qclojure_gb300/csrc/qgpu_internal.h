@@ -189,6 +189,11 @@ size_t sampler_scratch_bytes(int n, uint64_t shots);
 cudaError_t launch_sample(const void* s, int precision, int n, uint64_t shots, uint64_t seed, void* d_scratch,
                           uint64_t* d_outcomes, double* d_total, cudaStream_t st);
 
+// File-scope sampler scratch of qg_state_sample_noalloc (noalloc.cu): its device
+// address for `device` (which must be current), resolved once per device, and its size.
+constexpr int kNoAllocSampleMaxQubits = 24;
+cudaError_t noalloc_sample_scratch(int device, void** ptr, size_t* bytes);
+
 int reduce_blocks_for(int n);
 unsigned long long kernel_launch_count();
 

@@ -1500,6 +1500,56 @@ int qg_state_sample(void* state, uint64_t shots, uint64_t seed, uint64_t* host_o
   return state_err(s, rc, err);
 }
 
+// Same kernels and outcomes as qg_state_sample; the scratch is the file-scope array
+// of noalloc.cu and the outcomes go to caller-owned device memory. Every scratch
+// word is written by an earlier kernel of the same call before it is read, so
+// nothing needs clearing between calls.
+static int st_sample_noalloc(State* s, uint64_t shots, uint64_t seed, uint64_t* d_out, std::string* err) {
+  if (s->n > kNoAllocSampleMaxQubits) {
+    *err = "qg_state_sample_noalloc: " + std::to_string(s->n) + " qubits exceed its fixed scratch (at most " +
+           std::to_string(kNoAllocSampleMaxQubits) + " qubits)";
+    return QG_ERR_INVALID_ARG;
+  }
+  if (shots) {
+    cudaPointerAttributes pa{};
+    CK(cudaPointerGetAttributes(&pa, d_out), "outcome buffer attributes");
+    const bool device_ok = pa.type == cudaMemoryTypeDevice || pa.type == cudaMemoryTypeManaged ||
+                           (pa.type == cudaMemoryTypeHost && pa.devicePointer != nullptr);
+    if (!device_ok || (pa.type == cudaMemoryTypeDevice && pa.device != s->ctx->device)) {
+      *err = "qg_state_sample_noalloc: outcomes must be device memory of the state's device";
+      return QG_ERR_INVALID_ARG;
+    }
+  }
+  void* scratch = nullptr;
+  size_t cap = 0;
+  CK(noalloc_sample_scratch(s->ctx->device, &scratch, &cap), "sampler scratch address");
+  const size_t need = sampler_scratch_bytes(s->n, shots);
+  const size_t total_off = (need + 255) / 256 * 256;
+  if (total_off + sizeof(double) > cap) {
+    *err = "qg_state_sample_noalloc: sampler scratch too small";
+    return QG_ERR_INVALID_ARG;
+  }
+  double* d_total = (double*)((char*)scratch + total_off);
+  CK(launch_sample(s->d, s->prec, s->n, shots, seed, scratch, d_out, d_total, s->stream), "sample");
+  double total = 0;
+  CK(cudaMemcpyAsync(&total, d_total, sizeof(double), cudaMemcpyDeviceToHost, s->stream), "D2H total");
+  CK(cudaStreamSynchronize(s->stream), "sync");
+  const double norm_tol = s->prec == QG_C64 ? 1e-4 : 1e-8;
+  if (std::fabs(total - 1.0) > norm_tol) {
+    *err = "State is not properly normalized (total probability " + std::to_string(total) + ")";
+    return QG_ERR_NOT_NORMALIZED;
+  }
+  return QG_OK;
+}
+
+int qg_state_sample_noalloc(void* state, uint64_t shots, uint64_t seed, uint64_t* device_outcomes) {
+  if (!state || (shots && !device_outcomes)) return QG_ERR_INVALID_ARG;
+  State* s = (State*)state;
+  cudaSetDevice(s->ctx->device);
+  std::string err;
+  return state_err(s, st_sample_noalloc(s, shots, seed, device_outcomes, &err), err);
+}
+
 int qg_state_pauli_expectation(void* state, const char* pauli, double* out) {
   if (!state || !pauli || !out) return QG_ERR_INVALID_ARG;
   State* s = (State*)state;

@@ -100,6 +100,12 @@ class DeviceState:
         self._ck(self.lib.qg_state_sample(self.h, C.c_uint64(shots), C.c_uint64(seed), out.ctypes.data_as(A.U64P)))
         return out[:shots]
 
+    def sample_noalloc(self, shots: int, seed: int, device_outcomes: int) -> None:
+        """Write `shots` outcomes (uint64) to caller-owned device memory at address
+        `device_outcomes`; no device allocation (states of at most 24 qubits)."""
+        self._ck(self.lib.qg_state_sample_noalloc(self.h, C.c_uint64(shots), C.c_uint64(seed),
+                                                  C.c_void_p(device_outcomes)))
+
     def pauli_expectation(self, pauli: str) -> float:
         out = C.c_double()
         self._ck(self.lib.qg_state_pauli_expectation(self.h, pauli.encode(), C.byref(out)))
