@@ -298,7 +298,8 @@ def main():
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "f64" if args.precision == "c128" else "f32", "data": "synthetic",
+        "vs_baseline": None,
+        "dtype": "f32x2 double-float (f64 storage)" if args.precision == "c128" else "f32", "data": "synthetic",
         "config": {"workload": f"layered-{n}x{args.depth}+qft{n}", "n_qubits": n, "depth": args.depth,
                    "gates": gates, "precision": args.precision, "fusion": args.fusion,
                    "parallelism": f"replicas{world}", "l2": "state larger than L2 (no flush needed)"},
