@@ -471,8 +471,22 @@ void plan_register_groups(std::vector<TOp>& ops, int k) {
       rb |= req;
       ++j;
     }
-    // pad with the highest free local bits so the thread bits stay low (coalesced shared memory)
-    for (int b = k - 1; b >= 0 && __builtin_popcount(rb) < 3; --b) rb |= 1u << b;
+    // Pad the register bits with the local bits that the group's conditions use most
+    // (phase masks, controls): a condition on register bits selects registers at
+    // compile time, one on thread bits costs every register of a divergent warp.
+    // Ties go to the highest bit so the thread bits stay low.
+    int uses[32] = {0};
+    for (size_t q = i; q < j; ++q) {
+      const uint32_t cm = ops[q].kind == OK_U2 || ops[q].kind == OK_SWAP ? ops[q].lcmask : ops[q].lmask;
+      for (int b = 0; b < k; ++b)
+        if (cm & (1u << b)) ++uses[b];
+    }
+    while (__builtin_popcount(rb) < 3) {
+      int best = -1;
+      for (int b = k - 1; b >= 0; --b)
+        if (!(rb & (1u << b)) && (best < 0 || uses[b] > uses[best])) best = b;
+      rb |= 1u << best;
+    }
     int pos[3], np = 0;
     for (int b = 0; b < k && np < 3; ++b)
       if (rb & (1u << b)) pos[np++] = b;
@@ -559,7 +573,8 @@ int schedule(int n, int precision, int fusion, int fuse_k, const std::vector<GOp
   }
 
   const int k = tile_bits_for(n, precision);
-  const int klow_min = std::min(k, 5);
+  // bits 0..klow_min-1 stay local in every pass: contiguous 128-byte runs in HBM
+  const int klow_min = std::min(k, precision == QG_C64 ? 4 : 3);
   const uint64_t low_mask = (klow_min >= 64) ? ~0ULL : ((1ULL << klow_min) - 1);
 
   // Optional dense-block fusion: rewrite gate runs into OK_DENSE ops first.

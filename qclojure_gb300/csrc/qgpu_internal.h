@@ -145,9 +145,16 @@ cudaError_t launch_plain_op(void* s, int precision, int n, const GOp& op, cudaSt
 // d_states: device array of amplitude pointers; d_kops: compact op records on the
 // device (encode_kops) for state 0, indexed by pd's op range; state s uses the
 // records ops_stride further on (0: all states share one list).
-cudaError_t launch_tile_pass(int precision, int arithmetic, int n, const PassDesc& pd, void* const* d_states,
-                             int nstates, const void* d_kops, int64_t ops_stride, const double* d_dense,
-                             cudaStream_t st);
+// io (double-float arithmetic only): bit 0 = the state arrives as float pairs
+// (re.hi, re.lo, im.hi, im.lo) written by the previous pass, bit 1 = leave it as
+// float pairs for the next pass; without the bit the state is IEEE doubles.
+constexpr int kTileInPairs = 1, kTileOutPairs = 2;
+cudaError_t launch_tile_pass(int precision, int arithmetic, int io, int n, const PassDesc& pd,
+                             void* const* d_states, int nstates, const void* d_kops, int64_t ops_stride,
+                             const double* d_dense, cudaStream_t st);
+// io bits for step i of a program: consecutive double-float tiled passes hand the
+// state over as float pairs; the first converts from doubles, the last back.
+int tile_pass_io(const Program& prog, size_t step);
 int max_ops_per_tile_pass();
 size_t kop_record_bytes();
 // batched sweep kernels (sweep.cu)

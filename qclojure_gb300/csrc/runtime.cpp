@@ -306,7 +306,8 @@ static int exec_program(State* s, const Program& prog, uint64_t seed, const std:
     if (st.kind == Step::PLAIN_OP) {
       e = launch_plain_op(s->d, s->prec, s->n, st.op, s->stream);
     } else if (st.kind == Step::TILE_PASS) {
-      e = launch_tile_pass(s->prec, prog.arith, s->n, st.pass, s->d_self, 1, d_kops, 0, d_dense, s->stream);
+      e = launch_tile_pass(s->prec, prog.arith, tile_pass_io(prog, i), s->n, st.pass, s->d_self, 1, d_kops, 0,
+                           d_dense, s->stream);
     } else {
       rc = do_measure(s, st.mqubits, seed, measure_index++, nullptr, nullptr, err);
     }
@@ -1740,7 +1741,8 @@ static cudaError_t launch_group_passes(Sweep* sw, SweepGroup& g) {
     PassDesc pd = g.progs[0].steps[g.pass_steps[p]].pass;
     pd.op_begin = 0;
     pd.op_end = g.pass_nops[p];
-    e = launch_tile_pass(sw->prec, g.progs[0].arith, g.n, pd, g.d_states, (int)g.members.size(),
+    e = launch_tile_pass(sw->prec, g.progs[0].arith, tile_pass_io(g.progs[0], g.pass_steps[p]), g.n, pd,
+                         g.d_states, (int)g.members.size(),
                          (const unsigned char*)g.d_kops + rec * (size_t)g.pass_off[p], g.pass_nops[p], nullptr,
                          sw->stream);
   }

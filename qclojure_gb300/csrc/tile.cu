@@ -19,8 +19,9 @@
 //          dense row sum (src/org/soulspace/qclojure/domain/gate.clj:384-395),
 //          so results are bit-identical to the plain per-gate kernels;
 //   PolF   complex64, FP32 with the same operation order;
-//   PolDF  complex128 stored as IEEE doubles in HBM, computed as double-float
-//          pairs on the FP32 pipes (df64.cuh); within 1e-14 per pass.
+//   PolDFT complex128 computed as double-float pairs on the FP32 pipes
+//          (df64.cuh), within 1e-14 per pass; HBM holds IEEE doubles at the
+//          ends of a run of passes and float pairs between them.
 #include <cstdio>
 #include <cstring>
 #include <type_traits>
@@ -52,6 +53,8 @@ struct PolExact {
   using Reg = V;
   static constexpr int kElem = sizeof(V);  // bytes per amplitude in HBM and shared memory
   static constexpr bool kDense = true;     // dense fused blocks supported
+  static constexpr int kCst = sizeof(R) == 8 ? 0 : 1;
+  static constexpr bool kInPairs = false, kOutPairs = false;
   struct Cst {
     R m[8];
   };
@@ -121,25 +124,33 @@ using PolD = PolExact<double, double2>;
 using PolF = PolExact<float, float2>;
 
 // ---------------------------------------------------------------------------
-// double-float policy: HBM holds double2, registers and shared memory hold
-// (re.hi, re.lo, im.hi, im.lo) after the first layout
+// double-float policy: registers and shared memory hold (re.hi, re.lo, im.hi,
+// im.lo). Between the passes of one program HBM holds the same pairs (IO bit 0:
+// the input is in pair form, bit 1: the output is written in pair form); the
+// first pass of a run converts from IEEE doubles and the last one back, so the
+// passes in between convert nothing.
 // ---------------------------------------------------------------------------
-struct PolDF {
+template <int IO>
+struct PolDFT {
   using Reg = dfc;
   static constexpr int kElem = 16;
   static constexpr bool kDense = false;  // dense fused blocks run with PolD
+  static constexpr bool kInPairs = (IO & 1) != 0, kOutPairs = (IO & 2) != 0;
+  static constexpr int kCst = 2;
   struct Cst {
     float h[8], l[8];
   };
-  __device__ static dfc load_raw(const unsigned char* sm, int pos) {
-    return load_dfc(reinterpret_cast<const double2*>(sm)[pos]);
-  }
   __device__ static dfc load_work(const unsigned char* sm, int pos) {
     float4 v = reinterpret_cast<const float4*>(sm)[pos];
     return dfc{v.x, v.y, v.z, v.w};
   }
+  __device__ static dfc load_raw(const unsigned char* sm, int pos) {
+    if constexpr (kInPairs) return load_work(sm, pos);
+    else return load_dfc(reinterpret_cast<const double2*>(sm)[pos]);
+  }
   __device__ static void store_raw(unsigned char* sm, int pos, const dfc& v) {
-    reinterpret_cast<double2*>(sm)[pos] = store_dfc(v);
+    if constexpr (kOutPairs) reinterpret_cast<float4*>(sm)[pos] = make_float4(v.rh, v.rl, v.ih, v.il);
+    else reinterpret_cast<double2*>(sm)[pos] = store_dfc(v);
   }
   __device__ static void store_work(unsigned char* sm, int pos, const dfc& v) {
     reinterpret_cast<float4*>(sm)[pos] = make_float4(v.rh, v.rl, v.ih, v.il);
@@ -236,33 +247,34 @@ __device__ __forceinline__ uint64_t tile_base(const PassDesc& pd, uint64_t tile)
   return base;
 }
 
-// issue the copies of one tile (every thread: K*ELEM/16/T copies of 16 bytes)
+// Each thread moves the same CPT 16-byte pieces of every tile: piece i of thread
+// x is local copy c = x + i*T. Its byte offset from the tile base in HBM (goff)
+// and its swizzled shared-memory offset (soff) are computed once per launch.
 template <int ELEM>
-__device__ __forceinline__ void load_tile(unsigned char* buf, const unsigned char* gstate, uint64_t base,
-                                          const uint64_t* hioff, const TileGeo& g) {
-  constexpr int PER = 16 / ELEM;  // amplitudes per 16-byte copy
-  const uint32_t lowmask = (1u << g.klow) - 1;
-  const int ncopies = g.K / PER;
-  for (int c = threadIdx.x; c < ncopies; c += g.T) {
-    const int l = c * PER;
-    const uint64_t gi = base | (l & lowmask) | hioff[l >> g.klow];
-    cp_async16(buf + (size_t)swz<ELEM>(l) * ELEM, gstate + gi * ELEM);
+struct CopyPlan {
+  static constexpr int PER = 16 / ELEM;  // amplitudes per 16-byte copy
+  static constexpr int CPT = ELEM / 2;   // copies per thread: (K*ELEM/16) / (K/8)
+  uint64_t goff[CPT];
+  uint32_t soff[CPT];
+  __device__ void init(const uint64_t* hioff, const TileGeo& g) {
+    const uint32_t lowmask = (1u << g.klow) - 1;
+#pragma unroll
+    for (int i = 0; i < CPT; ++i) {
+      const int l = ((int)threadIdx.x + i * g.T) * PER;
+      goff[i] = ((uint64_t)(l & lowmask) | hioff[l >> g.klow]) * ELEM;
+      soff[i] = (uint32_t)swz<ELEM>(l) * ELEM;
+    }
   }
-}
-
-template <int ELEM>
-__device__ __forceinline__ void store_tile(const unsigned char* buf, unsigned char* gstate, uint64_t base,
-                                           const uint64_t* hioff, const TileGeo& g) {
-  constexpr int PER = 16 / ELEM;
-  const uint32_t lowmask = (1u << g.klow) - 1;
-  const int ncopies = g.K / PER;
-  for (int c = threadIdx.x; c < ncopies; c += g.T) {
-    const int l = c * PER;
-    const uint64_t gi = base | (l & lowmask) | hioff[l >> g.klow];
-    const uint4 v = *reinterpret_cast<const uint4*>(buf + (size_t)swz<ELEM>(l) * ELEM);
-    *reinterpret_cast<uint4*>(gstate + gi * ELEM) = v;
+  __device__ void load(unsigned char* buf, const unsigned char* gtile) const {
+#pragma unroll
+    for (int i = 0; i < CPT; ++i) cp_async16(buf + soff[i], gtile + goff[i]);
   }
-}
+  __device__ void store(const unsigned char* buf, unsigned char* gtile) const {
+#pragma unroll
+    for (int i = 0; i < CPT; ++i)
+      *reinterpret_cast<uint4*>(gtile + goff[i]) = *reinterpret_cast<const uint4*>(buf + soff[i]);
+  }
+};
 
 // ---- register-level op application ----------------------------------------
 // ---------------------------------------------------------------------------
@@ -273,7 +285,7 @@ enum KCode : int32_t {
   KC_LAYOUT = 0,   // tmask/tval/rmr = register bits rb0/rb1/rb2, c[0..8) = lj (bit patterns)
   KC_DENSE = 1,    // tmask = dk, tval = doff, rmr = dbits (4 bits each)
   KC_U2 = 16,      // + cls * 4 + register position
-  KC_PHASE = 48,   // + phase class
+  KC_PHASE = 128,  // + phase class * 8 + register mask (the registers whose bits must all be 1)
   KC_SWAP = 56,    // + register pair (0: {0,1}, 1: {0,2}, 2: {1,2}) + 3 * iswap
   KC_BLOCKADE = 62,
   KC_PARITY = 63,
@@ -293,29 +305,21 @@ constexpr int kMaxKOps = 320;
 static_assert(sizeof(KOp) == 96, "KOp layout");
 
 template <class P>
-__device__ __forceinline__ typename P::Cst kcst(const KOp& op);
-template <>
-__device__ __forceinline__ PolD::Cst kcst<PolD>(const KOp& op) {
-  PolD::Cst c;
-  const double* d = reinterpret_cast<const double*>(op.c);
+__device__ __forceinline__ typename P::Cst kcst(const KOp& op) {
+  typename P::Cst c;
+  if constexpr (P::kCst == 0) {  // 8 doubles
+    const double* d = reinterpret_cast<const double*>(op.c);
 #pragma unroll
-  for (int q = 0; q < 8; ++q) c.m[q] = d[q];
-  return c;
-}
-template <>
-__device__ __forceinline__ PolF::Cst kcst<PolF>(const KOp& op) {
-  PolF::Cst c;
+    for (int q = 0; q < 8; ++q) c.m[q] = d[q];
+  } else if constexpr (P::kCst == 1) {  // 8 floats
 #pragma unroll
-  for (int q = 0; q < 8; ++q) c.m[q] = op.c[q];
-  return c;
-}
-template <>
-__device__ __forceinline__ PolDF::Cst kcst<PolDF>(const KOp& op) {
-  PolDF::Cst c;
+    for (int q = 0; q < 8; ++q) c.m[q] = op.c[q];
+  } else {  // 8 float pairs: hi[8], lo[8]
 #pragma unroll
-  for (int q = 0; q < 8; ++q) {
-    c.h[q] = op.c[q];
-    c.l[q] = op.c[8 + q];
+    for (int q = 0; q < 8; ++q) {
+      c.h[q] = op.c[q];
+      c.l[q] = op.c[8 + q];
+    }
   }
   return c;
 }
@@ -323,21 +327,60 @@ __device__ __forceinline__ PolDF::Cst kcst<PolDF>(const KOp& op) {
 // Register slot j holds local index lt | lj[j]; bit q of j is register position q.
 // A conditional op tests its thread bits once per thread and its register
 // positions (cr, uniform) per slot with compile-time slot numbers.
+__device__ __forceinline__ void csel_swap(bool c, float& a, float& b) {
+  const float x = c ? b : a;
+  b = c ? a : b;
+  a = x;
+}
+__device__ __forceinline__ void csel_swap(bool c, double& a, double& b) {
+  const double x = c ? b : a;
+  b = c ? a : b;
+  a = x;
+}
+__device__ __forceinline__ void csel_swap(bool c, float2& a, float2& b) {
+  csel_swap(c, a.x, b.x);
+  csel_swap(c, a.y, b.y);
+}
+__device__ __forceinline__ void csel_swap(bool c, double2& a, double2& b) {
+  csel_swap(c, a.x, b.x);
+  csel_swap(c, a.y, b.y);
+}
+__device__ __forceinline__ void csel_swap(bool c, dfc& a, dfc& b) {
+  csel_swap(c, a.rh, b.rh);
+  csel_swap(c, a.rl, b.rl);
+  csel_swap(c, a.ih, b.ih);
+  csel_swap(c, a.il, b.il);
+}
+
+// tc: the op's thread / tile condition. A conditional X (CNOT-like) swaps with
+// selects instead of a divergent branch; other classes branch on tc.
 template <class P, int CLS, int RP, bool COND>
-__device__ __forceinline__ void u2_regs(typename P::Reg (&r)[kRegs], const typename P::Cst& c, uint32_t cr) {
+__device__ __forceinline__ void u2_regs(typename P::Reg (&r)[kRegs], const typename P::Cst& c, uint32_t cr, bool tc) {
+  if constexpr (COND && CLS == U2_X) {
 #pragma unroll
-  for (int q = 0; q < 4; ++q) {
-    const int j0 = ((q >> RP) << (RP + 1)) | (q & ((1 << RP) - 1));
-    const int j1 = j0 | (1 << RP);
-    if (!COND || (j0 & cr) == cr) P::template u2<CLS>(c, r[j0], r[j1]);
+    for (int q = 0; q < 4; ++q) {
+      const int j0 = ((q >> RP) << (RP + 1)) | (q & ((1 << RP) - 1));
+      const int j1 = j0 | (1 << RP);
+      csel_swap(tc && (j0 & cr) == cr, r[j0], r[j1]);
+    }
+  } else {
+    if (COND && !tc) return;
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      const int j0 = ((q >> RP) << (RP + 1)) | (q & ((1 << RP) - 1));
+      const int j1 = j0 | (1 << RP);
+      if (!COND || (j0 & cr) == cr) P::template u2<CLS>(c, r[j0], r[j1]);
+    }
   }
 }
 
-template <class P, int CLS, bool COND>
-__device__ __forceinline__ void phase_regs(typename P::Reg (&r)[kRegs], const typename P::Cst& c, uint32_t cr) {
+// A phase touches only the registers whose bits include CR (compile time), so
+// a phase conditioned on register bits costs its share of the registers.
+template <class P, int CLS, int CR>
+__device__ __forceinline__ void phase_regs(typename P::Reg (&r)[kRegs], const typename P::Cst& c) {
 #pragma unroll
   for (int j = 0; j < kRegs; ++j)
-    if (!COND || (j & cr) == cr) r[j] = P::template phase<CLS>(c, r[j]);
+    if ((j & CR) == CR) r[j] = P::template phase<CLS>(c, r[j]);
 }
 
 template <class P, int A, int B>  // swap register bits A < B: pairs with bit A = 1, bit B = 0
@@ -412,16 +455,19 @@ __device__ void dense_smem(unsigned char* buf, const KOp& op, const double* dens
 }
 
 #define QG_U2_CASES(CLS)                                                                              \
-  case KC_U2 + CLS * 4 + 0: u2_regs<P, CLS, 0, false>(r, kcst<P>(op), 0); break;                      \
-  case KC_U2 + CLS * 4 + 1: u2_regs<P, CLS, 1, false>(r, kcst<P>(op), 0); break;                      \
-  case KC_U2 + CLS * 4 + 2: u2_regs<P, CLS, 2, false>(r, kcst<P>(op), 0); break;                      \
-  case KF_COND | (KC_U2 + CLS * 4 + 0): if (tc) u2_regs<P, CLS, 0, true>(r, kcst<P>(op), cr); break; \
-  case KF_COND | (KC_U2 + CLS * 4 + 1): if (tc) u2_regs<P, CLS, 1, true>(r, kcst<P>(op), cr); break; \
-  case KF_COND | (KC_U2 + CLS * 4 + 2): if (tc) u2_regs<P, CLS, 2, true>(r, kcst<P>(op), cr); break;
+  case KC_U2 + CLS * 4 + 0: u2_regs<P, CLS, 0, false>(r, kcst<P>(op), 0, true); break;               \
+  case KC_U2 + CLS * 4 + 1: u2_regs<P, CLS, 1, false>(r, kcst<P>(op), 0, true); break;               \
+  case KC_U2 + CLS * 4 + 2: u2_regs<P, CLS, 2, false>(r, kcst<P>(op), 0, true); break;               \
+  case KF_COND | (KC_U2 + CLS * 4 + 0): u2_regs<P, CLS, 0, true>(r, kcst<P>(op), cr, tc); break;     \
+  case KF_COND | (KC_U2 + CLS * 4 + 1): u2_regs<P, CLS, 1, true>(r, kcst<P>(op), cr, tc); break;     \
+  case KF_COND | (KC_U2 + CLS * 4 + 2): u2_regs<P, CLS, 2, true>(r, kcst<P>(op), cr, tc); break;
 
-#define QG_PHASE_CASES(CLS)                                                                         \
-  case KC_PHASE + CLS: phase_regs<P, CLS, false>(r, kcst<P>(op), 0); break;                         \
-  case KF_COND | (KC_PHASE + CLS): if (tc) phase_regs<P, CLS, true>(r, kcst<P>(op), cr); break;
+#define QG_PHASE_CR(CLS, CR)                                                                 \
+  case KC_PHASE + CLS * 8 + CR: phase_regs<P, CLS, CR>(r, kcst<P>(op)); break;               \
+  case KF_COND | (KC_PHASE + CLS * 8 + CR): if (tc) phase_regs<P, CLS, CR>(r, kcst<P>(op)); break;
+#define QG_PHASE_CASES(CLS) \
+  QG_PHASE_CR(CLS, 0) QG_PHASE_CR(CLS, 1) QG_PHASE_CR(CLS, 2) QG_PHASE_CR(CLS, 3) \
+  QG_PHASE_CR(CLS, 4) QG_PHASE_CR(CLS, 5) QG_PHASE_CR(CLS, 6) QG_PHASE_CR(CLS, 7)
 
 // Apply the pass's ops to the tile in buf. Returns with the tile in raw format.
 template <class P>
@@ -524,11 +570,19 @@ __device__ void run_ops(unsigned char* buf, const KOp* __restrict__ sops, int no
   if (in_regs) {
 #pragma unroll
     for (int j = 0; j < kRegs; ++j) P::store_raw(buf, pos[j], r[j]);
+  } else if constexpr (P::kInPairs != P::kOutPairs) {
+    if (raw) {  // no op loaded the tile: convert it in place (each thread its own slots)
+      for (int l = threadIdx.x; l < g.K; l += g.T) {
+        const int p = swz<E>(l);
+        P::store_raw(buf, p, P::load_raw(buf, p));
+      }
+    }
   }
   __syncthreads();
 }
 
 #undef QG_U2_CASES
+#undef QG_PHASE_CR
 #undef QG_PHASE_CASES
 
 // States processed by one launch: all share the pass structure (PassDesc, op
@@ -560,6 +614,13 @@ __global__ void __launch_bounds__(512, 1) k_tile2(const PassDesc pd, const Batch
       if ((h >> (j - g.klow)) & 1) off |= 1ULL << pd.lbits[j];
     hioff[h] = off;
   }
+  // mask of the local bit positions: the next tile's base is the deposit increment
+  // ((base | lm) + 1) & ~lm, which carries through the local positions
+  uint64_t lm = 0;
+  for (int j = 0; j < g.k; ++j) lm |= 1ULL << pd.lbits[j];
+  __syncthreads();  // hioff is complete
+  CopyPlan<E> cp;
+  cp.init(hioff, g);
   // contiguous range of (state, tile) work items for this CTA
   const uint64_t W = ntiles * (uint64_t)ba.nstates;
   const uint64_t w0 = W * blockIdx.x / gridDim.x, w1 = W * (blockIdx.x + 1) / gridDim.x;
@@ -578,23 +639,25 @@ __global__ void __launch_bounds__(512, 1) k_tile2(const PassDesc pd, const Batch
     }
     staged = si;
     __syncthreads();
-    load_tile<E>(smem, state, tile_base(pd, t0), hioff, g);
+    uint64_t base = tile_base(pd, t0);
+    cp.load(smem, state + base * E);
     cp_commit();
     int i = 0;
     for (uint64_t tile = t0; tile < t1; ++tile, ++i) {
       unsigned char* cur = smem + (i & 1) * tile_bytes;
+      const uint64_t nbase = ((base | lm) + 1) & ~lm;
       if (tile + 1 < t1) {
-        load_tile<E>(smem + ((i + 1) & 1) * tile_bytes, state, tile_base(pd, tile + 1), hioff, g);
+        cp.load(smem + ((i + 1) & 1) * tile_bytes, state + nbase * E);
         cp_commit();
         cp_wait<1>();
       } else {
         cp_wait<0>();
       }
       __syncthreads();
-      const uint64_t base = tile_base(pd, tile);
       run_ops<P>(cur, sops, nops, dense, base, g);
-      store_tile<E>(cur, state, base, hioff, g);
+      cp.store(cur, state + base * E);
       __syncthreads();  // the buffer is refilled two tiles later
+      base = nbase;
     }
     w += t1 - t0;
   }
@@ -637,10 +700,10 @@ void build_kops(KOp* out, const TOp* ops, int64_t nops) {
         k.gmask = k.gval = t.gcmask;
         cond = cond || t.gcmask != 0;
         break;
-      case OK_PHASE:
-        k.code = KC_PHASE + t.cls;
+      case OK_PHASE:  // register bits are part of the code; tmask / gmask make it conditional
+        k.code = KC_PHASE + t.cls * 8 + (int)(t.rmask & 7u);
         k.gmask = k.gval = t.gmask;
-        cond = cond || t.gmask != 0;
+        cond = t.tmask != 0 || t.gmask != 0;
         break;
       case OK_SWAP: {
         const int a = t.dbits[0], b = t.dbits[1];
@@ -689,8 +752,8 @@ cudaError_t launch_t(int n, const PassDesc& pd, const BatchArgs& ba, const doubl
   if (grid > work) grid = work;
   // One fixed limit for every launch: worker threads launch passes of different
   // sizes concurrently, and a per-launch value could undercut another thread's launch.
-  // two 64 KiB tile buffers, the largest op list, the chunk-offset table
-  constexpr size_t kSmemLimit = 2 * (size_t(64) << 10) + sizeof(KOp) * kMaxKOps + 8 * 256;
+  // two 64 KiB tile buffers, the largest op list, the chunk-offset table (2^(12-3) entries)
+  constexpr size_t kSmemLimit = 2 * (size_t(64) << 10) + sizeof(KOp) * kMaxKOps + 8 * 512;
   static_assert(kSmemLimit <= 227 * 1024, "shared memory");
   if (smem > kSmemLimit) return cudaErrorInvalidValue;
   cudaError_t e = cudaFuncSetAttribute(k_tile2<P>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmemLimit);
@@ -702,19 +765,29 @@ cudaError_t launch_t(int n, const PassDesc& pd, const BatchArgs& ba, const doubl
 
 }  // namespace
 
+int tile_pass_io(const Program& prog, size_t step) {
+  if (prog.arith != QG_ARITH_DOUBLE_FLOAT) return 0;
+  auto tiled = [&](size_t j) { return j < prog.steps.size() && prog.steps[j].kind == Step::TILE_PASS; };
+  if (!tiled(step)) return 0;
+  int io = 0;
+  if (step > 0 && tiled(step - 1)) io |= kTileInPairs;
+  if (tiled(step + 1)) io |= kTileOutPairs;
+  return io;
+}
+
 int max_ops_per_tile_pass() { return kMaxKOps; }
 size_t kop_record_bytes() { return sizeof(KOp); }
 
 void encode_kops(int precision, int arithmetic, const TOp* tops, int64_t count, void* out) {
   KOp* k = reinterpret_cast<KOp*>(out);
   if (precision == QG_C64) build_kops<PolF>(k, tops, count);
-  else if (arithmetic == QG_ARITH_DOUBLE_FLOAT) build_kops<PolDF>(k, tops, count);
+  else if (arithmetic == QG_ARITH_DOUBLE_FLOAT) build_kops<PolDFT<0>>(k, tops, count);
   else build_kops<PolD>(k, tops, count);
 }
 
-cudaError_t launch_tile_pass(int precision, int arithmetic, int n, const PassDesc& pd, void* const* d_states,
-                             int nstates, const void* d_kops, int64_t ops_stride, const double* d_dense,
-                             cudaStream_t st) {
+cudaError_t launch_tile_pass(int precision, int arithmetic, int io, int n, const PassDesc& pd,
+                             void* const* d_states, int nstates, const void* d_kops, int64_t ops_stride,
+                             const double* d_dense, cudaStream_t st) {
   if (pd.k < 3 || pd.k > kMaxTileBits) return cudaErrorInvalidValue;
   BatchArgs ba;
   ba.states = reinterpret_cast<unsigned char* const*>(d_states);
@@ -722,7 +795,14 @@ cudaError_t launch_tile_pass(int precision, int arithmetic, int n, const PassDes
   ba.ops_stride = ops_stride;
   ba.nstates = nstates;
   if (precision == QG_C64) return launch_t<PolF>(n, pd, ba, d_dense, st);
-  if (arithmetic == QG_ARITH_DOUBLE_FLOAT) return launch_t<PolDF>(n, pd, ba, d_dense, st);
+  if (arithmetic == QG_ARITH_DOUBLE_FLOAT) {
+    switch (io & 3) {
+      case 0: return launch_t<PolDFT<0>>(n, pd, ba, d_dense, st);
+      case 1: return launch_t<PolDFT<1>>(n, pd, ba, d_dense, st);
+      case 2: return launch_t<PolDFT<2>>(n, pd, ba, d_dense, st);
+      default: return launch_t<PolDFT<3>>(n, pd, ba, d_dense, st);
+    }
+  }
   return launch_t<PolD>(n, pd, ba, d_dense, st);
 }
 

@@ -346,6 +346,26 @@ def test_every_gate_c128_double_float(gpu_ctx_df, oracle, n):
         assert np.max(np.abs(st.download() - ref)) <= 1e-12
 
 
+def test_double_float_mid_circuit_measurement(gpu_ctx_df, oracle):
+    """Measurements split the runs of double-float passes: the state is handed over
+    as float pairs inside a run and converted back to doubles at each measurement."""
+    from qclojure_gb300 import workloads
+
+    n = 16
+    c = workloads.layered_circuit(n, 8, seed=18)
+    c["operations"] = c["operations"] + [{"operation-type": "measure",
+                                          "operation-params": {"measurement-qubits": [3, 0, 15]}}] + \
+        workloads.layered_circuit(n, 6, seed=19)["operations"] + \
+        [{"operation-type": "measure", "operation-params": {"measurement-qubits": [11]}}] + \
+        workloads.layered_circuit(n, 2, seed=20)["operations"]
+    with gpu_ctx_df.state(n) as st:
+        for seed in (1, 2):
+            ref = oracle.run(c, seed=seed)
+            st.set_basis(0)
+            st.apply(c, fusion="tiled", seed=seed)
+            assert np.max(np.abs(st.download() - ref)) <= 1e-12
+
+
 def test_double_float_deep_circuit_error(gpu_ctx_df, oracle):
     """300 layers (4500 gates) on 10 qubits: accumulated error stays below 1e-12."""
     from qclojure_gb300 import workloads
