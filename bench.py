@@ -285,6 +285,13 @@ def main():
     peak, peak_src = measured_peaks()
     mean_pass = statistics.mean(dom) if dom else float("nan")
     achieved = pass_bytes / (mean_pass / 1e3) / 1e9 if dom else float("nan")
+    # DRAM bytes per tiled pass from an ncu capture of the same kernel on a 26-qubit state
+    # (dram__bytes_read.sum + dram__bytes_write.sum = 2.086e9 per launch), scaled by the
+    # amplitudes processed: profiles/k_tile2_PolDFT_c128_layered30x40_qft30.md
+    traffic, traffic_src = None, None
+    if args.precision == "c128" and args.fusion == "tiled":
+        traffic = 2.086e9 * 2 ** (n - 26)
+        traffic_src = "ncu capture at 26 qubits x 2^(n-26)"
     # time of the 40 random layers alone, per layer
     st.set_basis(0)
     tl0 = torch.cuda.Event(enable_timing=True)
@@ -306,8 +313,9 @@ def main():
         "layer_ms": layer_ms,
         "hbm_passes_per_step": len(pass_ms),
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                     "frac": achieved / peak if dom else None, "traffic": None,
-                     "kernel": "k_tile<double>" if args.precision == "c128" else "k_tile<float>",
+                     "frac": achieved / peak if dom else None, "traffic": traffic,
+                     "traffic_source": traffic_src,
+                     "kernel": "k_tile2<PolDFT>" if args.precision == "c128" else "k_tile2<PolF>",
                      "peak_source": peak_src, "pass_bytes": pass_bytes, "mean_pass_ms": mean_pass,
                      "passes": len(dom)},
         "gpu_launches": int(l1.value - l0.value),
@@ -386,6 +394,31 @@ def main():
                        "d2h_bytes_per_step": 1024 * 8 * 2, "ms_per_step": dt * 1e3,
                        "path": "qg_submit -> qg_wait -> qg_result_counts/shots (1024 shots)"}
         sim.close()
+
+        # memory ceiling: 33-qubit complex128 and 34-qubit complex64 (128 GiB each), depth 30 of
+        # {H,S,T,RZ} on every qubit + CZ on a random matching, in place, then 10^6 shots
+        ceiling = {}
+        for cn, cprec in ((33, "c128"), (34, "c64")):
+            cc = workloads.ceiling_circuit(cn, 30, seed=args.seed)
+            with ctx.state(cn, cprec) as sc:
+                _, scs = sc.device_ptr()
+                cstream = torch.cuda.ExternalStream(scs, device=torch.device("cuda", local))
+                ca = torch.cuda.Event(enable_timing=True)
+                cb = torch.cuda.Event(enable_timing=True)
+                ca.record(cstream)
+                sc.apply(cc, fusion=args.fusion)
+                cb.record(cstream)
+                cb.synchronize()
+                gms = ca.elapsed_time(cb)
+                t0 = time.perf_counter()
+                sc.sample(1_000_000, 3)
+                sms = (time.perf_counter() - t0) * 1e3
+            cg = len(cc["operations"])
+            ceiling[cprec] = {"n_qubits": cn, "state_gib": (16 if cprec == "c128" else 8) * 2**cn / 2**30,
+                              "gates": cg, "gates_ms": gms, "gate_amps_per_s": cg * 2**cn / (gms / 1e3),
+                              "shots": 1_000_000, "shots_ms": sms}
+        ceiling["workload"] = "ceiling: depth 30 of {H,S,T,RZ} + CZ matching, in place, 10^6 shots"
+        line["memory_ceiling"] = ceiling
         rate, desc, threads = cpu_reference_rate(n, gates, 8.0)
         line["cpu_baseline"] = {"value": rate, "unit": UNIT, "cores": threads, "kind": "port", "sample": desc}
     else:
