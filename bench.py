@@ -160,6 +160,95 @@ def cpu_reference_rate(n: int, gates_per_step: int, budget_s: float, threads: in
 
 
 # ---------------------------------------------------------------------------
+def replay_trace(sim, trace, timeout_s=900.0):
+    """Submit each job of `trace` at its arrival time through the job API and wait for all.
+    Latency of a job = its submission delay + queue + execution time on the runtime's clock.
+    Returns (circuits/s over first arrival .. last completion, latencies in ms, jobs that
+    shared a small-job launch, largest such launch)."""
+    import ctypes as C
+
+    from qclojure_gb300 import _abi as A
+
+    ids = [None] * len(trace)
+    lag = [0.0] * len(trace)
+    t0 = time.perf_counter()
+
+    def submitter():
+        for k, job in enumerate(trace):
+            wait = t0 + job["arrival-s"] - time.perf_counter()
+            if wait > 0:
+                time.sleep(wait)
+            ids[k] = sim.submit_circuit(job["circuit"], {"result-specs": job["result-specs"]})
+            lag[k] = time.perf_counter() - (t0 + job["arrival-s"])
+
+    th = threading.Thread(target=submitter)
+    th.start()
+    th.join()
+    lat, batched, max_batch = [], 0, 0
+    for k, jid in enumerate(ids):
+        s = sim.wait(jid, int(timeout_s * 1e3))
+        if s != "completed":
+            raise RuntimeError(f"serving job {k} ended {s}")
+    t_end = time.perf_counter()
+    for k, jid in enumerate(ids):
+        info = A.QgJobInfo()
+        sim._lib.qg_job_details(sim._ctx, C.c_uint64(sim._jid(jid)), C.byref(info))
+        lat.append(lag[k] * 1e3 + info.queue_time_ms + info.execution_time_ms)
+        if info.batched_with > 1:
+            batched += 1
+        max_batch = max(max_batch, info.batched_with)
+        sim.free_job(jid)
+    return len(trace) / (t_end - t0), lat, batched, max_batch
+
+
+def serving_leg(num_jobs=100, rates=(100, 1000, 5000), seed=11):
+    """Serving stream: Poisson arrivals, n = 8 + Geometric(0.15) capped at 28, depth U{10..200}
+    of the layered recipe, 90% shot jobs (1k..100k shots) and 10% Pauli-string expectations.
+    complex64 served (continuous batching, concurrent worker streams) against plain complex128
+    per job (one HBM pass per gate, one job at a time) on the same jobs."""
+    from qclojure_gb300 import workloads
+    from qclojure_gb300.backend import create_simulator
+
+    def pct(v, q):
+        s = sorted(v)
+        return s[min(len(s) - 1, int(round(q * (len(s) - 1))))]
+
+    out = {"workload": f"{num_jobs} jobs: n = 8 + Geometric(0.15) capped at 28, depth U{{10..200}} layered, "
+                       "90% shots U{1k..100k}, 10% Pauli expectation", "c64_served": {}}
+    sim = create_simulator({"precision": "c64", "fusion": "tiled", "workers": 16, "seed": 5})
+    try:
+        replay_trace(sim, workloads.serving_trace(24, 1000.0, seed + 99, max_qubits=14))  # warm-up
+        for r in rates:
+            trace = workloads.serving_trace(num_jobs, float(r), seed)
+            cps, lat, nb, mb = replay_trace(sim, trace)
+            out["c64_served"][str(r)] = {"circuits_per_s": cps, "p50_ms": pct(lat, 0.5), "p99_ms": pct(lat, 0.99),
+                                         "jobs_batched": nb, "largest_batch": mb}
+    finally:
+        sim.close()
+    trace = workloads.serving_trace(num_jobs, float(rates[-1]), seed)
+    plain = create_simulator({"precision": "c128", "fusion": "plain", "workers": 1, "seed": 5,
+                              "arithmetic": "exact"})
+    try:
+        lat = []
+        t0 = time.perf_counter()
+        for job in trace:
+            t1 = time.perf_counter()
+            jid = plain.submit_circuit(job["circuit"], {"result-specs": job["result-specs"]})
+            if plain.wait(jid, 900_000) != "completed":
+                raise RuntimeError("plain job failed")
+            lat.append((time.perf_counter() - t1) * 1e3)
+            plain.free_job(jid)
+        dt = time.perf_counter() - t0
+    finally:
+        plain.close()
+    out["plain_c128_per_job"] = {"circuits_per_s": num_jobs / dt, "p50_ms": pct(lat, 0.5), "p99_ms": pct(lat, 0.99),
+                                 "note": "same jobs, one at a time, one HBM pass per gate"}
+    top = out["c64_served"][str(rates[-1])]["circuits_per_s"]
+    out["served_over_plain"] = top / out["plain_c128_per_job"]["circuits_per_s"]
+    return out
+
+
+# ---------------------------------------------------------------------------
 def run_reference(args):
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
@@ -419,6 +508,7 @@ def main():
                               "shots": 1_000_000, "shots_ms": sms}
         ceiling["workload"] = "ceiling: depth 30 of {H,S,T,RZ} + CZ matching, in place, 10^6 shots"
         line["memory_ceiling"] = ceiling
+        line["serving"] = serving_leg()
         rate, desc, threads = cpu_reference_rate(n, gates, 8.0)
         line["cpu_baseline"] = {"value": rate, "unit": UNIT, "cores": threads, "kind": "port", "sample": desc}
     else:

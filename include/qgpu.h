@@ -207,6 +207,8 @@ typedef struct qg_job_info {
   int64_t num_distinct_outcomes;
   int32_t has_results;            /* QG_RES_* flags that are available                    */
   int32_t error_code;
+  int32_t batched_with;           /* jobs that shared its small-job launch (0: ran alone) */
+  int32_t reserved;
 } qg_job_info;
 
 /* ---- context ------------------------------------------------------------ */

@@ -116,7 +116,8 @@ class QgJobInfo(C.Structure):
     _fields_ = [("status", C.c_int32), ("num_qubits", C.c_int32), ("precision", C.c_int32),
                 ("num_passes", C.c_int32), ("execution_time_ms", C.c_double), ("device_time_ms", C.c_double),
                 ("queue_time_ms", C.c_double), ("shots", C.c_uint64), ("num_distinct_outcomes", C.c_int64),
-                ("has_results", C.c_int32), ("error_code", C.c_int32)]
+                ("has_results", C.c_int32), ("error_code", C.c_int32), ("batched_with", C.c_int32),
+                ("reserved", C.c_int32)]
 
 
 class QgSweepStats(C.Structure):

@@ -340,7 +340,8 @@ class GpuStateVectorSimulator:
         _check(self._lib.qg_job_details(self._ctx, C.c_uint64(jid), C.byref(info)))
         results = self._results(jid, info)
         return {"job-status": "completed", "results": results, "execution-time-ms": info.execution_time_ms,
-                "device-time-ms": info.device_time_ms, "hbm-passes": info.num_passes, "job-id": job_id}
+                "device-time-ms": info.device_time_ms, "hbm-passes": info.num_passes,
+                "batched-with": info.batched_with, "job-id": job_id}
 
     def _results(self, jid: int, info) -> dict:
         meta = self._meta.get(jid, {})
@@ -469,10 +470,38 @@ class GpuStateVectorSimulator:
 
     # -- BatchJobBackend -----------------------------------------------------------
     def batch_submit(self, circuits: list[dict], options: dict | None = None) -> str:
-        ids = [self.submit_circuit(c, options) for c in circuits]
+        """batch-submit (backend.clj:136-168): all circuits share the options and are queued
+        together (nothing is queued if one is invalid), so small ones run in shared launches."""
+        options = options or {}
+        for c in circuits:
+            validate_circuit(c)
+        specs = options.get("result-specs") or {}
+        sized = any(k in specs for k in ("hamiltonian", "amplitudes", "fidelity")) or bool(
+            isinstance(specs.get("probabilities"), Mapping) and specs["probabilities"].get("targets"))
+        if len({c["num-qubits"] for c in circuits}) > 1 and sized:
+            raise CircuitError("shared result specs that name qubits or basis states need equal qubit counts")
+        encs = [encode(c) for c in circuits]
         bid = f"gpu_batch_{len(self._batches) + 1}_{int(time.time() * 1000)}"
+        if not circuits:
+            with self._lock:
+                self._batches[bid] = (0, [])
+            return bid
+        opts, keep, meta0 = self._build_options(circuits[0], options)
+        arr = (A.QgCircuit * len(encs))(*[e.c for e in encs])
+        jobs = (C.c_uint64 * len(encs))()
+        cbid = C.c_uint64()
+        _check(self._lib.qg_batch_submit(self._ctx, arr, len(encs), C.byref(opts), C.byref(cbid), jobs),
+               self._lib, self._ctx)
+        ms = int(time.time() * 1000)
+        ids = []
         with self._lock:
-            self._batches[bid] = (0, ids)
+            for k, c in enumerate(circuits):
+                jid = int(jobs[k])
+                self._meta[jid] = dict(meta0, circuit=c, n=c["num-qubits"])
+                sid = f"gpu_job_{jid}_{ms}"
+                self._ids[sid] = jid
+                ids.append(sid)
+            self._batches[bid] = (cbid.value, ids)
         return bid
 
     def batch_status(self, batch_id: str) -> dict:

@@ -156,6 +156,17 @@ cudaError_t launch_tile_pass(int precision, int arithmetic, int io, int n, const
 // state over as float pairs; the first converts from doubles, the last back.
 int tile_pass_io(const Program& prog, size_t step);
 int max_ops_per_tile_pass();
+// Small jobs (tiled programs of 5..kMaxSmallJobQubits qubits: one tile per state)
+// run whole in one CTA each; one launch per qubit count (k_tile_jobs).
+constexpr int kMaxSmallJobQubits = 12;
+struct TileJobRec {
+  void* state;          // device amplitudes (IEEE layout of the job's precision)
+  int64_t op_begin;     // first op record of the job in the launch's record array
+  int32_t npasses;      // passes of the job's program
+  int32_t pass_begin;   // index of its first pass in the launch's op-count array
+};
+cudaError_t launch_tile_jobs(int precision, int arithmetic, int n, const TileJobRec* d_jobs, int njobs,
+                             const void* d_kops, const int32_t* d_pass_nops, cudaStream_t st);
 size_t kop_record_bytes();
 // batched sweep kernels (sweep.cu)
 int diag_max_groups();

@@ -20,6 +20,7 @@
 #include <mutex>
 #include <string>
 #include <thread>
+#include <tuple>
 #include <vector>
 
 #include "qgpu_internal.h"
@@ -514,6 +515,8 @@ struct Job {
   std::unique_ptr<State> state;       // final state kept on the device
   bool state_pinned = false;          // requested by :state-vector; never evicted
   uint64_t batch = 0;
+  std::unique_ptr<Program> prog;      // compiled by the worker that admitted the job
+  int batched_with = 0;               // jobs that shared its small-job launch (0: run alone)
 };
 
 struct Ctx {
@@ -526,7 +529,15 @@ struct Ctx {
   std::deque<uint64_t> queue;
   std::map<uint64_t, std::vector<uint64_t>> batches;
   std::vector<std::thread> workers;
+  // compiled small jobs (one tile per state) waiting for the batcher, which runs
+  // everything ready of one qubit count in one launch
+  std::deque<std::shared_ptr<Job>> ready;
+  std::condition_variable ready_cv;
+  std::thread batcher;
   bool stop = false;
+  bool batch_stop = false;  // set after the workers have exited
+  int small_queued = 0;     // queued jobs of the small-job lane
+  int compiling = 0;        // small jobs admitted and being compiled
   uint64_t next_id = 1;
   uint64_t hbm_budget = 0, hbm_in_use = 0, hbm_total = 0;
   int sm_count = 0;
@@ -576,31 +587,59 @@ static bool make_room(Ctx* c, size_t need) {
   return c->hbm_in_use + need <= c->hbm_budget;
 }
 
+static int compile_job(Ctx* c, Job* j, std::string* err) {
+  auto prog = std::make_unique<Program>();
+  qg_circuit circ{j->n, (int32_t)j->ops.size(), j->ops.data()};
+  const int rc = compile_program(&circ, j->precision, j->fusion, c->cfg.fuse_k, j->arith, prog.get(), err);
+  if (rc == QG_OK) j->prog = std::move(prog);
+  return rc;
+}
+
+// Jobs of the small-job lane: tiled fusion and 5..12 qubits (one tile per state).
+static bool small_eligible(const Job* j) {
+  return j->fusion == QG_FUSE_TILED && j->n >= 5 && j->n <= kMaxSmallJobQubits;
+}
+
+// A small job's state is one tile (5..12 qubits) and its program is tiled passes only.
+static bool small_job(const Job* j) {
+  if (!j->prog || j->fusion != QG_FUSE_TILED || j->n < 5 || j->n > kMaxSmallJobQubits) return false;
+  for (const Step& s : j->prog->steps)
+    if (s.kind != Step::TILE_PASS) return false;
+  return true;
+}
+
+// Allocate the job's state on `stream` and set it to |0...0> or the initial state.
+static int init_job_state(Ctx* c, Job* j, cudaStream_t stream, State* st, std::string* err) {
+  st->ctx = c;
+  int rc = state_alloc(st, j->n, j->precision, stream, err);
+  if (rc != QG_OK) return rc;
+  if (!j->initial.empty()) return upload_c128(st, j->initial.data(), err);
+  cudaError_t e = launch_set_basis(st->d, st->prec, st->n, 0, stream);
+  return e == cudaSuccess ? QG_OK : cuda_fail(err, e, "zero-state");
+}
+
+static int job_results(Ctx* c, Job* j, std::unique_ptr<State> st, cudaStream_t stream, int rc, std::string err);
+
 static int run_job(Ctx* c, Job* j, cudaStream_t stream) {
   std::string err;
-  int rc;
-  Program prog;
-  qg_circuit circ{j->n, (int32_t)j->ops.size(), j->ops.data()};
-  rc = compile_program(&circ, j->precision, j->fusion, c->cfg.fuse_k, j->arith, &prog, &err);
+  int rc = j->prog ? QG_OK : compile_job(c, j, &err);
   if (rc != QG_OK) {
     j->error_code = rc;
     j->error = err;
     return rc;
   }
   auto st = std::make_unique<State>();
-  st->ctx = c;
-  rc = state_alloc(st.get(), j->n, j->precision, stream, &err);
-  if (rc == QG_OK) {
-    if (!j->initial.empty()) rc = upload_c128(st.get(), j->initial.data(), &err);
-    else {
-      cudaError_t e = launch_set_basis(st->d, st->prec, st->n, 0, stream);
-      if (e != cudaSuccess) rc = cuda_fail(&err, e, "zero-state");
-    }
-  }
+  rc = init_job_state(c, j, stream, st.get(), &err);
   ExecStats stats;
-  if (rc == QG_OK) rc = exec_program(st.get(), prog, j->seed, &j->cancel, &stats, &err);
+  if (rc == QG_OK) rc = exec_program(st.get(), *j->prog, j->seed, &j->cancel, &stats, &err);
   j->device_ms = stats.device_ms;
   j->passes = stats.passes;
+  return job_results(c, j, std::move(st), stream, rc, std::move(err));
+}
+
+// Result extraction on the final state (result.clj:179-457), then keep the state
+// for later reads or release it.
+static int job_results(Ctx* c, Job* j, std::unique_ptr<State> st, cudaStream_t stream, int rc, std::string err) {
   const SpecCopy& sp = j->spec;
   const uint64_t N = 1ULL << j->n;
   if (rc == QG_OK && (sp.flags & QG_RES_MEASUREMENTS)) {
@@ -741,7 +780,22 @@ static int run_job(Ctx* c, Job* j, cudaStream_t stream) {
   return rc;
 }
 
-static void worker_loop(Ctx* c) {
+// Release the job's HBM reservation unless its final state is kept, and publish the outcome.
+static void complete_job(Ctx* c, Job* j, int rc) {
+  const size_t need = job_bytes(j->n, j->precision);
+  {
+    std::lock_guard<std::mutex> g(c->mu);
+    if (need <= c->hbm_budget && !j->state) c->hbm_in_use -= std::min(c->hbm_in_use, need);
+  }
+  c->cv.notify_all();
+  if (rc == QG_OK) finish_job(c, j, QG_JOB_COMPLETED);
+  else if (rc == QG_ERR_CANCELLED) finish_job(c, j, QG_JOB_CANCELLED);
+  else finish_job(c, j, QG_JOB_FAILED);
+}
+
+// Workers of the small-job lane compile small jobs and hand them to the batcher,
+// so small jobs never wait behind large ones; the other workers run large jobs.
+static void worker_loop(Ctx* c, bool small_lane) {
   cudaSetDevice(c->device);
   cudaStream_t stream;
   cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking);
@@ -751,19 +805,22 @@ static void worker_loop(Ctx* c) {
       std::unique_lock<std::mutex> lk(c->mu);
       for (;;) {
         if (c->stop) break;
-        // first queued job that fits (jobs that can never fit fail at once)
+        // first queued job of this lane that fits (jobs that can never fit fail at once)
         bool picked = false;
         for (auto it = c->queue.begin(); it != c->queue.end(); ++it) {
           auto jj = c->jobs.find(*it);
           if (jj == c->jobs.end() || jj->second->status.load() != QG_JOB_QUEUED) {
+            if (jj != c->jobs.end() && small_eligible(jj->second.get())) --c->small_queued;
             c->queue.erase(it);
             picked = true;  // rescan
             break;
           }
+          if (small_eligible(jj->second.get()) != small_lane) continue;
           size_t need = job_bytes(jj->second->n, jj->second->precision);
           if (need > c->hbm_budget) {
             j = jj->second;
             c->queue.erase(it);
+            if (small_lane) --c->small_queued;
             picked = true;
             break;
           }
@@ -771,6 +828,7 @@ static void worker_loop(Ctx* c) {
             c->hbm_in_use += need;
             j = jj->second;
             c->queue.erase(it);
+            if (small_lane) --c->small_queued;
             picked = true;
             break;
           }
@@ -785,29 +843,164 @@ static void worker_loop(Ctx* c) {
         j->status.store(QG_JOB_CANCELLED);
       } else {
         j->status.store(QG_JOB_RUNNING);
+        if (small_lane) ++c->compiling;
       }
     }
     if (j->status.load() == QG_JOB_CANCELLED) {
-      c->done_cv.notify_all();
+      complete_job(c, j.get(), QG_ERR_CANCELLED);  // releases the HBM reservation
       continue;
     }
     const size_t need = job_bytes(j->n, j->precision);
-    int rc;
+    int rc = QG_OK;
     if (need > c->hbm_budget) {
       j->error_code = QG_ERR_OOM;
       j->error = "state of " + std::to_string(j->n) + " qubits does not fit the HBM budget";
       rc = QG_ERR_OOM;
+      if (small_lane) {
+        std::lock_guard<std::mutex> g(c->mu);
+        --c->compiling;
+      }
     } else {
-      rc = run_job(c, j.get(), stream);
+      if (small_lane) {
+        // compile here (the lane's workers compile in parallel) and hand the job to the batcher
+        std::string err;
+        rc = compile_job(c, j.get(), &err);
+        const bool batch = rc == QG_OK && small_job(j.get());
+        {
+          std::lock_guard<std::mutex> g(c->mu);
+          if (batch) c->ready.push_back(j);
+          --c->compiling;
+        }
+        c->ready_cv.notify_all();
+        if (batch) continue;
+        if (rc != QG_OK) {
+          j->error_code = rc;
+          j->error = err;
+        }
+      }
+      if (rc == QG_OK) rc = run_job(c, j.get(), stream);  // mid-circuit measurements run per job
     }
+    complete_job(c, j.get(), rc);
+  }
+  cudaStreamSynchronize(stream);
+  cudaStreamDestroy(stream);
+}
+
+
+// ---------------------------------------------------------------------------
+// Continuous batching of small jobs. Workers admit jobs as they arrive (HBM
+// budget) and compile them; small ones (one tile per state) wait in `ready`.
+// The batcher takes everything ready, groups it by qubit count, precision and
+// arithmetic, and runs each group in one k_tile_jobs launch (one CTA per job)
+// while larger jobs run on the workers' streams. Jobs that arrive meanwhile go
+// into the next batch.
+// ---------------------------------------------------------------------------
+constexpr size_t kMaxBatchJobs = 4096;
+constexpr int kBatchWindowUs = 2000;   // longest wait for jobs still being admitted
+constexpr int kSmallLaneWorkers = 4;
+
+static void run_batch(Ctx* c, std::vector<std::shared_ptr<Job>>& batch, cudaStream_t stream) {
+  std::map<std::tuple<int, int, int>, std::vector<Job*>> groups;
+  for (auto& j : batch) {
+    if (j->cancel.load()) {
+      complete_job(c, j.get(), QG_ERR_CANCELLED);
+      continue;
+    }
+    groups[std::make_tuple(j->n, j->precision, j->prog->arith)].push_back(j.get());
+  }
+  const size_t rec = kop_record_bytes();
+  for (auto& kv : groups) {
+    std::vector<Job*>& js = kv.second;
+    const int n = std::get<0>(kv.first), prec = std::get<1>(kv.first), arith = std::get<2>(kv.first);
+    const size_t m = js.size();
+    std::vector<std::unique_ptr<State>> sts(m);
+    std::vector<int> rcs(m, QG_OK);
+    std::vector<std::string> errs(m);
+    std::vector<TileJobRec> recs;
+    std::vector<int32_t> nops;
+    std::vector<size_t> members;
+    size_t total_ops = 0;
+    for (size_t i = 0; i < m; ++i) {
+      sts[i] = std::make_unique<State>();
+      rcs[i] = init_job_state(c, js[i], stream, sts[i].get(), &errs[i]);
+      if (rcs[i] != QG_OK) continue;
+      TileJobRec r;
+      r.state = sts[i]->d;
+      r.op_begin = (int64_t)total_ops;
+      r.pass_begin = (int32_t)nops.size();
+      r.npasses = 0;
+      for (const Step& s : js[i]->prog->steps) {
+        nops.push_back((int32_t)(s.pass.op_end - s.pass.op_begin));
+        ++r.npasses;
+      }
+      total_ops += js[i]->prog->tops.size();
+      recs.push_back(r);
+      members.push_back(i);
+    }
+    float ms = 0;
+    if (!recs.empty()) {
+      // one upload: op records (16-byte aligned), job records, per-pass op counts
+      const size_t b_ops = rec * total_ops, b_recs = sizeof(TileJobRec) * recs.size();
+      std::vector<unsigned char> host(b_ops + b_recs + sizeof(int32_t) * nops.size() + 16);
+      size_t off = 0;
+      for (size_t q : members) {
+        const Program& pr = *js[q]->prog;
+        encode_kops(prec, pr.arith, pr.tops.data(), (int64_t)pr.tops.size(), host.data() + off);
+        off += rec * pr.tops.size();
+      }
+      std::memcpy(host.data() + b_ops, recs.data(), b_recs);
+      if (!nops.empty()) std::memcpy(host.data() + b_ops + b_recs, nops.data(), sizeof(int32_t) * nops.size());
+      unsigned char* d = nullptr;
+      cudaEvent_t e0 = nullptr, e1 = nullptr;
+      cudaError_t e = cudaMallocAsync((void**)&d, host.size(), stream);
+      if (e == cudaSuccess) e = cudaMemcpyAsync(d, host.data(), host.size(), cudaMemcpyHostToDevice, stream);
+      if (e == cudaSuccess) e = cudaEventCreate(&e0);
+      if (e == cudaSuccess) e = cudaEventCreate(&e1);
+      if (e == cudaSuccess) e = cudaEventRecord(e0, stream);
+      if (e == cudaSuccess)
+        e = launch_tile_jobs(prec, arith, n, reinterpret_cast<const TileJobRec*>(d + b_ops), (int)recs.size(), d,
+                             reinterpret_cast<const int32_t*>(d + b_ops + b_recs), stream);
+      if (e == cudaSuccess) e = cudaEventRecord(e1, stream);
+      if (e == cudaSuccess) e = cudaStreamSynchronize(stream);
+      if (e == cudaSuccess) cudaEventElapsedTime(&ms, e0, e1);
+      if (e0) cudaEventDestroy(e0);
+      if (e1) cudaEventDestroy(e1);
+      if (d) cudaFreeAsync(d, stream);
+      if (e != cudaSuccess)
+        for (size_t q : members) rcs[q] = cuda_fail(&errs[q], e, "small-job batch");
+    }
+    for (size_t i = 0; i < m; ++i) {
+      Job* j = js[i];
+      j->device_ms = ms;
+      j->passes = j->prog->hbm_passes;
+      j->batched_with = (int)recs.size();
+      const int rc = job_results(c, j, std::move(sts[i]), stream, rcs[i], std::move(errs[i]));
+      complete_job(c, j, rc);
+    }
+  }
+}
+
+static void batcher_loop(Ctx* c) {
+  cudaSetDevice(c->device);
+  cudaStream_t stream;
+  cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking);
+  for (;;) {
+    std::vector<std::shared_ptr<Job>> batch;
     {
-      std::lock_guard<std::mutex> g(c->mu);
-      if (need <= c->hbm_budget && !j->state) c->hbm_in_use -= std::min(c->hbm_in_use, need);
+      std::unique_lock<std::mutex> lk(c->mu);
+      c->ready_cv.wait(lk, [&] { return c->batch_stop || !c->ready.empty(); });
+      if (c->ready.empty()) break;  // batch_stop and nothing left
+      // gathering window: small jobs already queued or being compiled join this batch
+      const auto deadline = Clock::now() + std::chrono::microseconds(kBatchWindowUs);
+      while (!c->batch_stop && (c->compiling > 0 || c->small_queued > 0) && c->ready.size() < kMaxBatchJobs &&
+             c->ready_cv.wait_until(lk, deadline) != std::cv_status::timeout) {
+      }
+      while (!c->ready.empty() && batch.size() < kMaxBatchJobs) {
+        batch.push_back(c->ready.front());
+        c->ready.pop_front();
+      }
     }
-    c->cv.notify_all();
-    if (rc == QG_OK) finish_job(c, j.get(), QG_JOB_COMPLETED);
-    else if (rc == QG_ERR_CANCELLED) finish_job(c, j.get(), QG_JOB_CANCELLED);
-    else finish_job(c, j.get(), QG_JOB_FAILED);
+    run_batch(c, batch, stream);
   }
   cudaStreamSynchronize(stream);
   cudaStreamDestroy(stream);
@@ -881,8 +1074,9 @@ static int copy_spec(const qg_result_spec* in, int n, SpecCopy* out, std::string
   return QG_OK;
 }
 
-static int submit_one(Ctx* c, const qg_circuit* circ, const qg_options* opt, uint64_t batch, uint64_t* id_out) {
-  if (!circ || !id_out) return QG_ERR_INVALID_ARG;
+// Validate a circuit and its options into a Job (not yet queued).
+static int prepare_job(Ctx* c, const qg_circuit* circ, const qg_options* opt, std::shared_ptr<Job>* out) {
+  if (!circ) return QG_ERR_INVALID_ARG;
   std::string err;
   // validate now (ideal_simulator.clj relies on :pre checks in backend.clj:228-230)
   {
@@ -918,17 +1112,36 @@ static int submit_one(Ctx* c, const qg_circuit* circ, const qg_options* opt, uin
     set_ctx_error(c, "circuit exceeds max-qubits of this backend");
     return QG_ERR_OOM;
   }
-  j->submitted = Clock::now();
-  j->batch = batch;
+  *out = std::move(j);
+  return QG_OK;
+}
+
+// Queue prepared jobs in one step (a batch arrives together) and assign their ids.
+static void enqueue_jobs(Ctx* c, std::vector<std::shared_ptr<Job>>& js, uint64_t batch, uint64_t* ids_out) {
+  const auto now = Clock::now();
   {
     std::lock_guard<std::mutex> g(c->mu);
-    j->id = c->next_id++;
-    c->jobs[j->id] = j;
-    c->queue.push_back(j->id);
-    if (batch) c->batches[batch].push_back(j->id);
+    for (size_t i = 0; i < js.size(); ++i) {
+      Job* j = js[i].get();
+      j->submitted = now;
+      j->batch = batch;
+      j->id = c->next_id++;
+      c->jobs[j->id] = js[i];
+      c->queue.push_back(j->id);
+      if (small_eligible(j)) ++c->small_queued;
+      if (batch) c->batches[batch].push_back(j->id);
+      if (ids_out) ids_out[i] = j->id;
+    }
   }
   c->cv.notify_all();
-  *id_out = j->id;
+}
+
+static int submit_one(Ctx* c, const qg_circuit* circ, const qg_options* opt, uint64_t* id_out) {
+  if (!circ || !id_out) return QG_ERR_INVALID_ARG;
+  std::vector<std::shared_ptr<Job>> js(1);
+  const int rc = prepare_job(c, circ, opt, &js[0]);
+  if (rc != QG_OK) return rc;
+  enqueue_jobs(c, js, 0, id_out);
   return QG_OK;
 }
 
@@ -985,7 +1198,9 @@ int qg_ctx_create(const qg_config* cfg, void** ctx_out) {
     uint64_t thr = UINT64_MAX;
     cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &thr);
   }
-  for (int w = 0; w < c->cfg.workers; ++w) c->workers.emplace_back(worker_loop, c);
+  for (int w = 0; w < c->cfg.workers; ++w) c->workers.emplace_back(worker_loop, c, false);
+  for (int w = 0; w < kSmallLaneWorkers; ++w) c->workers.emplace_back(worker_loop, c, true);
+  c->batcher = std::thread(batcher_loop, c);
   *ctx_out = c;
   return QG_OK;
 }
@@ -1000,6 +1215,12 @@ int qg_ctx_destroy(void* ctx) {
   }
   c->cv.notify_all();
   for (auto& t : c->workers) t.join();
+  {
+    std::lock_guard<std::mutex> g(c->mu);
+    c->batch_stop = true;
+  }
+  c->ready_cv.notify_all();
+  if (c->batcher.joinable()) c->batcher.join();
   cudaSetDevice(c->device);
   for (auto& kv : c->jobs)
     if (kv.second->state) {
@@ -1030,7 +1251,7 @@ int qg_ctx_capabilities(void* ctx, int32_t* mq128, int32_t* mq64, uint64_t* hbm_
 
 int qg_submit(void* ctx, const qg_circuit* circuit, const qg_options* options, uint64_t* job_out) {
   if (!ctx) return QG_ERR_INVALID_ARG;
-  return submit_one((Ctx*)ctx, circuit, options, 0, job_out);
+  return submit_one((Ctx*)ctx, circuit, options, job_out);
 }
 
 int qg_job_status(void* ctx, uint64_t job, int32_t* status_out) {
@@ -1127,6 +1348,7 @@ int qg_job_details(void* ctx, uint64_t job, qg_job_info* out) {
   out->num_distinct_outcomes = (int64_t)j->counts.size();
   out->has_results = j->has & (j->state ? ~0 : ~QG_RES_STATE_VECTOR);
   out->error_code = j->error_code;
+  out->batched_with = j->batched_with;
   return QG_OK;
 }
 
@@ -1336,18 +1558,19 @@ int qg_batch_submit(void* ctx, const qg_circuit* circuits, int32_t count, const 
                     uint64_t* batch_out, uint64_t* jobs_out) {
   if (!ctx || !circuits || count < 0 || !batch_out) return QG_ERR_INVALID_ARG;
   Ctx* c = (Ctx*)ctx;
+  // all or nothing: every circuit is validated before any job is queued
+  std::vector<std::shared_ptr<Job>> js((size_t)count);
+  for (int i = 0; i < count; ++i) {
+    const int rc = prepare_job(c, &circuits[i], options, &js[(size_t)i]);
+    if (rc != QG_OK) return rc;
+  }
   uint64_t bid;
   {
     std::lock_guard<std::mutex> g(c->mu);
     bid = c->next_id++;
     c->batches[bid];
   }
-  for (int i = 0; i < count; ++i) {
-    uint64_t id = 0;
-    int rc = submit_one(c, &circuits[i], options, bid, &id);
-    if (rc != QG_OK) return rc;
-    if (jobs_out) jobs_out[i] = id;
-  }
+  enqueue_jobs(c, js, bid, jobs_out);
   *batch_out = bid;
   return QG_OK;
 }

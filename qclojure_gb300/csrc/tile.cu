@@ -663,6 +663,69 @@ __global__ void __launch_bounds__(512, 1) k_tile2(const PassDesc pd, const Batch
   }
 }
 
+// Small jobs: a state of n <= 12 qubits is one tile, so one CTA runs a whole job.
+// The state is loaded into shared memory once, every pass of the job's program
+// (op records staged pass by pass) is applied to it there, and it is stored
+// once. One launch serves many jobs of the same qubit count, one CTA each. The
+// op records and their order are those of the job's own program, so the
+// results equal a per-job run of the same program.
+template <class P>
+__global__ void __launch_bounds__(512, 1) k_tile_jobs(int n, const TileJobRec* __restrict__ jobs, int njobs,
+                                                      const KOp* __restrict__ kops,
+                                                      const int32_t* __restrict__ pass_nops) {
+  constexpr int E = P::kElem;
+  extern __shared__ __align__(128) unsigned char smem[];
+  TileGeo g;
+  g.k = n;
+  g.K = 1 << n;
+  g.klow = n;
+  g.T = blockDim.x;
+  unsigned char* tile = smem;
+  KOp* sops = reinterpret_cast<KOp*>(smem + (size_t)g.K * E);
+  uint64_t* hioff = reinterpret_cast<uint64_t*>(sops + kMaxKOps);
+  if (threadIdx.x == 0) hioff[0] = 0;  // every bit is local
+  __syncthreads();
+  CopyPlan<E> cp;
+  cp.init(hioff, g);
+  for (int jx = blockIdx.x; jx < njobs; jx += gridDim.x) {
+    const TileJobRec jr = jobs[jx];
+    unsigned char* state = reinterpret_cast<unsigned char*>(jr.state);
+    cp.load(tile, state);
+    cp_commit();
+    cp_wait<0>();
+    __syncthreads();
+    if constexpr (P::kInPairs) {  // IEEE doubles -> float pairs, each thread its own slots
+      for (int l = threadIdx.x; l < g.K; l += g.T) {
+        const int q = swz<E>(l);
+        const dfc v = load_dfc(reinterpret_cast<const double2*>(tile)[q]);
+        reinterpret_cast<float4*>(tile)[q] = make_float4(v.rh, v.rl, v.ih, v.il);
+      }
+    }
+    int64_t ob = jr.op_begin;
+    for (int p = 0; p < jr.npasses; ++p) {
+      const int nops = pass_nops[jr.pass_begin + p];
+      __syncthreads();  // the previous pass's readers of sops are done
+      const uint4* src = reinterpret_cast<const uint4*>(kops + ob);
+      uint4* dst = reinterpret_cast<uint4*>(sops);
+      const int words = nops * (int)(sizeof(KOp) / 16);
+      for (int q = threadIdx.x; q < words; q += g.T) dst[q] = src[q];
+      __syncthreads();
+      run_ops<P>(tile, sops, nops, nullptr, 0, g);  // ends with a barrier
+      ob += nops;
+    }
+    if constexpr (P::kOutPairs) {  // float pairs -> IEEE doubles
+      for (int l = threadIdx.x; l < g.K; l += g.T) {
+        const int q = swz<E>(l);
+        const float4 v = reinterpret_cast<const float4*>(tile)[q];
+        reinterpret_cast<double2*>(tile)[q] = store_dfc(dfc{v.x, v.y, v.z, v.w});
+      }
+      __syncthreads();
+    }
+    cp.store(tile, state);
+    __syncthreads();  // the tile buffer is reloaded for the next job
+  }
+}
+
 // Host: translate TOps into the compact records of policy P.
 template <class P>
 void build_kops(KOp* out, const TOp* ops, int64_t nops) {
@@ -783,6 +846,30 @@ void encode_kops(int precision, int arithmetic, const TOp* tops, int64_t count, 
   if (precision == QG_C64) build_kops<PolF>(k, tops, count);
   else if (arithmetic == QG_ARITH_DOUBLE_FLOAT) build_kops<PolDFT<0>>(k, tops, count);
   else build_kops<PolD>(k, tops, count);
+}
+
+template <class P>
+cudaError_t launch_jobs_t(int n, const TileJobRec* d_jobs, int njobs, const KOp* d_kops, const int32_t* d_pass_nops,
+                          cudaStream_t st) {
+  constexpr int E = P::kElem;
+  const int K = 1 << n;
+  const int threads = K / kRegs;
+  if (n < 5 || n > kMaxSmallJobQubits || njobs < 1) return cudaErrorInvalidValue;
+  const size_t smem = (size_t)K * E + sizeof(KOp) * kMaxKOps + 16;
+  cudaError_t e = cudaFuncSetAttribute(k_tile_jobs<P>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       (int)((size_t(64) << 10) + sizeof(KOp) * kMaxKOps + 16));
+  if (e != cudaSuccess) return e;
+  k_tile_jobs<P><<<(unsigned)njobs, threads, smem, st>>>(n, d_jobs, njobs, d_kops, d_pass_nops);
+  count_launch(1);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_tile_jobs(int precision, int arithmetic, int n, const TileJobRec* d_jobs, int njobs,
+                             const void* d_kops, const int32_t* d_pass_nops, cudaStream_t st) {
+  const KOp* k = reinterpret_cast<const KOp*>(d_kops);
+  if (precision == QG_C64) return launch_jobs_t<PolF>(n, d_jobs, njobs, k, d_pass_nops, st);
+  if (arithmetic == QG_ARITH_DOUBLE_FLOAT) return launch_jobs_t<PolDFT<3>>(n, d_jobs, njobs, k, d_pass_nops, st);
+  return launch_jobs_t<PolD>(n, d_jobs, njobs, k, d_pass_nops, st);
 }
 
 cudaError_t launch_tile_pass(int precision, int arithmetic, int io, int n, const PassDesc& pd,

@@ -1,0 +1,114 @@
+"""Serving: a mixed stream of jobs behind the job API with continuous batching.
+
+Jobs of 5..12 qubits (one tile per state) are compiled by the worker that admits
+them and run by the batcher, which groups everything ready by qubit count and
+runs each group in one launch, one CTA per job. Larger jobs run concurrently on
+the workers' streams.
+
+Each job's result is the same alone and in the mix: the final state is bit-identical
+and the shot outcomes are identical. Alone means submitted by itself, and also run
+through the per-pass state API. The results are also within tolerance of the oracle:
+complex128 ≤ 1e-12 per amplitude and outcomes identical; complex64 ≤ 2e-5 per amplitude.
+"""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def _stream(seed, count=36, cap=16):
+    """Test-sized stream with the serving mix's shape: n = 8 + Geometric(0.15), capped;
+    nine jobs in ten want shots, the tenth a Pauli-string expectation."""
+    from qclojure_gb300 import workloads
+
+    rng = np.random.default_rng(seed)
+    jobs = []
+    for i in range(count):
+        n = int(min(8 + rng.geometric(0.15) - 1, cap))
+        c = workloads.layered_circuit(n, int(rng.integers(2, 10)), seed=seed * 1000 + i)
+        if i % 10 == 9:
+            pauli = "".join("IXYZ"[k] for k in rng.integers(0, 4, n))
+            spec = {"hamiltonian": [{"coefficient": 1.0, "pauli-string": pauli}], "state-vector": True}
+        else:
+            spec = SHOT_SPEC
+        jobs.append((c, {"result-specs": spec}))
+    return jobs
+
+
+SHOT_SPEC = {"measurements": {"shots": 700}, "state-vector": True}
+
+
+def _sv(r):
+    return np.asarray(r["results"]["final-state"]["state-vector"])
+
+
+@pytest.mark.parametrize("precision,arith,tol", [("c64", "exact", 2e-5), ("c128", "double-float", 1e-12),
+                                                 ("c128", "exact", 0.0)])
+def test_mix_equals_alone_and_oracle(oracle, precision, arith, tol):
+    from qclojure_gb300.backend import create_simulator
+    from qclojure_gb300.state import Context
+
+    jobs = _stream(3)
+    sim = create_simulator({"precision": precision, "fusion": "tiled", "workers": 4, "seed": 9,
+                            "arithmetic": arith})
+    ctx = Context(seed=9, arithmetic=arith)
+    try:
+        # the mix: shot jobs arrive together (one batch submission), the others right after
+        shot = [k for k, (c, o) in enumerate(jobs) if o["result-specs"] is SHOT_SPEC]
+        bid = sim.batch_submit([jobs[k][0] for k in shot], {"result-specs": SHOT_SPEC})
+        ids = [None] * len(jobs)
+        for k, jid in zip(shot, sim.batch_status(bid)["job-statuses"]):
+            ids[k] = jid
+        for k, (c, o) in enumerate(jobs):
+            if ids[k] is None:
+                ids[k] = sim.submit_circuit(c, o)
+        for j in ids:
+            assert sim.wait(j, 300_000) == "completed"
+        mix = [sim.job_result(j) for j in ids]
+        assert max(r["batched-with"] for r in mix) > 1, "no small jobs shared a launch"
+        for (c, o), r in zip(jobs, mix):
+            a_id = sim.submit_circuit(c, o)  # alone
+            assert sim.wait(a_id, 300_000) == "completed"
+            a = sim.job_result(a_id)
+            assert np.array_equal(_sv(r), _sv(a))
+            with ctx.state(c["num-qubits"], precision) as st:  # alone, per-pass kernels
+                st.apply(c, fusion="tiled")
+                assert np.array_equal(_sv(r), st.download())
+            res, ares = r["results"], a["results"]
+            ref = oracle.run(c)
+            assert np.max(np.abs(_sv(r) - ref)) <= tol
+            if "measurement-results" in res:
+                assert res["measurement-results"]["measurement-outcomes"] == \
+                    ares["measurement-results"]["measurement-outcomes"]
+                if precision == "c128":
+                    shots = len(res["measurement-results"]["measurement-outcomes"])
+                    assert np.array_equal(np.array(res["measurement-results"]["measurement-outcomes"], np.uint64),
+                                          oracle.sample(ref, shots, 9))
+            else:
+                e = res["hamiltonian-result"]["energy-expectation"]
+                assert e == ares["hamiltonian-result"]["energy-expectation"]
+                p = o["result-specs"]["hamiltonian"][0]["pauli-string"]
+                assert abs(e - oracle.pauli_expectation(ref, p)) <= max(tol, 1e-12) * 10
+            sim.free_job(r["job-id"])
+            sim.free_job(a_id)
+    finally:
+        ctx.close()
+        sim.close()
+
+
+def test_cancel_small_job_waiting_in_queue():
+    """A queued small job can be cancelled; the rest of its batch completes."""
+    from qclojure_gb300 import workloads
+    from qclojure_gb300.backend import create_simulator
+
+    sim = create_simulator({"precision": "c64", "fusion": "tiled", "workers": 1, "seed": 1})
+    try:
+        big = sim.submit_circuit(workloads.layered_circuit(24, 30, seed=1), {})
+        small = [sim.submit_circuit(workloads.layered_circuit(10, 5, seed=s), {}) for s in range(6)]
+        assert sim.cancel_job(small[3]) in ("cancelled", "cannot-cancel")
+        assert sim.wait(big, 300_000) == "completed"
+        for k, j in enumerate(small):
+            s = sim.wait(j, 300_000)
+            assert s == "completed" or (k == 3 and s == "cancelled")
+    finally:
+        sim.close()
