@@ -77,6 +77,17 @@ enum {
   QG_ARITH_DOUBLE_FLOAT = 1  /* float pairs on the FP32 pipes (about 48 bits), doubles in HBM          */
 };
 
+/* ---- specialised pass kernels ------------------------------------------ */
+/* A tiled pass of a complex64 or double-float complex128 program can run as its own
+   kernel, generated from the pass's gates and compiled at run time (NVRTC, cached per
+   device by generated source), instead of the interpreting tiled kernel. AUTO uses
+   them for states of 29 qubits and more; without NVRTC every pass runs interpreted. */
+enum {
+  QG_PASS_KERNELS_AUTO = 0,
+  QG_PASS_KERNELS_OFF = 1,
+  QG_PASS_KERNELS_ALWAYS = 2
+};
+
 /* ---- fusion modes ------------------------------------------------------ */
 enum {
   QG_FUSE_PLAIN = 0,   /* one HBM pass per gate (the plain method)                    */
@@ -186,7 +197,7 @@ typedef struct qg_config {
   uint64_t hbm_budget_bytes;      /* 0 = free HBM minus a reserve                        */
   uint64_t seed;                  /* default seed                                        */
   int32_t arithmetic;             /* QG_ARITH_* for complex128 tiled passes              */
-  int32_t reserved;
+  int32_t pass_kernels;           /* QG_PASS_KERNELS_*                                   */
 } qg_config;
 
 typedef struct qg_queue_info {    /* queue-status (ideal_simulator.clj:165-176) + device fields */
@@ -208,7 +219,7 @@ typedef struct qg_job_info {
   int32_t has_results;            /* QG_RES_* flags that are available                    */
   int32_t error_code;
   int32_t batched_with;           /* jobs that shared its small-job launch (0: ran alone) */
-  int32_t reserved;
+  int32_t specialised_passes;     /* tiled passes that ran as specialised kernels         */
 } qg_job_info;
 
 /* ---- context ------------------------------------------------------------ */
@@ -271,6 +282,12 @@ int qg_state_download(void* state, double* host_c128);
 /* Apply a circuit in place with the given fusion mode; mid-circuit measurements draw
    from seed. passes_out (may be NULL) receives the number of HBM passes. */
 int qg_state_apply(void* state, const qg_circuit* circuit, int32_t fusion, uint64_t seed, int32_t* passes_out);
+/* No counterpart in the reference: compile (and cache) the specialised pass kernels
+   that qg_state_apply would use for this circuit on this state, without running it,
+   so a later apply starts at once. specialised_out receives how many passes have a
+   kernel (0 when the context's pass-kernel setting or the circuit uses none). */
+int qg_state_prepare(void* state, const qg_circuit* circuit, int32_t fusion, double* compile_ms_out,
+                     int32_t* specialised_out);
 /* probabilities (state.clj:658-682) into a host buffer of 2^n doubles. */
 int qg_state_probabilities(void* state, double* host_out);
 /* Shot sampling (state.clj:869-913 rule: first outcome whose cumulative probability
@@ -343,12 +360,22 @@ int qg_sweep_destroy(void* sweep);
 /* ---- measurement (no counterpart in the reference) ----------------------------
    qg_state_profile applies a circuit like qg_state_apply and records a CUDA event
    pair around every HBM pass on the state's stream: pass_ms[i] is the duration of
-   pass i and pass_kind[i] its kind (0 plain gate, 1 tiled pass, 2 measurement).
+   pass i and pass_kind[i] its kind (0 plain gate, 1 tiled pass, 2 measurement,
+   3 tiled pass run by its specialised kernel).
    qg_kernel_launches reports how many kernels this library has launched in the
    process so far. */
 int qg_state_profile(void* state, const qg_circuit* circuit, int32_t fusion, uint64_t seed, float* pass_ms,
                      int32_t* pass_kind, int32_t cap, int32_t* n_passes);
 int qg_kernel_launches(uint64_t* count);
+/* Specialised pass kernels (no counterpart in the reference). qg_pass_kernels_build
+   generates and compiles the kernels of a circuit's tiled passes for sm_103a without
+   loading them (no device needed): QG_OK with the kernel count and compile time,
+   QG_ERR_DEVICE with the compiler's message in err_buf when a compile fails,
+   QG_ERR_UNSUPPORTED when NVRTC is not available. qg_pass_kernels_info reports whether
+   NVRTC is available and the compiled-program cache's hits and misses. */
+int qg_pass_kernels_build(const qg_circuit* circuit, int32_t precision, int32_t arithmetic, int32_t* kernels_out,
+                          double* compile_ms_out, char* err_buf, int64_t err_len);
+int qg_pass_kernels_info(int32_t* available, uint64_t* cache_hits, uint64_t* cache_misses);
 
 #ifdef __cplusplus
 }

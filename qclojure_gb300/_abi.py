@@ -50,6 +50,8 @@ CANCEL_OUTCOME = {0: "cancelled", 1: "cannot-cancel", 2: "not-found"}
 QG_C128, QG_C64 = 0, 1
 QG_FUSE_PLAIN, QG_FUSE_TILED, QG_FUSE_DENSE = 0, 1, 2
 QG_ARITH_EXACT, QG_ARITH_DOUBLE_FLOAT = 0, 1
+QG_PASS_KERNELS_AUTO, QG_PASS_KERNELS_OFF, QG_PASS_KERNELS_ALWAYS = 0, 1, 2
+PASS_KERNELS = {"auto": 0, "off": 1, "always": 2}
 
 # opcodes
 OP = dict(
@@ -102,7 +104,7 @@ class QgOptions(C.Structure):
 class QgConfig(C.Structure):
     _fields_ = [("device", C.c_int32), ("precision", C.c_int32), ("fusion", C.c_int32), ("fuse_k", C.c_int32),
                 ("max_qubits", C.c_int32), ("workers", C.c_int32), ("hbm_budget_bytes", C.c_uint64),
-                ("seed", C.c_uint64), ("arithmetic", C.c_int32), ("reserved", C.c_int32)]
+                ("seed", C.c_uint64), ("arithmetic", C.c_int32), ("pass_kernels", C.c_int32)]
 
 
 class QgQueueInfo(C.Structure):
@@ -117,7 +119,7 @@ class QgJobInfo(C.Structure):
                 ("num_passes", C.c_int32), ("execution_time_ms", C.c_double), ("device_time_ms", C.c_double),
                 ("queue_time_ms", C.c_double), ("shots", C.c_uint64), ("num_distinct_outcomes", C.c_int64),
                 ("has_results", C.c_int32), ("error_code", C.c_int32), ("batched_with", C.c_int32),
-                ("reserved", C.c_int32)]
+                ("specialised_passes", C.c_int32)]
 
 
 class QgSweepStats(C.Structure):
@@ -169,6 +171,7 @@ SIGNATURES = {
     "qg_state_upload": ([P, DP], C.c_int),
     "qg_state_download": ([P, DP], C.c_int),
     "qg_state_apply": ([P, C.POINTER(QgCircuit), I32, U64, I32P], C.c_int),
+    "qg_state_prepare": ([P, C.POINTER(QgCircuit), I32, DP, I32P], C.c_int),
     "qg_state_probabilities": ([P, DP], C.c_int),
     "qg_state_sample": ([P, U64, U64, U64P], C.c_int),
     "qg_state_sample_noalloc": ([P, U64, U64, P], C.c_int),
@@ -182,6 +185,8 @@ SIGNATURES = {
     "qg_state_synchronize": ([P], C.c_int),
     "qg_state_profile": ([P, C.POINTER(QgCircuit), I32, U64, C.POINTER(C.c_float), I32P, I32, I32P], C.c_int),
     "qg_kernel_launches": ([U64P], C.c_int),
+    "qg_pass_kernels_build": ([C.POINTER(QgCircuit), I32, I32, I32P, DP, C.c_char_p, I64], C.c_int),
+    "qg_pass_kernels_info": ([I32P, U64P, U64P], C.c_int),
     "qg_sweep_create": ([P, C.POINTER(QgCircuit), I32, I32, I32, C.POINTER(P)], C.c_int),
     "qg_sweep_update": ([P, C.POINTER(QgCircuit), I32], C.c_int),
     "qg_sweep_run": ([P, I32P, DP, C.c_char_p, DP, C.POINTER(QgSweepStats)], C.c_int),

@@ -41,14 +41,34 @@ def _stale(out: Path, deps: list[Path]) -> bool:
     return any(d.stat().st_mtime > t for d in deps)
 
 
+EMBEDDED = {"kEmbedPassPrelude": "pass_prelude.cuh", "kEmbedDf64": "df64.cuh"}
+
+
+def write_embedded(obj_dir: Path) -> Path:
+    """The device prelude of the specialised pass kernels, as C strings: NVRTC
+    compiles it at run time together with each program's generated passes."""
+    out = obj_dir / "embedded_sources.cpp"
+    parts = ["// generated by qclojure_gb300/build.py from csrc/*.cuh\nnamespace qg {\n"]
+    for sym, name in EMBEDDED.items():
+        text = (CSRC / name).read_text()
+        assert ")QGEMBED" not in text
+        parts.append(f'extern const char {sym}[] = R"QGEMBED({text})QGEMBED";\n')
+    parts.append("}  // namespace qg\n")
+    body = "".join(parts)
+    if not out.exists() or out.read_text() != body:
+        out.write_text(body)
+    return out
+
+
 def build_library(force: bool = False, verbose: bool = False) -> Path:
     srcs = sources()
-    headers = list(CSRC.glob("*.h")) + list(INCLUDE.glob("*.h"))
+    headers = list(CSRC.glob("*.h")) + list(CSRC.glob("*.cuh")) + list(INCLUDE.glob("*.h"))
     if not force and not _stale(LIB, srcs + headers + [Path(__file__)]):
         return LIB
     nvcc = nvcc_path()
     obj_dir = OUT_DIR / "obj"
     obj_dir.mkdir(parents=True, exist_ok=True)
+    srcs = srcs + [write_embedded(obj_dir)]
     common = ["-O3", "-std=c++17", "-Xcompiler", "-fPIC", "-I", str(INCLUDE), "-lineinfo"]
 
     def compile_one(src: Path) -> Path:

@@ -15,7 +15,9 @@
 // magnitudes below 2^-126 are flushed to zero (absolute error < 1e-38).
 #pragma once
 
+#ifndef __CUDACC_RTC__
 #include <cstdint>
+#endif
 
 namespace qg {
 

@@ -1,0 +1,657 @@
+// Specialised pass kernels: one sm_103a kernel per tiled pass of a program.
+//
+// The tiled executor (tile.cu) interprets a pass's op records per tile: every
+// op costs a dispatch, a load of its coefficients and, because the op switch
+// joins all gate classes, copies of the amplitude registers at the join. For
+// large states the same pass runs over 2^(n-12) tiles, so this file turns each
+// pass into straight-line code instead: the generator below writes one CUDA
+// kernel per pass (matrix entries as exact hex-float literals, register slots,
+// layouts and conditions resolved), NVRTC compiles the kernels of a program for
+// sm_103a in a few parallel translation units, and the runtime launches them in
+// place of the interpreted passes. Compiled programs are cached per device by
+// their generated source, so repeated circuits (benchmark steps, served
+// duplicates) compile once.
+//
+// The arithmetic is that of the interpreted path's policies, applied in the same
+// gate order: complex64 in FP32 (with FMA contraction), complex128 as
+// double-float pairs on the FP32 pipes (pass_prelude.cuh). The exact FP64
+// policy and dense fused blocks stay with the interpreter.
+//
+// NVRTC is loaded with dlopen: without it (or when a compile fails) programs run
+// on the interpreted kernels, which are CUDA code on the same device.
+#include <dlfcn.h>
+#include <nvrtc.h>
+
+#include <algorithm>
+#include <chrono>
+#include <cstdio>
+#include <cstring>
+#include <memory>
+#include <mutex>
+#include <sstream>
+#include <thread>
+#include <unordered_map>
+
+#include "qgpu_internal.h"
+
+namespace qg {
+
+extern const char kEmbedPassPrelude[];
+extern const char kEmbedDf64[];
+
+namespace {
+
+struct NvrtcApi {
+  decltype(&nvrtcCreateProgram) create = nullptr;
+  decltype(&nvrtcCompileProgram) compile = nullptr;
+  decltype(&nvrtcGetProgramLogSize) log_size = nullptr;
+  decltype(&nvrtcGetProgramLog) log = nullptr;
+  decltype(&nvrtcGetCUBINSize) cubin_size = nullptr;
+  decltype(&nvrtcGetCUBIN) cubin = nullptr;
+  decltype(&nvrtcDestroyProgram) destroy = nullptr;
+  std::string error;  // empty when every entry point resolved
+};
+
+const NvrtcApi& nvrtc_api() {
+  static const NvrtcApi api = [] {
+    NvrtcApi a;
+    const char* names[] = {"libnvrtc.so.13", "libnvrtc.so", "/usr/local/cuda/lib64/libnvrtc.so.13"};
+    void* h = nullptr;
+    for (const char* nm : names)
+      if (!h) h = dlopen(nm, RTLD_NOW | RTLD_LOCAL);
+    if (!h) {
+      a.error = "NVRTC (libnvrtc.so.13) is not available";
+      return a;
+    }
+    a.create = reinterpret_cast<decltype(a.create)>(dlsym(h, "nvrtcCreateProgram"));
+    a.compile = reinterpret_cast<decltype(a.compile)>(dlsym(h, "nvrtcCompileProgram"));
+    a.log_size = reinterpret_cast<decltype(a.log_size)>(dlsym(h, "nvrtcGetProgramLogSize"));
+    a.log = reinterpret_cast<decltype(a.log)>(dlsym(h, "nvrtcGetProgramLog"));
+    a.cubin_size = reinterpret_cast<decltype(a.cubin_size)>(dlsym(h, "nvrtcGetCUBINSize"));
+    a.cubin = reinterpret_cast<decltype(a.cubin)>(dlsym(h, "nvrtcGetCUBIN"));
+    a.destroy = reinterpret_cast<decltype(a.destroy)>(dlsym(h, "nvrtcDestroyProgram"));
+    if (!a.create || !a.compile || !a.log_size || !a.log || !a.cubin_size || !a.cubin || !a.destroy)
+      a.error = "NVRTC lacks an entry point";
+    return a;
+  }();
+  return api;
+}
+
+// exact float literal (C++17 hexadecimal floating literal)
+std::string flit(float f) {
+  char b[64];
+  std::snprintf(b, sizeof(b), "%af", (double)f);
+  return b;
+}
+std::string hex64(uint64_t v) {
+  char b[40];
+  std::snprintf(b, sizeof(b), "0x%llxull", (unsigned long long)v);
+  return b;
+}
+std::string hex32(uint32_t v) {
+  char b[24];
+  std::snprintf(b, sizeof(b), "0x%xu", v);
+  return b;
+}
+
+inline bool hi_lo_nonzero(const TOp& t, int q) { return t.mf[8 + q] != 0.0f; }
+
+// ---------------------------------------------------------------------------
+// Source generation for one pass
+// ---------------------------------------------------------------------------
+class PassGen {
+ public:
+  PassGen(std::ostringstream& o, const PassDesc& pd, const TOp* ops, int nops, int prec, int io)
+      : o_(o), pd_(pd), ops_(ops), nops_(nops), df_(prec == QG_C128), io_(io) {}
+
+  // false: the pass holds an op the generator does not specialise
+  bool supported() const {
+    for (int i = 0; i < nops_; ++i)
+      if (ops_[i].kind == OK_DENSE) return false;
+    return true;
+  }
+
+  void emit(int id) {
+    const int E = df_ ? 16 : 8;
+    uint64_t lm = 0;
+    for (int j = 0; j < pd_.k; ++j) lm |= 1ULL << pd_.lbits[j];
+    o_ << "namespace p" << id << " {\nstruct P {\n";
+    o_ << "  static constexpr int E = " << E << ", K_BITS = " << pd_.k << ", KLOW = " << pd_.klow << ";\n";
+    o_ << "  static constexpr qgp::u64 LM = " << hex64(lm) << ";\n";
+    // run offsets: bit j - klow of the run index h deposits at lbits[j]
+    o_ << "  static __device__ __forceinline__ qgp::u64 hioff(int h) {\n    qgp::u64 o = 0;\n";
+    for (int j = pd_.klow; j < pd_.k; ++j)
+      o_ << "    o |= (qgp::u64)((h >> " << (j - pd_.klow) << ") & 1) << " << pd_.lbits[j] << ";\n";
+    o_ << "    return o;\n  }\n";
+    o_ << "  static __device__ __forceinline__ qgp::u64 tile_base(qgp::u64 t) {\n    return 0";
+    for (int r = 0; r < pd_.nruns; ++r)
+      o_ << " | (((t >> " << pd_.run_src[r] << ") & " << hex64((1ULL << pd_.run_len[r]) - 1) << ") << "
+         << pd_.run_dst[r] << ")";
+    o_ << ";\n  }\n";
+    o_ << "  static __device__ __forceinline__ void body(unsigned char* buf, qgp::u64 base) {\n";
+    o_ << "    using namespace qgp;\n    const unsigned tid = threadIdx.x;\n    (void)base; (void)tid;\n";
+    body();
+    o_ << "  }\n};\n}  // namespace p" << id << "\n";
+    o_ << "extern \"C\" __global__ void __launch_bounds__(512, " << (df_ ? 1 : 2) << ") qgp_" << id
+       << "(unsigned char* __restrict__ state, unsigned long long ntiles) {\n  qgp::run_pass<p" << id
+       << "::P>(state, ntiles);\n}\n\n";
+  }
+
+ private:
+  std::ostringstream& o_;
+  const PassDesc& pd_;
+  const TOp* ops_;
+  int nops_;
+  bool df_;
+  int io_;
+  // double-float: operations applied to each register since its last renormalisation
+  int since_[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+  static constexpr int kRenormEvery = 4;
+
+  void touched(int j) {
+    if (!df_) return;
+    if (++since_[j] >= kRenormEvery) {
+      o_ << "    r" << j << " = DF::renorm(r" << j << ");\n";
+      since_[j] = 0;
+    }
+  }
+  void renorm_all() {
+    for (int j = 0; j < 8; ++j)
+      if (df_ && since_[j] > 0) {
+        o_ << "    r" << j << " = DF::renorm(r" << j << ");\n";
+        since_[j] = 0;
+      }
+  }
+
+  const char* pol() const { return df_ ? "DF" : "F32"; }
+  std::string ld_raw() const { return df_ && !(io_ & kTileInPairs) ? "DF::ld_doubles" : std::string(pol()) + "::ld_work"; }
+  std::string st_raw() const { return df_ && !(io_ & kTileOutPairs) ? "DF::st_doubles" : std::string(pol()) + "::st_work"; }
+
+  // coefficient q of a TOp: hi literal, lo literal (double-float) or the float (complex64)
+  std::string h(const TOp& t, int q) const { return flit(df_ ? t.mf[q] : (float)t.m[q]); }
+  std::string l(const TOp& t, int q) const { return flit(t.mf[8 + q]); }
+  std::string b(bool v) const { return v ? "true" : "false"; }
+
+  // condition on tile bits (gm, gv) and thread bits (tm, tv); empty when unconditional
+  std::string cond(uint64_t gm, uint64_t gv, uint32_t tm, uint32_t tv) const {
+    std::string c;
+    if (gm) c += "((base & " + hex64(gm) + ") == " + hex64(gv) + ")";
+    if (tm) {
+      if (!c.empty()) c += " && ";
+      c += "((lt & " + hex32(tm) + ") == " + hex32(tv) + ")";
+    }
+    return c;
+  }
+
+  std::string cmul(const TOp& t, int qr, int qi, const std::string& x) const {
+    if (df_)
+      return "df_cmul<" + b(hi_lo_nonzero(t, qr)) + ", " + b(hi_lo_nonzero(t, qi)) + ">(" + h(t, qr) + ", " + l(t, qr) +
+             ", " + h(t, qi) + ", " + l(t, qi) + ", " + x + ")";
+    return "f_cmul(" + h(t, qr) + ", " + h(t, qi) + ", " + x + ")";
+  }
+
+  void u2_pair(const TOp& t, const std::string& a, const std::string& c) {
+    const double* m = t.m;
+    switch (t.cls) {
+      case U2_GENERAL:
+        if (df_) {
+          o_ << "      { const dfc y0 = df_row(" << h(t, 0) << ", " << l(t, 0) << ", " << h(t, 1) << ", " << l(t, 1) << ", "
+             << h(t, 2) << ", " << l(t, 2) << ", " << h(t, 3) << ", " << l(t, 3) << ", " << a << ", " << c << ");\n";
+          o_ << "        const dfc y1 = df_row(" << h(t, 4) << ", " << l(t, 4) << ", " << h(t, 5) << ", " << l(t, 5)
+             << ", " << h(t, 6) << ", " << l(t, 6) << ", " << h(t, 7) << ", " << l(t, 7) << ", " << a << ", " << c
+             << ");\n";
+        } else {
+          o_ << "      { const float2 y0 = f_row(" << h(t, 0) << ", " << h(t, 1) << ", " << h(t, 2) << ", " << h(t, 3)
+             << ", " << a << ", " << c << ");\n";
+          o_ << "        const float2 y1 = f_row(" << h(t, 4) << ", " << h(t, 5) << ", " << h(t, 6) << ", " << h(t, 7)
+             << ", " << a << ", " << c << ");\n";
+        }
+        o_ << "        " << a << " = y0; " << c << " = y1; }\n";
+        break;
+      case U2_REAL:
+        if (m[0] == m[2] && m[0] == m[4] && m[6] == -m[0]) {  // [[c, c], [c, -c]]
+          if (df_)
+            o_ << "      df_hadamard<" << b(hi_lo_nonzero(t, 0)) << ">(" << h(t, 0) << ", " << l(t, 0) << ", " << a
+               << ", " << c << ");\n";
+          else
+            o_ << "      f_hadamard(" << h(t, 0) << ", " << a << ", " << c << ");\n";
+        } else if (df_) {
+          o_ << "      df_real<" << b(hi_lo_nonzero(t, 0)) << ", " << b(hi_lo_nonzero(t, 2)) << ", "
+             << b(hi_lo_nonzero(t, 4)) << ", " << b(hi_lo_nonzero(t, 6)) << ">(" << h(t, 0) << ", " << l(t, 0) << ", "
+             << h(t, 2) << ", " << l(t, 2) << ", " << h(t, 4) << ", " << l(t, 4) << ", " << h(t, 6) << ", " << l(t, 6)
+             << ", " << a << ", " << c << ");\n";
+        } else {
+          o_ << "      f_real(" << h(t, 0) << ", " << h(t, 2) << ", " << h(t, 4) << ", " << h(t, 6) << ", " << a << ", "
+             << c << ");\n";
+        }
+        break;
+      case U2_RXLIKE:  // m0 = (a, 0), m1 = (0, b), m2 = (0, c), m3 = (d, 0)
+        if (df_)
+          o_ << "      df_rxlike<" << b(hi_lo_nonzero(t, 0)) << ", " << b(hi_lo_nonzero(t, 3)) << ", "
+             << b(hi_lo_nonzero(t, 5)) << ", " << b(hi_lo_nonzero(t, 6)) << ">(" << h(t, 0) << ", " << l(t, 0) << ", "
+             << h(t, 3) << ", " << l(t, 3) << ", " << h(t, 5) << ", " << l(t, 5) << ", " << h(t, 6) << ", " << l(t, 6)
+             << ", " << a << ", " << c << ");\n";
+        else
+          o_ << "      f_rxlike(" << h(t, 0) << ", " << h(t, 3) << ", " << h(t, 5) << ", " << h(t, 6) << ", " << a
+             << ", " << c << ");\n";
+        break;
+      case U2_DIAG:
+        o_ << "      " << a << " = " << cmul(t, 0, 1, a) << ";\n";
+        o_ << "      " << c << " = " << cmul(t, 6, 7, c) << ";\n";
+        break;
+      case U2_ANTIDIAG:
+        o_ << "      { const " << (df_ ? "dfc" : "float2") << " y0 = " << cmul(t, 2, 3, c) << ";\n";
+        o_ << "        " << c << " = " << cmul(t, 4, 5, a) << "; " << a << " = y0; }\n";
+        break;
+      case U2_X:
+        o_ << "      { const " << (df_ ? "dfc" : "float2") << " y = " << a << "; " << a << " = " << c << "; " << c
+           << " = y; }\n";
+        break;
+      default: {  // U2_IMAG_ANTI: m1 = +-i, m2 = +-i
+        const std::string f1 = std::string(pol()) + (m[3] > 0 ? "::mul_i" : "::mul_mi");
+        const std::string f2 = std::string(pol()) + (m[5] > 0 ? "::mul_i" : "::mul_mi");
+        o_ << "      { const " << (df_ ? "dfc" : "float2") << " y0 = " << f1 << "(" << c << ");\n";
+        o_ << "        " << c << " = " << f2 << "(" << a << "); " << a << " = y0; }\n";
+      } break;
+    }
+  }
+
+  static std::string r(int j) { return "r" + std::to_string(j); }
+
+  void op(const TOp& t) {
+    const uint32_t cr = t.rmask & 7u;
+    switch (t.kind) {
+      case OK_U2: {
+        const int rp = t.t2;
+        const std::string c = cond(t.gcmask, t.gcmask, t.tmask, t.tval);
+        o_ << "    {  // U2 class " << t.cls << " on register bit " << rp << "\n";
+        if (!c.empty()) o_ << "    if (" << c << ") {\n";
+        std::vector<int> done;
+        for (int q = 0; q < 4; ++q) {
+          const int j0 = ((q >> rp) << (rp + 1)) | (q & ((1 << rp) - 1));
+          const int j1 = j0 | (1 << rp);
+          if ((j0 & cr) != cr) continue;
+          u2_pair(t, r(j0), r(j1));
+          if (t.cls != U2_X && t.cls != U2_IMAG_ANTI) {
+            done.push_back(j0);
+            done.push_back(j1);
+          }
+        }
+        if (!c.empty()) o_ << "    }\n";
+        o_ << "    }\n";
+        for (int j : done) touched(j);
+      } break;
+      case OK_PHASE: {
+        const std::string c = cond(t.gmask, t.gmask, t.tmask, t.tval);
+        o_ << "    {  // phase class " << t.cls << "\n";
+        if (!c.empty()) o_ << "    if (" << c << ") {\n";
+        for (int j = 0; j < 8; ++j) {
+          if ((j & cr) != cr) continue;
+          std::string v;
+          if (t.cls == PH_GENERAL) v = cmul(t, 0, 1, r(j));
+          else if (t.cls == PH_NEG) v = std::string(pol()) + "::neg(" + r(j) + ")";
+          else if (t.cls == PH_I) v = std::string(pol()) + "::mul_i(" + r(j) + ")";
+          else v = std::string(pol()) + "::mul_mi(" + r(j) + ")";
+          o_ << "      " << r(j) << " = " << v << ";\n";
+        }
+        if (!c.empty()) o_ << "    }\n";
+        o_ << "    }\n";
+        if (t.cls == PH_GENERAL)
+          for (int j = 0; j < 8; ++j)
+            if ((j & cr) == cr) touched(j);
+      } break;
+      case OK_SWAP: {
+        const int A = t.dbits[0], B = t.dbits[1];
+        const bool isw = (t.flags & 1) != 0;
+        const std::string c = cond(t.gcmask, t.gcmask, t.tmask, t.tval);
+        o_ << "    {  // swap of register bits " << A << ", " << B << (isw ? " (iSWAP)" : "") << "\n";
+        if (!c.empty()) o_ << "    if (" << c << ") {\n";
+        for (int j = 0; j < 8; ++j) {
+          if (!((j >> A) & 1) || ((j >> B) & 1) || (j & cr) != cr) continue;
+          const int p = j ^ (1 << A) ^ (1 << B);
+          const std::string T = df_ ? "dfc" : "float2";
+          if (df_) since_[j] = since_[p] = std::max(since_[j], since_[p]);  // conditional: either may move
+          if (isw)
+            o_ << "      { const " << T << " y = " << r(j) << "; " << r(j) << " = " << pol() << "::mul_i(" << r(p)
+               << "); " << r(p) << " = " << pol() << "::mul_i(y); }\n";
+          else
+            o_ << "      { const " << T << " y = " << r(j) << "; " << r(j) << " = " << r(p) << "; " << r(p)
+               << " = y; }\n";
+        }
+        if (!c.empty()) o_ << "    }\n";
+        o_ << "    }\n";
+      } break;
+      case OK_BLOCKADE: {
+        o_ << "    {  // blockade phase\n      const int cnt = __popcll(base & " << hex64(t.gmask) << ") + __popc(lt & "
+           << hex32(t.tmask) << ");\n";
+        for (int j = 0; j < 8; ++j) {
+          const int need = 1 - __builtin_popcount((unsigned)j & cr);
+          if (need < 0) continue;
+          o_ << "      if (cnt == " << need << ") " << r(j) << " = " << cmul(t, 0, 1, r(j)) << ";\n";
+        }
+        o_ << "    }\n";
+        for (int j = 0; j < 8; ++j)
+          if (1 - __builtin_popcount((unsigned)j & cr) >= 0) touched(j);
+      } break;
+      case OK_PARITY: {
+        o_ << "    {  // parity phase\n      const bool par = ((__popcll(base & " << hex64(t.gmask) << ") + __popc(lt & "
+           << hex32(t.tmask) << ")) & 1) != 0;\n";
+        // even register parity takes (par ? p1 : p0), odd (par ? p0 : p1)
+        const int nq = df_ ? 4 : 2;
+        for (int side = 0; side < 2; ++side) {
+          for (int q = 0; q < nq; ++q) {
+            // DF: q = 0 re.h, 1 re.l, 2 im.h, 3 im.l ; F32: q = 0 re, 1 im
+            auto lit = [&](int entry) {
+              const int idx = 2 * entry + (df_ ? q / 2 : q);
+              return df_ ? ((q & 1) ? l(t, idx) : h(t, idx)) : h(t, idx);
+            };
+            const std::string e0 = lit(0), e1 = lit(1);
+            o_ << "      const float c" << side << "_" << q << " = par ? " << (side == 0 ? e1 : e0) << " : "
+               << (side == 0 ? e0 : e1) << ";\n";
+          }
+        }
+        for (int j = 0; j < 8; ++j) {
+          const int side = __builtin_popcount((unsigned)j & cr) & 1;
+          const std::string s = "c" + std::to_string(side) + "_";
+          if (df_)
+            o_ << "      " << r(j) << " = df_cmul<true, true>(" << s << "0, " << s << "1, " << s << "2, " << s << "3, "
+               << r(j) << ");\n";
+          else
+            o_ << "      " << r(j) << " = f_cmul(" << s << "0, " << s << "1, " << r(j) << ");\n";
+        }
+        o_ << "    }\n";
+        for (int j = 0; j < 8; ++j) touched(j);
+      } break;
+      case OK_COLLAPSE: {
+        const std::string c = cond(t.gmask, t.gval, t.tmask, t.tval);
+        const uint32_t rv = t.rval & 7u;
+        o_ << "    {  // collapse\n      const bool tc = " << (c.empty() ? "true" : c) << ";\n";
+        for (int j = 0; j < 8; ++j) {
+          if ((j & cr) == rv) {
+            const std::string sc = df_ ? "df_scale<" + b(hi_lo_nonzero(t, 0)) + ">(" + h(t, 0) + ", " + l(t, 0) + ", " +
+                                             r(j) + ")"
+                                       : "f_scale(" + h(t, 0) + ", " + r(j) + ")";
+            o_ << "      " << r(j) << " = tc ? " << sc << " : " << pol() << "::zero();\n";
+          } else {
+            o_ << "      " << r(j) << " = " << pol() << "::zero();\n";
+          }
+          touched(j);
+        }
+        o_ << "    }\n";
+      } break;
+      default: break;
+    }
+  }
+
+  void body() {
+    const std::string V = df_ ? "dfc" : "float2";
+    const int E = df_ ? 16 : 8;
+    o_ << "    " << V << " r0, r1, r2, r3, r4, r5, r6, r7;\n    int q0, q1, q2, q3, q4, q5, q6, q7;\n    unsigned lt = 0;\n";
+    o_ << "    (void)lt;\n";
+    bool in_regs = false, raw = true;
+    for (int i = 0; i < nops_; ++i) {
+      const TOp& t = ops_[i];
+      if (t.kind == OK_LAYOUT) {
+        if (in_regs) {
+          renorm_all();
+          for (int j = 0; j < 8; ++j) o_ << "    " << pol() << "::st_work(buf, q" << j << ", r" << j << ");\n";
+          o_ << "    __syncthreads();\n";
+          raw = false;
+        }
+        o_ << "    lt = ins3<" << t.dbits[0] << ", " << t.dbits[1] << ", " << t.dbits[2] << ">(tid);\n";
+        for (int j = 0; j < 8; ++j) o_ << "    q" << j << " = swz<" << E << ">((int)(lt | " << hex32(t.lj[j]) << "));\n";
+        const std::string ld = raw ? ld_raw() : std::string(pol()) + "::ld_work";
+        for (int j = 0; j < 8; ++j) o_ << "    r" << j << " = " << ld << "(buf, q" << j << ");\n";
+        for (int j = 0; j < 8; ++j) since_[j] = 0;
+        in_regs = true;
+        continue;
+      }
+      op(t);
+    }
+    if (in_regs) {
+      if (io_ & kTileOutPairs) renorm_all();  // st_doubles normalises on its own
+      for (int j = 0; j < 8; ++j) o_ << "    " << st_raw() << "(buf, q" << j << ", r" << j << ");\n";
+    } else if (df_ && ((io_ & kTileInPairs) != 0) != ((io_ & kTileOutPairs) != 0)) {
+      // no op loaded the tile: convert its storage form in place, each thread its own slots
+      o_ << "    for (int l = (int)tid; l < (1 << K_BITS); l += (1 << K_BITS) / 8) {\n"
+         << "      const int q = swz<16>(l);\n      " << st_raw() << "(buf, q, " << ld_raw() << "(buf, q));\n    }\n";
+    }
+    o_ << "    __syncthreads();\n";
+  }
+};
+
+// ---------------------------------------------------------------------------
+// Compilation and the per-device cache
+// ---------------------------------------------------------------------------
+struct Unit {
+  std::string src;
+  std::vector<int> steps;  // program steps of the kernels in this unit (kernel qgp_<step>)
+  std::vector<char> cubin;
+  std::string err;
+};
+
+void compile_unit(Unit* u) {
+  const NvrtcApi& api = nvrtc_api();
+  nvrtcProgram p = nullptr;
+  const char* hdr_src[2] = {kEmbedPassPrelude, kEmbedDf64};
+  const char* hdr_names[2] = {"pass_prelude.cuh", "df64.cuh"};
+  if (api.create(&p, u->src.c_str(), "passes.cu", 2, hdr_src, hdr_names) != NVRTC_SUCCESS) {
+    u->err = "nvrtcCreateProgram failed";
+    return;
+  }
+  const char* opts[] = {"--gpu-architecture=sm_103a", "--std=c++17", "--fmad=false", "-default-device"};
+  const nvrtcResult rc = api.compile(p, 4, opts);
+  if (rc != NVRTC_SUCCESS) {
+    size_t n = 0;
+    api.log_size(p, &n);
+    std::string log(n, '\0');
+    if (n) api.log(p, &log[0]);
+    u->err = "pass kernel compile failed: " + log.substr(0, 2000);
+    api.destroy(&p);
+    return;
+  }
+  size_t n = 0;
+  api.cubin_size(p, &n);
+  u->cubin.resize(n);
+  api.cubin(p, u->cubin.data());
+  api.destroy(&p);
+}
+
+struct Compiled : PassKernels {
+  std::vector<cudaLibrary_t> libs;
+  std::vector<cudaKernel_t> kernel;  // per program step (nullptr: interpreted)
+  std::vector<int> smem;             // dynamic shared memory per step
+  double compile_ms = 0;
+  ~Compiled() {
+    for (cudaLibrary_t l : libs) cudaLibraryUnload(l);
+  }
+};
+
+std::mutex g_mu;
+std::unordered_map<std::string, std::shared_ptr<Compiled>> g_cache[64];  // per device, keyed by source
+size_t g_cache_hits = 0, g_cache_misses = 0;
+
+}  // namespace
+
+const char* pass_kernels_unavailable() {
+  const NvrtcApi& api = nvrtc_api();
+  return api.error.empty() ? nullptr : api.error.c_str();
+}
+
+namespace {
+
+// Generate the program's supported passes and group them into translation units.
+bool generate_units(const Program& prog, int prec, std::vector<Unit>* units, std::string* key, std::string* why) {
+  if (prec == QG_C128 && prog.arith != QG_ARITH_DOUBLE_FLOAT) {
+    *why = "complex128 exact arithmetic runs interpreted";
+    return false;
+  }
+  std::vector<std::pair<int, std::string>> pieces;
+  size_t total = 0;
+  for (size_t i = 0; i < prog.steps.size(); ++i) {
+    const Step& st = prog.steps[i];
+    if (st.kind != Step::TILE_PASS || st.pass.k != 12) continue;
+    const TOp* ops = prog.tops.data() + st.pass.op_begin;
+    const int nops = (int)(st.pass.op_end - st.pass.op_begin);
+    std::ostringstream o;
+    PassGen g(o, st.pass, ops, nops, prec, tile_pass_io(prog, i));
+    if (!g.supported()) continue;
+    g.emit((int)i);
+    pieces.emplace_back((int)i, o.str());
+    total += pieces.back().second.size();
+  }
+  if (pieces.empty()) {
+    *why = "no pass to specialise";
+    return false;
+  }
+  *key = std::to_string(prec) + ":";
+  key->reserve(total + 64);
+  for (auto& p : pieces) *key += p.second;
+  // one unit per host thread; passes dealt largest first to the smallest unit (the
+  // compile time of a pass grows faster than its source, so big passes go alone)
+  const unsigned hw = std::max(1u, std::thread::hardware_concurrency());
+  const size_t nunits = std::min<size_t>(pieces.size(), std::min(hw, 32u));
+  units->assign(nunits, Unit());
+  std::vector<size_t> load(nunits, 0), order(pieces.size());
+  for (size_t i = 0; i < order.size(); ++i) order[i] = i;
+  std::sort(order.begin(), order.end(),
+            [&](size_t a, size_t b) { return pieces[a].second.size() > pieces[b].second.size(); });
+  for (size_t u = 0; u < nunits; ++u) (*units)[u].src = "#include \"pass_prelude.cuh\"\n\n";
+  for (size_t i : order) {
+    const size_t u = std::min_element(load.begin(), load.end()) - load.begin();
+    (*units)[u].src += pieces[i].second;
+    (*units)[u].steps.push_back(pieces[i].first);
+    load[u] += pieces[i].second.size() * (1 + pieces[i].second.size() / 16384);
+  }
+  return true;
+}
+
+// Compile every unit (in parallel threads); false with the first error.
+bool compile_units(std::vector<Unit>& units, std::string* why) {
+  if (const char* e = pass_kernels_unavailable()) {
+    *why = e;
+    return false;
+  }
+  std::vector<std::thread> th;
+  for (size_t u = 1; u < units.size(); ++u) th.emplace_back(compile_unit, &units[u]);
+  compile_unit(&units[0]);
+  for (auto& t : th) t.join();
+  for (Unit& u : units)
+    if (!u.err.empty()) {
+      *why = u.err;
+      return false;
+    }
+  return true;
+}
+
+}  // namespace
+
+int pass_kernels_build_only(const Program& prog, int prec, int* kernels, double* compile_ms, std::string* why) {
+  std::vector<Unit> units;
+  std::string key;
+  *kernels = 0;
+  *compile_ms = 0;
+  if (!generate_units(prog, prec, &units, &key, why)) return 0;
+  const auto t0 = std::chrono::steady_clock::now();
+  if (!compile_units(units, why)) return -1;
+  *compile_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+  for (Unit& u : units) *kernels += (int)u.steps.size();
+  return 1;
+}
+
+std::string pass_kernels_source(const Program& prog, int prec) {
+  std::vector<Unit> units;
+  std::string key, why;
+  if (!generate_units(prog, prec, &units, &key, &why)) return std::string();
+  std::string s;
+  for (Unit& u : units) s += u.src;
+  return s;
+}
+
+std::shared_ptr<const PassKernels> pass_kernels_for(const Program& prog, int prec, int device, std::string* why) {
+  if (device < 0 || device >= 64) {
+    *why = "device ordinal out of range";
+    return nullptr;
+  }
+  std::vector<Unit> units;
+  std::string key;
+  if (!generate_units(prog, prec, &units, &key, why)) return nullptr;
+  {
+    std::lock_guard<std::mutex> lk(g_mu);
+    auto it = g_cache[device].find(key);
+    if (it != g_cache[device].end()) {
+      ++g_cache_hits;
+      return it->second;
+    }
+  }
+  const auto t0 = std::chrono::steady_clock::now();
+  if (!compile_units(units, why)) return nullptr;
+  auto c = std::make_shared<Compiled>();
+  c->kernel.assign(prog.steps.size(), nullptr);
+  c->smem.assign(prog.steps.size(), 0);
+  const int E = prec == QG_C128 ? 16 : 8;
+  for (Unit& u : units) {
+    cudaLibrary_t lib = nullptr;
+    cudaError_t e = cudaLibraryLoadData(&lib, u.cubin.data(), nullptr, nullptr, 0, nullptr, nullptr, 0);
+    if (e != cudaSuccess) {
+      *why = std::string("loading pass kernels: ") + cudaGetErrorString(e);
+      return nullptr;
+    }
+    c->libs.push_back(lib);
+    for (int s : u.steps) {
+      cudaKernel_t k = nullptr;
+      const std::string name = "qgp_" + std::to_string(s);
+      e = cudaLibraryGetKernel(&k, lib, name.c_str());
+      if (e != cudaSuccess) {
+        *why = "pass kernel " + name + " missing";
+        return nullptr;
+      }
+      const int smem = 2 * (1 << prog.steps[s].pass.k) * E;
+      e = cudaKernelSetAttributeForDevice(k, cudaFuncAttributeMaxDynamicSharedMemorySize, smem, device);
+      if (e != cudaSuccess) {
+        *why = std::string("pass kernel attribute: ") + cudaGetErrorString(e);
+        return nullptr;
+      }
+      c->kernel[s] = k;
+      c->smem[s] = smem;
+    }
+  }
+  c->compile_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+  std::lock_guard<std::mutex> lk(g_mu);
+  ++g_cache_misses;
+  auto& slot = g_cache[device][key];
+  if (!slot) slot = c;
+  return slot;
+}
+
+bool pass_kernel_ready(const PassKernels& pk, size_t step) {
+  const Compiled& c = static_cast<const Compiled&>(pk);
+  return step < c.kernel.size() && c.kernel[step] != nullptr;
+}
+
+double pass_kernels_compile_ms(const PassKernels& pk) { return static_cast<const Compiled&>(pk).compile_ms; }
+
+cudaError_t launch_pass_kernel(const PassKernels& pk, size_t step, int n, const PassDesc& pd, void* state, int prec,
+                               cudaStream_t st) {
+  const Compiled& c = static_cast<const Compiled&>(pk);
+  if (step >= c.kernel.size() || !c.kernel[step]) return cudaErrorInvalidValue;
+  const uint64_t ntiles = 1ULL << (n - pd.k);
+  const int per_sm = prec == QG_C128 ? 1 : 2;
+  uint64_t grid = (uint64_t)kSMCount * per_sm;
+  if (grid > ntiles) grid = ntiles;
+  unsigned long long nt = ntiles;
+  unsigned char* sp = static_cast<unsigned char*>(state);
+  void* args[2] = {&sp, &nt};
+  cudaError_t e = cudaLaunchKernel((const void*)c.kernel[step], dim3((unsigned)grid), dim3(512), args,
+                                   (size_t)c.smem[step], st);
+  count_launch(1);
+  return e;
+}
+
+void pass_kernel_cache_stats(size_t* hits, size_t* misses) {
+  std::lock_guard<std::mutex> lk(g_mu);
+  *hits = g_cache_hits;
+  *misses = g_cache_misses;
+}
+
+}  // namespace qg

@@ -1,0 +1,303 @@
+// Device prelude of the specialised pass kernels (pass_kernels.cpp).
+//
+// A tiled pass (one HBM read and write of the state that applies a run of
+// gates, see tile.cu) is compiled into its own kernel: the generated code
+// names every gate with its matrix entries as literals, its register slots and
+// its conditions, so the gate run is straight-line code with no op dispatch.
+// This file holds what every such kernel shares:
+//   - run_pass<P>: the tile loop (cp.async double-buffered 16-byte copies into
+//     an XOR-swizzled shared-memory tile, P::body applied to the tile, coalesced
+//     16-byte stores), with the pass geometry supplied by P;
+//   - the complex arithmetic of the two policies the generator emits:
+//       complex128 as double-float pairs (hi + lo floats, about 48 bits) on the
+//       FP32 pipes, with error-free products (FMA) and sums (TwoSum); results
+//       are left unnormalised (the pair (s, t) of a rounded sum and its
+//       collected error) and renormalised by the generated code after a few
+//       operations on a register and before it is stored;
+//       complex64 in FP32 with FMA contraction.
+// It is compiled by NVRTC together with df64.cuh; it includes no system header.
+#pragma once
+
+#include "df64.cuh"
+
+namespace qgp {
+
+using qg::dfc;
+typedef unsigned long long u64;
+
+__device__ __forceinline__ void cp_async16(void* smem, const void* gmem) {
+  const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(s), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_wait() { asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory"); }
+
+// XOR swizzle of the shared-memory tile (16-byte units, 8 per 128-byte row);
+// 8-byte amplitudes move in 16-byte pairs.
+template <int E>
+__device__ __forceinline__ int swz(int l) {
+  if (E == 16) return l ^ ((l >> 3) & 7);
+  return l ^ (((l >> 4) & 7) << 1);
+}
+
+// Local index of a thread with zeros inserted at register bits A < B < C.
+template <int A, int B, int C>
+__device__ __forceinline__ unsigned ins3(unsigned t) {
+  t = ((t >> A) << (A + 1)) | (t & ((1u << A) - 1));
+  t = ((t >> B) << (B + 1)) | (t & ((1u << B) - 1));
+  t = ((t >> C) << (C + 1)) | (t & ((1u << C) - 1));
+  return t;
+}
+
+// ---------------------------------------------------------------------------
+// double-float scalars. A value is the unevaluated sum h + l of two floats.
+// tprod: a * x with a a constant pair (ah, al) -> (p, e), p = fl(ah*xh) and e
+// its exact error plus the cross terms ah*xl, al*xh and al*xl (AL = false:
+// al == 0). Operands are unnormalised, so xl may be as large as 2^-22 |xh|
+// and keep the sign of xh (the conversion from doubles truncates hi); the
+// al*xl term is kept for that reason: dropped, it would scale every amplitude
+// by the same relative 2^-48-ish bias per product and make the norm drift.
+// ---------------------------------------------------------------------------
+template <bool AL>
+__device__ __forceinline__ void tprod(float ah, float al, float xh, float xl, float& p, float& e) {
+  p = ah * xh;
+  e = fmaf(ah, xh, -p);
+  e = fmaf(ah, xl, e);
+  if (AL) {
+    e = fmaf(al, xh, e);
+    e = fmaf(al, xl, e);
+  }
+}
+// Knuth's TwoSum: s = fl(a + b), e = (a + b) - s exactly.
+__device__ __forceinline__ void tsum(float a, float b, float& s, float& e) {
+  s = a + b;
+  const float bb = s - a;
+  e = (a - (s - bb)) + (b - bb);
+}
+// a*x + b*y, unnormalised
+template <bool AL, bool BL>
+__device__ __forceinline__ void dot2(float ah, float al, float xh, float xl, float bh, float bl, float yh, float yl,
+                                     float& sh, float& sl) {
+  float p1, e1, p2, e2, err;
+  tprod<AL>(ah, al, xh, xl, p1, e1);
+  tprod<BL>(bh, bl, yh, yl, p2, e2);
+  tsum(p1, p2, sh, err);
+  sl = (e1 + e2) + err;
+}
+// x + y, unnormalised
+__device__ __forceinline__ void add2(float xh, float xl, float yh, float yl, float& sh, float& sl) {
+  float err;
+  tsum(xh, yh, sh, err);
+  sl = (xl + yl) + err;
+}
+// Fast2Sum: bring the collected error back under the leading float. The
+// generated code applies it to a register after a few products (and before a
+// register goes to shared memory): left to grow, the low float random-walks to
+// a sizeable fraction of the high one and its roundings no longer average out
+// (the state's norm then drifts by ~1e-11 over a thousand gates).
+__device__ __forceinline__ void fast2(float& h, float& l) {
+  const float s = h + l;
+  l = l - (s - h);
+  h = s;
+}
+// normalised pair (|l| <= ulp(h)/2) for the conversion to IEEE doubles
+__device__ __forceinline__ void norm2(float& h, float& l) {
+  float s, e;
+  tsum(h, l, s, e);
+  h = s;
+  l = e;
+}
+
+// ---- complex double-float ------------------------------------------------
+struct DF {
+  typedef dfc V;
+  static constexpr int E = 16;
+  static __device__ __forceinline__ V ld_work(const unsigned char* b, int pos) {
+    const float4 v = reinterpret_cast<const float4*>(b)[pos];
+    return dfc{v.x, v.y, v.z, v.w};
+  }
+  static __device__ __forceinline__ void st_work(unsigned char* b, int pos, const V& v) {
+    reinterpret_cast<float4*>(b)[pos] = make_float4(v.rh, v.rl, v.ih, v.il);
+  }
+  static __device__ __forceinline__ V ld_doubles(const unsigned char* b, int pos) {
+    return qg::load_dfc(reinterpret_cast<const double2*>(b)[pos]);
+  }
+  static __device__ __forceinline__ void st_doubles(unsigned char* b, int pos, V v) {
+    norm2(v.rh, v.rl);
+    norm2(v.ih, v.il);
+    reinterpret_cast<double2*>(b)[pos] = qg::store_dfc(v);
+  }
+  static __device__ __forceinline__ V renorm(V v) {
+    fast2(v.rh, v.rl);
+    fast2(v.ih, v.il);
+    return v;
+  }
+  static __device__ __forceinline__ V zero() { return dfc{0.f, 0.f, 0.f, 0.f}; }
+  static __device__ __forceinline__ V neg(const V& x) { return dfc{-x.rh, -x.rl, -x.ih, -x.il}; }
+  static __device__ __forceinline__ V mul_i(const V& x) { return dfc{-x.ih, -x.il, x.rh, x.rl}; }
+  static __device__ __forceinline__ V mul_mi(const V& x) { return dfc{x.ih, x.il, -x.rh, -x.rl}; }
+};
+
+// (gr + i gi) * x
+template <bool RL, bool IL>
+__device__ __forceinline__ dfc df_cmul(float grh, float grl, float gih, float gil, const dfc& x) {
+  dfc y;
+  dot2<RL, IL>(grh, grl, x.rh, x.rl, -gih, -gil, x.ih, x.il, y.rh, y.rl);
+  dot2<RL, IL>(grh, grl, x.ih, x.il, gih, gil, x.rh, x.rl, y.ih, y.il);
+  return y;
+}
+// a real scalar times x
+template <bool AL>
+__device__ __forceinline__ dfc df_scale(float ah, float al, const dfc& x) {
+  dfc y;
+  tprod<AL>(ah, al, x.rh, x.rl, y.rh, y.rl);
+  tprod<AL>(ah, al, x.ih, x.il, y.ih, y.il);
+  return y;
+}
+// y = a*x0 + b*x1 for complex constants a, b (8 floats: a.re h/l, a.im h/l, b.re h/l, b.im h/l)
+__device__ __forceinline__ dfc df_row(float arh, float arl, float aih, float ail, float brh, float brl, float bih,
+                                      float bil, const dfc& x0, const dfc& x1) {
+  dfc y;
+  float uh, ul, vh, vl;
+  dot2<true, true>(arh, arl, x0.rh, x0.rl, -aih, -ail, x0.ih, x0.il, uh, ul);
+  dot2<true, true>(brh, brl, x1.rh, x1.rl, -bih, -bil, x1.ih, x1.il, vh, vl);
+  add2(uh, ul, vh, vl, y.rh, y.rl);
+  dot2<true, true>(arh, arl, x0.ih, x0.il, aih, ail, x0.rh, x0.rl, uh, ul);
+  dot2<true, true>(brh, brl, x1.ih, x1.il, bih, bil, x1.rh, x1.rl, vh, vl);
+  add2(uh, ul, vh, vl, y.ih, y.il);
+  return y;
+}
+// real 2x2 [[a, b], [c, d]]
+template <bool AL, bool BL, bool CL, bool DL>
+__device__ __forceinline__ void df_real(float ah, float al, float bh, float bl, float ch, float cl, float dh, float dl,
+                                        dfc& x0, dfc& x1) {
+  dfc y0, y1;
+  dot2<AL, BL>(ah, al, x0.rh, x0.rl, bh, bl, x1.rh, x1.rl, y0.rh, y0.rl);
+  dot2<AL, BL>(ah, al, x0.ih, x0.il, bh, bl, x1.ih, x1.il, y0.ih, y0.il);
+  dot2<CL, DL>(ch, cl, x0.rh, x0.rl, dh, dl, x1.rh, x1.rl, y1.rh, y1.rl);
+  dot2<CL, DL>(ch, cl, x0.ih, x0.il, dh, dl, x1.ih, x1.il, y1.ih, y1.il);
+  x0 = y0;
+  x1 = y1;
+}
+// [[c, c], [c, -c]] (Hadamard-shaped): the sum and difference first, one product each
+template <bool CL>
+__device__ __forceinline__ void df_hadamard(float ch, float cl, dfc& x0, dfc& x1) {
+  float sh, sl, dh, dl;
+  dfc y0, y1;
+  add2(x0.rh, x0.rl, x1.rh, x1.rl, sh, sl);
+  add2(x0.rh, x0.rl, -x1.rh, -x1.rl, dh, dl);
+  tprod<CL>(ch, cl, sh, sl, y0.rh, y0.rl);
+  tprod<CL>(ch, cl, dh, dl, y1.rh, y1.rl);
+  add2(x0.ih, x0.il, x1.ih, x1.il, sh, sl);
+  add2(x0.ih, x0.il, -x1.ih, -x1.il, dh, dl);
+  tprod<CL>(ch, cl, sh, sl, y0.ih, y0.il);
+  tprod<CL>(ch, cl, dh, dl, y1.ih, y1.il);
+  x0 = y0;
+  x1 = y1;
+}
+// [[a, i b], [i c, d]] with a, b, c, d real (RX-shaped)
+template <bool AL, bool BL, bool CL, bool DL>
+__device__ __forceinline__ void df_rxlike(float ah, float al, float bh, float bl, float ch, float cl, float dh, float dl,
+                                          dfc& x0, dfc& x1) {
+  dfc y0, y1;
+  dot2<AL, BL>(ah, al, x0.rh, x0.rl, -bh, -bl, x1.ih, x1.il, y0.rh, y0.rl);
+  dot2<AL, BL>(ah, al, x0.ih, x0.il, bh, bl, x1.rh, x1.rl, y0.ih, y0.il);
+  dot2<DL, CL>(dh, dl, x1.rh, x1.rl, -ch, -cl, x0.ih, x0.il, y1.rh, y1.rl);
+  dot2<CL, DL>(ch, cl, x0.rh, x0.rl, dh, dl, x1.ih, x1.il, y1.ih, y1.il);
+  x0 = y0;
+  x1 = y1;
+}
+
+// ---- complex64 -------------------------------------------------------------
+struct F32 {
+  typedef float2 V;
+  static constexpr int E = 8;
+  static __device__ __forceinline__ V ld_work(const unsigned char* b, int pos) {
+    return reinterpret_cast<const float2*>(b)[pos];
+  }
+  static __device__ __forceinline__ void st_work(unsigned char* b, int pos, const V& v) {
+    reinterpret_cast<float2*>(b)[pos] = v;
+  }
+  static __device__ __forceinline__ V zero() { return make_float2(0.f, 0.f); }
+  static __device__ __forceinline__ V neg(const V& x) { return make_float2(-x.x, -x.y); }
+  static __device__ __forceinline__ V mul_i(const V& x) { return make_float2(-x.y, x.x); }
+  static __device__ __forceinline__ V mul_mi(const V& x) { return make_float2(x.y, -x.x); }
+};
+__device__ __forceinline__ float2 f_cmul(float gr, float gi, float2 x) {
+  return make_float2(fmaf(gr, x.x, -(gi * x.y)), fmaf(gr, x.y, gi * x.x));
+}
+__device__ __forceinline__ float2 f_scale(float a, float2 x) { return make_float2(a * x.x, a * x.y); }
+__device__ __forceinline__ float2 f_row(float ar, float ai, float br, float bi, float2 x0, float2 x1) {
+  return make_float2(fmaf(ar, x0.x, fmaf(-ai, x0.y, fmaf(br, x1.x, -(bi * x1.y)))),
+                     fmaf(ar, x0.y, fmaf(ai, x0.x, fmaf(br, x1.y, bi * x1.x))));
+}
+__device__ __forceinline__ void f_real(float a, float b, float c, float d, float2& x0, float2& x1) {
+  const float2 y0 = make_float2(fmaf(a, x0.x, b * x1.x), fmaf(a, x0.y, b * x1.y));
+  const float2 y1 = make_float2(fmaf(c, x0.x, d * x1.x), fmaf(c, x0.y, d * x1.y));
+  x0 = y0;
+  x1 = y1;
+}
+__device__ __forceinline__ void f_hadamard(float c, float2& x0, float2& x1) {
+  const float2 y0 = make_float2(c * (x0.x + x1.x), c * (x0.y + x1.y));
+  const float2 y1 = make_float2(c * (x0.x - x1.x), c * (x0.y - x1.y));
+  x0 = y0;
+  x1 = y1;
+}
+__device__ __forceinline__ void f_rxlike(float a, float b, float c, float d, float2& x0, float2& x1) {
+  const float2 y0 = make_float2(fmaf(a, x0.x, -(b * x1.y)), fmaf(a, x0.y, b * x1.x));
+  const float2 y1 = make_float2(fmaf(d, x1.x, -(c * x0.y)), fmaf(c, x0.x, d * x1.y));
+  x0 = y0;
+  x1 = y1;
+}
+
+// ---------------------------------------------------------------------------
+// The tile loop. P supplies: E (bytes per amplitude in HBM), K_BITS, KLOW,
+// LM (mask of the local bit positions), hioff(h) (HBM offset, in amplitudes,
+// of the h-th 2^KLOW-amplitude run of a tile), tile_base(t) (first amplitude
+// of tile t) and body(buf, base) (the gate run on the tile in shared memory;
+// it ends with a barrier). Each CTA walks a contiguous range of tiles; the
+// next tile is prefetched while the current one is computed.
+// ---------------------------------------------------------------------------
+template <class P>
+__device__ __forceinline__ void run_pass(unsigned char* __restrict__ state, u64 ntiles) {
+  constexpr int E = P::E, K = 1 << P::K_BITS, T = K / 8, PER = 16 / E, CPT = E / 2;
+  extern __shared__ __align__(128) unsigned char smem[];
+  u64 goff[CPT];
+  unsigned soff[CPT];
+#pragma unroll
+  for (int i = 0; i < CPT; ++i) {
+    const int l = ((int)threadIdx.x + i * T) * PER;
+    goff[i] = ((u64)(l & ((1 << P::KLOW) - 1)) | P::hioff(l >> P::KLOW)) * E;
+    soff[i] = (unsigned)swz<E>(l) * E;
+  }
+  const u64 w0 = ntiles * blockIdx.x / gridDim.x, w1 = ntiles * (blockIdx.x + 1) / gridDim.x;
+  if (w0 >= w1) return;
+  u64 base = P::tile_base(w0);
+#pragma unroll
+  for (int i = 0; i < CPT; ++i) cp_async16(smem + soff[i], state + base * E + goff[i]);
+  cp_commit();
+  int it = 0;
+  for (u64 t = w0; t < w1; ++t, ++it) {
+    unsigned char* cur = smem + (it & 1) * (K * E);
+    const u64 nb = ((base | P::LM) + 1) & ~P::LM;
+    if (t + 1 < w1) {
+      unsigned char* nxt = smem + ((it + 1) & 1) * (K * E);
+#pragma unroll
+      for (int i = 0; i < CPT; ++i) cp_async16(nxt + soff[i], state + nb * E + goff[i]);
+      cp_commit();
+      cp_wait<1>();
+    } else {
+      cp_wait<0>();
+    }
+    __syncthreads();
+    P::body(cur, base);
+#pragma unroll
+    for (int i = 0; i < CPT; ++i)
+      *reinterpret_cast<uint4*>(state + base * E + goff[i]) = *reinterpret_cast<const uint4*>(cur + soff[i]);
+    __syncthreads();  // this buffer is refilled two tiles later
+    base = nb;
+  }
+}
+
+}  // namespace qgp

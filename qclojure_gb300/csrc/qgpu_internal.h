@@ -3,6 +3,7 @@
 #pragma once
 
 #include <cstdint>
+#include <memory>
 #include <string>
 #include <vector>
 
@@ -168,6 +169,29 @@ struct TileJobRec {
 cudaError_t launch_tile_jobs(int precision, int arithmetic, int n, const TileJobRec* d_jobs, int njobs,
                              const void* d_kops, const int32_t* d_pass_nops, cudaStream_t st);
 size_t kop_record_bytes();
+// ---------------------------------------------------------------------------
+// Specialised pass kernels (pass_kernels.cpp): every tiled pass of a program
+// (complex64, or complex128 double-float) compiled by NVRTC into its own
+// straight-line kernel; cached per device by generated source.
+// ---------------------------------------------------------------------------
+constexpr int kSMCount = 152;
+struct PassKernels {
+  virtual ~PassKernels() = default;
+};
+// nullptr (with the reason in why) when the program has nothing to specialise,
+// NVRTC is missing or a compile or load failed: the caller runs it interpreted.
+std::shared_ptr<const PassKernels> pass_kernels_for(const Program& prog, int prec, int device, std::string* why);
+bool pass_kernel_ready(const PassKernels& pk, size_t step);
+double pass_kernels_compile_ms(const PassKernels& pk);
+cudaError_t launch_pass_kernel(const PassKernels& pk, size_t step, int n, const PassDesc& pd, void* state, int prec,
+                               cudaStream_t st);
+// NVRTC availability (nullptr when usable, else the reason).
+const char* pass_kernels_unavailable();
+// Generate and compile without loading (no device needed): 1 compiled, 0 nothing
+// to specialise, -1 a compile error (in why).
+int pass_kernels_build_only(const Program& prog, int prec, int* kernels, double* compile_ms, std::string* why);
+std::string pass_kernels_source(const Program& prog, int prec);
+void pass_kernel_cache_stats(size_t* hits, size_t* misses);
 // batched sweep kernels (sweep.cu)
 int diag_max_groups();
 size_t diag_state_bytes();

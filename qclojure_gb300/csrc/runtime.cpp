@@ -151,6 +151,8 @@ static int download_c128(State* s, double* host, std::string* err) {
 struct ExecStats {
   double device_ms = 0;
   int passes = 0;
+  int specialised = 0;                     // tiled passes that ran as specialised kernels
+  double compile_ms = 0;                   // host time to obtain them (0 on a cache hit)
   std::vector<float>* pass_ms = nullptr;  // per-step CUDA-event times when profiling
   std::vector<int>* pass_kind = nullptr;
 };
@@ -267,10 +269,25 @@ static int do_measure(State* s, const std::vector<int>& qubits, uint64_t seed, u
   return QG_OK;
 }
 
+// Specialised pass kernels are used for states of at least this many qubits
+// (QG_PASS_KERNELS_AUTO). A pass kernel compiles in about 0.1 s of host time
+// (in parallel over the host cores); an interpreted 29-qubit double-float pass
+// takes about 13 ms on the device, so from here on even a circuit that runs once
+// gains, while smaller one-off jobs (the serving stream) would lose.
+constexpr int kPassKernelMinQubits = 29;
+
+static std::shared_ptr<const PassKernels> maybe_pass_kernels(const State* s, const Program& prog);
+
 static int exec_program(State* s, const Program& prog, uint64_t seed, const std::atomic<bool>* cancel,
                         ExecStats* stats, std::string* err) {
   double* d_dense = nullptr;
   void* d_kops = nullptr;
+  std::shared_ptr<const PassKernels> pk;
+  {
+    const auto t0 = Clock::now();
+    pk = maybe_pass_kernels(s, prog);
+    if (stats) stats->compile_ms = ms_since(t0);
+  }
   if (!prog.tops.empty()) {
     std::vector<unsigned char> kops(kop_record_bytes() * prog.tops.size());
     encode_kops(s->prec, prog.arith, prog.tops.data(), (int64_t)prog.tops.size(), kops.data());
@@ -292,7 +309,9 @@ static int exec_program(State* s, const Program& prog, uint64_t seed, const std:
   int rc = QG_OK;
   const bool profile = stats && stats->pass_ms;
   std::vector<cudaEvent_t> evs;
+  std::vector<int> spec_step;
   if (profile) {
+    spec_step.assign(prog.steps.size(), 0);
     evs.resize(prog.steps.size() + 1);
     for (auto& ev : evs) CK(cudaEventCreate(&ev), "event");
   }
@@ -307,8 +326,14 @@ static int exec_program(State* s, const Program& prog, uint64_t seed, const std:
     if (st.kind == Step::PLAIN_OP) {
       e = launch_plain_op(s->d, s->prec, s->n, st.op, s->stream);
     } else if (st.kind == Step::TILE_PASS) {
-      e = launch_tile_pass(s->prec, prog.arith, tile_pass_io(prog, i), s->n, st.pass, s->d_self, 1, d_kops, 0,
-                           d_dense, s->stream);
+      if (pk && pass_kernel_ready(*pk, i)) {
+        e = launch_pass_kernel(*pk, i, s->n, st.pass, s->d, s->prec, s->stream);
+        if (stats) ++stats->specialised;
+        if (profile) spec_step[i] = 1;
+      } else {
+        e = launch_tile_pass(s->prec, prog.arith, tile_pass_io(prog, i), s->n, st.pass, s->d_self, 1, d_kops, 0,
+                             d_dense, s->stream);
+      }
     } else {
       rc = do_measure(s, st.mqubits, seed, measure_index++, nullptr, nullptr, err);
     }
@@ -329,7 +354,8 @@ static int exec_program(State* s, const Program& prog, uint64_t seed, const std:
       float t = 0;
       if (rc == QG_OK) cudaEventElapsedTime(&t, evs[i], evs[i + 1]);
       stats->pass_ms->push_back(t);
-      stats->pass_kind->push_back(prog.steps[i].kind == Step::PLAIN_OP ? 0 : prog.steps[i].kind == Step::TILE_PASS ? 1 : 2);
+      const Step::Kind k = prog.steps[i].kind;
+      stats->pass_kind->push_back(k == Step::PLAIN_OP ? 0 : k == Step::TILE_PASS ? (spec_step[i] ? 3 : 1) : 2);
     }
     for (auto& ev : evs) cudaEventDestroy(ev);
   }
@@ -517,6 +543,7 @@ struct Job {
   uint64_t batch = 0;
   std::unique_ptr<Program> prog;      // compiled by the worker that admitted the job
   int batched_with = 0;               // jobs that shared its small-job launch (0: run alone)
+  int specialised = 0;                // tiled passes run as specialised kernels
 };
 
 struct Ctx {
@@ -544,6 +571,17 @@ struct Ctx {
   std::string last_error;
   std::mutex err_mu;
 };
+
+static std::shared_ptr<const PassKernels> maybe_pass_kernels(const State* s, const Program& prog) {
+  const Ctx* c = s->ctx;
+  if (!c || prog.tops.empty()) return nullptr;
+  if (s->prec == QG_C128 && prog.arith != QG_ARITH_DOUBLE_FLOAT) return nullptr;
+  const int mode = c->cfg.pass_kernels;
+  if (mode == QG_PASS_KERNELS_OFF) return nullptr;
+  if (mode != QG_PASS_KERNELS_ALWAYS && s->n < kPassKernelMinQubits) return nullptr;
+  std::string why;
+  return pass_kernels_for(prog, s->prec, c->device, &why);
+}
 
 static void set_ctx_error(Ctx* c, const std::string& e) {
   std::lock_guard<std::mutex> g(c->err_mu);
@@ -634,6 +672,7 @@ static int run_job(Ctx* c, Job* j, cudaStream_t stream) {
   if (rc == QG_OK) rc = exec_program(st.get(), *j->prog, j->seed, &j->cancel, &stats, &err);
   j->device_ms = stats.device_ms;
   j->passes = stats.passes;
+  j->specialised = stats.specialised;
   return job_results(c, j, std::move(st), stream, rc, std::move(err));
 }
 
@@ -1349,6 +1388,7 @@ int qg_job_details(void* ctx, uint64_t job, qg_job_info* out) {
   out->has_results = j->has & (j->state ? ~0 : ~QG_RES_STATE_VECTOR);
   out->error_code = j->error_code;
   out->batched_with = j->batched_with;
+  out->specialised_passes = j->specialised;
   return QG_OK;
 }
 
@@ -1705,6 +1745,29 @@ int qg_state_apply(void* state, const qg_circuit* circuit, int32_t fusion, uint6
   return state_err(s, rc, err);
 }
 
+int qg_state_prepare(void* state, const qg_circuit* circuit, int32_t fusion, double* compile_ms_out,
+                     int32_t* specialised_out) {
+  if (!state || !circuit) return QG_ERR_INVALID_ARG;
+  State* s = (State*)state;
+  if (circuit->num_qubits != s->n) {
+    set_ctx_error(s->ctx, "circuit and state have mismatched number of qubits");
+    return QG_ERR_INVALID_ARG;
+  }
+  cudaSetDevice(s->ctx->device);
+  std::string err;
+  Program prog;
+  int rc = compile_program(circuit, s->prec, fusion, s->ctx->cfg.fuse_k, s->ctx->cfg.arithmetic, &prog, &err);
+  if (rc != QG_OK) return state_err(s, rc, err);
+  const auto t0 = Clock::now();
+  auto pk = maybe_pass_kernels(s, prog);
+  if (compile_ms_out) *compile_ms_out = ms_since(t0);
+  int cnt = 0;
+  if (pk)
+    for (size_t i = 0; i < prog.steps.size(); ++i) cnt += pass_kernel_ready(*pk, i) ? 1 : 0;
+  if (specialised_out) *specialised_out = cnt;
+  return QG_OK;
+}
+
 int qg_state_probabilities(void* state, double* host_out) {
   if (!state || !host_out) return QG_ERR_INVALID_ARG;
   State* s = (State*)state;
@@ -1874,6 +1937,39 @@ int qg_state_profile(void* state, const qg_circuit* circuit, int32_t fusion, uin
     if (pass_ms) pass_ms[i] = ms[i];
     if (pass_kind) pass_kind[i] = kinds[i];
   }
+  return QG_OK;
+}
+
+int qg_pass_kernels_build(const qg_circuit* circuit, int32_t precision, int32_t arithmetic, int32_t* kernels_out,
+                          double* compile_ms_out, char* err_buf, int64_t err_len) {
+  if (!circuit || (precision != QG_C128 && precision != QG_C64)) return QG_ERR_INVALID_ARG;
+  std::string err;
+  Program prog;
+  const int arith = arithmetic == QG_ARITH_DOUBLE_FLOAT ? QG_ARITH_DOUBLE_FLOAT : QG_ARITH_EXACT;
+  int rc = compile_program(circuit, precision, QG_FUSE_TILED, 4, arith, &prog, &err);
+  if (rc == QG_OK) {
+    int kernels = 0;
+    double ms = 0;
+    const int r = pass_kernels_build_only(prog, precision, &kernels, &ms, &err);
+    if (kernels_out) *kernels_out = kernels;
+    if (compile_ms_out) *compile_ms_out = ms;
+    if (r < 0) rc = QG_ERR_DEVICE;
+    else if (r == 0 && pass_kernels_unavailable()) rc = QG_ERR_UNSUPPORTED;
+  }
+  if (err_buf && err_len > 0) {
+    const size_t n = std::min<size_t>(err.size(), (size_t)err_len - 1);
+    std::memcpy(err_buf, err.data(), n);
+    err_buf[n] = 0;
+  }
+  return rc;
+}
+
+int qg_pass_kernels_info(int32_t* available, uint64_t* cache_hits, uint64_t* cache_misses) {
+  if (available) *available = pass_kernels_unavailable() ? 0 : 1;
+  size_t h = 0, m = 0;
+  pass_kernel_cache_stats(&h, &m);
+  if (cache_hits) *cache_hits = h;
+  if (cache_misses) *cache_misses = m;
   return QG_OK;
 }
 

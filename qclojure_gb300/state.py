@@ -19,7 +19,7 @@ class Context:
     """A library context on one GPU (no job workers are needed for direct state use)."""
 
     def __init__(self, device: int = 0, precision: str = "c128", fusion: str = "tiled", fusion_width: int = 4,
-                 workers: int = 1, seed: int = 0, arithmetic: str = "double-float"):
+                 workers: int = 1, seed: int = 0, arithmetic: str = "double-float", pass_kernels: str = "auto"):
         self.lib = A.load_library()
         cfg = A.QgConfig()
         cfg.device = device
@@ -29,6 +29,7 @@ class Context:
         cfg.workers = workers
         cfg.seed = seed
         cfg.arithmetic = ARITHMETIC[arithmetic]
+        cfg.pass_kernels = A.PASS_KERNELS[pass_kernels]
         ctx = C.c_void_p()
         _check(self.lib.qg_ctx_create(C.byref(cfg), C.byref(ctx)))
         self.ctx = ctx
@@ -89,6 +90,27 @@ class DeviceState:
         passes = C.c_int32()
         self._ck(self.lib.qg_state_apply(self.h, enc.ref(), FUSIONS[fusion], C.c_uint64(seed), C.byref(passes)))
         return passes.value
+
+    def prepare(self, circuit: dict, fusion: str = "tiled") -> tuple[float, int]:
+        """Compile the circuit's specialised pass kernels ahead of apply(); returns
+        (compile milliseconds, passes that have a kernel)."""
+        enc = encode(circuit)
+        ms, cnt = C.c_double(), C.c_int32()
+        self._ck(self.lib.qg_state_prepare(self.h, enc.ref(), FUSIONS[fusion], C.byref(ms), C.byref(cnt)))
+        return ms.value, cnt.value
+
+    def profile(self, circuit: dict, fusion: str = "tiled", seed: int = 0) -> tuple[np.ndarray, np.ndarray]:
+        """Apply like apply() and return per-pass device times (ms) and kinds
+        (0 plain gate, 1 tiled pass, 2 measurement, 3 tiled pass run by its
+        specialised kernel)."""
+        enc = encode(circuit)
+        cap = 1 << 16
+        ms = (C.c_float * cap)()
+        kinds = (C.c_int32 * cap)()
+        n = C.c_int32()
+        self._ck(self.lib.qg_state_profile(self.h, enc.ref(), FUSIONS[fusion], C.c_uint64(seed), ms, kinds, cap,
+                                           C.byref(n)))
+        return np.array(ms[:n.value], np.float64), np.array(kinds[:n.value], np.int32)
 
     def probabilities(self) -> np.ndarray:
         out = np.empty(1 << self.n, np.float64)

@@ -1,0 +1,145 @@
+"""Specialised pass kernels (one generated, NVRTC-compiled kernel per tiled pass)
+against the CPU oracle, through the C ABI.
+
+The contexts here force the specialised kernels for every state size
+(pass_kernels="always"), so small states that the oracle finishes in seconds
+exercise the same generated code the large states run. Tolerances:
+  complex128 double-float   max |d amp| <= 1e-12 against the FP64 oracle
+  complex64                 max |d amp| <= 2e-5, probability TVD <= 1e-5
+  sampled outcomes          identical to the oracle's for the same seed (c128)
+"""
+import numpy as np
+import pytest
+
+from test_gpu_parity import _inverse, every_gate_circuit
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def ctx_df(built):
+    from qclojure_gb300.state import Context
+
+    ctx = Context(seed=1, arithmetic="double-float", pass_kernels="always")
+    yield ctx
+    ctx.close()
+
+
+@pytest.fixture(scope="module")
+def ctx_off(built):
+    from qclojure_gb300.state import Context
+
+    ctx = Context(seed=1, arithmetic="double-float", pass_kernels="off")
+    yield ctx
+    ctx.close()
+
+
+def _run(ctx, circuit, precision, seed=0):
+    st = ctx.state(circuit["num-qubits"], precision)
+    st.set_basis(0)
+    ms, kinds = st.profile(circuit, fusion="tiled", seed=seed)
+    return st, kinds
+
+
+@pytest.mark.parametrize("n", [12, 14, 17, 20])
+def test_layered_c128_df_specialised(ctx_df, oracle, n):
+    from qclojure_gb300 import workloads
+
+    c = workloads.layered_circuit(n, 20 if n <= 14 else 8, seed=300 + n)
+    ref = oracle.run(c)
+    st, kinds = _run(ctx_df, c, "c128")
+    with st:
+        assert np.count_nonzero(kinds == 3) > 0 and np.count_nonzero(kinds == 1) == 0, kinds
+        got = st.download()
+        assert np.max(np.abs(got - ref)) <= 1e-12, np.max(np.abs(got - ref))
+        assert np.array_equal(st.sample(2000, 5), oracle.sample(ref, 2000, 5))
+
+
+@pytest.mark.parametrize("n", [13, 16])
+def test_every_gate_c128_df_specialised(ctx_df, oracle, n):
+    c = every_gate_circuit(n, seed=400 + n)
+    ref = oracle.run(c)
+    st, kinds = _run(ctx_df, c, "c128")
+    with st:
+        assert np.count_nonzero(kinds == 3) > 0
+        err = np.max(np.abs(st.download() - ref))
+        assert err <= 1e-12, err
+
+
+def test_qft_c128_df_specialised(ctx_df, oracle):
+    """The QFT passes (long runs of controlled phases on thread and tile bits)."""
+    from qclojure_gb300 import workloads
+
+    n = 16
+    c = workloads.large_circuit(n, 3, seed=9)
+    ref = oracle.run(c)
+    st, kinds = _run(ctx_df, c, "c128")
+    with st:
+        err = np.max(np.abs(st.download() - ref))
+        assert err <= 1e-12, err
+
+
+def test_df_mid_circuit_measurement_specialised(ctx_df, oracle):
+    """Measurements split runs of passes: pair/double hand-over at every boundary."""
+    from qclojure_gb300 import workloads
+
+    n = 15
+    c = workloads.layered_circuit(n, 6, seed=31)
+    c["operations"] = c["operations"] + [{"operation-type": "measure",
+                                          "operation-params": {"measurement-qubits": [2, 14]}}] + \
+        workloads.layered_circuit(n, 5, seed=32)["operations"]
+    for seed in (1, 2):
+        ref = oracle.run(c, seed=seed)
+        st, kinds = _run(ctx_df, c, "c128", seed=seed)
+        with st:
+            assert np.count_nonzero(kinds == 2) == 1
+            assert np.max(np.abs(st.download() - ref)) <= 1e-12
+
+
+@pytest.mark.parametrize("n", [12, 16, 20])
+def test_layered_c64_specialised(ctx_df, oracle, n):
+    from qclojure_gb300 import workloads
+
+    c = workloads.layered_circuit(n, 12, seed=500 + n)
+    ref = oracle.run(c)
+    st, kinds = _run(ctx_df, c, "c64")
+    with st:
+        assert np.count_nonzero(kinds == 3) > 0
+        got = st.download()
+        assert np.max(np.abs(got - ref)) <= 2e-5
+        tvd = 0.5 * np.sum(np.abs(np.abs(got) ** 2 - np.abs(ref) ** 2))
+        assert tvd <= 1e-5, tvd
+
+
+def test_every_gate_c64_specialised(ctx_df, oracle):
+    c = every_gate_circuit(14, seed=614)
+    ref = oracle.run(c)
+    st, kinds = _run(ctx_df, c, "c64")
+    with st:
+        assert np.max(np.abs(st.download() - ref)) <= 2e-5
+
+
+def test_specialised_matches_interpreted(ctx_df, ctx_off):
+    """The same program through both executors: equal within the double-float bound."""
+    from qclojure_gb300 import workloads
+
+    c = workloads.large_circuit(18, 4, seed=5)
+    a, ka = _run(ctx_df, c, "c128")
+    b, kb = _run(ctx_off, c, "c128")
+    with a, b:
+        assert np.all(ka != 1) and np.all(kb != 3)
+        assert np.max(np.abs(a.download() - b.download())) <= 1e-12
+
+
+def test_inverse_at_24_qubits_specialised(ctx_df):
+    from qclojure_gb300 import workloads
+
+    n = 24
+    c = workloads.large_circuit(n, 4, seed=11)
+    st = ctx_df.state(n, "c128")
+    with st:
+        st.set_basis(0)
+        st.apply(c)
+        st.apply(_inverse(c))
+        assert abs(st.pauli_expectation("Z" * n) - 1.0) <= 1e-12
+        assert np.all(st.sample(300, 2) == 0)
