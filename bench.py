@@ -46,6 +46,8 @@ def parse():
     ap.add_argument("--precision", choices=["c128", "c64"], default="c128")
     ap.add_argument("--fusion", choices=["plain", "tiled", "dense"], default="tiled")
     ap.add_argument("--no-extras", action="store_true", help="skip the c64 / e2e / cpu-baseline legs")
+    ap.add_argument("--pass-kernels", choices=["auto", "always", "off"], default="auto",
+                    help="specialised per-pass kernels (auto: states of 29 qubits and more)")
     ap.add_argument("--seed", type=int, default=1)
     return ap.parse_args()
 
@@ -317,7 +319,7 @@ def main():
     gates = len(circ["operations"])
     N = 1 << n
     lib = A.load_library()
-    ctx = Context(device=local, workers=1, seed=7)
+    ctx = Context(device=local, workers=1, seed=7, pass_kernels=args.pass_kernels)
     st = ctx.state(n, args.precision)
     dptr, sptr = st.device_ptr()
     stream = torch.cuda.ExternalStream(sptr, device=torch.device("cuda", local))

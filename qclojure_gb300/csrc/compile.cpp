@@ -291,6 +291,30 @@ int lower_circuit(const qg_circuit* c, std::vector<GOp>* gops, std::vector<std::
   return QG_OK;
 }
 
+// Uncontrolled diagonal gates diag(d0, d1) become a phase d1/d0 on the bit-1 half
+// and a global factor d0, collected into one phase on every amplitude at the end:
+// a diagonal then costs one complex product on half the amplitudes instead of
+// one on each. Used with the double-float and complex64 policies, whose results
+// are held to a tolerance; the exact policy keeps the reference's products.
+void factor_global_phases(std::vector<GOp>* gops) {
+  cd global(1.0, 0.0);
+  bool any = false;
+  for (GOp& g : *gops) {
+    if (g.kind != OK_U2 || g.cls != U2_DIAG || g.cmask != 0) continue;
+    const cd d0(g.m[0], g.m[1]), d1(g.m[6], g.m[7]);
+    if (d0 == cd(0.0, 0.0)) continue;
+    const cd r = d1 / d0;
+    global *= d0;
+    any = true;
+    g = make_phase(1ULL << g.t, r.real(), r.imag());
+  }
+  gops->erase(std::remove_if(gops->begin(), gops->end(), [](const GOp& g) { return g.kind < 0; }), gops->end());
+  if (any) {
+    const GOp ph = make_phase(0, global.real(), global.imag());
+    if (ph.kind >= 0) gops->push_back(ph);
+  }
+}
+
 // ---------------------------------------------------------------------------
 // Scheduling
 // ---------------------------------------------------------------------------

@@ -146,7 +146,7 @@ class PassGen {
   int io_;
   // double-float: operations applied to each register since its last renormalisation
   int since_[8] = {0, 0, 0, 0, 0, 0, 0, 0};
-  static constexpr int kRenormEvery = 4;
+  static constexpr int kRenormEvery = 6;
 
   void touched(int j) {
     if (!df_) return;
@@ -383,6 +383,70 @@ class PassGen {
     }
   }
 
+  // A run of phase ops (diagonal, commuting with each other) multiplies each
+  // register by the product of the phases whose conditions it meets. The run
+  // collects those products per register-condition mask cr first (one complex
+  // product per op, whatever the number of registers it touches), then gives
+  // each register the product of the factors whose cr it contains.
+  static constexpr int kPhaseRunMin = 3;
+  void phase_run(int begin, int end) {
+    const std::string V = df_ ? "dfc" : "float2";
+    bool used[8] = {false, false, false, false, false, false, false, false};
+    int prods[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+    o_ << "    {  // run of " << (end - begin) << " phase ops\n";
+    for (int i = begin; i < end; ++i) {
+      const TOp& t = ops_[i];
+      const int cr = (int)(t.rmask & 7u);
+      const std::string c = cond(t.gmask, t.gmask, t.tmask, t.tval);
+      const std::string F = "F" + std::to_string(cr);
+      std::string lit;  // the phase as a value of the register type
+      if (t.cls == PH_GENERAL)
+        lit = df_ ? "dfc{" + h(t, 0) + ", " + l(t, 0) + ", " + h(t, 1) + ", " + l(t, 1) + "}"
+                  : "make_float2(" + h(t, 0) + ", " + h(t, 1) + ")";
+      else if (t.cls == PH_NEG)
+        lit = df_ ? "dfc{-1.0f, 0.0f, 0.0f, 0.0f}" : "make_float2(-1.0f, 0.0f)";
+      else if (t.cls == PH_I)
+        lit = df_ ? "dfc{0.0f, 0.0f, 1.0f, 0.0f}" : "make_float2(0.0f, 1.0f)";
+      else
+        lit = df_ ? "dfc{0.0f, 0.0f, -1.0f, 0.0f}" : "make_float2(0.0f, -1.0f)";
+      const std::string one = df_ ? "dfc{1.0f, 0.0f, 0.0f, 0.0f}" : "make_float2(1.0f, 0.0f)";
+      if (!used[cr]) {
+        used[cr] = true;
+        o_ << "      " << V << " " << F << " = " << (c.empty() ? lit : "(" + c + ") ? " + lit + " : " + one) << ";\n";
+        continue;
+      }
+      std::string upd;
+      if (t.cls == PH_GENERAL) upd = cmul(t, 0, 1, F);
+      else if (t.cls == PH_NEG) upd = std::string(pol()) + "::neg(" + F + ")";
+      else if (t.cls == PH_I) upd = std::string(pol()) + "::mul_i(" + F + ")";
+      else upd = std::string(pol()) + "::mul_mi(" + F + ")";
+      o_ << "      " << (c.empty() ? "" : "if (" + c + ") ") << F << " = " << upd << ";\n";
+      if (df_ && t.cls == PH_GENERAL && ++prods[cr] >= kRenormEvery) {
+        o_ << "      " << F << " = DF::renorm(" << F << ");\n";
+        prods[cr] = 0;
+      }
+    }
+    for (int j = 0; j < 8; ++j) {
+      std::vector<int> fs;
+      for (int cr = 0; cr < 8; ++cr)
+        if (used[cr] && (j & cr) == cr) fs.push_back(cr);
+      if (fs.empty()) continue;
+      std::string g = "F" + std::to_string(fs[0]);
+      for (size_t q = 1; q < fs.size(); ++q) {
+        const std::string f = "F" + std::to_string(fs[q]);
+        g = df_ ? "df_cmul<true, true>(" + f + ".rh, " + f + ".rl, " + f + ".ih, " + f + ".il, " + g + ")"
+                : "f_cmul(" + f + ".x, " + f + ".y, " + g + ")";
+      }
+      o_ << "      { const " << V << " G = " << g << ";\n";
+      if (df_)
+        o_ << "        r" << j << " = df_cmul<true, true>(G.rh, G.rl, G.ih, G.il, r" << j << "); }\n";
+      else
+        o_ << "        r" << j << " = f_cmul(G.x, G.y, r" << j << "); }\n";
+      touched(j);
+    }
+    o_ << "    }\n";
+  }
+
   void body() {
     const std::string V = df_ ? "dfc" : "float2";
     const int E = df_ ? 16 : 8;
@@ -405,6 +469,15 @@ class PassGen {
         for (int j = 0; j < 8; ++j) since_[j] = 0;
         in_regs = true;
         continue;
+      }
+      if (t.kind == OK_PHASE) {
+        int j = i;
+        while (j < nops_ && ops_[j].kind == OK_PHASE) ++j;
+        if (j - i >= kPhaseRunMin) {
+          phase_run(i, j);
+          i = j - 1;
+          continue;
+        }
       }
       op(t);
     }

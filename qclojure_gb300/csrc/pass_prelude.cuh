@@ -53,21 +53,14 @@ __device__ __forceinline__ unsigned ins3(unsigned t) {
 // ---------------------------------------------------------------------------
 // double-float scalars. A value is the unevaluated sum h + l of two floats.
 // tprod: a * x with a a constant pair (ah, al) -> (p, e), p = fl(ah*xh) and e
-// its exact error plus the cross terms ah*xl, al*xh and al*xl (AL = false:
-// al == 0). Operands are unnormalised, so xl may be as large as 2^-22 |xh|
-// and keep the sign of xh (the conversion from doubles truncates hi); the
-// al*xl term is kept for that reason: dropped, it would scale every amplitude
-// by the same relative 2^-48-ish bias per product and make the norm drift.
+// its exact error plus the cross terms ah*xl and al*xh (AL = false: al == 0).
 // ---------------------------------------------------------------------------
 template <bool AL>
 __device__ __forceinline__ void tprod(float ah, float al, float xh, float xl, float& p, float& e) {
   p = ah * xh;
   e = fmaf(ah, xh, -p);
   e = fmaf(ah, xl, e);
-  if (AL) {
-    e = fmaf(al, xh, e);
-    e = fmaf(al, xl, e);
-  }
+  if (AL) e = fmaf(al, xh, e);
 }
 // Knuth's TwoSum: s = fl(a + b), e = (a + b) - s exactly.
 __device__ __forceinline__ void tsum(float a, float b, float& s, float& e) {

@@ -130,6 +130,9 @@ struct Program {
 // err receives a message in the reference's words).
 int lower_circuit(const qg_circuit* c, std::vector<GOp>* gops, std::vector<std::vector<int>>* measures,
                   std::vector<int>* measure_at, std::string* err);
+// Tolerance-held policies only: uncontrolled diagonal gates to phases plus one
+// global phase at the end (no effect on the positions of earlier ops).
+void factor_global_phases(std::vector<GOp>* gops);
 // Schedule GOps into passes for the given fusion mode.
 int schedule(int n, int precision, int fusion, int fuse_k, const std::vector<GOp>& gops,
              const std::vector<std::vector<int>>& measures, const std::vector<int>& measure_at,

@@ -377,6 +377,8 @@ static int compile_program(const qg_circuit* c, int precision, int fusion, int f
   std::vector<int> measure_at;
   int rc = lower_circuit(c, &gops, &measures, &measure_at, err);
   if (rc != QG_OK) return rc;
+  if (fusion == QG_FUSE_TILED && (precision == QG_C64 || prog->arith == QG_ARITH_DOUBLE_FLOAT))
+    factor_global_phases(&gops);
   return schedule(c->num_qubits, precision, fusion, fuse_k, gops, measures, measure_at, prog, err);
 }
 
