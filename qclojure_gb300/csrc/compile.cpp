@@ -565,7 +565,7 @@ void plan_register_groups(std::vector<TOp>& ops, int k) {
 
 int schedule(int n, int precision, int fusion, int fuse_k, const std::vector<GOp>& gops,
              const std::vector<std::vector<int>>& measures, const std::vector<int>& measure_at, Program* prog,
-             std::string* err) {
+             std::string* err, bool reorder) {
   prog->n = n;
   prog->steps.clear();
   prog->tops.clear();
@@ -656,10 +656,18 @@ int schedule(int n, int precision, int fusion, int fuse_k, const std::vector<GOp
     for (size_t g = 0; g < gops.size(); ++g) orig_index.push_back(g);
   }
 
-  // Greedy pass formation.
+  // Greedy pass formation with look-ahead (reorder): an op later in the circuit
+  // joins the pass when its non-diagonal bits fit the tile and it touches no
+  // qubit of an op left out before it (so it commutes past every op it
+  // overtakes). Ops stay in circuit order inside a pass and never cross a
+  // measurement. Overtaking changes the order of roundings, so the exact policy
+  // (bit-identical to the reference's gate order) forms passes strictly in order.
+  std::vector<char> done(ops.size(), 0);
+  const uint64_t all_bits = n >= 64 ? ~0ULL : ((1ULL << n) - 1);
   size_t oi = 0;
   mi = 0;
   while (oi < ops.size() || mi < measures.size()) {
+    while (oi < ops.size() && done[oi]) ++oi;
     // measurements that come before the next op
     size_t next_gate = oi < ops.size() ? orig_index[oi] : gops.size();
     if (mi < measures.size() && (size_t)measure_at[mi] <= next_gate) {
@@ -681,13 +689,28 @@ int schedule(int n, int precision, int fusion, int fuse_k, const std::vector<GOp
     }
     // at most half the kernel-parameter op records: every gate may need a layout op before it
     const size_t max_ops = (size_t)max_ops_per_tile_pass() / 2;
-    while (oi < limit && oi - begin < max_ops) {
-      uint64_t r = required_local(ops[oi]);
-      if (__builtin_popcountll(L | r) > k) break;
-      L |= r;
-      ++oi;
+    // Ops left out so far: bits they change (non-diagonal targets) and bits they
+    // read or phase. A later op commutes past them when its own non-diagonal
+    // bits avoid both sets and its diagonal bits (controls, phase masks) avoid
+    // the changed ones: diagonal ops commute with each other.
+    std::vector<size_t> members;
+    uint64_t changed = 0, seen = 0;
+    for (size_t j = begin; j < limit && members.size() < max_ops; ++j) {
+      if (done[j]) continue;
+      const uint64_t tb = touched(ops[j]), r = required_local(ops[j]);
+      const bool commutes = (r & seen) == 0 && ((tb & ~r) & changed) == 0;
+      if (commutes && __builtin_popcountll(L | r) <= k) {
+        L |= r;
+        members.push_back(j);
+        done[j] = 1;
+      } else {
+        if (!reorder) break;
+        changed |= r;
+        seen |= tb;
+        if ((changed & all_bits) == all_bits) break;
+      }
     }
-    if (oi == begin) {  // cannot happen for k >= 5 (at most 5 bits per op) but keep it safe
+    if (members.empty()) {  // cannot happen for k >= 5 (at most 5 bits per op) but keep it safe
       *err = "operation wider than a tile";
       return QG_ERR_UNSUPPORTED;
     }
@@ -700,7 +723,7 @@ int schedule(int n, int precision, int fusion, int fuse_k, const std::vector<GOp
     for (int b = 0; b < 64; ++b) lpos[b] = -1;
     for (int j = 0; j < s.pass.k; ++j) lpos[s.pass.lbits[j]] = j;
     std::vector<TOp> pass_ops;
-    for (size_t j = begin; j < oi; ++j) pass_ops.push_back(localize(ops[j], lpos, n));
+    for (size_t j : members) pass_ops.push_back(localize(ops[j], lpos, n));
     plan_register_groups(pass_ops, s.pass.k);
     s.pass.op_begin = (int64_t)prog->tops.size();
     for (TOp& t : pass_ops) {

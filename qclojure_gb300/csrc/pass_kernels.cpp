@@ -99,24 +99,125 @@ inline bool hi_lo_nonzero(const TOp& t, int q) { return t.mf[8 + q] != 0.0f; }
 // ---------------------------------------------------------------------------
 // Source generation for one pass
 // ---------------------------------------------------------------------------
+// Register planning for the generated kernels: every thread holds 2^R amplitudes
+// whose local indices differ in R "register bits". Consecutive ops whose
+// non-diagonal bits fit in R bits share one layout; the remaining register bits
+// go to the local bits the group's conditions use most, so those conditions
+// select registers at compile time. (The interpreter plans the same way with
+// R = 3 in compile.cpp; here R is a property of the kernel shape.)
+std::vector<TOp> plan_layouts(const TOp* ops, int nops, int k, int R) {
+  std::vector<TOp> in;
+  for (int i = 0; i < nops; ++i)
+    if (ops[i].kind != OK_LAYOUT) in.push_back(ops[i]);
+  std::vector<TOp> out;
+  auto required = [](const TOp& t) -> uint32_t {
+    if (t.kind == OK_U2) return 1u << t.t;
+    if (t.kind == OK_SWAP) return (1u << t.t) | (1u << t.t2);
+    return 0u;
+  };
+  size_t i = 0;
+  while (i < in.size()) {
+    uint32_t rb = 0;
+    size_t j = i;
+    while (j < in.size() && __builtin_popcount(rb | required(in[j])) <= R) rb |= required(in[j++]);
+    int uses[32] = {0};
+    for (size_t q = i; q < j; ++q) {
+      const uint32_t cm = in[q].kind == OK_U2 || in[q].kind == OK_SWAP ? in[q].lcmask : in[q].lmask;
+      for (int b = 0; b < k; ++b)
+        if (cm & (1u << b)) ++uses[b];
+    }
+    while (__builtin_popcount(rb) < R) {
+      int best = -1;
+      for (int b = k - 1; b >= 0; --b)
+        if (!(rb & (1u << b)) && (best < 0 || uses[b] > uses[best])) best = b;
+      rb |= 1u << best;
+    }
+    int pos[5], np = 0;
+    for (int b = 0; b < k && np < R; ++b)
+      if (rb & (1u << b)) pos[np++] = b;
+    TOp lay;
+    std::memset(&lay, 0, sizeof(lay));
+    lay.kind = OK_LAYOUT;
+    for (int q = 0; q < R; ++q) lay.dbits[q] = pos[q];
+    out.push_back(lay);
+    auto rpos = [&](int b) {
+      for (int q = 0; q < R; ++q)
+        if (pos[q] == b) return q;
+      return -1;
+    };
+    auto reg_part = [&](uint32_t m) {
+      uint32_t r = 0;
+      for (int q = 0; q < R; ++q)
+        if (m & (1u << pos[q])) r |= 1u << q;
+      return r;
+    };
+    for (size_t q = i; q < j; ++q) {
+      TOp t = in[q];
+      uint32_t m = 0, v = 0;
+      if (t.kind == OK_U2) {
+        t.t2 = rpos(t.t);
+        m = v = t.lcmask;
+      } else if (t.kind == OK_SWAP) {
+        const int a = rpos(t.t), b = rpos(t.t2);
+        t.dbits[0] = a < b ? a : b;
+        t.dbits[1] = a < b ? b : a;
+        m = v = t.lcmask;
+      } else if (t.kind == OK_PHASE) {
+        m = v = t.lmask;
+      } else if (t.kind == OK_COLLAPSE) {
+        m = t.lmask;
+        v = t.lval;
+      } else {  // BLOCKADE, PARITY: the mask selects the bits to count
+        m = t.lmask;
+        v = 0;
+      }
+      t.rmask = reg_part(m);
+      t.rval = reg_part(v);
+      t.tmask = m & ~rb;
+      t.tval = v & ~rb;
+      out.push_back(t);
+    }
+    i = j;
+  }
+  return out;
+}
+
+// Kernel shape: register bits per thread, tile buffers, CTAs per SM.
+struct Shape {
+  int rbits, bufs, ctas;
+};
+// Measured on the 30-qubit layered + QFT circuit: double-float keeps 8 registers
+// per thread, two tile buffers and one CTA per SM (16 registers per thread spill
+// at two CTAs and starve latency hiding at one); complex64 runs two CTAs per SM.
+Shape shape_for(int prec) {
+  if (prec == QG_C128) return Shape{3, 2, 1};
+  return Shape{3, 2, 2};
+}
+
 class PassGen {
  public:
   PassGen(std::ostringstream& o, const PassDesc& pd, const TOp* ops, int nops, int prec, int io)
-      : o_(o), pd_(pd), ops_(ops), nops_(nops), df_(prec == QG_C128), io_(io) {}
+      : o_(o), pd_(pd), df_(prec == QG_C128), io_(io), sh_(shape_for(prec)) {
+    for (int i = 0; i < nops; ++i)
+      if (ops[i].kind == OK_DENSE) unsupported_ = true;
+    if (!unsupported_) plan_ = plan_layouts(ops, nops, pd.k, sh_.rbits);
+    // pairs handed over by the previous pass may carry unnormalised operations
+    if (io & kTileInPairs) carry_ = kRenormEvery / 2 - 1;
+    ops_ = plan_.data();
+    nops_ = (int)plan_.size();
+    ns_ = 1 << sh_.rbits;
+  }
 
   // false: the pass holds an op the generator does not specialise
-  bool supported() const {
-    for (int i = 0; i < nops_; ++i)
-      if (ops_[i].kind == OK_DENSE) return false;
-    return true;
-  }
+  bool supported() const { return !unsupported_; }
 
   void emit(int id) {
     const int E = df_ ? 16 : 8;
     uint64_t lm = 0;
     for (int j = 0; j < pd_.k; ++j) lm |= 1ULL << pd_.lbits[j];
     o_ << "namespace p" << id << " {\nstruct P {\n";
-    o_ << "  static constexpr int E = " << E << ", K_BITS = " << pd_.k << ", KLOW = " << pd_.klow << ";\n";
+    o_ << "  static constexpr int E = " << E << ", K_BITS = " << pd_.k << ", KLOW = " << pd_.klow
+       << ", R_BITS = " << sh_.rbits << ", BUFS = " << sh_.bufs << ";\n";
     o_ << "  static constexpr qgp::u64 LM = " << hex64(lm) << ";\n";
     // run offsets: bit j - klow of the run index h deposits at lbits[j]
     o_ << "  static __device__ __forceinline__ qgp::u64 hioff(int h) {\n    qgp::u64 o = 0;\n";
@@ -132,7 +233,8 @@ class PassGen {
     o_ << "    using namespace qgp;\n    const unsigned tid = threadIdx.x;\n    (void)base; (void)tid;\n";
     body();
     o_ << "  }\n};\n}  // namespace p" << id << "\n";
-    o_ << "extern \"C\" __global__ void __launch_bounds__(512, " << (df_ ? 1 : 2) << ") qgp_" << id
+    o_ << "extern \"C\" __global__ void __launch_bounds__(" << ((1 << pd_.k) >> sh_.rbits) << ", " << sh_.ctas
+       << ") qgp_" << id
        << "(unsigned char* __restrict__ state, unsigned long long ntiles) {\n  qgp::run_pass<p" << id
        << "::P>(state, ntiles);\n}\n\n";
   }
@@ -140,12 +242,16 @@ class PassGen {
  private:
   std::ostringstream& o_;
   const PassDesc& pd_;
-  const TOp* ops_;
-  int nops_;
   bool df_;
   int io_;
+  Shape sh_;
+  bool unsupported_ = false;
+  std::vector<TOp> plan_;
+  const TOp* ops_ = nullptr;
+  int nops_ = 0;
+  int ns_ = 8;  // registers (amplitudes) per thread
   // double-float: operations applied to each register since its last renormalisation
-  int since_[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+  int since_[16] = {0};
   static constexpr int kRenormEvery = 6;
 
   void touched(int j) {
@@ -155,13 +261,20 @@ class PassGen {
       since_[j] = 0;
     }
   }
-  void renorm_all() {
-    for (int j = 0; j < 8; ++j)
-      if (df_ && since_[j] > 0) {
+  // Before registers go to shared memory: renormalise those halfway to the
+  // limit; the rest keep their count, and after the next layout every register
+  // starts from the largest count left (it may hold any of the stored values).
+  void renorm_for_store() {
+    if (!df_) return;
+    for (int j = 0; j < ns_; ++j)
+      if (since_[j] >= kRenormEvery / 2) {
         o_ << "    r" << j << " = DF::renorm(r" << j << ");\n";
         since_[j] = 0;
       }
+    carry_ = 0;
+    for (int j = 0; j < ns_; ++j) carry_ = std::max(carry_, since_[j]);
   }
+  int carry_ = 0;
 
   const char* pol() const { return df_ ? "DF" : "F32"; }
   std::string ld_raw() const { return df_ && !(io_ & kTileInPairs) ? "DF::ld_doubles" : std::string(pol()) + "::ld_work"; }
@@ -259,7 +372,7 @@ class PassGen {
   static std::string r(int j) { return "r" + std::to_string(j); }
 
   void op(const TOp& t) {
-    const uint32_t cr = t.rmask & 7u;
+    const uint32_t cr = t.rmask & (uint32_t)(ns_ - 1);
     switch (t.kind) {
       case OK_U2: {
         const int rp = t.t2;
@@ -267,7 +380,7 @@ class PassGen {
         o_ << "    {  // U2 class " << t.cls << " on register bit " << rp << "\n";
         if (!c.empty()) o_ << "    if (" << c << ") {\n";
         std::vector<int> done;
-        for (int q = 0; q < 4; ++q) {
+        for (int q = 0; q < ns_ / 2; ++q) {
           const int j0 = ((q >> rp) << (rp + 1)) | (q & ((1 << rp) - 1));
           const int j1 = j0 | (1 << rp);
           if ((j0 & cr) != cr) continue;
@@ -285,7 +398,7 @@ class PassGen {
         const std::string c = cond(t.gmask, t.gmask, t.tmask, t.tval);
         o_ << "    {  // phase class " << t.cls << "\n";
         if (!c.empty()) o_ << "    if (" << c << ") {\n";
-        for (int j = 0; j < 8; ++j) {
+        for (int j = 0; j < ns_; ++j) {
           if ((j & cr) != cr) continue;
           std::string v;
           if (t.cls == PH_GENERAL) v = cmul(t, 0, 1, r(j));
@@ -297,7 +410,7 @@ class PassGen {
         if (!c.empty()) o_ << "    }\n";
         o_ << "    }\n";
         if (t.cls == PH_GENERAL)
-          for (int j = 0; j < 8; ++j)
+          for (int j = 0; j < ns_; ++j)
             if ((j & cr) == cr) touched(j);
       } break;
       case OK_SWAP: {
@@ -306,7 +419,7 @@ class PassGen {
         const std::string c = cond(t.gcmask, t.gcmask, t.tmask, t.tval);
         o_ << "    {  // swap of register bits " << A << ", " << B << (isw ? " (iSWAP)" : "") << "\n";
         if (!c.empty()) o_ << "    if (" << c << ") {\n";
-        for (int j = 0; j < 8; ++j) {
+        for (int j = 0; j < ns_; ++j) {
           if (!((j >> A) & 1) || ((j >> B) & 1) || (j & cr) != cr) continue;
           const int p = j ^ (1 << A) ^ (1 << B);
           const std::string T = df_ ? "dfc" : "float2";
@@ -324,13 +437,13 @@ class PassGen {
       case OK_BLOCKADE: {
         o_ << "    {  // blockade phase\n      const int cnt = __popcll(base & " << hex64(t.gmask) << ") + __popc(lt & "
            << hex32(t.tmask) << ");\n";
-        for (int j = 0; j < 8; ++j) {
+        for (int j = 0; j < ns_; ++j) {
           const int need = 1 - __builtin_popcount((unsigned)j & cr);
           if (need < 0) continue;
           o_ << "      if (cnt == " << need << ") " << r(j) << " = " << cmul(t, 0, 1, r(j)) << ";\n";
         }
         o_ << "    }\n";
-        for (int j = 0; j < 8; ++j)
+        for (int j = 0; j < ns_; ++j)
           if (1 - __builtin_popcount((unsigned)j & cr) >= 0) touched(j);
       } break;
       case OK_PARITY: {
@@ -350,7 +463,7 @@ class PassGen {
                << (side == 0 ? e0 : e1) << ";\n";
           }
         }
-        for (int j = 0; j < 8; ++j) {
+        for (int j = 0; j < ns_; ++j) {
           const int side = __builtin_popcount((unsigned)j & cr) & 1;
           const std::string s = "c" + std::to_string(side) + "_";
           if (df_)
@@ -360,13 +473,13 @@ class PassGen {
             o_ << "      " << r(j) << " = f_cmul(" << s << "0, " << s << "1, " << r(j) << ");\n";
         }
         o_ << "    }\n";
-        for (int j = 0; j < 8; ++j) touched(j);
+        for (int j = 0; j < ns_; ++j) touched(j);
       } break;
       case OK_COLLAPSE: {
         const std::string c = cond(t.gmask, t.gval, t.tmask, t.tval);
-        const uint32_t rv = t.rval & 7u;
+        const uint32_t rv = t.rval & (uint32_t)(ns_ - 1);
         o_ << "    {  // collapse\n      const bool tc = " << (c.empty() ? "true" : c) << ";\n";
-        for (int j = 0; j < 8; ++j) {
+        for (int j = 0; j < ns_; ++j) {
           if ((j & cr) == rv) {
             const std::string sc = df_ ? "df_scale<" + b(hi_lo_nonzero(t, 0)) + ">(" + h(t, 0) + ", " + l(t, 0) + ", " +
                                              r(j) + ")"
@@ -391,12 +504,12 @@ class PassGen {
   static constexpr int kPhaseRunMin = 3;
   void phase_run(int begin, int end) {
     const std::string V = df_ ? "dfc" : "float2";
-    bool used[8] = {false, false, false, false, false, false, false, false};
-    int prods[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+    bool used[16] = {false};
+    int prods[16] = {0};
     o_ << "    {  // run of " << (end - begin) << " phase ops\n";
     for (int i = begin; i < end; ++i) {
       const TOp& t = ops_[i];
-      const int cr = (int)(t.rmask & 7u);
+      const int cr = (int)(t.rmask & (uint32_t)(ns_ - 1));
       const std::string c = cond(t.gmask, t.gmask, t.tmask, t.tval);
       const std::string F = "F" + std::to_string(cr);
       std::string lit;  // the phase as a value of the register type
@@ -426,9 +539,9 @@ class PassGen {
         prods[cr] = 0;
       }
     }
-    for (int j = 0; j < 8; ++j) {
+    for (int j = 0; j < ns_; ++j) {
       std::vector<int> fs;
-      for (int cr = 0; cr < 8; ++cr)
+      for (int cr = 0; cr < ns_; ++cr)
         if (used[cr] && (j & cr) == cr) fs.push_back(cr);
       if (fs.empty()) continue;
       std::string g = "F" + std::to_string(fs[0]);
@@ -450,23 +563,37 @@ class PassGen {
   void body() {
     const std::string V = df_ ? "dfc" : "float2";
     const int E = df_ ? 16 : 8;
-    o_ << "    " << V << " r0, r1, r2, r3, r4, r5, r6, r7;\n    int q0, q1, q2, q3, q4, q5, q6, q7;\n    unsigned lt = 0;\n";
+    o_ << "    " << V;
+    for (int j = 0; j < ns_; ++j) o_ << (j ? ", r" : " r") << j;
+    o_ << ";\n    int";
+    for (int j = 0; j < ns_; ++j) o_ << (j ? ", q" : " q") << j;
+    o_ << ";\n    unsigned lt = 0;\n";
     o_ << "    (void)lt;\n";
     bool in_regs = false, raw = true;
     for (int i = 0; i < nops_; ++i) {
       const TOp& t = ops_[i];
       if (t.kind == OK_LAYOUT) {
         if (in_regs) {
-          renorm_all();
-          for (int j = 0; j < 8; ++j) o_ << "    " << pol() << "::st_work(buf, q" << j << ", r" << j << ");\n";
+          renorm_for_store();
+          for (int j = 0; j < ns_; ++j) o_ << "    " << pol() << "::st_work(buf, q" << j << ", r" << j << ");\n";
           o_ << "    __syncthreads();\n";
           raw = false;
         }
-        o_ << "    lt = ins3<" << t.dbits[0] << ", " << t.dbits[1] << ", " << t.dbits[2] << ">(tid);\n";
-        for (int j = 0; j < 8; ++j) o_ << "    q" << j << " = swz<" << E << ">((int)(lt | " << hex32(t.lj[j]) << "));\n";
+        // thread bits: zeros inserted at the register positions (ascending)
+        o_ << "    lt = tid;\n";
+        for (int q = 0; q < sh_.rbits; ++q) {
+          const int b = t.dbits[q];
+          o_ << "    lt = ((lt >> " << b << ") << " << (b + 1) << ") | (lt & " << hex32((1u << b) - 1) << ");\n";
+        }
+        for (int j = 0; j < ns_; ++j) {
+          uint32_t lj = 0;
+          for (int q = 0; q < sh_.rbits; ++q)
+            if ((j >> q) & 1) lj |= 1u << t.dbits[q];
+          o_ << "    q" << j << " = swz<" << E << ">((int)(lt | " << hex32(lj) << "));\n";
+        }
         const std::string ld = raw ? ld_raw() : std::string(pol()) + "::ld_work";
-        for (int j = 0; j < 8; ++j) o_ << "    r" << j << " = " << ld << "(buf, q" << j << ");\n";
-        for (int j = 0; j < 8; ++j) since_[j] = 0;
+        for (int j = 0; j < ns_; ++j) o_ << "    r" << j << " = " << ld << "(buf, q" << j << ");\n";
+        for (int j = 0; j < ns_; ++j) since_[j] = carry_;
         in_regs = true;
         continue;
       }
@@ -482,11 +609,11 @@ class PassGen {
       op(t);
     }
     if (in_regs) {
-      if (io_ & kTileOutPairs) renorm_all();  // st_doubles normalises on its own
-      for (int j = 0; j < 8; ++j) o_ << "    " << st_raw() << "(buf, q" << j << ", r" << j << ");\n";
+      if (io_ & kTileOutPairs) renorm_for_store();  // st_doubles normalises on its own
+      for (int j = 0; j < ns_; ++j) o_ << "    " << st_raw() << "(buf, q" << j << ", r" << j << ");\n";
     } else if (df_ && ((io_ & kTileInPairs) != 0) != ((io_ & kTileOutPairs) != 0)) {
       // no op loaded the tile: convert its storage form in place, each thread its own slots
-      o_ << "    for (int l = (int)tid; l < (1 << K_BITS); l += (1 << K_BITS) / 8) {\n"
+      o_ << "    for (int l = (int)tid; l < (1 << K_BITS); l += (1 << K_BITS) >> R_BITS) {\n"
          << "      const int q = swz<16>(l);\n      " << st_raw() << "(buf, q, " << ld_raw() << "(buf, q));\n    }\n";
     }
     o_ << "    __syncthreads();\n";
@@ -679,7 +806,8 @@ std::shared_ptr<const PassKernels> pass_kernels_for(const Program& prog, int pre
         *why = "pass kernel " + name + " missing";
         return nullptr;
       }
-      const int smem = 2 * (1 << prog.steps[s].pass.k) * E;
+      const Shape sh = shape_for(prec);
+      const int smem = sh.bufs * (1 << prog.steps[s].pass.k) * E;
       e = cudaKernelSetAttributeForDevice(k, cudaFuncAttributeMaxDynamicSharedMemorySize, smem, device);
       if (e != cudaSuccess) {
         *why = std::string("pass kernel attribute: ") + cudaGetErrorString(e);
@@ -709,14 +837,14 @@ cudaError_t launch_pass_kernel(const PassKernels& pk, size_t step, int n, const 
   const Compiled& c = static_cast<const Compiled&>(pk);
   if (step >= c.kernel.size() || !c.kernel[step]) return cudaErrorInvalidValue;
   const uint64_t ntiles = 1ULL << (n - pd.k);
-  const int per_sm = prec == QG_C128 ? 1 : 2;
-  uint64_t grid = (uint64_t)kSMCount * per_sm;
+  const Shape sh = shape_for(prec);
+  uint64_t grid = (uint64_t)kSMCount * sh.ctas;
   if (grid > ntiles) grid = ntiles;
   unsigned long long nt = ntiles;
   unsigned char* sp = static_cast<unsigned char*>(state);
   void* args[2] = {&sp, &nt};
-  cudaError_t e = cudaLaunchKernel((const void*)c.kernel[step], dim3((unsigned)grid), dim3(512), args,
-                                   (size_t)c.smem[step], st);
+  cudaError_t e = cudaLaunchKernel((const void*)c.kernel[step], dim3((unsigned)grid),
+                                   dim3((unsigned)((1 << pd.k) >> sh.rbits)), args, (size_t)c.smem[step], st);
   count_launch(1);
   return e;
 }

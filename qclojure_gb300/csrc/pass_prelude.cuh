@@ -41,15 +41,6 @@ __device__ __forceinline__ int swz(int l) {
   return l ^ (((l >> 4) & 7) << 1);
 }
 
-// Local index of a thread with zeros inserted at register bits A < B < C.
-template <int A, int B, int C>
-__device__ __forceinline__ unsigned ins3(unsigned t) {
-  t = ((t >> A) << (A + 1)) | (t & ((1u << A) - 1));
-  t = ((t >> B) << (B + 1)) | (t & ((1u << B) - 1));
-  t = ((t >> C) << (C + 1)) | (t & ((1u << C) - 1));
-  return t;
-}
-
 // ---------------------------------------------------------------------------
 // double-float scalars. A value is the unevaluated sum h + l of two floats.
 // tprod: a * x with a a constant pair (ah, al) -> (p, e), p = fl(ah*xh) and e
@@ -246,15 +237,17 @@ __device__ __forceinline__ void f_rxlike(float a, float b, float c, float d, flo
 
 // ---------------------------------------------------------------------------
 // The tile loop. P supplies: E (bytes per amplitude in HBM), K_BITS, KLOW,
-// LM (mask of the local bit positions), hioff(h) (HBM offset, in amplitudes,
-// of the h-th 2^KLOW-amplitude run of a tile), tile_base(t) (first amplitude
-// of tile t) and body(buf, base) (the gate run on the tile in shared memory;
-// it ends with a barrier). Each CTA walks a contiguous range of tiles; the
-// next tile is prefetched while the current one is computed.
+// R_BITS (each of the 2^(K_BITS - R_BITS) threads holds 2^R_BITS amplitudes),
+// BUFS (1: one tile buffer, the SM's other CTAs overlap their copies with this
+// one's arithmetic; 2: the next tile is prefetched into a second buffer), LM
+// (mask of the local bit positions), hioff(h) (HBM offset, in amplitudes, of the
+// h-th 2^KLOW-amplitude run of a tile), tile_base(t) (first amplitude of tile t)
+// and body(buf, base) (the gate run on the tile in shared memory; it ends with a
+// barrier). Each CTA walks a contiguous range of tiles.
 // ---------------------------------------------------------------------------
 template <class P>
 __device__ __forceinline__ void run_pass(unsigned char* __restrict__ state, u64 ntiles) {
-  constexpr int E = P::E, K = 1 << P::K_BITS, T = K / 8, PER = 16 / E, CPT = E / 2;
+  constexpr int E = P::E, K = 1 << P::K_BITS, T = K >> P::R_BITS, PER = 16 / E, CPT = (K * E / 16) / T;
   extern __shared__ __align__(128) unsigned char smem[];
   u64 goff[CPT];
   unsigned soff[CPT];
@@ -267,6 +260,22 @@ __device__ __forceinline__ void run_pass(unsigned char* __restrict__ state, u64 
   const u64 w0 = ntiles * blockIdx.x / gridDim.x, w1 = ntiles * (blockIdx.x + 1) / gridDim.x;
   if (w0 >= w1) return;
   u64 base = P::tile_base(w0);
+  if (P::BUFS == 1) {
+    for (u64 t = w0; t < w1; ++t) {
+#pragma unroll
+      for (int i = 0; i < CPT; ++i) cp_async16(smem + soff[i], state + base * E + goff[i]);
+      cp_commit();
+      cp_wait<0>();
+      __syncthreads();
+      P::body(smem, base);
+#pragma unroll
+      for (int i = 0; i < CPT; ++i)
+        *reinterpret_cast<uint4*>(state + base * E + goff[i]) = *reinterpret_cast<const uint4*>(smem + soff[i]);
+      __syncthreads();  // the buffer is refilled by the next tile
+      base = ((base | P::LM) + 1) & ~P::LM;
+    }
+    return;
+  }
 #pragma unroll
   for (int i = 0; i < CPT; ++i) cp_async16(smem + soff[i], state + base * E + goff[i]);
   cp_commit();

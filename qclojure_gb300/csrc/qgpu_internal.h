@@ -133,10 +133,11 @@ int lower_circuit(const qg_circuit* c, std::vector<GOp>* gops, std::vector<std::
 // Tolerance-held policies only: uncontrolled diagonal gates to phases plus one
 // global phase at the end (no effect on the positions of earlier ops).
 void factor_global_phases(std::vector<GOp>* gops);
-// Schedule GOps into passes for the given fusion mode.
+// Schedule GOps into passes for the given fusion mode; reorder lets commuting ops
+// overtake each other to fill passes (tolerance-held policies only).
 int schedule(int n, int precision, int fusion, int fuse_k, const std::vector<GOp>& gops,
              const std::vector<std::vector<int>>& measures, const std::vector<int>& measure_at,
-             Program* prog, std::string* err);
+             Program* prog, std::string* err, bool reorder);
 
 // ---------------------------------------------------------------------------
 // Kernel launchers (kernels.cu). All return cudaError_t from the launch.

@@ -368,8 +368,10 @@ static int exec_program(State* s, const Program& prog, uint64_t seed, const std:
   return rc;
 }
 
+// reorder = false keeps passes in circuit order even for tolerance-held policies:
+// sweeps batch circuits whose pass structure must not depend on their graphs.
 static int compile_program(const qg_circuit* c, int precision, int fusion, int fuse_k, int arith, Program* prog,
-                           std::string* err) {
+                           std::string* err, bool reorder = true) {
   // dense fused blocks are evaluated in FP64 (FMA) whatever the arithmetic setting
   prog->arith = (fusion == QG_FUSE_DENSE || arith != QG_ARITH_DOUBLE_FLOAT) ? QG_ARITH_EXACT : QG_ARITH_DOUBLE_FLOAT;
   std::vector<GOp> gops;
@@ -377,9 +379,10 @@ static int compile_program(const qg_circuit* c, int precision, int fusion, int f
   std::vector<int> measure_at;
   int rc = lower_circuit(c, &gops, &measures, &measure_at, err);
   if (rc != QG_OK) return rc;
-  if (fusion == QG_FUSE_TILED && (precision == QG_C64 || prog->arith == QG_ARITH_DOUBLE_FLOAT))
-    factor_global_phases(&gops);
-  return schedule(c->num_qubits, precision, fusion, fuse_k, gops, measures, measure_at, prog, err);
+  const bool tolerance_held = precision == QG_C64 || prog->arith == QG_ARITH_DOUBLE_FLOAT;
+  if (fusion == QG_FUSE_TILED && tolerance_held) factor_global_phases(&gops);
+  return schedule(c->num_qubits, precision, fusion, fuse_k, gops, measures, measure_at, prog, err,
+                  reorder && fusion == QG_FUSE_TILED && tolerance_held);
 }
 
 // ---------------------------------------------------------------------------
@@ -2112,7 +2115,7 @@ int qg_sweep_create(void* ctx, const qg_circuit* circuits, int32_t count, int32_
   std::map<std::vector<int64_t>, int> by_sig;
   for (int i = 0; i < count; ++i) {
     Program prog;
-    int rc = compile_program(&circuits[i], precision, QG_FUSE_TILED, c->cfg.fuse_k, sw->arith, &prog, &err);
+    int rc = compile_program(&circuits[i], precision, QG_FUSE_TILED, c->cfg.fuse_k, sw->arith, &prog, &err, false);
     if (rc != QG_OK) {
       set_ctx_error(c, "circuit " + std::to_string(i) + ": " + err);
       sweep_free(sw);
@@ -2215,7 +2218,8 @@ int qg_sweep_update(void* sweep, const qg_circuit* circuits, int32_t count) {
   std::string err;
   for (int i = 0; i < count; ++i) {
     Program prog;
-    int rc = compile_program(&circuits[i], sw->prec, QG_FUSE_TILED, sw->ctx->cfg.fuse_k, sw->arith, &prog, &err);
+    int rc = compile_program(&circuits[i], sw->prec, QG_FUSE_TILED, sw->ctx->cfg.fuse_k, sw->arith, &prog, &err,
+                             false);
     if (rc != QG_OK) {
       set_ctx_error(sw->ctx, err);
       return rc;
