@@ -115,14 +115,36 @@ std::vector<TOp> plan_layouts(const TOp* ops, int nops, int k, int R) {
     if (t.kind == OK_SWAP) return (1u << t.t) | (1u << t.t2);
     return 0u;
   };
-  size_t i = 0;
-  while (i < in.size()) {
-    uint32_t rb = 0;
-    size_t j = i;
-    while (j < in.size() && __builtin_popcount(rb | required(in[j])) <= R) rb |= required(in[j++]);
+  auto cond_bits = [](const TOp& t) -> uint32_t {
+    return t.kind == OK_U2 || t.kind == OK_SWAP ? t.lcmask : t.lmask;
+  };
+  // Groups are formed with look-ahead: an op joins the current layout when its
+  // non-diagonal bits fit the register bits and it commutes with every op left
+  // out before it (no shared bit that either changes; tile bits are only ever
+  // diagonal, so local bits decide). Fewer layouts mean fewer trips through
+  // shared memory and fewer barriers.
+  std::vector<char> taken(in.size(), 0);
+  size_t first = 0;
+  while (first < in.size()) {
+    uint32_t rb = 0, changed = 0, seen = 0;
+    std::vector<TOp> grp;
+    for (size_t j = first; j < in.size(); ++j) {
+      if (taken[j]) continue;
+      const uint32_t req = required(in[j]), tb = req | cond_bits(in[j]);
+      const bool commutes = (req & seen) == 0 && ((tb & ~req) & changed) == 0;
+      if (commutes && __builtin_popcount(rb | req) <= R) {
+        rb |= req;
+        grp.push_back(in[j]);
+        taken[j] = 1;
+      } else {
+        changed |= req;
+        seen |= tb;
+      }
+    }
+    while (first < in.size() && taken[first]) ++first;
     int uses[32] = {0};
-    for (size_t q = i; q < j; ++q) {
-      const uint32_t cm = in[q].kind == OK_U2 || in[q].kind == OK_SWAP ? in[q].lcmask : in[q].lmask;
+    for (const TOp& t : grp) {
+      const uint32_t cm = cond_bits(t);
       for (int b = 0; b < k; ++b)
         if (cm & (1u << b)) ++uses[b];
     }
@@ -151,8 +173,8 @@ std::vector<TOp> plan_layouts(const TOp* ops, int nops, int k, int R) {
         if (m & (1u << pos[q])) r |= 1u << q;
       return r;
     };
-    for (size_t q = i; q < j; ++q) {
-      TOp t = in[q];
+    for (const TOp& t0 : grp) {
+      TOp t = t0;
       uint32_t m = 0, v = 0;
       if (t.kind == OK_U2) {
         t.t2 = rpos(t.t);
@@ -177,7 +199,6 @@ std::vector<TOp> plan_layouts(const TOp* ops, int nops, int k, int R) {
       t.tval = v & ~rb;
       out.push_back(t);
     }
-    i = j;
   }
   return out;
 }
@@ -188,10 +209,11 @@ struct Shape {
 };
 // Measured on the 30-qubit layered + QFT circuit: double-float keeps 8 registers
 // per thread, two tile buffers and one CTA per SM (16 registers per thread spill
-// at two CTAs and starve latency hiding at one); complex64 runs two CTAs per SM.
+// at two CTAs and starve latency hiding at one); complex64 holds 16 registers per
+// thread with two buffers and two CTAs per SM.
 Shape shape_for(int prec) {
   if (prec == QG_C128) return Shape{3, 2, 1};
-  return Shape{3, 2, 2};
+  return Shape{4, 2, 2};
 }
 
 class PassGen {
