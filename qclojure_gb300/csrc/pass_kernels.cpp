@@ -795,19 +795,39 @@ std::shared_ptr<const PassKernels> pass_kernels_for(const Program& prog, int pre
     *why = "device ordinal out of range";
     return nullptr;
   }
-  std::vector<Unit> units;
-  std::string key;
-  if (!generate_units(prog, prec, &units, &key, why)) return nullptr;
+  // cache key: the program's passes as bytes (descriptors, hand-over form, op
+  // records), which determine the generated source; generating it for every
+  // run of a cached program would cost more than a lookup
+  std::string key = std::to_string(prec) + ":" + std::to_string(prog.arith) + ":";
+  for (size_t i = 0; i < prog.steps.size(); ++i) {
+    const Step& st = prog.steps[i];
+    key += (char)st.kind;
+    if (st.kind != Step::TILE_PASS) continue;
+    const int io = tile_pass_io(prog, i);
+    key.append(reinterpret_cast<const char*>(&io), sizeof(io));
+    key.append(reinterpret_cast<const char*>(&st.pass), sizeof(PassDesc));
+    key.append(reinterpret_cast<const char*>(prog.tops.data() + st.pass.op_begin),
+               sizeof(TOp) * (size_t)(st.pass.op_end - st.pass.op_begin));
+  }
   {
     std::lock_guard<std::mutex> lk(g_mu);
     auto it = g_cache[device].find(key);
     if (it != g_cache[device].end()) {
       ++g_cache_hits;
+      if (!it->second) *why = "this program's pass kernels failed to compile before";
       return it->second;
     }
   }
+  auto remember_failure = [&]() {
+    std::lock_guard<std::mutex> lk(g_mu);
+    g_cache[device].emplace(key, nullptr);
+    return nullptr;
+  };
+  std::vector<Unit> units;
+  std::string src_key;
+  if (!generate_units(prog, prec, &units, &src_key, why)) return nullptr;
   const auto t0 = std::chrono::steady_clock::now();
-  if (!compile_units(units, why)) return nullptr;
+  if (!compile_units(units, why)) return remember_failure();
   auto c = std::make_shared<Compiled>();
   c->kernel.assign(prog.steps.size(), nullptr);
   c->smem.assign(prog.steps.size(), 0);
