@@ -384,6 +384,39 @@ def _qubits_with_spans(op: dict, n: int):
 
 
 def circuit_depth(circuit: Circuit) -> int:
+    """circuit.clj:1375-1449: an op's layer is one past the latest layer among its
+    qubits, the spans (min..max qubit ranges of multi-qubit ops) that overlap its
+    own span, and, for an op without a span, the spans covering its qubits. Two
+    spans overlap exactly when some qubit lies in both, and a span's layer only
+    grows, so the latest layer of any span covering qubit q is kept per qubit
+    (cover[q]); each op then costs O(n) instead of a scan of every span seen."""
+    ops = circuit["operations"]
+    n = circuit["num-qubits"]
+    if not ops:
+        return 0
+    qubit_layers = [0] * n
+    cover = [0] * n
+    max_layer = 0
+    for op in ops:
+        qubits, spans = _qubits_with_spans(op, n)
+        qubits = [q for q in qubits if q is not None]
+        mq = max([qubit_layers[q] for q in qubits], default=0)
+        ms = max([cover[q] for a, b in spans for q in range(max(a, 0), min(b, n - 1) + 1)], default=0)
+        mc = max([cover[q] for q in qubits if 0 <= q < n], default=0) if not spans else 0
+        new = 1 + max(mq, ms, mc)
+        for q in qubits:
+            qubit_layers[q] = new
+        for a, b in spans:
+            for q in range(max(a, 0), min(b, n - 1) + 1):
+                if cover[q] < new:
+                    cover[q] = new
+        max_layer = max(max_layer, new)
+    return max_layer
+
+
+def _circuit_depth_by_spans(circuit: Circuit) -> int:
+    """The same layering by a scan of every span seen (the reference's form); kept
+    to check circuit_depth against."""
     ops = circuit["operations"]
     n = circuit["num-qubits"]
     if not ops:

@@ -105,3 +105,16 @@ def test_qft_op_counts():
     assert all(o["operation-params"]["angle"] == math.pi / 2 ** (o["operation-params"]["control"]
                                                                 - o["operation-params"]["target"])
                for o in ops if o["operation-type"] == "rydberg-cphase")
+
+
+def test_circuit_depth_per_qubit_cover_equals_span_scan():
+    """circuit_depth keeps the latest covering-span layer per qubit; it must agree
+    with the scan over every span (the reference's form) on mixed circuits."""
+    from qclojure_gb300 import workloads
+    from qclojure_gb300.circuit import _circuit_depth_by_spans, circuit_depth
+    from test_gpu_parity import every_gate_circuit
+
+    for seed in range(12):
+        for c in (workloads.large_circuit(10, 4, seed), every_gate_circuit(8, seed),
+                  workloads.layered_circuit(6, 7, seed), workloads.qaoa_maxcut(12, 2, seed)):
+            assert circuit_depth(c) == _circuit_depth_by_spans(c)
