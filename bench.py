@@ -379,11 +379,12 @@ def main():
     mean_pass = statistics.mean(dom) if dom else float("nan")
     achieved = pass_bytes / (mean_pass / 1e3) / 1e9 if dom else float("nan")
     # DRAM bytes per tiled pass from an ncu capture of the same kernel on a 26-qubit state
-    # (dram__bytes_read.sum + dram__bytes_write.sum = 2.086e9 per launch), scaled by the
-    # amplitudes processed: profiles/k_tile2_PolDFT_c128_layered30x40_qft30.md
+    # (dram__bytes_read.sum + dram__bytes_write.sum = 2.087e9 per c128 launch, 1.012e9 per c64
+    # launch), scaled by the amplitudes processed:
+    # profiles/qgp_pass_c128_doublefloat_layered30x40_qft30.md, profiles/qgp_pass_c64_layered26x12_qft26.md
     traffic, traffic_src = None, None
-    if args.precision == "c128" and args.fusion == "tiled":
-        traffic = 2.086e9 * 2 ** (n - 26)
+    if args.fusion == "tiled":
+        traffic = (2.087e9 if args.precision == "c128" else 1.012e9) * 2 ** (n - 26)
         traffic_src = "ncu capture at 26 qubits x 2^(n-26)"
     # time of the 40 random layers alone, per layer
     st.prepare(layers_only, fusion=args.fusion)
@@ -415,7 +416,10 @@ def main():
                      + ("double-float)" if args.precision == "c128" else "complex64)")
                      if dom_kind == 3 else ("k_tile2<PolDFT>" if args.precision == "c128" else "k_tile2<PolF>"),
                      "peak_source": peak_src, "pass_bytes": pass_bytes, "mean_pass_ms": mean_pass,
-                     "passes": len(dom)},
+                     "passes": len(dom),
+                     "note": "passes are bound by instruction issue, not HBM: ncu on the same kernel "
+                             "(26 qubits) shows 66-70% issue active and 21-27% DRAM throughput for "
+                             "double-float complex128 (profiles/qgp_pass_c128_doublefloat_layered30x40_qft30.md)"},
         "gpu_launches": int(l1.value - l0.value),
         "clocks": ck,
     }
@@ -439,7 +443,17 @@ def main():
             b.record(stream64)
             b.synchronize()
             ms64 = a.elapsed_time(b) / args.steps
-            line["c64"] = {"value": gates * N / (ms64 / 1e3), "ms_per_step": ms64, "compile_ms": c64_compile_ms}
+            st64.set_basis(0)
+            p64, k64 = st64.profile(circ, fusion=args.fusion)
+            d64 = [t for t, k in zip(p64, k64) if k in (1, 3)]
+            m64 = statistics.mean(d64) if d64 else float("nan")
+            a64 = 2 * 8 * N / (m64 / 1e3) / 1e9 if d64 else float("nan")
+            line["c64"] = {"value": gates * N / (ms64 / 1e3), "ms_per_step": ms64, "compile_ms": c64_compile_ms,
+                           "hbm_passes_per_step": len(p64),
+                           "roofline": {"bound": "hbm", "achieved": a64, "peak": peak, "unit": "GB/s",
+                                        "frac": a64 / peak if d64 else None,
+                                        "traffic": 1.012e9 * 2 ** (n - 26), "mean_pass_ms": m64,
+                                        "kernel": "qgp_<pass> (specialised tiled pass, complex64)"}}
             st64.close()
         # batched parameter sweep: 1024 QAOA MaxCut circuits (p=3, n uniform over 12..24 even),
         # one launch per pass over all states of a size, replayed from CUDA graphs
