@@ -106,15 +106,40 @@ inline bool hi_lo_nonzero(const TOp& t, int q) { return t.mf[8 + q] != 0.0f; }
 // select registers at compile time. (The interpreter plans the same way with
 // R = 3 in compile.cpp; here R is a property of the kernel shape.)
 std::vector<TOp> plan_layouts(const TOp* ops, int nops, int k, int R) {
-  std::vector<TOp> in;
-  for (int i = 0; i < nops; ++i)
-    if (ops[i].kind != OK_LAYOUT) in.push_back(ops[i]);
-  std::vector<TOp> out;
   auto required = [](const TOp& t) -> uint32_t {
     if (t.kind == OK_U2) return 1u << t.t;
     if (t.kind == OK_SWAP) return (1u << t.t) | (1u << t.t2);
     return 0u;
   };
+  // Phase gates sink to the latest point they can reach: a phase commutes with
+  // every gate that does not change one of its bits, so it waits until a gate
+  // targets one of them (or the pass ends). Phases then arrive in runs, which the
+  // generator applies through shared per-mask factors (phase_run).
+  std::vector<TOp> in;
+  {
+    std::vector<TOp> pending;
+    auto flush = [&](uint32_t bits, bool all) {
+      std::vector<TOp> keep;
+      for (const TOp& p : pending) {
+        if (all || (p.lmask & bits)) in.push_back(p);
+        else keep.push_back(p);
+      }
+      pending.swap(keep);
+    };
+    for (int i = 0; i < nops; ++i) {
+      const TOp& t = ops[i];
+      if (t.kind == OK_LAYOUT) continue;
+      if (t.kind == OK_PHASE) {
+        pending.push_back(t);
+        continue;
+      }
+      const bool diagonal_other = t.kind == OK_BLOCKADE || t.kind == OK_PARITY || t.kind == OK_COLLAPSE;
+      flush(required(t), diagonal_other || t.kind == OK_DENSE);
+      in.push_back(t);
+    }
+    flush(0, true);
+  }
+  std::vector<TOp> out;
   auto cond_bits = [](const TOp& t) -> uint32_t {
     return t.kind == OK_U2 || t.kind == OK_SWAP ? t.lcmask : t.lmask;
   };
@@ -228,6 +253,7 @@ class PassGen {
     ops_ = plan_.data();
     nops_ = (int)plan_.size();
     ns_ = 1 << sh_.rbits;
+    if (ns_ > kMaxRegs) unsupported_ = true;  // the generator's per-register tables hold 16
   }
 
   // false: the pass holds an op the generator does not specialise
@@ -271,9 +297,10 @@ class PassGen {
   std::vector<TOp> plan_;
   const TOp* ops_ = nullptr;
   int nops_ = 0;
-  int ns_ = 8;  // registers (amplitudes) per thread
+  int ns_ = 8;  // registers (amplitudes) per thread: at most kMaxRegs
+  static constexpr int kMaxRegs = 16;
   // double-float: operations applied to each register since its last renormalisation
-  int since_[16] = {0};
+  int since_[kMaxRegs] = {0};
   static constexpr int kRenormEvery = 6;
 
   void touched(int j) {
@@ -521,63 +548,115 @@ class PassGen {
   // A run of phase ops (diagonal, commuting with each other) multiplies each
   // register by the product of the phases whose conditions it meets. The run
   // collects those products per register-condition mask cr first (one complex
-  // product per op, whatever the number of registers it touches), then gives
-  // each register the product of the factors whose cr it contains.
+  // product per op, whatever the number of registers it touches); exact unit
+  // phases (-1, +-i) without a runtime condition are only counted (a power of i
+  // per mask). Register j then needs H[j] = product of the factors of every mask
+  // contained in j: a subset-product transform builds all H[j] with at most
+  // R 2^(R-1) products. The run is emitted this way when that costs fewer complex
+  // products than applying each op to its registers.
   static constexpr int kPhaseRunMin = 3;
+  bool unit_phase(const TOp& t) const { return t.cls != PH_GENERAL; }
+  int unit_power(const TOp& t) const { return t.cls == PH_NEG ? 2 : t.cls == PH_I ? 1 : 3; }
+
+  // complex products of the run form; *ok = false when it would not pay
   void phase_run(int begin, int end) {
+    const int R = sh_.rbits;
+    // cost of the op-by-op form: complex products
+    int cost_ops = 0;
+    for (int i = begin; i < end; ++i) {
+      const TOp& t = ops_[i];
+      if (unit_phase(t)) continue;
+      const int cr = (int)(t.rmask & (uint32_t)(ns_ - 1));
+      cost_ops += 1 << (R - __builtin_popcount((unsigned)cr));
+    }
+    // the run form: factor updates, subset products, applications
+    bool gen[kMaxRegs] = {false};
+    int unit[kMaxRegs] = {0};
+    int cost_run = 0;
+    for (int i = begin; i < end; ++i) {
+      const TOp& t = ops_[i];
+      const int cr = (int)(t.rmask & (uint32_t)(ns_ - 1));
+      const bool runtime = t.gmask != 0 || t.tmask != 0;
+      if (unit_phase(t) && !runtime) continue;
+      if (gen[cr] && !unit_phase(t)) ++cost_run;
+      gen[cr] = true;
+    }
+    bool def[kMaxRegs];
+    for (int j = 0; j < ns_; ++j) def[j] = gen[j];
+    for (int b = 0; b < R; ++b)
+      for (int j = 0; j < ns_; ++j)
+        if ((j >> b) & 1) {
+          if (def[j] && def[j ^ (1 << b)]) ++cost_run;
+          def[j] = def[j] || def[j ^ (1 << b)];
+        }
+    for (int j = 0; j < ns_; ++j) cost_run += def[j] ? 1 : 0;
+    if (cost_run >= cost_ops) {
+      for (int i = begin; i < end; ++i) op(ops_[i]);
+      return;
+    }
     const std::string V = df_ ? "dfc" : "float2";
-    bool used[16] = {false};
-    int prods[16] = {0};
+    auto mul = [&](const std::string& f, const std::string& g) {  // f * g, both variables
+      return df_ ? "df_cmul<true, true>(" + f + ".rh, " + f + ".rl, " + f + ".ih, " + f + ".il, " + g + ")"
+                 : "f_cmul(" + f + ".x, " + f + ".y, " + g + ")";
+    };
+    auto rot = [&](int pw, const std::string& x) {  // x * i^pw
+      pw &= 3;
+      if (pw == 0) return x;
+      return std::string(pol()) + (pw == 1 ? "::mul_i(" : pw == 2 ? "::neg(" : "::mul_mi(") + x + ")";
+    };
+    bool made[kMaxRegs] = {false};
+    int prods[kMaxRegs] = {0};
     o_ << "    {  // run of " << (end - begin) << " phase ops\n";
+    const std::string one = df_ ? "dfc{1.0f, 0.0f, 0.0f, 0.0f}" : "make_float2(1.0f, 0.0f)";
     for (int i = begin; i < end; ++i) {
       const TOp& t = ops_[i];
       const int cr = (int)(t.rmask & (uint32_t)(ns_ - 1));
       const std::string c = cond(t.gmask, t.gmask, t.tmask, t.tval);
+      if (unit_phase(t) && c.empty()) {
+        unit[cr] += unit_power(t);
+        continue;
+      }
       const std::string F = "F" + std::to_string(cr);
       std::string lit;  // the phase as a value of the register type
       if (t.cls == PH_GENERAL)
         lit = df_ ? "dfc{" + h(t, 0) + ", " + l(t, 0) + ", " + h(t, 1) + ", " + l(t, 1) + "}"
                   : "make_float2(" + h(t, 0) + ", " + h(t, 1) + ")";
-      else if (t.cls == PH_NEG)
-        lit = df_ ? "dfc{-1.0f, 0.0f, 0.0f, 0.0f}" : "make_float2(-1.0f, 0.0f)";
-      else if (t.cls == PH_I)
-        lit = df_ ? "dfc{0.0f, 0.0f, 1.0f, 0.0f}" : "make_float2(0.0f, 1.0f)";
       else
-        lit = df_ ? "dfc{0.0f, 0.0f, -1.0f, 0.0f}" : "make_float2(0.0f, -1.0f)";
-      const std::string one = df_ ? "dfc{1.0f, 0.0f, 0.0f, 0.0f}" : "make_float2(1.0f, 0.0f)";
-      if (!used[cr]) {
-        used[cr] = true;
+        lit = rot(unit_power(t), one);
+      if (!made[cr]) {
+        made[cr] = true;
         o_ << "      " << V << " " << F << " = " << (c.empty() ? lit : "(" + c + ") ? " + lit + " : " + one) << ";\n";
         continue;
       }
-      std::string upd;
-      if (t.cls == PH_GENERAL) upd = cmul(t, 0, 1, F);
-      else if (t.cls == PH_NEG) upd = std::string(pol()) + "::neg(" + F + ")";
-      else if (t.cls == PH_I) upd = std::string(pol()) + "::mul_i(" + F + ")";
-      else upd = std::string(pol()) + "::mul_mi(" + F + ")";
+      const std::string upd = t.cls == PH_GENERAL ? cmul(t, 0, 1, F) : rot(unit_power(t), F);
       o_ << "      " << (c.empty() ? "" : "if (" + c + ") ") << F << " = " << upd << ";\n";
       if (df_ && t.cls == PH_GENERAL && ++prods[cr] >= kRenormEvery) {
         o_ << "      " << F << " = DF::renorm(" << F << ");\n";
         prods[cr] = 0;
       }
     }
+    // subset products H[j] = prod over masks cr contained in j of F[cr]
+    for (int j = 0; j < ns_; ++j)
+      if (made[j]) o_ << "      " << V << " H" << j << " = F" << j << ";\n";
+    bool have[kMaxRegs];
+    for (int j = 0; j < ns_; ++j) have[j] = made[j];
+    for (int b = 0; b < R; ++b)
+      for (int j = ns_ - 1; j >= 0; --j)
+        if (((j >> b) & 1) && have[j ^ (1 << b)]) {
+          const std::string lo = "H" + std::to_string(j ^ (1 << b));
+          if (have[j]) o_ << "      H" << j << " = " << mul(lo, "H" + std::to_string(j)) << ";\n";
+          else o_ << "      " << V << " H" << j << " = " << lo << ";\n";
+          have[j] = true;
+        }
     for (int j = 0; j < ns_; ++j) {
-      std::vector<int> fs;
+      int pw = 0;
       for (int cr = 0; cr < ns_; ++cr)
-        if (used[cr] && (j & cr) == cr) fs.push_back(cr);
-      if (fs.empty()) continue;
-      std::string g = "F" + std::to_string(fs[0]);
-      for (size_t q = 1; q < fs.size(); ++q) {
-        const std::string f = "F" + std::to_string(fs[q]);
-        g = df_ ? "df_cmul<true, true>(" + f + ".rh, " + f + ".rl, " + f + ".ih, " + f + ".il, " + g + ")"
-                : "f_cmul(" + f + ".x, " + f + ".y, " + g + ")";
-      }
-      o_ << "      { const " << V << " G = " << g << ";\n";
-      if (df_)
-        o_ << "        r" << j << " = df_cmul<true, true>(G.rh, G.rl, G.ih, G.il, r" << j << "); }\n";
-      else
-        o_ << "        r" << j << " = f_cmul(G.x, G.y, r" << j << "); }\n";
-      touched(j);
+        if ((j & cr) == cr) pw += unit[cr];
+      if (!have[j] && (pw & 3) == 0) continue;
+      std::string v = "r" + std::to_string(j);
+      if (have[j]) v = mul("H" + std::to_string(j), v);
+      o_ << "      r" << j << " = " << rot(pw, v) << ";\n";
+      if (have[j]) touched(j);
     }
     o_ << "    }\n";
   }
