@@ -337,7 +337,7 @@ typedef struct qg_sweep_stats {
   int32_t groups;         /* batches of equal structure                           */
   int32_t launches;       /* kernel launches per run (inside the graphs)          */
   int32_t graphs;         /* groups replayed from a CUDA graph                    */
-  int32_t reserved;
+  int32_t specialised;    /* groups whose passes run as specialised kernels       */
   uint64_t state_bytes;   /* HBM held by the sweep's states                       */
 } qg_sweep_stats;
 

@@ -243,11 +243,17 @@ Shape shape_for(int prec) {
 
 class PassGen {
  public:
-  PassGen(std::ostringstream& o, const PassDesc& pd, const TOp* ops, int nops, int prec, int io)
-      : o_(o), pd_(pd), df_(prec == QG_C128), io_(io), sh_(shape_for(prec)) {
-    for (int i = 0; i < nops; ++i)
+  // table = true: the matrix entries are read from a per-state table in shared
+  // memory (cs[16 * op + q], op numbered in the pass's own op order) instead of
+  // literals, so one kernel serves every state of a parameter sweep.
+  PassGen(std::ostringstream& o, const PassDesc& pd, const TOp* ops, int nops, int prec, int io, bool table = false)
+      : o_(o), pd_(pd), df_(prec == QG_C128), io_(io), tab_(table), sh_(shape_for(prec)) {
+    std::vector<TOp> tagged(ops, ops + nops);
+    for (int i = 0; i < nops; ++i) {
+      tagged[i].pad1 = i;  // the op's row in the coefficient table
       if (ops[i].kind == OK_DENSE) unsupported_ = true;
-    if (!unsupported_) plan_ = plan_layouts(ops, nops, pd.k, sh_.rbits);
+    }
+    if (!unsupported_) plan_ = plan_layouts(tagged.data(), nops, pd.k, sh_.rbits);
     // pairs handed over by the previous pass may carry unnormalised operations
     if (io & kTileInPairs) carry_ = kRenormEvery / 2 - 1;
     ops_ = plan_.data();
@@ -263,7 +269,8 @@ class PassGen {
     const int E = df_ ? 16 : 8;
     uint64_t lm = 0;
     for (int j = 0; j < pd_.k; ++j) lm |= 1ULL << pd_.lbits[j];
-    o_ << "namespace p" << id << " {\nstruct P {\n";
+    const std::string ns = (tab_ ? "s" : "p") + std::to_string(id);
+    o_ << "namespace " << ns << " {\nstruct P {\n";
     o_ << "  static constexpr int E = " << E << ", K_BITS = " << pd_.k << ", KLOW = " << pd_.klow
        << ", R_BITS = " << sh_.rbits << ", BUFS = " << sh_.bufs << ";\n";
     o_ << "  static constexpr qgp::u64 LM = " << hex64(lm) << ";\n";
@@ -277,14 +284,19 @@ class PassGen {
       o_ << " | (((t >> " << pd_.run_src[r] << ") & " << hex64((1ULL << pd_.run_len[r]) - 1) << ") << "
          << pd_.run_dst[r] << ")";
     o_ << ";\n  }\n";
-    o_ << "  static __device__ __forceinline__ void body(unsigned char* buf, qgp::u64 base) {\n";
-    o_ << "    using namespace qgp;\n    const unsigned tid = threadIdx.x;\n    (void)base; (void)tid;\n";
+    o_ << "  static __device__ __forceinline__ void body(unsigned char* buf, qgp::u64 base, "
+          "const float* __restrict__ cs) {\n";
+    o_ << "    using namespace qgp;\n    const unsigned tid = threadIdx.x;\n    (void)base; (void)tid; (void)cs;\n";
     body();
-    o_ << "  }\n};\n}  // namespace p" << id << "\n";
-    o_ << "extern \"C\" __global__ void __launch_bounds__(" << ((1 << pd_.k) >> sh_.rbits) << ", " << sh_.ctas
-       << ") qgp_" << id
-       << "(unsigned char* __restrict__ state, unsigned long long ntiles) {\n  qgp::run_pass<p" << id
-       << "::P>(state, ntiles);\n}\n\n";
+    o_ << "  }\n};\n}  // namespace " << ns << "\n";
+    o_ << "extern \"C\" __global__ void __launch_bounds__(" << ((1 << pd_.k) >> sh_.rbits) << ", " << sh_.ctas << ") ";
+    if (tab_)
+      o_ << "qgs_" << id << "(unsigned char* const* __restrict__ states, const float* __restrict__ coefs, int ncoef, "
+         << "unsigned long long ntiles, int nstates) {\n  qgp::run_pass_batch<" << ns
+         << "::P>(states, coefs, ncoef, ntiles, nstates);\n}\n\n";
+    else
+      o_ << "qgp_" << id << "(unsigned char* __restrict__ state, unsigned long long ntiles) {\n  qgp::run_pass<" << ns
+         << "::P>(state, ntiles);\n}\n\n";
   }
 
  private:
@@ -292,6 +304,7 @@ class PassGen {
   const PassDesc& pd_;
   bool df_;
   int io_;
+  bool tab_;
   Shape sh_;
   bool unsupported_ = false;
   std::vector<TOp> plan_;
@@ -329,9 +342,17 @@ class PassGen {
   std::string ld_raw() const { return df_ && !(io_ & kTileInPairs) ? "DF::ld_doubles" : std::string(pol()) + "::ld_work"; }
   std::string st_raw() const { return df_ && !(io_ & kTileOutPairs) ? "DF::st_doubles" : std::string(pol()) + "::st_work"; }
 
-  // coefficient q of a TOp: hi literal, lo literal (double-float) or the float (complex64)
-  std::string h(const TOp& t, int q) const { return flit(df_ ? t.mf[q] : (float)t.m[q]); }
-  std::string l(const TOp& t, int q) const { return flit(t.mf[8 + q]); }
+  // coefficient q of a TOp: hi literal, lo literal (double-float) or the float
+  // (complex64); with a table, the entries of the current state in shared memory
+  std::string h(const TOp& t, int q) const {
+    if (tab_) return "cs[" + std::to_string(16 * t.pad1 + q) + "]";
+    return flit(df_ ? t.mf[q] : (float)t.m[q]);
+  }
+  std::string l(const TOp& t, int q) const {
+    if (tab_) return "cs[" + std::to_string(16 * t.pad1 + 8 + q) + "]";
+    return flit(t.mf[8 + q]);
+  }
+  bool lo_nz(const TOp& t, int q) const { return tab_ || hi_lo_nonzero(t, q); }
   std::string b(bool v) const { return v ? "true" : "false"; }
 
   // condition on tile bits (gm, gv) and thread bits (tm, tv); empty when unconditional
@@ -347,7 +368,7 @@ class PassGen {
 
   std::string cmul(const TOp& t, int qr, int qi, const std::string& x) const {
     if (df_)
-      return "df_cmul<" + b(hi_lo_nonzero(t, qr)) + ", " + b(hi_lo_nonzero(t, qi)) + ">(" + h(t, qr) + ", " + l(t, qr) +
+      return "df_cmul<" + b(lo_nz(t, qr)) + ", " + b(lo_nz(t, qi)) + ">(" + h(t, qr) + ", " + l(t, qr) +
              ", " + h(t, qi) + ", " + l(t, qi) + ", " + x + ")";
     return "f_cmul(" + h(t, qr) + ", " + h(t, qi) + ", " + x + ")";
   }
@@ -373,13 +394,13 @@ class PassGen {
       case U2_REAL:
         if (m[0] == m[2] && m[0] == m[4] && m[6] == -m[0]) {  // [[c, c], [c, -c]]
           if (df_)
-            o_ << "      df_hadamard<" << b(hi_lo_nonzero(t, 0)) << ">(" << h(t, 0) << ", " << l(t, 0) << ", " << a
+            o_ << "      df_hadamard<" << b(lo_nz(t, 0)) << ">(" << h(t, 0) << ", " << l(t, 0) << ", " << a
                << ", " << c << ");\n";
           else
             o_ << "      f_hadamard(" << h(t, 0) << ", " << a << ", " << c << ");\n";
         } else if (df_) {
-          o_ << "      df_real<" << b(hi_lo_nonzero(t, 0)) << ", " << b(hi_lo_nonzero(t, 2)) << ", "
-             << b(hi_lo_nonzero(t, 4)) << ", " << b(hi_lo_nonzero(t, 6)) << ">(" << h(t, 0) << ", " << l(t, 0) << ", "
+          o_ << "      df_real<" << b(lo_nz(t, 0)) << ", " << b(lo_nz(t, 2)) << ", "
+             << b(lo_nz(t, 4)) << ", " << b(lo_nz(t, 6)) << ">(" << h(t, 0) << ", " << l(t, 0) << ", "
              << h(t, 2) << ", " << l(t, 2) << ", " << h(t, 4) << ", " << l(t, 4) << ", " << h(t, 6) << ", " << l(t, 6)
              << ", " << a << ", " << c << ");\n";
         } else {
@@ -389,8 +410,8 @@ class PassGen {
         break;
       case U2_RXLIKE:  // m0 = (a, 0), m1 = (0, b), m2 = (0, c), m3 = (d, 0)
         if (df_)
-          o_ << "      df_rxlike<" << b(hi_lo_nonzero(t, 0)) << ", " << b(hi_lo_nonzero(t, 3)) << ", "
-             << b(hi_lo_nonzero(t, 5)) << ", " << b(hi_lo_nonzero(t, 6)) << ">(" << h(t, 0) << ", " << l(t, 0) << ", "
+          o_ << "      df_rxlike<" << b(lo_nz(t, 0)) << ", " << b(lo_nz(t, 3)) << ", "
+             << b(lo_nz(t, 5)) << ", " << b(lo_nz(t, 6)) << ">(" << h(t, 0) << ", " << l(t, 0) << ", "
              << h(t, 3) << ", " << l(t, 3) << ", " << h(t, 5) << ", " << l(t, 5) << ", " << h(t, 6) << ", " << l(t, 6)
              << ", " << a << ", " << c << ");\n";
         else
@@ -530,7 +551,7 @@ class PassGen {
         o_ << "    {  // collapse\n      const bool tc = " << (c.empty() ? "true" : c) << ";\n";
         for (int j = 0; j < ns_; ++j) {
           if ((j & cr) == rv) {
-            const std::string sc = df_ ? "df_scale<" + b(hi_lo_nonzero(t, 0)) + ">(" + h(t, 0) + ", " + l(t, 0) + ", " +
+            const std::string sc = df_ ? "df_scale<" + b(lo_nz(t, 0)) + ">(" + h(t, 0) + ", " + l(t, 0) + ", " +
                                              r(j) + ")"
                                        : "f_scale(" + h(t, 0) + ", " + r(j) + ")";
             o_ << "      " << r(j) << " = tc ? " << sc << " : " << pol() << "::zero();\n";
@@ -782,7 +803,8 @@ const char* pass_kernels_unavailable() {
 namespace {
 
 // Generate the program's supported passes and group them into translation units.
-bool generate_units(const Program& prog, int prec, std::vector<Unit>* units, std::string* key, std::string* why) {
+bool generate_units(const Program& prog, int prec, std::vector<Unit>* units, std::string* key, std::string* why,
+                    bool table = false) {
   if (prec == QG_C128 && prog.arith != QG_ARITH_DOUBLE_FLOAT) {
     *why = "complex128 exact arithmetic runs interpreted";
     return false;
@@ -795,7 +817,7 @@ bool generate_units(const Program& prog, int prec, std::vector<Unit>* units, std
     const TOp* ops = prog.tops.data() + st.pass.op_begin;
     const int nops = (int)(st.pass.op_end - st.pass.op_begin);
     std::ostringstream o;
-    PassGen g(o, st.pass, ops, nops, prec, tile_pass_io(prog, i));
+    PassGen g(o, st.pass, ops, nops, prec, tile_pass_io(prog, i), table);
     if (!g.supported()) continue;
     g.emit((int)i);
     pieces.emplace_back((int)i, o.str());
@@ -869,15 +891,12 @@ std::string pass_kernels_source(const Program& prog, int prec) {
   return s;
 }
 
-std::shared_ptr<const PassKernels> pass_kernels_for(const Program& prog, int prec, int device, std::string* why) {
-  if (device < 0 || device >= 64) {
-    *why = "device ordinal out of range";
-    return nullptr;
-  }
-  // cache key: the program's passes as bytes (descriptors, hand-over form, op
-  // records), which determine the generated source; generating it for every
-  // run of a cached program would cost more than a lookup
-  std::string key = std::to_string(prec) + ":" + std::to_string(prog.arith) + ":";
+std::string pass_structure_key(const Program& prog, bool table) {
+  // the program's passes as bytes (descriptors, hand-over form, op records), which
+  // determine the generated source; with a coefficient table the entries' values
+  // are left out and only the value-dependent code choices are kept (the
+  // Hadamard shape of a real 2x2, the signs of an imaginary antidiagonal)
+  std::string key = std::to_string(prog.arith) + (table ? ":table:" : ":lit:");
   for (size_t i = 0; i < prog.steps.size(); ++i) {
     const Step& st = prog.steps[i];
     key += (char)st.kind;
@@ -885,9 +904,30 @@ std::shared_ptr<const PassKernels> pass_kernels_for(const Program& prog, int pre
     const int io = tile_pass_io(prog, i);
     key.append(reinterpret_cast<const char*>(&io), sizeof(io));
     key.append(reinterpret_cast<const char*>(&st.pass), sizeof(PassDesc));
-    key.append(reinterpret_cast<const char*>(prog.tops.data() + st.pass.op_begin),
-               sizeof(TOp) * (size_t)(st.pass.op_end - st.pass.op_begin));
+    for (int64_t o = st.pass.op_begin; o < st.pass.op_end; ++o) {
+      TOp t = prog.tops[o];
+      if (table) {
+        const double* m = t.m;
+        const char shape[3] = {(char)(t.cls == U2_REAL && m[0] == m[2] && m[0] == m[4] && m[6] == -m[0]),
+                               (char)(m[3] > 0), (char)(m[5] > 0)};
+        std::memset(t.m, 0, sizeof(t.m));
+        std::memset(t.mf, 0, sizeof(t.mf));
+        key.append(shape, 3);
+      }
+      key.append(reinterpret_cast<const char*>(&t), sizeof(TOp));
+    }
   }
+  return key;
+}
+
+std::shared_ptr<const PassKernels> pass_kernels_for(const Program& prog, int prec, int device, std::string* why,
+                                                    bool table) {
+  if (device < 0 || device >= 64) {
+    *why = "device ordinal out of range";
+    return nullptr;
+  }
+  // generating the source for every run of a cached program would cost more than a lookup
+  const std::string key = std::to_string(prec) + ":" + pass_structure_key(prog, table);
   {
     std::lock_guard<std::mutex> lk(g_mu);
     auto it = g_cache[device].find(key);
@@ -904,7 +944,7 @@ std::shared_ptr<const PassKernels> pass_kernels_for(const Program& prog, int pre
   };
   std::vector<Unit> units;
   std::string src_key;
-  if (!generate_units(prog, prec, &units, &src_key, why)) return nullptr;
+  if (!generate_units(prog, prec, &units, &src_key, why, table)) return nullptr;
   const auto t0 = std::chrono::steady_clock::now();
   if (!compile_units(units, why)) return remember_failure();
   auto c = std::make_shared<Compiled>();
@@ -921,14 +961,15 @@ std::shared_ptr<const PassKernels> pass_kernels_for(const Program& prog, int pre
     c->libs.push_back(lib);
     for (int s : u.steps) {
       cudaKernel_t k = nullptr;
-      const std::string name = "qgp_" + std::to_string(s);
+      const std::string name = (table ? "qgs_" : "qgp_") + std::to_string(s);
       e = cudaLibraryGetKernel(&k, lib, name.c_str());
       if (e != cudaSuccess) {
         *why = "pass kernel " + name + " missing";
         return nullptr;
       }
       const Shape sh = shape_for(prec);
-      const int smem = sh.bufs * (1 << prog.steps[s].pass.k) * E;
+      const PassDesc& pd = prog.steps[s].pass;
+      const int smem = sh.bufs * (1 << pd.k) * E + (table ? 16 * 4 * (int)(pd.op_end - pd.op_begin) : 0);
       e = cudaKernelSetAttributeForDevice(k, cudaFuncAttributeMaxDynamicSharedMemorySize, smem, device);
       if (e != cudaSuccess) {
         *why = std::string("pass kernel attribute: ") + cudaGetErrorString(e);
@@ -968,6 +1009,43 @@ cudaError_t launch_pass_kernel(const PassKernels& pk, size_t step, int n, const 
                                    dim3((unsigned)((1 << pd.k) >> sh.rbits)), args, (size_t)c.smem[step], st);
   count_launch(1);
   return e;
+}
+
+cudaError_t launch_pass_kernel_batch(const PassKernels& pk, size_t step, int n, const PassDesc& pd,
+                                     void* const* d_states, int nstates, const float* d_coefs, int prec,
+                                     cudaStream_t st) {
+  const Compiled& c = static_cast<const Compiled&>(pk);
+  if (step >= c.kernel.size() || !c.kernel[step] || nstates < 1) return cudaErrorInvalidValue;
+  const uint64_t ntiles = 1ULL << (n - pd.k);
+  const Shape sh = shape_for(prec);
+  uint64_t grid = (uint64_t)kSMCount * sh.ctas;
+  if (grid > ntiles * (uint64_t)nstates) grid = ntiles * (uint64_t)nstates;
+  unsigned long long nt = ntiles;
+  int ns = nstates;
+  int ncoef = 16 * (int)(pd.op_end - pd.op_begin);
+  void* states = const_cast<void**>(d_states);
+  const float* coefs = d_coefs;
+  void* args[5] = {&states, &coefs, &ncoef, &nt, &ns};
+  cudaError_t e = cudaLaunchKernel((const void*)c.kernel[step], dim3((unsigned)grid),
+                                   dim3((unsigned)((1 << pd.k) >> sh.rbits)), args, (size_t)c.smem[step], st);
+  count_launch(1);
+  return e;
+}
+
+// Coefficient rows of one pass for the table form: 16 floats per op, in the
+// pass's op order (double-float: hi[8], lo[8]; complex64: the 8 entries as floats).
+void pass_coefficients(const Program& prog, size_t step, int prec, float* out) {
+  const PassDesc& pd = prog.steps[step].pass;
+  for (int64_t o = pd.op_begin; o < pd.op_end; ++o) {
+    const TOp& t = prog.tops[o];
+    float* row = out + 16 * (o - pd.op_begin);
+    if (prec == QG_C128) {
+      std::memcpy(row, t.mf, sizeof(float) * 16);
+    } else {
+      for (int q = 0; q < 8; ++q) row[q] = (float)t.m[q];
+      for (int q = 8; q < 16; ++q) row[q] = 0.0f;
+    }
+  }
 }
 
 void pass_kernel_cache_stats(size_t* hits, size_t* misses) {

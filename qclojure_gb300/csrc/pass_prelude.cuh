@@ -242,8 +242,9 @@ __device__ __forceinline__ void f_rxlike(float a, float b, float c, float d, flo
 // one's arithmetic; 2: the next tile is prefetched into a second buffer), LM
 // (mask of the local bit positions), hioff(h) (HBM offset, in amplitudes, of the
 // h-th 2^KLOW-amplitude run of a tile), tile_base(t) (first amplitude of tile t)
-// and body(buf, base) (the gate run on the tile in shared memory; it ends with a
-// barrier). Each CTA walks a contiguous range of tiles.
+// and body(buf, base, cs) (the gate run on the tile in shared memory; it ends
+// with a barrier; cs holds the matrix entries when they come from a table). Each
+// CTA walks a contiguous range of tiles.
 // ---------------------------------------------------------------------------
 template <class P>
 __device__ __forceinline__ void run_pass(unsigned char* __restrict__ state, u64 ntiles) {
@@ -267,7 +268,7 @@ __device__ __forceinline__ void run_pass(unsigned char* __restrict__ state, u64 
       cp_commit();
       cp_wait<0>();
       __syncthreads();
-      P::body(smem, base);
+      P::body(smem, base, nullptr);
 #pragma unroll
       for (int i = 0; i < CPT; ++i)
         *reinterpret_cast<uint4*>(state + base * E + goff[i]) = *reinterpret_cast<const uint4*>(smem + soff[i]);
@@ -293,12 +294,73 @@ __device__ __forceinline__ void run_pass(unsigned char* __restrict__ state, u64 
       cp_wait<0>();
     }
     __syncthreads();
-    P::body(cur, base);
+    P::body(cur, base, nullptr);
 #pragma unroll
     for (int i = 0; i < CPT; ++i)
       *reinterpret_cast<uint4*>(state + base * E + goff[i]) = *reinterpret_cast<const uint4*>(cur + soff[i]);
     __syncthreads();  // this buffer is refilled two tiles later
     base = nb;
+  }
+}
+
+// The same pass over many states of one structure (a parameter sweep): work
+// items are (state, tile) pairs; a CTA walks a contiguous range of them and,
+// whenever it reaches a new state, stages that state's matrix entries (ncoef
+// floats at coefs + state * ncoef) into shared memory after the tile buffers.
+template <class P>
+__device__ __forceinline__ void run_pass_batch(unsigned char* const* __restrict__ states,
+                                               const float* __restrict__ coefs, int ncoef, u64 ntiles, int nstates) {
+  constexpr int E = P::E, K = 1 << P::K_BITS, T = K >> P::R_BITS, PER = 16 / E, CPT = (K * E / 16) / T;
+  extern __shared__ __align__(128) unsigned char smem[];
+  float* cs = reinterpret_cast<float*>(smem + P::BUFS * K * E);
+  u64 goff[CPT];
+  unsigned soff[CPT];
+#pragma unroll
+  for (int i = 0; i < CPT; ++i) {
+    const int l = ((int)threadIdx.x + i * T) * PER;
+    goff[i] = ((u64)(l & ((1 << P::KLOW) - 1)) | P::hioff(l >> P::KLOW)) * E;
+    soff[i] = (unsigned)swz<E>(l) * E;
+  }
+  const u64 W = ntiles * (u64)nstates;
+  const u64 w0 = W * blockIdx.x / gridDim.x, w1 = W * (blockIdx.x + 1) / gridDim.x;
+  for (u64 w = w0; w < w1;) {
+    const int si = (int)(w / ntiles);
+    const u64 t0 = w - (u64)si * ntiles;
+    const u64 t1 = (ntiles - t0 < w1 - w) ? ntiles : t0 + (w1 - w);
+    unsigned char* state = states[si];
+    __syncthreads();  // the previous state's readers of cs are done
+    for (int q = (int)threadIdx.x; q < ncoef; q += T) cs[q] = coefs[(u64)si * ncoef + q];
+    u64 base = P::tile_base(t0);
+#pragma unroll
+    for (int i = 0; i < CPT; ++i) cp_async16(smem + soff[i], state + base * E + goff[i]);
+    cp_commit();
+    int it = 0;
+    for (u64 t = t0; t < t1; ++t, ++it) {
+      unsigned char* cur = smem + (P::BUFS == 2 ? (it & 1) : 0) * (K * E);
+      const u64 nb = ((base | P::LM) + 1) & ~P::LM;
+      if (P::BUFS == 2 && t + 1 < t1) {
+        unsigned char* nxt = smem + ((it + 1) & 1) * (K * E);
+#pragma unroll
+        for (int i = 0; i < CPT; ++i) cp_async16(nxt + soff[i], state + nb * E + goff[i]);
+        cp_commit();
+        cp_wait<1>();
+      } else {
+        cp_wait<0>();
+      }
+      __syncthreads();
+      P::body(cur, base, cs);
+#pragma unroll
+      for (int i = 0; i < CPT; ++i)
+        *reinterpret_cast<uint4*>(state + base * E + goff[i]) = *reinterpret_cast<const uint4*>(cur + soff[i]);
+      __syncthreads();  // the buffer is refilled by a later tile
+      if (P::BUFS == 1 && t + 1 < t1) {
+#pragma unroll
+        for (int i = 0; i < CPT; ++i) cp_async16(smem + soff[i], state + nb * E + goff[i]);
+        cp_commit();
+      }
+      base = nb;
+    }
+    w += t1 - t0;
   }
 }
 

@@ -184,7 +184,18 @@ struct PassKernels {
 };
 // nullptr (with the reason in why) when the program has nothing to specialise,
 // NVRTC is missing or a compile or load failed: the caller runs it interpreted.
-std::shared_ptr<const PassKernels> pass_kernels_for(const Program& prog, int prec, int device, std::string* why);
+// table = true: one kernel per pass for every program of the same structure (a
+// sweep group); matrix entries come from per-state coefficient rows.
+std::shared_ptr<const PassKernels> pass_kernels_for(const Program& prog, int prec, int device, std::string* why,
+                                                    bool table = false);
+// Programs with equal keys share table-form kernels (coefficients left out).
+std::string pass_structure_key(const Program& prog, bool table);
+// Launch the table form over nstates states; d_coefs holds nstates rows of
+// 16 * (ops of the pass) floats (pass_coefficients of each state's program).
+cudaError_t launch_pass_kernel_batch(const PassKernels& pk, size_t step, int n, const PassDesc& pd,
+                                     void* const* d_states, int nstates, const float* d_coefs, int prec,
+                                     cudaStream_t st);
+void pass_coefficients(const Program& prog, size_t step, int prec, float* out);
 bool pass_kernel_ready(const PassKernels& pk, size_t step);
 double pass_kernels_compile_ms(const PassKernels& pk);
 cudaError_t launch_pass_kernel(const PassKernels& pk, size_t step, int n, const PassDesc& pd, void* state, int prec,

@@ -2006,6 +2006,11 @@ struct SweepGroup {
   std::vector<std::unique_ptr<State>> views;
   cudaGraphExec_t exec = nullptr;
   int launches = 0;
+  // table-form specialised kernels (one per pass, shared by the members), or null
+  std::shared_ptr<const PassKernels> pk;
+  float* d_coefs = nullptr;               // per pass: [member][16 x ops] matrix entries
+  std::vector<float> coefs_host;
+  std::vector<int64_t> coef_off;          // first float of each pass's rows
 };
 
 struct Sweep {
@@ -2058,10 +2063,61 @@ static void encode_group_kops(Sweep* sw, SweepGroup& g) {
     }
 }
 
+static void encode_group_coefs(Sweep* sw, SweepGroup& g) {
+  for (size_t p = 0; p < g.pass_steps.size(); ++p) {
+    const size_t row = 16 * (size_t)g.pass_nops[p];
+    for (size_t m = 0; m < g.members.size(); ++m)
+      pass_coefficients(g.progs[m], (size_t)g.pass_steps[p], sw->prec,
+                        g.coefs_host.data() + g.coef_off[p] + row * m);
+  }
+}
+
+// Table-form kernels for a batched group whose members share one structure:
+// compiled once (cached by structure), coefficients uploaded per member.
+static void setup_group_pass_kernels(Sweep* sw, SweepGroup& g) {
+  const Ctx* c = sw->ctx;
+  if (c->cfg.pass_kernels == QG_PASS_KERNELS_OFF) return;
+  if (sw->prec == QG_C128 && sw->arith != QG_ARITH_DOUBLE_FLOAT) return;
+  const std::string k0 = pass_structure_key(g.progs[0], true);
+  for (size_t m = 1; m < g.progs.size(); ++m)
+    if (pass_structure_key(g.progs[m], true) != k0) return;
+  std::string why;
+  auto pk = pass_kernels_for(g.progs[0], sw->prec, c->device, &why, true);
+  if (!pk) return;
+  for (int ps : g.pass_steps)
+    if (!pass_kernel_ready(*pk, (size_t)ps)) return;
+  int64_t off = 0;
+  g.coef_off.clear();
+  for (size_t p = 0; p < g.pass_steps.size(); ++p) {
+    g.coef_off.push_back(off);
+    off += 16 * (int64_t)g.pass_nops[p] * (int64_t)g.members.size();
+  }
+  g.coefs_host.assign((size_t)std::max<int64_t>(off, 1), 0.0f);
+  encode_group_coefs(sw, g);
+  if (cudaMallocAsync((void**)&g.d_coefs, sizeof(float) * g.coefs_host.size(), sw->stream) != cudaSuccess) {
+    g.d_coefs = nullptr;
+    cudaGetLastError();
+    return;
+  }
+  if (cudaMemcpyAsync(g.d_coefs, g.coefs_host.data(), sizeof(float) * g.coefs_host.size(), cudaMemcpyHostToDevice,
+                      sw->stream) != cudaSuccess) {
+    cudaFreeAsync(g.d_coefs, sw->stream);
+    g.d_coefs = nullptr;
+    return;
+  }
+  g.pk = pk;
+}
+
 static cudaError_t launch_group_passes(Sweep* sw, SweepGroup& g) {
   const size_t rec = kop_record_bytes();
   cudaError_t e = launch_batch_zero(g.slab, sw->prec, g.n, (int)g.members.size(), sw->stream);
   for (size_t p = 0; p < g.pass_steps.size() && e == cudaSuccess; ++p) {
+    if (g.pk) {
+      e = launch_pass_kernel_batch(*g.pk, (size_t)g.pass_steps[p], g.n, g.progs[0].steps[g.pass_steps[p]].pass,
+                                   g.d_states, (int)g.members.size(), g.d_coefs + g.coef_off[p], sw->prec,
+                                   sw->stream);
+      continue;
+    }
     PassDesc pd = g.progs[0].steps[g.pass_steps[p]].pass;
     pd.op_begin = 0;
     pd.op_end = g.pass_nops[p];
@@ -2083,6 +2139,7 @@ static void sweep_free(Sweep* sw) {
     if (g.slab) cudaFreeAsync(g.slab, sw->stream);
     if (g.d_states) cudaFreeAsync(g.d_states, sw->stream);
     if (g.d_kops) cudaFreeAsync(g.d_kops, sw->stream);
+    if (g.d_coefs) cudaFreeAsync(g.d_coefs, sw->stream);
   }
   if (sw->stream) {
     cudaStreamSynchronize(sw->stream);
@@ -2187,6 +2244,7 @@ int qg_sweep_create(void* ctx, const qg_circuit* circuits, int32_t count, int32_
       sweep_free(sw);
       return QG_ERR_DEVICE;
     }
+    setup_group_pass_kernels(sw, g);
     cudaStreamSynchronize(sw->stream);
     g.launches = 1 + (int)g.pass_steps.size();
     // capture the group's passes once; runs replay the graph
@@ -2226,7 +2284,8 @@ int qg_sweep_update(void* sweep, const qg_circuit* circuits, int32_t count) {
     }
     SweepGroup& g = sw->groups[sw->where[i].first];
     Program& old = g.progs[sw->where[i].second];
-    if (pass_signature(prog) != pass_signature(old)) {
+    if (pass_signature(prog) != pass_signature(old) ||
+        (g.pk && pass_structure_key(prog, true) != pass_structure_key(old, true))) {
       set_ctx_error(sw->ctx, "circuit " + std::to_string(i) + " changed its structure; create a new sweep");
       return QG_ERR_INVALID_ARG;
     }
@@ -2238,6 +2297,12 @@ int qg_sweep_update(void* sweep, const qg_circuit* circuits, int32_t count) {
     if (cudaMemcpyAsync(g.d_kops, g.kops_host.data(), g.kops_host.size(), cudaMemcpyHostToDevice, sw->stream) !=
         cudaSuccess)
       return QG_ERR_DEVICE;
+    if (g.pk) {
+      encode_group_coefs(sw, g);
+      if (cudaMemcpyAsync(g.d_coefs, g.coefs_host.data(), sizeof(float) * g.coefs_host.size(),
+                          cudaMemcpyHostToDevice, sw->stream) != cudaSuccess)
+        return QG_ERR_DEVICE;
+    }
   }
   return cudaStreamSynchronize(sw->stream) == cudaSuccess ? QG_OK : QG_ERR_DEVICE;
 }
@@ -2385,6 +2450,9 @@ int qg_sweep_run(void* sweep, const int32_t* term_offsets, const double* coeffic
     stats->groups = (int32_t)sw->groups.size();
     stats->launches = launches;
     stats->graphs = graphs;
+    int spec = 0;
+    for (auto& g : sw->groups) spec += g.pk ? 1 : 0;
+    stats->specialised = spec;
     stats->state_bytes = sw->bytes;
   }
   cudaEventDestroy(e0);

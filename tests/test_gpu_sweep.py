@@ -88,3 +88,56 @@ def test_sweep_general_hamiltonian_fallback(gpu_ctx, oracle):
         en, _ = sw.run(hams)
     for c, h, e in zip(circs, hams, en):
         assert abs(e - oracle.hamiltonian_expectation(oracle.run(c), h)) <= 1e-12
+
+
+def _same_graph_set(n, count, seed, angle_seed=None):
+    """One QAOA structure (graph) with fresh angles per circuit: the variational case."""
+    from qclojure_gb300 import workloads
+
+    base = workloads.qaoa_maxcut(n, 3, seed)
+    rng = np.random.default_rng(seed + 1 if angle_seed is None else angle_seed)
+    out = []
+    for _ in range(count):
+        g = rng.uniform(0, math.pi, 3)
+        b = rng.uniform(0, math.pi / 2, 3)
+        ops, k_rzz, k_rx = [], 0, 0
+        for op in base["operations"]:
+            t = op["operation-type"]
+            if t == "rzz":
+                layer = k_rzz // len(base["edges"])
+                op = {**op, "operation-params": {**op["operation-params"], "angle": float(2 * g[layer])}}
+                k_rzz += 1
+            elif t == "rx":
+                layer = k_rx // n
+                op = {**op, "operation-params": {**op["operation-params"], "angle": float(2 * b[layer])}}
+                k_rx += 1
+            ops.append(op)
+        out.append({**base, "operations": ops})
+    return out
+
+
+@pytest.mark.parametrize("precision,tol", [("c128", 1e-10), ("c64", 1e-4)])
+def test_same_structure_sweep_specialised(gpu_ctx, oracle, precision, tol):
+    """Members of one structure share table-form specialised kernels (matrix entries
+    per state in shared memory); energies and states match the oracle."""
+    from qclojure_gb300.sweep import Sweep
+
+    circs = _same_graph_set(14, 5, seed=21) + _same_graph_set(16, 4, seed=22)
+    with Sweep(gpu_ctx, circs, precision=precision, arithmetic="double-float") as sw:
+        en, st = sw.run([c["hamiltonian"] for c in circs])
+        assert st["specialised"] == 2, st
+        for c, e in zip(circs, en):
+            ref = _energy(oracle, c)
+            assert abs(e - ref) <= tol * max(1.0, abs(ref)), (e, ref)
+        if precision == "c128":
+            for k in (0, 6):
+                assert np.max(np.abs(sw.state(k) - oracle.run(circs[k]))) <= 1e-12
+        # new angles through update: the kernels stay, the coefficient rows change
+        new = _same_graph_set(14, 5, seed=21, angle_seed=77) + _same_graph_set(16, 4, seed=22, angle_seed=78)
+        sw.update(new)
+        en2, st2 = sw.run([c["hamiltonian"] for c in new])
+        assert st2["specialised"] == 2
+        for c, e in zip(new, en2):
+            ref = _energy(oracle, c)
+            assert abs(e - ref) <= tol * max(1.0, abs(ref)), (e, ref)
+        assert np.max(np.abs(en - en2)) > 1e-6
