@@ -24,6 +24,7 @@
 
 #include <algorithm>
 #include <chrono>
+#include <complex>
 #include <cstdio>
 #include <cstring>
 #include <memory>
@@ -105,12 +106,17 @@ inline bool hi_lo_nonzero(const TOp& t, int q) { return t.mf[8 + q] != 0.0f; }
 // go to the local bits the group's conditions use most, so those conditions
 // select registers at compile time. (The interpreter plans the same way with
 // R = 3 in compile.cpp; here R is a property of the kernel shape.)
-std::vector<TOp> plan_layouts(const TOp* ops, int nops, int k, int R) {
+// table = true (kernels shared by the states of a sweep group): parity and
+// blockade masks are data (they differ between members, for instance between
+// QAOA graphs), so the layout must not depend on them: ops keep their order
+// (no sinking, no look-ahead) and the free register bits ignore those masks.
+std::vector<TOp> plan_layouts(const TOp* ops, int nops, int k, int R, bool table = false) {
   auto required = [](const TOp& t) -> uint32_t {
     if (t.kind == OK_U2) return 1u << t.t;
     if (t.kind == OK_SWAP) return (1u << t.t) | (1u << t.t2);
     return 0u;
   };
+  auto data_mask = [&](const TOp& t) { return table && (t.kind == OK_PARITY || t.kind == OK_BLOCKADE); };
   // Phase gates sink to the latest point they can reach: a phase commutes with
   // every gate that does not change one of its bits, so it waits until a gate
   // targets one of them (or the pass ends). Phases then arrive in runs, which the
@@ -129,7 +135,7 @@ std::vector<TOp> plan_layouts(const TOp* ops, int nops, int k, int R) {
     for (int i = 0; i < nops; ++i) {
       const TOp& t = ops[i];
       if (t.kind == OK_LAYOUT) continue;
-      if (t.kind == OK_PHASE) {
+      if (t.kind == OK_PHASE && !table) {
         pending.push_back(t);
         continue;
       }
@@ -140,7 +146,8 @@ std::vector<TOp> plan_layouts(const TOp* ops, int nops, int k, int R) {
     flush(0, true);
   }
   std::vector<TOp> out;
-  auto cond_bits = [](const TOp& t) -> uint32_t {
+  auto cond_bits = [&](const TOp& t) -> uint32_t {
+    if (data_mask(t)) return 0u;
     return t.kind == OK_U2 || t.kind == OK_SWAP ? t.lcmask : t.lmask;
   };
   // Groups are formed with look-ahead: an op joins the current layout when its
@@ -162,6 +169,7 @@ std::vector<TOp> plan_layouts(const TOp* ops, int nops, int k, int R) {
         grp.push_back(in[j]);
         taken[j] = 1;
       } else {
+        if (table) break;
         changed |= req;
         seen |= tb;
       }
@@ -228,6 +236,32 @@ std::vector<TOp> plan_layouts(const TOp* ops, int nops, int k, int R) {
   return out;
 }
 
+// Runs of at least two consecutive parity ops (RZZ) with equal phase pairs: their
+// combined phase depends only on how many of them see odd parity, m, so each
+// register takes one entry of a table of p0^(E-m) p1^m instead of E products.
+bool same_parity_phases(const TOp& a, const TOp& b) {
+  return a.kind == OK_PARITY && b.kind == OK_PARITY && a.m[0] == b.m[0] && a.m[1] == b.m[1] && a.m[2] == b.m[2] &&
+         a.m[3] == b.m[3];
+}
+// [begin, end) of the parity run starting at ops[i], or end = i + 1 when none
+int parity_run_end(const TOp* ops, int nops, int i) {
+  int j = i + 1;
+  while (j < nops && same_parity_phases(ops[i], ops[j])) ++j;
+  return j;
+}
+// p0^(E-m) p1^m for m = 0..E, in FP64
+std::vector<std::complex<double>> parity_table(const TOp& t, int E) {
+  const std::complex<double> p0(t.m[0], t.m[1]), p1(t.m[2], t.m[3]);
+  std::vector<std::complex<double>> tab(E + 1);
+  for (int m = 0; m <= E; ++m) {
+    std::complex<double> v(1.0, 0.0);
+    for (int q = 0; q < E - m; ++q) v *= p0;
+    for (int q = 0; q < m; ++q) v *= p1;
+    tab[m] = v;
+  }
+  return tab;
+}
+
 // Kernel shape: register bits per thread, tile buffers, CTAs per SM.
 struct Shape {
   int rbits, bufs, ctas;
@@ -247,13 +281,14 @@ class PassGen {
   // memory (cs[16 * op + q], op numbered in the pass's own op order) instead of
   // literals, so one kernel serves every state of a parameter sweep.
   PassGen(std::ostringstream& o, const PassDesc& pd, const TOp* ops, int nops, int prec, int io, bool table = false)
-      : o_(o), pd_(pd), df_(prec == QG_C128), io_(io), tab_(table), sh_(shape_for(prec)) {
+      : out_(o), pd_(pd), df_(prec == QG_C128), io_(io), tab_(table), sh_(shape_for(prec)) {
     std::vector<TOp> tagged(ops, ops + nops);
     for (int i = 0; i < nops; ++i) {
       tagged[i].pad1 = i;  // the op's row in the coefficient table
       if (ops[i].kind == OK_DENSE) unsupported_ = true;
+      if (table && (ops[i].kind == OK_BLOCKADE || ops[i].kind == OK_COLLAPSE)) unsupported_ = true;
     }
-    if (!unsupported_) plan_ = plan_layouts(tagged.data(), nops, pd.k, sh_.rbits);
+    if (!unsupported_) plan_ = plan_layouts(tagged.data(), nops, pd.k, sh_.rbits, table);
     // pairs handed over by the previous pass may carry unnormalised operations
     if (io & kTileInPairs) carry_ = kRenormEvery / 2 - 1;
     ops_ = plan_.data();
@@ -270,37 +305,40 @@ class PassGen {
     uint64_t lm = 0;
     for (int j = 0; j < pd_.k; ++j) lm |= 1ULL << pd_.lbits[j];
     const std::string ns = (tab_ ? "s" : "p") + std::to_string(id);
-    o_ << "namespace " << ns << " {\nstruct P {\n";
-    o_ << "  static constexpr int E = " << E << ", K_BITS = " << pd_.k << ", KLOW = " << pd_.klow
-       << ", R_BITS = " << sh_.rbits << ", BUFS = " << sh_.bufs << ";\n";
-    o_ << "  static constexpr qgp::u64 LM = " << hex64(lm) << ";\n";
+    body();  // into o_; tables it needs go to pre_
+    out_ << "namespace " << ns << " {\n" << pre_.str() << "struct P {\n";
+    out_ << "  static constexpr int E = " << E << ", K_BITS = " << pd_.k << ", KLOW = " << pd_.klow
+         << ", R_BITS = " << sh_.rbits << ", BUFS = " << sh_.bufs << ";\n";
+    out_ << "  static constexpr qgp::u64 LM = " << hex64(lm) << ";\n";
     // run offsets: bit j - klow of the run index h deposits at lbits[j]
-    o_ << "  static __device__ __forceinline__ qgp::u64 hioff(int h) {\n    qgp::u64 o = 0;\n";
+    out_ << "  static __device__ __forceinline__ qgp::u64 hioff(int h) {\n    qgp::u64 o = 0;\n";
     for (int j = pd_.klow; j < pd_.k; ++j)
-      o_ << "    o |= (qgp::u64)((h >> " << (j - pd_.klow) << ") & 1) << " << pd_.lbits[j] << ";\n";
-    o_ << "    return o;\n  }\n";
-    o_ << "  static __device__ __forceinline__ qgp::u64 tile_base(qgp::u64 t) {\n    return 0";
+      out_ << "    o |= (qgp::u64)((h >> " << (j - pd_.klow) << ") & 1) << " << pd_.lbits[j] << ";\n";
+    out_ << "    return o;\n  }\n";
+    out_ << "  static __device__ __forceinline__ qgp::u64 tile_base(qgp::u64 t) {\n    return 0";
     for (int r = 0; r < pd_.nruns; ++r)
-      o_ << " | (((t >> " << pd_.run_src[r] << ") & " << hex64((1ULL << pd_.run_len[r]) - 1) << ") << "
-         << pd_.run_dst[r] << ")";
-    o_ << ";\n  }\n";
-    o_ << "  static __device__ __forceinline__ void body(unsigned char* buf, qgp::u64 base, "
-          "const float* __restrict__ cs) {\n";
-    o_ << "    using namespace qgp;\n    const unsigned tid = threadIdx.x;\n    (void)base; (void)tid; (void)cs;\n";
-    body();
-    o_ << "  }\n};\n}  // namespace " << ns << "\n";
-    o_ << "extern \"C\" __global__ void __launch_bounds__(" << ((1 << pd_.k) >> sh_.rbits) << ", " << sh_.ctas << ") ";
+      out_ << " | (((t >> " << pd_.run_src[r] << ") & " << hex64((1ULL << pd_.run_len[r]) - 1) << ") << "
+           << pd_.run_dst[r] << ")";
+    out_ << ";\n  }\n";
+    out_ << "  static __device__ __forceinline__ void body(unsigned char* buf, qgp::u64 base, "
+            "const float* __restrict__ cs) {\n";
+    out_ << "    using namespace qgp;\n    const unsigned tid = threadIdx.x;\n    (void)base; (void)tid; (void)cs;\n";
+    out_ << o_.str();
+    out_ << "  }\n};\n}  // namespace " << ns << "\n";
+    out_ << "extern \"C\" __global__ void __launch_bounds__(" << ((1 << pd_.k) >> sh_.rbits) << ", " << sh_.ctas
+         << ") ";
     if (tab_)
-      o_ << "qgs_" << id << "(unsigned char* const* __restrict__ states, const float* __restrict__ coefs, int ncoef, "
-         << "unsigned long long ntiles, int nstates) {\n  qgp::run_pass_batch<" << ns
-         << "::P>(states, coefs, ncoef, ntiles, nstates);\n}\n\n";
+      out_ << "qgs_" << id << "(unsigned char* const* __restrict__ states, const float* __restrict__ coefs, int ncoef, "
+           << "unsigned long long ntiles, int nstates) {\n  qgp::run_pass_batch<" << ns
+           << "::P>(states, coefs, ncoef, ntiles, nstates);\n}\n\n";
     else
-      o_ << "qgp_" << id << "(unsigned char* __restrict__ state, unsigned long long ntiles) {\n  qgp::run_pass<" << ns
-         << "::P>(state, ntiles);\n}\n\n";
+      out_ << "qgp_" << id << "(unsigned char* __restrict__ state, unsigned long long ntiles) {\n  qgp::run_pass<" << ns
+           << "::P>(state, ntiles);\n}\n\n";
   }
 
  private:
-  std::ostringstream& o_;
+  std::ostringstream& out_;
+  std::ostringstream o_;  // the body, generated first
   const PassDesc& pd_;
   bool df_;
   int io_;
@@ -682,6 +720,82 @@ class PassGen {
     o_ << "    }\n";
   }
 
+  // A run of E parity ops with one phase pair (p0 on even, p1 on odd parity):
+  // register j counts the ops that see odd parity, m_j, and is multiplied by
+  // p0^(E-m_j) p1^m_j from a table. With literal masks the register parities are
+  // resolved at generation time; with a coefficient table (sweep groups) the
+  // masks come from the op's row (tile bits in floats 12-13, thread bits in 14,
+  // register bits in 15, as raw bits) and the table's entries from the run's rows
+  // (entry m < E in floats 0-3 of row first + m, entry E in floats 4-7 of row first).
+  std::ostringstream pre_;  // namespace-scope declarations (literal phase tables)
+  int ntables_ = 0;
+  void parity_run(int begin, int end) {
+    const int E = end - begin;
+    o_ << "    {  // parity run of " << E << " ops\n      int";
+    for (int j = 0; j < ns_; ++j) o_ << (j ? ", m" : " m") << j << " = 0";
+    o_ << ";\n";
+    for (int e = begin; e < end; ++e) {
+      const TOp& t = ops_[e];
+      if (tab_) {
+        const int row = 16 * t.pad1;
+        o_ << "      { const qgp::u64 G = (qgp::u64)__float_as_uint(cs[" << row + 12
+           << "]) | ((qgp::u64)__float_as_uint(cs[" << row + 13 << "]) << 32);\n";
+        o_ << "        const unsigned T = __float_as_uint(cs[" << row + 14 << "]), R = __float_as_uint(cs[" << row + 15
+           << "]);\n";
+        o_ << "        const int o = (__popcll(base & G) + __popc(lt & T)) & 1;\n";
+        for (int j = 0; j < ns_; ++j) o_ << "        m" << j << " += o ^ (__popc(" << j << "u & R) & 1);\n";
+        o_ << "      }\n";
+        continue;
+      }
+      std::string oe;
+      if (t.gmask) oe += "__popcll(base & " + hex64(t.gmask) + ")";
+      if (t.tmask) oe += std::string(oe.empty() ? "" : " + ") + "__popc(lt & " + hex32(t.tmask) + ")";
+      const uint32_t R = t.rmask & (uint32_t)(ns_ - 1);
+      if (oe.empty()) {
+        for (int j = 0; j < ns_; ++j)
+          if (__builtin_popcount((unsigned)j & R) & 1) o_ << "      m" << j << " += 1;\n";
+        continue;
+      }
+      o_ << "      { const int o = (" << oe << ") & 1;\n";
+      for (int j = 0; j < ns_; ++j)
+        o_ << "        m" << j << " += " << ((__builtin_popcount((unsigned)j & R) & 1) ? "1 - o" : "o") << ";\n";
+      o_ << "      }\n";
+    }
+    std::string tab;
+    if (!tab_) {
+      tab = "PT" + std::to_string(ntables_++);
+      const auto ent = parity_table(ops_[begin], E);
+      pre_ << "static __device__ const " << (df_ ? "float4 " : "float2 ") << tab << "[" << (E + 1) << "] = {";
+      for (int m = 0; m <= E; ++m) {
+        const double re = ent[m].real(), im = ent[m].imag();
+        const float rh = (float)re, ih = (float)im;
+        if (df_)
+          pre_ << (m ? ", " : "") << "{" << flit(rh) << ", " << flit((float)(re - (double)rh)) << ", " << flit(ih)
+               << ", " << flit((float)(im - (double)ih)) << "}";
+        else
+          pre_ << (m ? ", " : "") << "{" << flit(rh) << ", " << flit(ih) << "}";
+      }
+      pre_ << "};\n";
+    }
+    const int first = 16 * ops_[begin].pad1;
+    for (int j = 0; j < ns_; ++j) {
+      if (tab_) {
+        o_ << "      { const int a = (m" << j << " < " << E << ") ? " << first << " + 16 * m" << j << " : " << first + 4
+           << ";\n";
+        if (df_) o_ << "        r" << j << " = df_cmul<true, true>(cs[a], cs[a + 1], cs[a + 2], cs[a + 3], r" << j << "); }\n";
+        else o_ << "        r" << j << " = f_cmul(cs[a], cs[a + 1], r" << j << "); }\n";
+      } else {
+        if (df_)
+          o_ << "      { const float4 v = " << tab << "[m" << j << "]; r" << j << " = df_cmul<true, true>(v.x, v.y, v.z, v.w, r"
+             << j << "); }\n";
+        else
+          o_ << "      { const float2 v = " << tab << "[m" << j << "]; r" << j << " = f_cmul(v.x, v.y, r" << j << "); }\n";
+      }
+      touched(j);
+    }
+    o_ << "    }\n";
+  }
+
   void body() {
     const std::string V = df_ ? "dfc" : "float2";
     const int E = df_ ? 16 : 8;
@@ -718,6 +832,14 @@ class PassGen {
         for (int j = 0; j < ns_; ++j) since_[j] = carry_;
         in_regs = true;
         continue;
+      }
+      if (t.kind == OK_PARITY) {
+        const int j = parity_run_end(ops_, nops_, i);
+        if (tab_ || j - i >= 2) {
+          parity_run(i, j);
+          i = j - 1;
+          continue;
+        }
       }
       if (t.kind == OK_PHASE) {
         int j = i;
@@ -904,15 +1026,26 @@ std::string pass_structure_key(const Program& prog, bool table) {
     const int io = tile_pass_io(prog, i);
     key.append(reinterpret_cast<const char*>(&io), sizeof(io));
     key.append(reinterpret_cast<const char*>(&st.pass), sizeof(PassDesc));
+    const TOp* prev = nullptr;
     for (int64_t o = st.pass.op_begin; o < st.pass.op_end; ++o) {
       TOp t = prog.tops[o];
       if (table) {
+        // the generator re-plans layouts, so the interpreter's layout records and
+        // layout-relative fields do not matter; parity masks are data
+        if (t.kind == OK_LAYOUT) continue;
         const double* m = t.m;
-        const char shape[3] = {(char)(t.cls == U2_REAL && m[0] == m[2] && m[0] == m[4] && m[6] == -m[0]),
-                               (char)(m[3] > 0), (char)(m[5] > 0)};
+        const char shape[4] = {(char)(t.cls == U2_REAL && m[0] == m[2] && m[0] == m[4] && m[6] == -m[0]),
+                               (char)(m[3] > 0), (char)(m[5] > 0),
+                               (char)(prev && same_parity_phases(*prev, prog.tops[o]))};
+        prev = &prog.tops[o];
         std::memset(t.m, 0, sizeof(t.m));
         std::memset(t.mf, 0, sizeof(t.mf));
-        key.append(shape, 3);
+        t.t2 = t.kind == OK_U2 ? 0 : t.t2;
+        t.rmask = t.rval = t.tmask = t.tval = 0;
+        std::memset(t.dbits, 0, sizeof(t.dbits));
+        std::memset(t.lj, 0, sizeof(t.lj));
+        if (t.kind == OK_PARITY) t.lmask = t.lval = 0, t.gmask = t.gval = 0;
+        key.append(shape, 4);
       }
       key.append(reinterpret_cast<const char*>(&t), sizeof(TOp));
     }
@@ -1033,18 +1166,61 @@ cudaError_t launch_pass_kernel_batch(const PassKernels& pk, size_t step, int n, 
 }
 
 // Coefficient rows of one pass for the table form: 16 floats per op, in the
-// pass's op order (double-float: hi[8], lo[8]; complex64: the 8 entries as floats).
+// pass's op order (double-float: hi[8], lo[8]; complex64: the 8 entries as
+// floats). Parity ops instead hold their masks under the kernel's layout (tile
+// bits in floats 12-13, thread bits in 14, register bits in 15, as raw bits) and,
+// per run, the table of combined phases (entry m < E in floats 0-3 of the run's
+// row m, entry E in floats 4-7 of its first row; complex64: 2 floats each).
 void pass_coefficients(const Program& prog, size_t step, int prec, float* out) {
   const PassDesc& pd = prog.steps[step].pass;
-  for (int64_t o = pd.op_begin; o < pd.op_end; ++o) {
-    const TOp& t = prog.tops[o];
-    float* row = out + 16 * (o - pd.op_begin);
+  const int nops = (int)(pd.op_end - pd.op_begin);
+  const TOp* ops = prog.tops.data() + pd.op_begin;
+  bool parity = false;
+  for (int i = 0; i < nops; ++i) {
+    const TOp& t = ops[i];
+    float* row = out + 16 * i;
+    parity = parity || t.kind == OK_PARITY;
     if (prec == QG_C128) {
       std::memcpy(row, t.mf, sizeof(float) * 16);
     } else {
       for (int q = 0; q < 8; ++q) row[q] = (float)t.m[q];
       for (int q = 8; q < 16; ++q) row[q] = 0.0f;
     }
+  }
+  if (!parity) return;
+  std::vector<TOp> tagged(ops, ops + nops);
+  for (int i = 0; i < nops; ++i) tagged[i].pad1 = i;
+  const std::vector<TOp> plan = plan_layouts(tagged.data(), nops, pd.k, shape_for(prec).rbits, true);
+  auto put = [&](float* at, std::complex<double> v) {
+    if (prec == QG_C128) {
+      const float rh = (float)v.real(), ih = (float)v.imag();
+      at[0] = rh;
+      at[1] = (float)(v.real() - (double)rh);
+      at[2] = ih;
+      at[3] = (float)(v.imag() - (double)ih);
+    } else {
+      at[0] = (float)v.real();
+      at[1] = (float)v.imag();
+      at[2] = at[3] = 0.0f;
+    }
+  };
+  for (size_t i = 0; i < plan.size(); ++i) {
+    if (plan[i].kind != OK_PARITY) continue;
+    const int end = parity_run_end(plan.data(), (int)plan.size(), (int)i);
+    const int E = end - (int)i;
+    const auto tab = parity_table(plan[i], E);
+    for (int e = 0; e < E; ++e) {
+      const TOp& t = plan[i + e];
+      float* row = out + 16 * t.pad1;
+      const uint32_t g0 = (uint32_t)t.gmask, g1 = (uint32_t)(t.gmask >> 32), tm = t.tmask, rm = t.rmask;
+      std::memcpy(row + 12, &g0, 4);
+      std::memcpy(row + 13, &g1, 4);
+      std::memcpy(row + 14, &tm, 4);
+      std::memcpy(row + 15, &rm, 4);
+      put(row, tab[e]);
+    }
+    put(out + 16 * plan[i].pad1 + 4, tab[E]);
+    i = (size_t)end - 1;
   }
 }
 

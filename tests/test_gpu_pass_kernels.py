@@ -119,6 +119,21 @@ def test_every_gate_c64_specialised(ctx_df, oracle):
         assert np.max(np.abs(st.download() - ref)) <= 2e-5
 
 
+@pytest.mark.parametrize("precision,tol", [("c128", 1e-12), ("c64", 2e-5)])
+def test_qaoa_parity_runs_specialised(ctx_df, oracle, precision, tol):
+    """QAOA MaxCut: each cost layer's RZZ gates (one angle) run as a parity-count
+    table per register instead of one complex product per gate."""
+    from qclojure_gb300 import workloads
+
+    for n, seed in ((14, 3), (18, 4)):
+        c = workloads.qaoa_maxcut(n, 3, seed)
+        ref = oracle.run(c)
+        st, kinds = _run(ctx_df, c, precision)
+        with st:
+            assert np.count_nonzero(kinds == 3) > 0
+            assert np.max(np.abs(st.download() - ref)) <= tol
+
+
 def test_specialised_matches_interpreted(ctx_df, ctx_off):
     """The same program through both executors: equal within the double-float bound."""
     from qclojure_gb300 import workloads

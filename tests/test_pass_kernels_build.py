@@ -53,3 +53,13 @@ def test_exact_arithmetic_is_not_specialised(lib):
 
     rc, kernels, _ = _build(lib, workloads.layered_circuit(12, 3, seed=1), 0, 0)
     assert rc == 0 and kernels == 0
+
+
+@pytest.mark.parametrize("precision,arithmetic", [(0, 1), (1, 0)], ids=["c128-double-float", "c64"])
+def test_qaoa_parity_runs_compile(lib, precision, arithmetic):
+    """QAOA cost layers: runs of RZZ with one angle become parity-count tables."""
+    from qclojure_gb300 import workloads
+
+    rc, kernels, err = _build(lib, workloads.qaoa_maxcut(16, 3, seed=4), precision, arithmetic)
+    assert rc == 0, err
+    assert kernels > 0
