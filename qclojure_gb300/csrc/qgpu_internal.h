@@ -210,11 +210,13 @@ void pass_kernel_cache_stats(size_t* hits, size_t* misses);
 // batched sweep kernels (sweep.cu)
 int diag_max_groups();
 size_t diag_state_bytes();
-void fill_diag_state(void* out, uint64_t zoff, int ngroups, const int* gcount);
+void fill_diag_state(void* out, uint64_t zoff, int ngroups, const int* gcount, const int* nid);
 cudaError_t launch_batch_zero(void* slab, int precision, int n, int nstates, cudaStream_t st);
+int diag_max_terms_per_group();
+uint32_t diag_qmask(uint64_t z);  // bit q: parity of q & bits 8..11 of z
 cudaError_t launch_diag_expect(void* const* d_states, int precision, int n, const void* d_diag, const uint64_t* d_z,
-                               int nstates, double* d_partial, const double* d_gcoef, double* d_energies,
-                               cudaStream_t st);
+                               const uint32_t* d_qm, int nstates, double* d_partial, const double* d_gcoef,
+                               double* d_energies, cudaStream_t st);
 void encode_kops(int precision, int arithmetic, const TOp* tops, int64_t count, void* out);
 void count_launch(int k);
 cudaError_t launch_c128_to_c64(const double* src, float* dst, uint64_t count, cudaStream_t st);

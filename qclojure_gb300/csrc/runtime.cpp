@@ -2011,6 +2011,14 @@ struct SweepGroup {
   float* d_coefs = nullptr;               // per pass: [member][16 x ops] matrix entries
   std::vector<float> coefs_host;
   std::vector<int64_t> coef_off;          // first float of each pass's rows
+  // energy tables of the diagonal path (kept between runs with equal terms)
+  bool diag = false;
+  void* d_diag = nullptr;
+  uint64_t* d_z = nullptr;                // nz z-masks, then nz 16-bit q-patterns (uint32)
+  size_t nz = 0;
+  double* d_gcoef = nullptr;
+  double* d_epart = nullptr;
+  double* d_en = nullptr;
 };
 
 struct Sweep {
@@ -2021,6 +2029,11 @@ struct Sweep {
   std::vector<SweepGroup> groups;
   std::vector<std::pair<int, int>> where;  // circuit -> (group, member)
   uint64_t bytes = 0;
+  // the term arrays the energy tables were built from
+  bool e_valid = false;
+  std::vector<int32_t> e_offsets;
+  std::vector<double> e_coefs;
+  std::string e_strings;
 };
 
 static std::vector<int64_t> pass_signature(const Program& p) {
@@ -2140,12 +2153,155 @@ static void sweep_free(Sweep* sw) {
     if (g.d_states) cudaFreeAsync(g.d_states, sw->stream);
     if (g.d_kops) cudaFreeAsync(g.d_kops, sw->stream);
     if (g.d_coefs) cudaFreeAsync(g.d_coefs, sw->stream);
+    for (void* p : {(void*)g.d_diag, (void*)g.d_z, (void*)g.d_gcoef, (void*)g.d_epart, (void*)g.d_en})
+      if (p) cudaFreeAsync(p, sw->stream);
   }
   if (sw->stream) {
     cudaStreamSynchronize(sw->stream);
     cudaStreamDestroy(sw->stream);
   }
   delete sw;
+}
+
+// Energies of every member: per group, the diagonal path (I/Z strings with at
+// most diag_max_groups() distinct coefficients, 12 qubits and more) runs one
+// k_diag_expect + k_diag_reduce over all members; other groups evaluate each
+// Pauli term on each member. The diagonal path's device tables (z masks, group
+// counts, coefficients) are kept between runs and rebuilt only when the term
+// arrays differ from the previous run's, and all groups share one sync.
+static int sweep_energies(Sweep* sw, const int32_t* term_offsets, const double* coefficients,
+                          const char* pauli_strings, double* energies, int* launches, std::string* err) {
+  const int count = sw->count;
+  std::vector<int64_t> char_off(count + 1, 0);
+  for (int i = 0; i < count; ++i) {
+    const int n = sw->groups[sw->where[i].first].n;
+    char_off[i + 1] = char_off[i] + (int64_t)(term_offsets[i + 1] - term_offsets[i]) * n;
+  }
+  const int64_t nterms = term_offsets[count];
+  const bool same = sw->e_valid && sw->e_offsets.size() == (size_t)count + 1 &&
+                    std::memcmp(sw->e_offsets.data(), term_offsets, sizeof(int32_t) * (count + 1)) == 0 &&
+                    std::memcmp(sw->e_coefs.data(), coefficients, sizeof(double) * (size_t)nterms) == 0 &&
+                    sw->e_strings.compare(0, std::string::npos, pauli_strings, (size_t)char_off[count]) == 0;
+  const int G = diag_max_groups();
+  if (!same) {
+    sw->e_valid = false;
+    for (auto& g : sw->groups) {
+      for (void* p : {(void*)g.d_diag, (void*)g.d_z, (void*)g.d_gcoef, (void*)g.d_epart, (void*)g.d_en})
+        if (p) cudaFreeAsync(p, sw->stream);
+      g.d_diag = nullptr, g.d_z = nullptr, g.d_gcoef = nullptr, g.d_epart = nullptr, g.d_en = nullptr;
+      const size_t S = g.members.size();
+      // diagonal path: every member's terms are I/Z strings with at most G distinct coefficients
+      bool diag = g.n >= 12;
+      std::vector<unsigned char> dstate(diag_state_bytes() * S);
+      std::vector<uint64_t> zs;
+      std::vector<double> gcoef(S * G, 0.0);
+      for (size_t m = 0; m < S && diag; ++m) {
+        const int ci = g.members[m];
+        std::vector<double> vals;
+        std::vector<std::vector<uint64_t>> per(G);
+        std::vector<int> nid(G, 0);
+        for (int t = term_offsets[ci]; t < term_offsets[ci + 1] && diag; ++t) {
+          const char* ps = pauli_strings + char_off[ci] + (int64_t)(t - term_offsets[ci]) * g.n;
+          uint64_t z = 0;
+          for (int q = 0; q < g.n; ++q) {
+            if (ps[q] == 'Z') z |= 1ULL << (g.n - 1 - q);
+            else if (ps[q] != 'I') diag = false;
+          }
+          int gi = -1;
+          for (size_t k = 0; k < vals.size(); ++k)
+            if (vals[k] == coefficients[t]) gi = (int)k;
+          if (gi < 0) {
+            if ((int)vals.size() == G) {
+              diag = false;
+              break;
+            }
+            gi = (int)vals.size();
+            vals.push_back(coefficients[t]);
+          }
+          if (z) per[gi].push_back(z);
+          else ++nid[gi];
+        }
+        if (!diag) break;
+        int gcount[8] = {0};
+        const uint64_t zoff = zs.size();
+        for (int k = 0; k < (int)vals.size(); ++k) {
+          gcount[k] = (int)per[k].size();
+          if (gcount[k] > diag_max_terms_per_group()) diag = false;
+          zs.insert(zs.end(), per[k].begin(), per[k].end());
+          gcoef[m * G + k] = vals[k];
+        }
+        if (!diag) break;
+        fill_diag_state(dstate.data() + diag_state_bytes() * m, zoff, (int)vals.size(), gcount, nid.data());
+      }
+      g.diag = diag;
+      if (!diag) continue;
+      const uint64_t chunks = 1ULL << (g.n - 12);
+      std::vector<uint32_t> qm(zs.size());
+      for (size_t q = 0; q < zs.size(); ++q) qm[q] = diag_qmask(zs[q]);
+      cudaError_t e = cudaMallocAsync(&g.d_diag, dstate.size(), sw->stream);
+      if (e == cudaSuccess)
+        e = cudaMallocAsync((void**)&g.d_z, (sizeof(uint64_t) + sizeof(uint32_t)) * std::max<size_t>(zs.size(), 1),
+                            sw->stream);
+      if (e == cudaSuccess) e = cudaMallocAsync((void**)&g.d_gcoef, sizeof(double) * gcoef.size(), sw->stream);
+      if (e == cudaSuccess) e = cudaMallocAsync((void**)&g.d_epart, sizeof(double) * G * chunks * S, sw->stream);
+      if (e == cudaSuccess) e = cudaMallocAsync((void**)&g.d_en, sizeof(double) * S, sw->stream);
+      if (e == cudaSuccess)
+        e = cudaMemcpyAsync(g.d_diag, dstate.data(), dstate.size(), cudaMemcpyHostToDevice, sw->stream);
+      if (e == cudaSuccess && !zs.empty())
+        e = cudaMemcpyAsync(g.d_z, zs.data(), sizeof(uint64_t) * zs.size(), cudaMemcpyHostToDevice, sw->stream);
+      if (e == cudaSuccess && !zs.empty())
+        e = cudaMemcpyAsync(g.d_z + zs.size(), qm.data(), sizeof(uint32_t) * qm.size(), cudaMemcpyHostToDevice,
+                            sw->stream);
+      g.nz = zs.size();
+      if (e == cudaSuccess)
+        e = cudaMemcpyAsync(g.d_gcoef, gcoef.data(), sizeof(double) * gcoef.size(), cudaMemcpyHostToDevice,
+                            sw->stream);
+      if (e == cudaSuccess) e = cudaStreamSynchronize(sw->stream);  // host tables die at scope end
+      if (e != cudaSuccess) return cuda_fail(err, e, "sweep energy tables");
+    }
+    sw->e_offsets.assign(term_offsets, term_offsets + count + 1);
+    sw->e_coefs.assign(coefficients, coefficients + nterms);
+    sw->e_strings.assign(pauli_strings, (size_t)char_off[count]);
+    sw->e_valid = true;
+  }
+  std::vector<std::vector<double>> en(sw->groups.size());
+  for (size_t gi = 0; gi < sw->groups.size(); ++gi) {
+    SweepGroup& g = sw->groups[gi];
+    if (!g.diag) continue;
+    const size_t S = g.members.size();
+    en[gi].resize(S);
+    cudaError_t e = launch_diag_expect(g.d_states, sw->prec, g.n, g.d_diag, g.d_z,
+                                       reinterpret_cast<const uint32_t*>(g.d_z + g.nz), (int)S, g.d_epart,
+                                       g.d_gcoef, g.d_en, sw->stream);
+    if (e == cudaSuccess)
+      e = cudaMemcpyAsync(en[gi].data(), g.d_en, sizeof(double) * S, cudaMemcpyDeviceToHost, sw->stream);
+    if (e != cudaSuccess) return cuda_fail(err, e, "sweep energies");
+    *launches += 2;
+  }
+  cudaError_t se = cudaStreamSynchronize(sw->stream);
+  if (se != cudaSuccess) return cuda_fail(err, se, "sweep energies");
+  for (size_t gi = 0; gi < sw->groups.size(); ++gi) {
+    SweepGroup& g = sw->groups[gi];
+    if (g.diag) {
+      for (size_t m = 0; m < g.members.size(); ++m) energies[g.members[m]] = en[gi][m];
+      continue;
+    }
+    for (size_t m = 0; m < g.members.size(); ++m) {
+      const int ci = g.members[m];
+      double energy = 0;
+      for (int t = term_offsets[ci]; t < term_offsets[ci + 1]; ++t) {
+        double v;
+        const int rc = st_pauli(g.views[m].get(), pauli_strings + char_off[ci] + (int64_t)(t - term_offsets[ci]) * g.n,
+                                &v, err);
+        if (rc != QG_OK) return rc;
+        const double term = coefficients[t] * v;
+        energy = (t == term_offsets[ci]) ? term : energy + term;
+        ++*launches;
+      }
+      energies[ci] = energy;
+    }
+  }
+  return QG_OK;
 }
 
 }  // namespace qg
@@ -2343,100 +2499,8 @@ int qg_sweep_run(void* sweep, const int32_t* term_offsets, const double* coeffic
   }
   cudaEventRecord(e1, sw->stream);
   // energies
-  if (rc == QG_OK && term_offsets && energies) {
-    std::vector<int64_t> char_off(sw->count + 1, 0);
-    for (int i = 0; i < sw->count; ++i) {
-      const int n = sw->groups[sw->where[i].first].n;
-      char_off[i + 1] = char_off[i] + (int64_t)(term_offsets[i + 1] - term_offsets[i]) * n;
-    }
-    const int G = diag_max_groups();
-    for (auto& g : sw->groups) {
-      const size_t S = g.members.size();
-      // batched path: every member's terms are I/Z strings with at most G distinct coefficients
-      bool diag = g.n >= 12;
-      std::vector<unsigned char> dstate(diag_state_bytes() * S);
-      std::vector<uint64_t> zs;
-      std::vector<double> gcoef(S * G, 0.0);
-      for (size_t m = 0; m < S && diag; ++m) {
-        const int ci = g.members[m];
-        std::vector<double> vals;
-        std::vector<std::vector<uint64_t>> per(G);
-        for (int t = term_offsets[ci]; t < term_offsets[ci + 1] && diag; ++t) {
-          const char* ps = pauli_strings + char_off[ci] + (int64_t)(t - term_offsets[ci]) * g.n;
-          uint64_t z = 0;
-          for (int q = 0; q < g.n; ++q) {
-            if (ps[q] == 'Z') z |= 1ULL << (g.n - 1 - q);
-            else if (ps[q] != 'I') diag = false;
-          }
-          int gi = -1;
-          for (size_t k = 0; k < vals.size(); ++k)
-            if (vals[k] == coefficients[t]) gi = (int)k;
-          if (gi < 0) {
-            if ((int)vals.size() == G) {
-              diag = false;
-              break;
-            }
-            gi = (int)vals.size();
-            vals.push_back(coefficients[t]);
-          }
-          per[gi].push_back(z);
-        }
-        if (!diag) break;
-        int gcount[8] = {0};
-        const uint64_t zoff = zs.size();
-        for (int k = 0; k < (int)vals.size(); ++k) {
-          gcount[k] = (int)per[k].size();
-          zs.insert(zs.end(), per[k].begin(), per[k].end());
-          gcoef[m * G + k] = vals[k];
-        }
-        fill_diag_state(dstate.data() + diag_state_bytes() * m, zoff, (int)vals.size(), gcount);
-      }
-      if (diag) {
-        const uint64_t chunks = 1ULL << (g.n - 12);
-        void* d_diag = nullptr;
-        uint64_t* d_z = nullptr;
-        double *d_gcoef = nullptr, *d_part = nullptr, *d_en = nullptr;
-        cudaError_t e = cudaMallocAsync(&d_diag, dstate.size(), sw->stream);
-        if (e == cudaSuccess) e = cudaMallocAsync((void**)&d_z, sizeof(uint64_t) * std::max<size_t>(zs.size(), 1), sw->stream);
-        if (e == cudaSuccess) e = cudaMallocAsync((void**)&d_gcoef, sizeof(double) * gcoef.size(), sw->stream);
-        if (e == cudaSuccess) e = cudaMallocAsync((void**)&d_part, sizeof(double) * G * chunks * S, sw->stream);
-        if (e == cudaSuccess) e = cudaMallocAsync((void**)&d_en, sizeof(double) * S, sw->stream);
-        if (e == cudaSuccess) e = cudaMemcpyAsync(d_diag, dstate.data(), dstate.size(), cudaMemcpyHostToDevice, sw->stream);
-        if (e == cudaSuccess && !zs.empty())
-          e = cudaMemcpyAsync(d_z, zs.data(), sizeof(uint64_t) * zs.size(), cudaMemcpyHostToDevice, sw->stream);
-        if (e == cudaSuccess)
-          e = cudaMemcpyAsync(d_gcoef, gcoef.data(), sizeof(double) * gcoef.size(), cudaMemcpyHostToDevice, sw->stream);
-        if (e == cudaSuccess)
-          e = launch_diag_expect(g.d_states, sw->prec, g.n, d_diag, d_z, (int)S, d_part, d_gcoef, d_en, sw->stream);
-        std::vector<double> en(S);
-        if (e == cudaSuccess)
-          e = cudaMemcpyAsync(en.data(), d_en, sizeof(double) * S, cudaMemcpyDeviceToHost, sw->stream);
-        if (e == cudaSuccess) e = cudaStreamSynchronize(sw->stream);
-        for (void* p : {(void*)d_diag, (void*)d_z, (void*)d_gcoef, (void*)d_part, (void*)d_en})
-          if (p) cudaFreeAsync(p, sw->stream);
-        if (e != cudaSuccess) {
-          rc = cuda_fail(&err, e, "sweep energies");
-          break;
-        }
-        launches += 2;
-        for (size_t m = 0; m < S; ++m) energies[g.members[m]] = en[m];
-      } else {
-        for (size_t m = 0; m < S && rc == QG_OK; ++m) {
-          const int ci = g.members[m];
-          double energy = 0;
-          for (int t = term_offsets[ci]; t < term_offsets[ci + 1] && rc == QG_OK; ++t) {
-            double v;
-            rc = st_pauli(g.views[m].get(), pauli_strings + char_off[ci] + (int64_t)(t - term_offsets[ci]) * g.n,
-                          &v, &err);
-            const double term = coefficients[t] * v;
-            energy = (t == term_offsets[ci]) ? term : energy + term;
-            ++launches;
-          }
-          energies[ci] = energy;
-        }
-      }
-    }
-  }
+  if (rc == QG_OK && term_offsets && energies) rc = sweep_energies(sw, term_offsets, coefficients, pauli_strings,
+                                                                   energies, &launches, &err);
   cudaEventRecord(e2, sw->stream);
   cudaError_t se = cudaEventSynchronize(e2);
   if (se != cudaSuccess && rc == QG_OK) rc = cuda_fail(&err, se, "sweep");

@@ -5,7 +5,8 @@
 //   k_batch_zero       every state of a slab to |0...0>
 //   k_diag_expect      per (state, chunk of 4096 amplitudes): sum_i p_i f_g(i) for each
 //                      coefficient group g of a diagonal Hamiltonian, where
-//                      f_g(i) = sum_{t in g} (-1)^popc(i & z_t) is an integer, so the
+//                      f_g(i) = sum_{t in g} (-1)^popc(i & z_t) is an integer (identity
+//                      strings, z_t = 0, only add their count), so the
 //                      energy is sum_g c_g * sum_i p_i f_g(i); partials are FP64
 //                      (FP32 within 32-amplitude runs) and written per work item
 //   k_diag_reduce      fixed-order FP64 (TwoSum) reduction of the partials per state
@@ -23,6 +24,7 @@ namespace {
 constexpr int kSMs = 152;
 constexpr int kChunkBits = 12;
 constexpr int kMaxGroups = 4;
+constexpr int kCountBits = 7;  // bit-sliced odd counts: at most 127 Z-strings per coefficient group
 
 template <typename V>
 __global__ void k_batch_zero(unsigned char* slab, uint64_t per_state, int nstates) {
@@ -39,16 +41,24 @@ __global__ void k_batch_zero(unsigned char* slab, uint64_t per_state, int nstate
 struct DiagState {
   uint64_t zoff;      // first z-mask of this state in the z array
   int32_t ngroups;    // coefficient groups (<= kMaxGroups)
-  int32_t gcount[kMaxGroups];
+  int32_t gcount[kMaxGroups];  // Z-strings with at least one Z per group (their masks are in the z array)
+  int32_t nid[kMaxGroups];     // identity strings per group: each adds +1 to f_g(i) for every i
 };
 
 __device__ __forceinline__ double p_of(double2 a) { return a.x * a.x + a.y * a.y; }
 __device__ __forceinline__ float p_of(float2 a) { return a.x * a.x + a.y * a.y; }
 
-// one CTA of 256 threads per work item (state, chunk); 16 amplitudes per thread
+// one CTA of 256 threads per work item (state, chunk); 16 amplitudes per thread,
+// i = i0 + 256 q (q = 0..15), so bits 8-11 of i are q and i0 has none of them.
+// A term's parity on amplitude q is parity(i0 & z) xor parity(q & z[8:12]); the
+// second part is a 16-bit pattern over q (qmask, from the host). Odd counts are
+// kept bit-sliced over the 16 amplitudes (bit q of slice k = bit k of the count
+// of amplitude q), so a term costs one population count and a 16-lane ripple add
+// instead of sixteen population counts.
 template <typename V, typename R>
 __global__ void __launch_bounds__(256) k_diag_expect(unsigned char* const* states, int n, const DiagState* __restrict__ ds,
-                                                    const uint64_t* __restrict__ zmasks, int nstates,
+                                                    const uint64_t* __restrict__ zmasks,
+                                                    const uint32_t* __restrict__ qmasks, int nstates,
                                                     double* __restrict__ partial) {
   const uint64_t chunks = 1ULL << (n - kChunkBits);
   const uint64_t items = chunks * (uint64_t)nstates;
@@ -59,24 +69,36 @@ __global__ void __launch_bounds__(256) k_diag_expect(unsigned char* const* state
     const V* amps = reinterpret_cast<const V*>(states[s]);
     const DiagState d = ds[s];
     double acc[kMaxGroups] = {0, 0, 0, 0};
-    const uint64_t i0 = (c << kChunkBits) + threadIdx.x;  // amplitude q of this thread: i0 + 256 q
+    const uint64_t i0 = (c << kChunkBits) + threadIdx.x;
     R p[16];
 #pragma unroll
     for (int q = 0; q < 16; ++q) p[q] = p_of(amps[i0 + (uint64_t)q * 256]);
     uint64_t zo = d.zoff;
     for (int g = 0; g < d.ngroups && g < kMaxGroups; ++g) {
-      int odd[16];
+      uint32_t sl[kCountBits];
 #pragma unroll
-      for (int q = 0; q < 16; ++q) odd[q] = 0;
+      for (int k = 0; k < kCountBits; ++k) sl[k] = 0;
       for (int t = 0; t < d.gcount[g]; ++t) {
-        const uint64_t z = zmasks[zo + t];
+        const uint32_t m = qmasks[zo + t];
+        uint32_t carry = (__popcll(i0 & zmasks[zo + t]) & 1) ? (~m & 0xFFFFu) : m;
 #pragma unroll
-        for (int q = 0; q < 16; ++q) odd[q] += __popcll((i0 + (uint64_t)q * 256) & z) & 1;
+        for (int k = 0; k < kCountBits; ++k) {
+          const uint32_t nc = sl[k] & carry;
+          sl[k] ^= carry;
+          carry = nc;
+        }
       }
       zo += d.gcount[g];
+      // odd count of amplitude q from the slices (integer work), then one
+      // multiply-add per amplitude: sum_q p_q (count_g - 2 odd_q)
       R run = 0;  // FP32 for complex64 within one 16-amplitude run, FP64 afterwards
 #pragma unroll
-      for (int q = 0; q < 16; ++q) run += p[q] * (R)(d.gcount[g] - 2 * odd[q]);
+      for (int q = 0; q < 16; ++q) {
+        int odd = 0;
+#pragma unroll
+        for (int k = 0; k < kCountBits; ++k) odd |= (int)((sl[k] >> q) & 1u) << k;
+        run += p[q] * (R)(d.gcount[g] + d.nid[g] - 2 * odd);
+      }
       acc[g] = (double)run;
     }
     // block reduction per group (fixed order)
@@ -132,27 +154,41 @@ cudaError_t launch_batch_zero(void* slab, int precision, int n, int nstates, cud
 }
 
 // host layout of DiagState: zoff, ngroups, gcount[kMaxGroups]
-void fill_diag_state(void* out, uint64_t zoff, int ngroups, const int* gcount) {
+void fill_diag_state(void* out, uint64_t zoff, int ngroups, const int* gcount, const int* nid) {
   DiagState d{};
   d.zoff = zoff;
   d.ngroups = ngroups;
-  for (int g = 0; g < kMaxGroups; ++g) d.gcount[g] = g < ngroups ? gcount[g] : 0;
+  for (int g = 0; g < kMaxGroups; ++g) {
+    d.gcount[g] = g < ngroups ? gcount[g] : 0;
+    d.nid[g] = g < ngroups ? nid[g] : 0;
+  }
   *reinterpret_cast<DiagState*>(out) = d;
 }
 
+int diag_max_terms_per_group() { return (1 << kCountBits) - 1; }
+
+uint32_t diag_qmask(uint64_t z) {
+  const uint32_t zq = (uint32_t)(z >> 8) & 15u;
+  uint32_t m = 0;
+  for (uint32_t q = 0; q < 16; ++q) m |= (uint32_t)(__builtin_popcount(q & zq) & 1) << q;
+  return m;
+}
+
 cudaError_t launch_diag_expect(void* const* d_states, int precision, int n, const void* d_diag, const uint64_t* d_z,
-                               int nstates, double* d_partial, const double* d_gcoef, double* d_energies,
-                               cudaStream_t st) {
+                               const uint32_t* d_qm, int nstates, double* d_partial, const double* d_gcoef,
+                               double* d_energies, cudaStream_t st) {
   if (n < kChunkBits) return cudaErrorInvalidValue;
   const uint64_t chunks = 1ULL << (n - kChunkBits);
   uint64_t items = chunks * (uint64_t)nstates;
   uint64_t grid = items < (uint64_t)kSMs * 8 ? items : (uint64_t)kSMs * 8;
   if (precision == QG_C64)
     k_diag_expect<float2, float><<<(unsigned)grid, 256, 0, st>>>((unsigned char* const*)d_states, n,
-                                                                 (const DiagState*)d_diag, d_z, nstates, d_partial);
+                                                                 (const DiagState*)d_diag, d_z, d_qm, nstates,
+                                                                 d_partial);
   else
     k_diag_expect<double2, double><<<(unsigned)grid, 256, 0, st>>>((unsigned char* const*)d_states, n,
-                                                                   (const DiagState*)d_diag, d_z, nstates, d_partial);
+                                                                   (const DiagState*)d_diag, d_z, d_qm, nstates,
+                                                                   d_partial);
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return e;
   k_diag_reduce<<<(nstates + 127) / 128, 128, 0, st>>>(d_partial, chunks, nstates, d_gcoef, d_energies);
