@@ -292,27 +292,65 @@ int lower_circuit(const qg_circuit* c, std::vector<GOp>* gops, std::vector<std::
 }
 
 // Uncontrolled diagonal gates diag(d0, d1) become a phase d1/d0 on the bit-1 half
-// and a global factor d0, collected into one phase on every amplitude at the end:
-// a diagonal then costs one complex product on half the amplitudes instead of
-// one on each. Used with the double-float and complex64 policies, whose results
-// are held to a tolerance; the exact policy keeps the reference's products.
-void factor_global_phases(std::vector<GOp>* gops) {
+// and a global factor d0; Hadamards [[s, s], [s, -s]] (s = 1/sqrt 2) become the
+// sum / difference [[1, 1], [1, -1]] and a global factor s. The factors are
+// collected and applied as one phase op on every amplitude before each
+// measurement and at the end of the circuit (the state is only unnormalised in
+// between), with an exact 2^-20 rescale after every 40 Hadamards so magnitudes
+// stay within the float range. A diagonal then costs one complex product on half
+// the amplitudes instead of one on each, and a Hadamard only sums. Used with the
+// double-float and complex64 policies, whose results are held to a tolerance;
+// the exact policy keeps the reference's products. measure_at (positions of
+// measurements before op indices) is rewritten for the new op list.
+void factor_global_phases(std::vector<GOp>* gops, std::vector<int>* measure_at) {
+  const double s2 = 1.0 / std::sqrt(2.0);
+  std::vector<GOp> out;
+  out.reserve(gops->size() + 8);
+  std::vector<int> newpos(gops->size() + 1, 0);
   cd global(1.0, 0.0);
-  bool any = false;
-  for (GOp& g : *gops) {
-    if (g.kind != OK_U2 || g.cls != U2_DIAG || g.cmask != 0) continue;
-    const cd d0(g.m[0], g.m[1]), d1(g.m[6], g.m[7]);
-    if (d0 == cd(0.0, 0.0)) continue;
-    const cd r = d1 / d0;
-    global *= d0;
-    any = true;
-    g = make_phase(1ULL << g.t, r.real(), r.imag());
+  int hk = 0;  // Hadamard factors s not yet applied
+  auto emit_scale = [&]() {
+    cd f = global;
+    for (int q = 0; q < hk; ++q) f *= s2;
+    const GOp ph = make_phase(0, f.real(), f.imag());
+    if (ph.kind >= 0) out.push_back(ph);
+    global = cd(1.0, 0.0);
+    hk = 0;
+  };
+  std::vector<char> measured_before(gops->size() + 1, 0);
+  for (int at : *measure_at)
+    if (at >= 0 && at <= (int)gops->size()) measured_before[at] = 1;
+  for (size_t i = 0; i < gops->size(); ++i) {
+    if (measured_before[i]) emit_scale();
+    newpos[i] = (int)out.size();
+    GOp g = (*gops)[i];
+    if (g.kind == OK_U2 && g.cls == U2_DIAG && g.cmask == 0) {
+      const cd d0(g.m[0], g.m[1]), d1(g.m[6], g.m[7]);
+      if (d0 != cd(0.0, 0.0)) {
+        const cd r = d1 / d0;
+        global *= d0;
+        g = make_phase(1ULL << g.t, r.real(), r.imag());
+      }
+    } else if (g.kind == OK_U2 && g.cls == U2_REAL && g.cmask == 0 && g.m[0] == s2 && g.m[2] == s2 && g.m[4] == s2 &&
+               g.m[6] == -s2) {
+      g.m[0] = g.m[2] = g.m[4] = 1.0;
+      g.m[6] = -1.0;
+      if (++hk == 40) {  // s^40 = 2^-20 exactly
+        const GOp ph = make_phase(0, 0x1p-20, 0.0);
+        out.push_back(g);
+        out.push_back(ph);
+        hk = 0;
+        continue;
+      }
+    }
+    if (g.kind >= 0) out.push_back(g);
   }
-  gops->erase(std::remove_if(gops->begin(), gops->end(), [](const GOp& g) { return g.kind < 0; }), gops->end());
-  if (any) {
-    const GOp ph = make_phase(0, global.real(), global.imag());
-    if (ph.kind >= 0) gops->push_back(ph);
-  }
+  if (measured_before[gops->size()]) emit_scale();
+  newpos[gops->size()] = (int)out.size();
+  if (!measured_before[gops->size()]) emit_scale();
+  for (int& at : *measure_at)
+    if (at >= 0 && at <= (int)gops->size()) at = newpos[at];
+  gops->swap(out);
 }
 
 // ---------------------------------------------------------------------------

@@ -24,6 +24,7 @@
 
 #include <algorithm>
 #include <chrono>
+#include <cmath>
 #include <complex>
 #include <cstdio>
 #include <cstring>
@@ -430,7 +431,9 @@ class PassGen {
         o_ << "        " << a << " = y0; " << c << " = y1; }\n";
         break;
       case U2_REAL:
-        if (m[0] == m[2] && m[0] == m[4] && m[6] == -m[0]) {  // [[c, c], [c, -c]]
+        if (m[0] == m[2] && m[0] == m[4] && m[6] == -m[0] && m[0] == 1.0 && !tab_) {  // [[1, 1], [1, -1]]
+          o_ << "      " << (df_ ? "df_sumdiff(" : "f_sumdiff(") << a << ", " << c << ");\n";
+        } else if (m[0] == m[2] && m[0] == m[4] && m[6] == -m[0]) {  // [[c, c], [c, -c]]
           if (df_)
             o_ << "      df_hadamard<" << b(lo_nz(t, 0)) << ">(" << h(t, 0) << ", " << l(t, 0) << ", " << a
                << ", " << c << ");\n";
@@ -509,7 +512,11 @@ class PassGen {
         for (int j = 0; j < ns_; ++j) {
           if ((j & cr) != cr) continue;
           std::string v;
-          if (t.cls == PH_GENERAL) v = cmul(t, 0, 1, r(j));
+          int ex = 0;
+          const bool pow2 = !tab_ && t.cls == PH_GENERAL && t.m[1] == 0.0 && t.m[0] != 0.0 &&
+                            std::frexp(std::fabs(t.m[0]), &ex) == 0.5;
+          if (pow2) v = std::string(df_ ? "df_pow2(" : "f_pow2(") + flit((float)t.m[0]) + ", " + r(j) + ")";
+          else if (t.cls == PH_GENERAL) v = cmul(t, 0, 1, r(j));
           else if (t.cls == PH_NEG) v = std::string(pol()) + "::neg(" + r(j) + ")";
           else if (t.cls == PH_I) v = std::string(pol()) + "::mul_i(" + r(j) + ")";
           else v = std::string(pol()) + "::mul_mi(" + r(j) + ")";

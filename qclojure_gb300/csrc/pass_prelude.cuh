@@ -180,6 +180,18 @@ __device__ __forceinline__ void df_hadamard(float ch, float cl, dfc& x0, dfc& x1
   x0 = y0;
   x1 = y1;
 }
+// [[1, 1], [1, -1]]: a Hadamard whose 1/sqrt 2 is applied later with the global factors
+__device__ __forceinline__ void df_sumdiff(dfc& x0, dfc& x1) {
+  dfc y0, y1;
+  add2(x0.rh, x0.rl, x1.rh, x1.rl, y0.rh, y0.rl);
+  add2(x0.rh, x0.rl, -x1.rh, -x1.rl, y1.rh, y1.rl);
+  add2(x0.ih, x0.il, x1.ih, x1.il, y0.ih, y0.il);
+  add2(x0.ih, x0.il, -x1.ih, -x1.il, y1.ih, y1.il);
+  x0 = y0;
+  x1 = y1;
+}
+// x times a power of two (exact)
+__device__ __forceinline__ dfc df_pow2(float c, const dfc& x) { return dfc{x.rh * c, x.rl * c, x.ih * c, x.il * c}; }
 // [[a, i b], [i c, d]] with a, b, c, d real (RX-shaped)
 template <bool AL, bool BL, bool CL, bool DL>
 __device__ __forceinline__ void df_rxlike(float ah, float al, float bh, float bl, float ch, float cl, float dh, float dl,
@@ -228,6 +240,13 @@ __device__ __forceinline__ void f_hadamard(float c, float2& x0, float2& x1) {
   x0 = y0;
   x1 = y1;
 }
+__device__ __forceinline__ void f_sumdiff(float2& x0, float2& x1) {
+  const float2 y0 = make_float2(x0.x + x1.x, x0.y + x1.y);
+  const float2 y1 = make_float2(x0.x - x1.x, x0.y - x1.y);
+  x0 = y0;
+  x1 = y1;
+}
+__device__ __forceinline__ float2 f_pow2(float c, float2 x) { return make_float2(x.x * c, x.y * c); }
 __device__ __forceinline__ void f_rxlike(float a, float b, float c, float d, float2& x0, float2& x1) {
   const float2 y0 = make_float2(fmaf(a, x0.x, -(b * x1.y)), fmaf(a, x0.y, b * x1.x));
   const float2 y1 = make_float2(fmaf(d, x1.x, -(c * x0.y)), fmaf(c, x0.x, d * x1.y));

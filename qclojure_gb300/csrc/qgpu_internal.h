@@ -130,9 +130,10 @@ struct Program {
 // err receives a message in the reference's words).
 int lower_circuit(const qg_circuit* c, std::vector<GOp>* gops, std::vector<std::vector<int>>* measures,
                   std::vector<int>* measure_at, std::string* err);
-// Tolerance-held policies only: uncontrolled diagonal gates to phases plus one
-// global phase at the end (no effect on the positions of earlier ops).
-void factor_global_phases(std::vector<GOp>* gops);
+// Tolerance-held policies only: uncontrolled diagonal gates to half-state phases
+// and Hadamards to sum / difference, their factors applied as one global op
+// before each measurement and at the end; measure_at is rewritten.
+void factor_global_phases(std::vector<GOp>* gops, std::vector<int>* measure_at);
 // Schedule GOps into passes for the given fusion mode; reorder lets commuting ops
 // overtake each other to fill passes (tolerance-held policies only).
 int schedule(int n, int precision, int fusion, int fuse_k, const std::vector<GOp>& gops,
