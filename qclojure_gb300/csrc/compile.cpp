@@ -291,31 +291,46 @@ int lower_circuit(const qg_circuit* c, std::vector<GOp>* gops, std::vector<std::
   return QG_OK;
 }
 
-// Uncontrolled diagonal gates diag(d0, d1) become a phase d1/d0 on the bit-1 half
-// and a global factor d0; Hadamards [[s, s], [s, -s]] (s = 1/sqrt 2) become the
-// sum / difference [[1, 1], [1, -1]] and a global factor s. The factors are
-// collected and applied as one phase op on every amplitude before each
-// measurement and at the end of the circuit (the state is only unnormalised in
-// between), with an exact 2^-20 rescale after every 40 Hadamards so magnitudes
-// stay within the float range. A diagonal then costs one complex product on half
-// the amplitudes instead of one on each, and a Hadamard only sums. Used with the
-// double-float and complex64 policies, whose results are held to a tolerance;
-// the exact policy keeps the reference's products. measure_at (positions of
-// measurements before op indices) is rewritten for the new op list.
-void factor_global_phases(std::vector<GOp>* gops, std::vector<int>* measure_at) {
+// Scalar factoring for the tolerance-held policies (double-float c128, c64):
+//   - uncontrolled diagonal gates diag(d0, d1) become a phase d1/d0 on the bit-1
+//     half and a global factor d0;
+//   - Hadamards [[s, s], [s, -s]] become the sum / difference [[1, 1], [1, -1]]
+//     and a factor s = 1/sqrt 2;
+//   - rotations with equal diagonal entries (RY-shaped [[c, -s], [s, c]], RX-shaped
+//     [[c, ib], [ib, c]]) become a form with unit diagonal, [[1, t], [u, +-1]],
+//     and a factor: the diagonal entry when it is the larger in magnitude, else the
+//     off-diagonal one, with an X (a register renaming) after the gate. Each output
+//     then needs one product and one sum instead of two products and a sum.
+// The collected factor is applied as one op on every amplitude before each
+// measurement and at the end of the circuit (the state is only scaled in
+// between); whenever its magnitude falls below 2^-20 the state is rescaled by
+// 2^-20 exactly, so magnitudes stay within the float range. The exact policy
+// keeps the reference's products. measure_at (positions of measurements before
+// op indices) is rewritten for the new op list. rotations = false leaves the
+// rotations alone: which form a rotation takes depends on its angle, and sweep
+// members of one structure must keep equal op lists.
+void factor_global_phases(std::vector<GOp>* gops, std::vector<int>* measure_at, bool rotations) {
   const double s2 = 1.0 / std::sqrt(2.0);
   std::vector<GOp> out;
   out.reserve(gops->size() + 8);
   std::vector<int> newpos(gops->size() + 1, 0);
-  cd global(1.0, 0.0);
-  int hk = 0;  // Hadamard factors s not yet applied
+  cd pending(1.0, 0.0);
   auto emit_scale = [&]() {
-    cd f = global;
-    for (int q = 0; q < hk; ++q) f *= s2;
-    const GOp ph = make_phase(0, f.real(), f.imag());
+    const GOp ph = make_phase(0, pending.real(), pending.imag());
     if (ph.kind >= 0) out.push_back(ph);
-    global = cd(1.0, 0.0);
-    hk = 0;
+    pending = cd(1.0, 0.0);
+  };
+  auto absorb = [&](cd f) {
+    pending *= f;
+    if (std::abs(pending) < 0x1p-20) {  // keep the unscaled amplitudes below 2^20 times their norm
+      out.push_back(make_phase(0, 0x1p-20, 0.0));
+      pending *= 0x1p20;
+    }
+  };
+  auto xgate = [&](int t) {
+    double m[8] = {0, 0, 1, 0, 1, 0, 0, 0};
+    GOp x = classify(m, t, 0);
+    return x;
   };
   std::vector<char> measured_before(gops->size() + 1, 0);
   for (int at : *measure_at)
@@ -324,26 +339,48 @@ void factor_global_phases(std::vector<GOp>* gops, std::vector<int>* measure_at) 
     if (measured_before[i]) emit_scale();
     newpos[i] = (int)out.size();
     GOp g = (*gops)[i];
-    if (g.kind == OK_U2 && g.cls == U2_DIAG && g.cmask == 0) {
-      const cd d0(g.m[0], g.m[1]), d1(g.m[6], g.m[7]);
-      if (d0 != cd(0.0, 0.0)) {
-        const cd r = d1 / d0;
-        global *= d0;
-        g = make_phase(1ULL << g.t, r.real(), r.imag());
-      }
-    } else if (g.kind == OK_U2 && g.cls == U2_REAL && g.cmask == 0 && g.m[0] == s2 && g.m[2] == s2 && g.m[4] == s2 &&
-               g.m[6] == -s2) {
-      g.m[0] = g.m[2] = g.m[4] = 1.0;
-      g.m[6] = -1.0;
-      if (++hk == 40) {  // s^40 = 2^-20 exactly
-        const GOp ph = make_phase(0, 0x1p-20, 0.0);
-        out.push_back(g);
-        out.push_back(ph);
-        hk = 0;
-        continue;
+    const double* m = g.m;
+    bool then_x = false;
+    cd f(1.0, 0.0);
+    if (g.kind == OK_U2 && g.cmask == 0) {
+      if (g.cls == U2_DIAG) {
+        const cd d0(m[0], m[1]), d1(m[6], m[7]);
+        if (d0 != cd(0.0, 0.0)) {
+          const cd r = d1 / d0;
+          f = d0;
+          g = make_phase(1ULL << g.t, r.real(), r.imag());
+        }
+      } else if (g.cls == U2_REAL && m[0] == s2 && m[2] == s2 && m[4] == s2 && m[6] == -s2) {
+        f = cd(s2, 0.0);
+        g.m[0] = g.m[2] = g.m[4] = 1.0;
+        g.m[6] = -1.0;
+      } else if (rotations && g.cls == U2_REAL && m[0] == m[6] && m[2] == -m[4] && m[0] != 0.0 && m[4] != 0.0) {
+        double n[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+        if (std::fabs(m[0]) >= std::fabs(m[4])) {  // c [[1, -s/c], [s/c, 1]]
+          f = cd(m[0], 0.0);
+          n[0] = 1.0, n[2] = m[2] / m[0], n[4] = m[4] / m[0], n[6] = 1.0;
+        } else {  // X then s [[1, c/s], [c/s, -1]]: the rows of X.R over s
+          f = cd(m[4], 0.0);
+          n[0] = 1.0, n[2] = m[6] / m[4], n[4] = m[0] / m[4], n[6] = m[2] / m[4];
+          then_x = true;
+        }
+        g = classify(n, g.t, 0);
+      } else if (rotations && g.cls == U2_RXLIKE && m[0] == m[6] && m[3] == m[5] && m[0] != 0.0 && m[3] != 0.0) {
+        double n[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+        if (std::fabs(m[0]) >= std::fabs(m[3])) {  // c [[1, i b/c], [i b/c, 1]]
+          f = cd(m[0], 0.0);
+          n[0] = 1.0, n[3] = m[3] / m[0], n[5] = m[5] / m[0], n[6] = 1.0;
+        } else {  // X then (i b) [[1, -i c/b], [-i c/b, 1]]
+          f = cd(0.0, m[3]);
+          n[0] = 1.0, n[3] = -m[0] / m[3], n[5] = -m[6] / m[3], n[6] = 1.0;
+          then_x = true;
+        }
+        g = classify(n, g.t, 0);
       }
     }
     if (g.kind >= 0) out.push_back(g);
+    if (then_x) out.push_back(xgate(g.t));
+    if (f != cd(1.0, 0.0)) absorb(f);
   }
   if (measured_before[gops->size()]) emit_scale();
   newpos[gops->size()] = (int)out.size();

@@ -431,7 +431,15 @@ class PassGen {
         o_ << "        " << a << " = y0; " << c << " = y1; }\n";
         break;
       case U2_REAL:
-        if (m[0] == m[2] && m[0] == m[4] && m[6] == -m[0] && m[0] == 1.0 && !tab_) {  // [[1, 1], [1, -1]]
+        if (!tab_ && m[0] == 1.0 && (m[6] == 1.0 || m[6] == -1.0) && !(m[2] == 1.0 && m[4] == 1.0)) {
+          // [[1, b], [c, +-1]]
+          const bool neg = m[6] < 0;
+          if (df_)
+            o_ << "      df_realunit<" << b(lo_nz(t, 2)) << ", " << b(lo_nz(t, 4)) << ", " << b(neg) << ">(" << h(t, 2)
+               << ", " << l(t, 2) << ", " << h(t, 4) << ", " << l(t, 4) << ", " << a << ", " << c << ");\n";
+          else
+            o_ << "      f_realunit<" << b(neg) << ">(" << h(t, 2) << ", " << h(t, 4) << ", " << a << ", " << c << ");\n";
+        } else if (m[0] == m[2] && m[0] == m[4] && m[6] == -m[0] && m[0] == 1.0 && !tab_) {  // [[1, 1], [1, -1]]
           o_ << "      " << (df_ ? "df_sumdiff(" : "f_sumdiff(") << a << ", " << c << ");\n";
         } else if (m[0] == m[2] && m[0] == m[4] && m[6] == -m[0]) {  // [[c, c], [c, -c]]
           if (df_)
@@ -450,7 +458,13 @@ class PassGen {
         }
         break;
       case U2_RXLIKE:  // m0 = (a, 0), m1 = (0, b), m2 = (0, c), m3 = (d, 0)
-        if (df_)
+        if (!tab_ && m[0] == 1.0 && m[6] == 1.0) {  // [[1, i b], [i c, 1]]
+          if (df_)
+            o_ << "      df_rxunit<" << b(lo_nz(t, 3)) << ", " << b(lo_nz(t, 5)) << ">(" << h(t, 3) << ", " << l(t, 3)
+               << ", " << h(t, 5) << ", " << l(t, 5) << ", " << a << ", " << c << ");\n";
+          else
+            o_ << "      f_rxunit(" << h(t, 3) << ", " << h(t, 5) << ", " << a << ", " << c << ");\n";
+        } else if (df_)
           o_ << "      df_rxlike<" << b(lo_nz(t, 0)) << ", " << b(lo_nz(t, 3)) << ", "
              << b(lo_nz(t, 5)) << ", " << b(lo_nz(t, 6)) << ">(" << h(t, 0) << ", " << l(t, 0) << ", "
              << h(t, 3) << ", " << l(t, 3) << ", " << h(t, 5) << ", " << l(t, 5) << ", " << h(t, 6) << ", " << l(t, 6)

@@ -190,6 +190,41 @@ __device__ __forceinline__ void df_sumdiff(dfc& x0, dfc& x1) {
   x0 = y0;
   x1 = y1;
 }
+// x + k*y for a constant pair k, unnormalised
+template <bool KL>
+__device__ __forceinline__ void axpy(float kh, float kl, float xh, float xl, float yh, float yl, float& zh, float& zl) {
+  float p, e, err;
+  tprod<KL>(kh, kl, yh, yl, p, e);
+  tsum(xh, p, zh, err);
+  zl = (xl + e) + err;
+}
+// [[1, b], [c, S]] (S = +-1): a real rotation with its diagonal factored out
+template <bool BL, bool CL, bool NEG>
+__device__ __forceinline__ void df_realunit(float bh, float bl, float ch, float cl, dfc& x0, dfc& x1) {
+  dfc y0, y1;
+  axpy<BL>(bh, bl, x0.rh, x0.rl, x1.rh, x1.rl, y0.rh, y0.rl);
+  axpy<BL>(bh, bl, x0.ih, x0.il, x1.ih, x1.il, y0.ih, y0.il);
+  if (NEG) {
+    axpy<CL>(ch, cl, -x1.rh, -x1.rl, x0.rh, x0.rl, y1.rh, y1.rl);
+    axpy<CL>(ch, cl, -x1.ih, -x1.il, x0.ih, x0.il, y1.ih, y1.il);
+  } else {
+    axpy<CL>(ch, cl, x1.rh, x1.rl, x0.rh, x0.rl, y1.rh, y1.rl);
+    axpy<CL>(ch, cl, x1.ih, x1.il, x0.ih, x0.il, y1.ih, y1.il);
+  }
+  x0 = y0;
+  x1 = y1;
+}
+// [[1, i b], [i c, 1]]: an RX-shaped rotation with its diagonal factored out
+template <bool BL, bool CL>
+__device__ __forceinline__ void df_rxunit(float bh, float bl, float ch, float cl, dfc& x0, dfc& x1) {
+  dfc y0, y1;
+  axpy<BL>(-bh, -bl, x0.rh, x0.rl, x1.ih, x1.il, y0.rh, y0.rl);
+  axpy<BL>(bh, bl, x0.ih, x0.il, x1.rh, x1.rl, y0.ih, y0.il);
+  axpy<CL>(-ch, -cl, x1.rh, x1.rl, x0.ih, x0.il, y1.rh, y1.rl);
+  axpy<CL>(ch, cl, x1.ih, x1.il, x0.rh, x0.rl, y1.ih, y1.il);
+  x0 = y0;
+  x1 = y1;
+}
 // x times a power of two (exact)
 __device__ __forceinline__ dfc df_pow2(float c, const dfc& x) { return dfc{x.rh * c, x.rl * c, x.ih * c, x.il * c}; }
 // [[a, i b], [i c, d]] with a, b, c, d real (RX-shaped)
@@ -247,6 +282,20 @@ __device__ __forceinline__ void f_sumdiff(float2& x0, float2& x1) {
   x1 = y1;
 }
 __device__ __forceinline__ float2 f_pow2(float c, float2 x) { return make_float2(x.x * c, x.y * c); }
+template <bool NEG>
+__device__ __forceinline__ void f_realunit(float b, float c, float2& x0, float2& x1) {
+  const float2 y0 = make_float2(fmaf(b, x1.x, x0.x), fmaf(b, x1.y, x0.y));
+  const float2 y1 = NEG ? make_float2(fmaf(c, x0.x, -x1.x), fmaf(c, x0.y, -x1.y))
+                        : make_float2(fmaf(c, x0.x, x1.x), fmaf(c, x0.y, x1.y));
+  x0 = y0;
+  x1 = y1;
+}
+__device__ __forceinline__ void f_rxunit(float b, float c, float2& x0, float2& x1) {
+  const float2 y0 = make_float2(fmaf(-b, x1.y, x0.x), fmaf(b, x1.x, x0.y));
+  const float2 y1 = make_float2(fmaf(-c, x0.y, x1.x), fmaf(c, x0.x, x1.y));
+  x0 = y0;
+  x1 = y1;
+}
 __device__ __forceinline__ void f_rxlike(float a, float b, float c, float d, float2& x0, float2& x1) {
   const float2 y0 = make_float2(fmaf(a, x0.x, -(b * x1.y)), fmaf(a, x0.y, b * x1.x));
   const float2 y1 = make_float2(fmaf(d, x1.x, -(c * x0.y)), fmaf(c, x0.x, d * x1.y));
