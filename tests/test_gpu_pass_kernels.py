@@ -158,3 +158,64 @@ def test_inverse_at_24_qubits_specialised(ctx_df):
         st.apply(_inverse(c))
         assert abs(st.pauli_expectation("Z" * n) - 1.0) <= 1e-12
         assert np.all(st.sample(300, 2) == 0)
+
+
+def _rotations_at_special_angles(n):
+    import math
+
+    ops = [{"operation-type": "h", "operation-params": {"target": q}} for q in range(n)]
+    angles = [0.0, math.pi / 2, math.pi, 3 * math.pi / 2, 2 * math.pi, math.pi - 1e-9, 1e-9, -math.pi / 4, 5.0]
+    for k, a in enumerate(angles):
+        for g in ("rx", "ry", "rz"):
+            ops.append({"operation-type": g, "operation-params": {"target": (k + len(g)) % n, "angle": a}})
+        ops.append({"operation-type": "cnot", "operation-params": {"control": k % n, "target": (k + 1) % n}})
+    return {"num-qubits": n, "operations": ops}
+
+
+@pytest.mark.parametrize("precision,tol", [("c128", 1e-12), ("c64", 2e-5)])
+def test_rotation_factoring_special_angles(ctx_df, oracle, precision, tol):
+    """Rotations become unit-diagonal forms plus a global scalar, with an X when the
+    off-diagonal entry dominates; angles where an entry vanishes or both are equal
+    must keep the reference's results."""
+    c = _rotations_at_special_angles(13)
+    ref = oracle.run(c)
+    st, kinds = _run(ctx_df, c, precision)
+    with st:
+        assert np.max(np.abs(st.download() - ref)) <= tol
+
+
+def test_deep_hadamard_chain_rescaling(ctx_df, oracle):
+    """2400 Hadamards: their 1/sqrt2 factors are collected with exact 2^-20
+    rescales, so the unscaled amplitudes never leave the float range."""
+    n = 12
+    ops = []
+    for layer in range(200):
+        ops += [{"operation-type": "h", "operation-params": {"target": q}} for q in range(n)]
+        ops.append({"operation-type": "t", "operation-params": {"target": layer % n}})
+    c = {"num-qubits": n, "operations": ops}
+    ref = oracle.run(c)
+    st, _ = _run(ctx_df, c, "c128")
+    with st:
+        assert np.max(np.abs(st.download() - ref)) <= 1e-12
+
+
+@pytest.mark.parametrize("precision,tol", [("c128", 1e-12), ("c64", 2e-5)])
+def test_parity_runs_with_mixed_angles(ctx_df, oracle, precision, tol):
+    """RZZ layers whose angles alternate split into several runs; a run of one angle
+    uses one parity-count table."""
+    import math
+
+    n = 14
+    rng = np.random.default_rng(3)
+    ops = [{"operation-type": "h", "operation-params": {"target": q}} for q in range(n)]
+    for layer in range(3):
+        for e in range(20):
+            a, b = (int(x) for x in rng.choice(n, 2, replace=False))
+            ang = 0.7 if (e // 3) % 2 == 0 else 1.9 + layer
+            ops.append({"operation-type": "rzz", "operation-params": {"qubit1": a, "qubit2": b, "angle": ang}})
+        ops += [{"operation-type": "rx", "operation-params": {"target": q, "angle": 0.3 + q / 7}} for q in range(n)]
+    c = {"num-qubits": n, "operations": ops}
+    ref = oracle.run(c)
+    st, _ = _run(ctx_df, c, precision)
+    with st:
+        assert np.max(np.abs(st.download() - ref)) <= tol
