@@ -639,6 +639,84 @@ class PassGen {
   int unit_power(const TOp& t) const { return t.cls == PH_NEG ? 2 : t.cls == PH_I ? 1 : 3; }
 
   // complex products of the run form; *ok = false when it would not pay
+  // exponent j (phase = w^j, w = exp(2 pi i / 2^30)) of an exact root phase op, or -1
+  static long long root_exponent(const TOp& t) {
+    if (t.cls == PH_I) return 1LL << 28;
+    if (t.cls == PH_NEG) return 1LL << 29;
+    if (t.cls == PH_MINUS_I) return 3LL << 28;
+    const double two_pi = 6.283185307179586476925286766559;
+    double phi = std::atan2(t.m[1], t.m[0]);
+    if (phi < 0) phi += two_pi;
+    const long long j = std::llround(phi / two_pi * 1073741824.0) & ((1LL << 30) - 1);
+    const double a = two_pi * (double)j / 1073741824.0;
+    if (std::fabs(std::cos(a) - t.m[0]) > 4e-16 || std::fabs(std::sin(a) - t.m[1]) > 4e-16) return -1;
+    return j;
+  }
+
+  // A run whose phases are all powers of w: integer exponents per register mask,
+  // added under their conditions, then one table product per register.
+  // budget: complex products of the cheapest other form; the root form costs,
+  // per register it touches, one product per table chunk plus the lookups
+  // (about 0.2 of a product in double-float, 2 in complex64, where a product is
+  // four instructions and a lookup a dependent load), and a fraction of a product
+  // per conditional exponent add
+  bool root_run(int begin, int end, double budget) {
+    if (tab_) return false;
+    std::vector<long long> ex(end - begin);
+    unsigned long long any = 0;
+    int conds = 0;
+    for (int i = begin; i < end; ++i) {
+      ex[i - begin] = root_exponent(ops_[i]);
+      if (ex[i - begin] < 0) return false;
+      any |= (unsigned long long)ex[i - begin];
+      if (ops_[i].gmask || ops_[i].tmask) ++conds;
+    }
+    const bool A = (any >> 20) & 1023, B = (any >> 10) & 1023, C = any & 1023;
+    const int chunks = (A ? 1 : 0) + (B ? 1 : 0) + (C ? 1 : 0);
+    const double cost = ns_ * chunks * (1.0 + (df_ ? 0.2 : 2.0)) + conds * (df_ ? 0.1 : 0.5);
+    if (cost >= budget) return false;
+    bool used[kMaxRegs] = {false};
+    unsigned long long konst[kMaxRegs] = {0};
+    o_ << "    {  // run of " << (end - begin) << " phase ops, exponents of exp(2 pi i / 2^30)\n";
+    for (int i = begin; i < end; ++i) {
+      const TOp& t = ops_[i];
+      const int cr = (int)(t.rmask & (uint32_t)(ns_ - 1));
+      const std::string c = cond(t.gmask, t.gmask, t.tmask, t.tval);
+      if (c.empty()) {
+        konst[cr] += (unsigned long long)ex[i - begin];
+        continue;
+      }
+      if (!used[cr]) {
+        used[cr] = true;
+        o_ << "      unsigned E" << cr << " = 0u;\n";
+      }
+      o_ << "      if (" << c << ") E" << cr << " += " << hex32((uint32_t)ex[i - begin]) << ";\n";
+    }
+    for (int j = 0; j < ns_; ++j) {
+      std::string sum;
+      unsigned long long k = 0;
+      bool any_j = false;
+      for (int cr = 0; cr < ns_; ++cr) {
+        if ((j & cr) != cr) continue;
+        k += konst[cr];
+        if (konst[cr]) any_j = true;
+        if (used[cr]) {
+          sum += (sum.empty() ? "E" : " + E") + std::to_string(cr);
+          any_j = true;
+        }
+      }
+      if (!any_j) continue;
+      k &= (1ULL << 30) - 1;
+      if (sum.empty() && k == 0) continue;
+      const std::string T = "((" + (sum.empty() ? std::string("0u") : sum) + " + " + hex32((uint32_t)k) + ") & 0x3fffffffu)";
+      o_ << "      r" << j << " = " << (df_ ? "df_root_mul_impl<" : "f_root_mul_impl<") << b(A) << ", " << b(B) << ", "
+         << b(C) << ">(" << T << ", r" << j << ");\n";
+      touched(j);
+    }
+    o_ << "    }\n";
+    return true;
+  }
+
   void phase_run(int begin, int end) {
     const int R = sh_.rbits;
     // cost of the op-by-op form: complex products
@@ -670,6 +748,7 @@ class PassGen {
           def[j] = def[j] || def[j ^ (1 << b)];
         }
     for (int j = 0; j < ns_; ++j) cost_run += def[j] ? 1 : 0;
+    if (root_run(begin, end, std::min(cost_run, cost_ops))) return;
     if (cost_run >= cost_ops) {
       for (int i = begin; i < end; ++i) op(ops_[i]);
       return;
@@ -922,6 +1001,32 @@ void compile_unit(Unit* u) {
   api.destroy(&p);
 }
 
+// w^(a 2^20), w^(b 2^10), w^c (w = exp(2 pi i / 2^30)) as double-float entries,
+// copied into a loaded module's qgp_roots table.
+cudaError_t fill_root_table(cudaLibrary_t lib) {
+  static const std::vector<float> host = [] {
+    std::vector<float> t(3072 * 4);
+    const double two_pi = 6.283185307179586476925286766559;
+    for (int part = 0; part < 3; ++part)
+      for (int i = 0; i < 1024; ++i) {
+        const double j = (double)i * (part == 0 ? 1048576.0 : part == 1 ? 1024.0 : 1.0);
+        const double a = two_pi * j / 1073741824.0, re = std::cos(a), im = std::sin(a);
+        float* e = &t[4 * (1024 * part + i)];
+        e[0] = (float)re;
+        e[1] = (float)(re - (double)e[0]);
+        e[2] = (float)im;
+        e[3] = (float)(im - (double)e[2]);
+      }
+    return t;
+  }();
+  void* d = nullptr;
+  size_t bytes = 0;
+  cudaError_t e = cudaLibraryGetGlobal(&d, &bytes, lib, "qgp_roots");
+  if (e != cudaSuccess) return e;
+  if (bytes != sizeof(float) * host.size()) return cudaErrorInvalidValue;
+  return cudaMemcpy(d, host.data(), bytes, cudaMemcpyHostToDevice);
+}
+
 struct Compiled : PassKernels {
   std::vector<cudaLibrary_t> libs;
   std::vector<cudaKernel_t> kernel;  // per program step (nullptr: interpreted)
@@ -1113,6 +1218,11 @@ std::shared_ptr<const PassKernels> pass_kernels_for(const Program& prog, int pre
       return nullptr;
     }
     c->libs.push_back(lib);
+    e = fill_root_table(lib);
+    if (e != cudaSuccess) {
+      *why = std::string("pass kernel tables: ") + cudaGetErrorString(e);
+      return nullptr;
+    }
     for (int s : u.steps) {
       cudaKernel_t k = nullptr;
       const std::string name = (table ? "qgs_" : "qgp_") + std::to_string(s);

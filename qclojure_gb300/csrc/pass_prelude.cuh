@@ -20,6 +20,12 @@
 
 #include "df64.cuh"
 
+// Powers of w = exp(2 pi i / 2^30) in three tables of 1024 (w^(a 2^20), w^(b 2^10),
+// w^c), double-float (re.hi, re.lo, im.hi, im.lo); filled by the host after the
+// module is loaded. Runs of phases that are all such powers (the controlled
+// phases of a QFT) add integer exponents and look the product up here.
+__device__ float4 qgp_roots[3072];
+
 namespace qgp {
 
 using qg::dfc;
@@ -225,6 +231,27 @@ __device__ __forceinline__ void df_rxunit(float bh, float bl, float ch, float cl
   x0 = y0;
   x1 = y1;
 }
+// x * w^T, the chunks the run needs selected at compile time
+template <bool A, bool B, bool C>
+__device__ __forceinline__ dfc df_root_mul_impl(unsigned T, const dfc& x) {
+  dfc g = dfc{1.0f, 0.0f, 0.0f, 0.0f};
+  bool have = false;
+  if (A) {
+    const float4 v = qgp_roots[(T >> 20) & 1023u];
+    g = dfc{v.x, v.y, v.z, v.w};
+    have = true;
+  }
+  if (B) {
+    const float4 v = qgp_roots[1024 + ((T >> 10) & 1023u)];
+    g = have ? df_cmul<true, true>(v.x, v.y, v.z, v.w, g) : dfc{v.x, v.y, v.z, v.w};
+    have = true;
+  }
+  if (C) {
+    const float4 v = qgp_roots[2048 + (T & 1023u)];
+    g = have ? df_cmul<true, true>(v.x, v.y, v.z, v.w, g) : dfc{v.x, v.y, v.z, v.w};
+  }
+  return df_cmul<true, true>(g.rh, g.rl, g.ih, g.il, x);
+}
 // x times a power of two (exact)
 __device__ __forceinline__ dfc df_pow2(float c, const dfc& x) { return dfc{x.rh * c, x.rl * c, x.ih * c, x.il * c}; }
 // [[a, i b], [i c, d]] with a, b, c, d real (RX-shaped)
@@ -282,6 +309,23 @@ __device__ __forceinline__ void f_sumdiff(float2& x0, float2& x1) {
   x1 = y1;
 }
 __device__ __forceinline__ float2 f_pow2(float c, float2 x) { return make_float2(x.x * c, x.y * c); }
+template <bool A, bool B, bool C>
+__device__ __forceinline__ float2 f_root_mul_impl(unsigned T, float2 x) {
+  float2 g = make_float2(1.0f, 0.0f);
+  if (A) {
+    const float4 v = qgp_roots[(T >> 20) & 1023u];
+    g = f_cmul(v.x, v.z, g);
+  }
+  if (B) {
+    const float4 v = qgp_roots[1024 + ((T >> 10) & 1023u)];
+    g = f_cmul(v.x, v.z, g);
+  }
+  if (C) {
+    const float4 v = qgp_roots[2048 + (T & 1023u)];
+    g = f_cmul(v.x, v.z, g);
+  }
+  return f_cmul(g.x, g.y, x);
+}
 template <bool NEG>
 __device__ __forceinline__ void f_realunit(float b, float c, float2& x0, float2& x1) {
   const float2 y0 = make_float2(fmaf(b, x1.x, x0.x), fmaf(b, x1.y, x0.y));
