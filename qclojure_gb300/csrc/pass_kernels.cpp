@@ -24,6 +24,7 @@
 
 #include <algorithm>
 #include <chrono>
+#include <list>
 #include <cmath>
 #include <complex>
 #include <cstdio>
@@ -1037,8 +1038,41 @@ struct Compiled : PassKernels {
   }
 };
 
+// Compiled programs per device, least recently used first out beyond
+// kMaxCachedPrograms (a serving process meets ever new circuits). An evicted
+// program's modules unload when its last user lets go: a run holds its program
+// until its passes have finished, a sweep for its lifetime.
+constexpr size_t kMaxCachedPrograms = 64;
+struct CacheEntry {
+  std::shared_ptr<Compiled> prog;  // nullptr: the compile failed
+  std::list<std::string>::iterator pos;
+};
+struct DeviceCache {
+  std::unordered_map<std::string, CacheEntry> map;
+  std::list<std::string> lru;  // most recent first
+  std::shared_ptr<Compiled>* find(const std::string& key) {
+    auto it = map.find(key);
+    if (it == map.end()) return nullptr;
+    lru.splice(lru.begin(), lru, it->second.pos);
+    return &it->second.prog;
+  }
+  std::shared_ptr<Compiled> insert(const std::string& key, std::shared_ptr<Compiled> p) {
+    auto it = map.find(key);
+    if (it != map.end()) {  // another thread compiled it meanwhile
+      if (!it->second.prog) it->second.prog = p;
+      return it->second.prog;
+    }
+    lru.push_front(key);
+    map.emplace(key, CacheEntry{p, lru.begin()});
+    while (map.size() > kMaxCachedPrograms) {
+      map.erase(lru.back());
+      lru.pop_back();
+    }
+    return p;
+  }
+};
 std::mutex g_mu;
-std::unordered_map<std::string, std::shared_ptr<Compiled>> g_cache[64];  // per device, keyed by source
+DeviceCache g_cache[64];
 size_t g_cache_hits = 0, g_cache_misses = 0;
 
 }  // namespace
@@ -1189,16 +1223,15 @@ std::shared_ptr<const PassKernels> pass_kernels_for(const Program& prog, int pre
   const std::string key = std::to_string(prec) + ":" + pass_structure_key(prog, table);
   {
     std::lock_guard<std::mutex> lk(g_mu);
-    auto it = g_cache[device].find(key);
-    if (it != g_cache[device].end()) {
+    if (std::shared_ptr<Compiled>* hit = g_cache[device].find(key)) {
       ++g_cache_hits;
-      if (!it->second) *why = "this program's pass kernels failed to compile before";
-      return it->second;
+      if (!*hit) *why = "this program's pass kernels failed to compile before";
+      return *hit;
     }
   }
   auto remember_failure = [&]() {
     std::lock_guard<std::mutex> lk(g_mu);
-    g_cache[device].emplace(key, nullptr);
+    g_cache[device].insert(key, nullptr);
     return nullptr;
   };
   std::vector<Unit> units;
@@ -1246,9 +1279,7 @@ std::shared_ptr<const PassKernels> pass_kernels_for(const Program& prog, int pre
   c->compile_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
   std::lock_guard<std::mutex> lk(g_mu);
   ++g_cache_misses;
-  auto& slot = g_cache[device][key];
-  if (!slot) slot = c;
-  return slot;
+  return g_cache[device].insert(key, c);
 }
 
 bool pass_kernel_ready(const PassKernels& pk, size_t step) {

@@ -219,3 +219,29 @@ def test_parity_runs_with_mixed_angles(ctx_df, oracle, precision, tol):
     st, _ = _run(ctx_df, c, precision)
     with st:
         assert np.max(np.abs(st.download() - ref)) <= tol
+
+
+def test_compiled_programs_are_cached(ctx_df):
+    """A second run of the same program reuses its compiled modules (cache hit);
+    a circuit with other angles compiles anew."""
+    import ctypes as C
+
+    from qclojure_gb300 import workloads
+
+    lib = ctx_df.lib
+
+    def info():
+        a, h, m = C.c_int32(), C.c_uint64(), C.c_uint64()
+        lib.qg_pass_kernels_info(C.byref(a), C.byref(h), C.byref(m))
+        return a.value, h.value, m.value
+
+    c = workloads.layered_circuit(14, 6, seed=808)
+    with ctx_df.state(14, "c128") as st:
+        st.apply(c)
+        _, h0, m0 = info()
+        st.apply(c)
+        avail, h1, m1 = info()
+        assert avail == 1 and h1 == h0 + 1 and m1 == m0
+        st.apply(workloads.layered_circuit(14, 6, seed=809))
+        _, h2, m2 = info()
+        assert m2 == m1 + 1
