@@ -306,10 +306,11 @@ int lower_circuit(const qg_circuit* c, std::vector<GOp>* gops, std::vector<std::
 // between); whenever its magnitude falls below 2^-20 the state is rescaled by
 // 2^-20 exactly, so magnitudes stay within the float range. The exact policy
 // keeps the reference's products. measure_at (positions of measurements before
-// op indices) is rewritten for the new op list. rotations = false leaves the
-// rotations alone: which form a rotation takes depends on its angle, and sweep
-// members of one structure must keep equal op lists.
-void factor_global_phases(std::vector<GOp>* gops, std::vector<int>* measure_at, bool rotations) {
+// op indices) is rewritten for the new op list. rotations = kFactorNone leaves
+// the rotations alone: sweep members of one structure must keep equal op lists,
+// and both the form a rotation takes and the number of rescales depend on the
+// angles.
+void factor_global_phases(std::vector<GOp>* gops, std::vector<int>* measure_at, int rotations) {
   const double s2 = 1.0 / std::sqrt(2.0);
   std::vector<GOp> out;
   out.reserve(gops->size() + 8);
@@ -322,7 +323,7 @@ void factor_global_phases(std::vector<GOp>* gops, std::vector<int>* measure_at, 
   };
   auto absorb = [&](cd f) {
     pending *= f;
-    if (std::abs(pending) < 0x1p-20) {  // keep the unscaled amplitudes below 2^20 times their norm
+    while (std::abs(pending) < 0x1p-20) {  // keep the unscaled amplitudes below 2^20 times their norm
       out.push_back(make_phase(0, 0x1p-20, 0.0));
       pending *= 0x1p20;
     }

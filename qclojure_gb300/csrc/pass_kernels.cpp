@@ -238,6 +238,15 @@ std::vector<TOp> plan_layouts(const TOp* ops, int nops, int k, int R, bool table
   return out;
 }
 
+// A real or RX-shaped 2x2 whose diagonal is (1, +-1) (a rotation with its
+// diagonal factored out): 1 = [[1, b], [c, 1]], 2 = [[1, b], [c, -1]], else 0.
+int unit_diagonal(const TOp& t) {
+  if (t.kind != OK_U2 || t.m[0] != 1.0 || t.m[1] != 0.0 || t.m[7] != 0.0) return 0;
+  if (t.cls == U2_RXLIKE && t.m[6] == 1.0) return 1;
+  if (t.cls == U2_REAL && !(t.m[2] == 1.0 && t.m[4] == 1.0)) return t.m[6] == 1.0 ? 1 : t.m[6] == -1.0 ? 2 : 0;
+  return 0;
+}
+
 // Runs of at least two consecutive parity ops (RZZ) with equal phase pairs: their
 // combined phase depends only on how many of them see odd parity, m, so each
 // register takes one entry of a table of p0^(E-m) p1^m instead of E products.
@@ -432,7 +441,7 @@ class PassGen {
         o_ << "        " << a << " = y0; " << c << " = y1; }\n";
         break;
       case U2_REAL:
-        if (!tab_ && m[0] == 1.0 && (m[6] == 1.0 || m[6] == -1.0) && !(m[2] == 1.0 && m[4] == 1.0)) {
+        if (unit_diagonal(t)) {
           // [[1, b], [c, +-1]]
           const bool neg = m[6] < 0;
           if (df_)
@@ -459,7 +468,7 @@ class PassGen {
         }
         break;
       case U2_RXLIKE:  // m0 = (a, 0), m1 = (0, b), m2 = (0, c), m3 = (d, 0)
-        if (!tab_ && m[0] == 1.0 && m[6] == 1.0) {  // [[1, i b], [i c, 1]]
+        if (unit_diagonal(t)) {  // [[1, i b], [i c, 1]]
           if (df_)
             o_ << "      df_rxunit<" << b(lo_nz(t, 3)) << ", " << b(lo_nz(t, 5)) << ">(" << h(t, 3) << ", " << l(t, 3)
                << ", " << h(t, 5) << ", " << l(t, 5) << ", " << a << ", " << c << ");\n";
@@ -1194,9 +1203,10 @@ std::string pass_structure_key(const Program& prog, bool table) {
         // layout-relative fields do not matter; parity masks are data
         if (t.kind == OK_LAYOUT) continue;
         const double* m = t.m;
-        const char shape[4] = {(char)(t.cls == U2_REAL && m[0] == m[2] && m[0] == m[4] && m[6] == -m[0]),
+        const char shape[5] = {(char)(t.cls == U2_REAL && m[0] == m[2] && m[0] == m[4] && m[6] == -m[0]),
                                (char)(m[3] > 0), (char)(m[5] > 0),
-                               (char)(prev && same_parity_phases(*prev, prog.tops[o]))};
+                               (char)(prev && same_parity_phases(*prev, prog.tops[o])),
+                               (char)(unit_diagonal(t))};
         prev = &prog.tops[o];
         std::memset(t.m, 0, sizeof(t.m));
         std::memset(t.mf, 0, sizeof(t.mf));
@@ -1205,7 +1215,7 @@ std::string pass_structure_key(const Program& prog, bool table) {
         std::memset(t.dbits, 0, sizeof(t.dbits));
         std::memset(t.lj, 0, sizeof(t.lj));
         if (t.kind == OK_PARITY) t.lmask = t.lval = 0, t.gmask = t.gval = 0;
-        key.append(shape, 4);
+        key.append(shape, 5);
       }
       key.append(reinterpret_cast<const char*>(&t), sizeof(TOp));
     }

@@ -133,7 +133,8 @@ int lower_circuit(const qg_circuit* c, std::vector<GOp>* gops, std::vector<std::
 // Tolerance-held policies only: uncontrolled diagonal gates to half-state phases
 // and Hadamards to sum / difference, their factors applied as one global op
 // before each measurement and at the end; measure_at is rewritten.
-void factor_global_phases(std::vector<GOp>* gops, std::vector<int>* measure_at, bool rotations);
+constexpr int kFactorNone = 0, kFactorRotations = 1;
+void factor_global_phases(std::vector<GOp>* gops, std::vector<int>* measure_at, int rotations);
 // Schedule GOps into passes for the given fusion mode; reorder lets commuting ops
 // overtake each other to fill passes (tolerance-held policies only).
 int schedule(int n, int precision, int fusion, int fuse_k, const std::vector<GOp>& gops,

@@ -380,7 +380,8 @@ static int compile_program(const qg_circuit* c, int precision, int fusion, int f
   int rc = lower_circuit(c, &gops, &measures, &measure_at, err);
   if (rc != QG_OK) return rc;
   const bool tolerance_held = precision == QG_C64 || prog->arith == QG_ARITH_DOUBLE_FLOAT;
-  if (fusion == QG_FUSE_TILED && tolerance_held) factor_global_phases(&gops, &measure_at, reorder);
+  if (fusion == QG_FUSE_TILED && tolerance_held)
+    factor_global_phases(&gops, &measure_at, reorder ? kFactorRotations : kFactorNone);
   return schedule(c->num_qubits, precision, fusion, fuse_k, gops, measures, measure_at, prog, err,
                   reorder && fusion == QG_FUSE_TILED && tolerance_held);
 }
