@@ -418,7 +418,7 @@ def main():
                      "peak_source": peak_src, "pass_bytes": pass_bytes, "mean_pass_ms": mean_pass,
                      "passes": len(dom),
                      "note": "passes are bound by instruction issue, not HBM: ncu on the same kernel "
-                             "(26 qubits) shows 66-70% issue active and 21-27% DRAM throughput for "
+                             "(26 qubits) shows 62-65% issue active and 23-29% DRAM throughput for "
                              "double-float complex128 (profiles/qgp_pass_c128_doublefloat_layered30x40_qft30.md)"},
         "gpu_launches": int(l1.value - l0.value),
         "clocks": ck,
