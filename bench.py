@@ -425,6 +425,25 @@ def main():
     }
 
     if rank == 0 and not args.no_extras:
+        # accuracy against an exact FP64 run of the same circuit: complex128 with every product
+        # and sum rounded in the reference's gate order (the path that is bit-identical to the
+        # oracle in the parity tests), compared on the device with the benchmarked result
+        ctx_x = Context(device=local, workers=1, seed=7, arithmetic="exact")
+        sx = ctx_x.state(n, "c128")
+        _, sxs = sx.device_ptr()
+        xstream = torch.cuda.ExternalStream(sxs, device=torch.device("cuda", local))
+        sx.set_basis(0)
+        xa = torch.cuda.Event(enable_timing=True)
+        xb = torch.cuda.Event(enable_timing=True)
+        xa.record(xstream)
+        sx.apply(circ, fusion=args.fusion)
+        xb.record(xstream)
+        xb.synchronize()
+        st.set_basis(0)
+        st.apply(circ, fusion=args.fusion)
+        accuracy = {"reference": "c128 exact FP64 arithmetic, gate order of the reference",
+                    "reference_ms": xa.elapsed_time(xb),
+                    ("c128_double_float" if args.precision == "c128" else "c64"): st.compare(sx)}
         # complex64 leg (same circuit)
         if args.precision == "c128":
             st64 = ctx.state(n, "c64")
@@ -454,7 +473,32 @@ def main():
                                         "frac": a64 / peak if d64 else None,
                                         "traffic": 1.012e9 * 2 ** (n - 26), "mean_pass_ms": m64,
                                         "kernel": "qgp_<pass> (specialised tiled pass, complex64)"}}
+            accuracy["c64"] = st64.compare(sx)  # the profile run above left the circuit's result
             st64.close()
+        sx.close()
+        ctx_x.close()
+        line["accuracy"] = accuracy
+        # dense fused blocks of k = 1..5 qubits (one HBM pass per block), per-pass bandwidth on
+        # the first two layers of the workload; dense blocks compute in FP64 (c128) or FP32 (c64)
+        dense_sample = workloads.layered_circuit(n, 2, args.seed + rank)
+        dense = {"sample": f"first 2 layers of layered-{n}x{args.depth} ({len(dense_sample['operations'])} gates)"}
+        for dprec in (("c128", "c64") if args.precision == "c128" else ("c64",)):
+            rows = {}
+            for k in range(1, 6):
+                with Context(device=local, workers=1, seed=7, fusion_width=k) as ctx_k:
+                    with ctx_k.state(n, dprec) as sk:
+                        sk.set_basis(0)
+                        sk.apply(dense_sample, fusion="dense")  # warm-up
+                        sk.set_basis(0)
+                        pk_ms, pk_kind = sk.profile(dense_sample, fusion="dense")
+                tiles = [t for t, kk in zip(pk_ms, pk_kind) if kk == 1]
+                bpp = 2 * (16 if dprec == "c128" else 8) * N
+                mean_k = statistics.mean(tiles) if tiles else float("nan")
+                rows[str(k)] = {"passes": len(pk_ms), "block_passes": len(tiles), "total_ms": float(sum(pk_ms)),
+                                "mean_block_pass_ms": mean_k,
+                                "block_pass_gbs": bpp / (mean_k / 1e3) / 1e9 if tiles else None}
+            dense[dprec] = rows
+        line["dense_blocks"] = dense
         # batched parameter sweep: 1024 QAOA MaxCut circuits (p=3, n uniform over 12..24 even),
         # one launch per pass over all states of a size, replayed from CUDA graphs
         from qclojure_gb300.sweep import Sweep

@@ -316,6 +316,11 @@ int qg_state_expectation_1q(void* state, const double* obs8, int32_t target, dou
 /* Sum of |a|^2 and <a|b> (complex_linear_algebra.clj:318,435), FP64 compensated. */
 int qg_state_norm2(void* state, double* out);
 int qg_state_inner(void* a, void* b, double* re, double* im);
+/* Accuracy of a state against a complex128 state of the same size (for instance an exact
+ * FP64 run of the same circuit); no reference counterpart. out3[0] = max_i |a_i - r_i|,
+ * out3[1] = 1 - |<r|a>|^2 / (<a|a><r|r>), out3[2] = 1/2 sum_i | |a_i|^2 - |r_i|^2 |
+ * (total variation distance of the outcome distributions). */
+int qg_state_compare(void* state, void* reference, double* out3);
 /* Partial measurement with collapse (state.clj:915-1014); outcome bit i <-> qubits[i]. */
 int qg_state_measure(void* state, const int32_t* qubits, int32_t count, uint64_t seed,
                      uint64_t* outcome_out, double* probability_out);

@@ -180,6 +180,7 @@ SIGNATURES = {
     "qg_state_expectation_1q": ([P, DP, I32, DP], C.c_int),
     "qg_state_norm2": ([P, DP], C.c_int),
     "qg_state_inner": ([P, P, DP, DP], C.c_int),
+    "qg_state_compare": ([P, P, DP], C.c_int),
     "qg_state_measure": ([P, I32P, I32, U64, U64P, DP], C.c_int),
     "qg_state_device_ptr": ([P, C.POINTER(P), C.POINTER(P)], C.c_int),
     "qg_state_synchronize": ([P], C.c_int),

@@ -727,6 +727,14 @@ int schedule(int n, int precision, int fusion, int fuse_k, const std::vector<GOp
       orig_index.push_back(gi);
       gi = gj;
     }
+    if (precision == QG_C64 && !prog->dense.empty()) {
+      // complex64 blocks multiply in FP32: the entries are stored as float pairs, so a
+      // block's offset in complex entries indexes a float2 array
+      std::vector<float> f(prog->dense.begin(), prog->dense.end());
+      std::vector<double> packed(f.size() / 2);
+      std::memcpy(packed.data(), f.data(), sizeof(float) * f.size());
+      prog->dense.swap(packed);
+    }
   } else {
     ops = gops;
     for (size_t g = 0; g < gops.size(); ++g) orig_index.push_back(g);

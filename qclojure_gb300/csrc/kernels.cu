@@ -398,6 +398,47 @@ __global__ void __launch_bounds__(256) k_inner(const typename C2<R>::T* __restri
   block_reduce_store<256>(im, d_part, gridDim.x + blockIdx.x);
 }
 
+// Distance of a state a (complex64 or complex128) from a complex128 state b, d_i = a_i - b_i.
+// Per block, as double-double partials: |d|^2, <b|d> (real, imaginary), |a|^2, |b|^2 and
+// sum_i | |a_i|^2 - |b_i|^2 |, the last as |Re(d_i conj(a_i + b_i))| so that it does not
+// cancel; and max_i |d_i|^2. 1 - F follows without cancellation from the identity
+// <a|a><b|b> - |<b|a>|^2 = <b|b><d|d> - |<b|d>|^2.
+template <typename R>
+__global__ void __launch_bounds__(256) k_compare(const typename C2<R>::T* __restrict__ a,
+                                                 const double2* __restrict__ b, uint64_t N, double* d_part,
+                                                 double* d_max) {
+  DD dd{0, 0}, re{0, 0}, im{0, 0}, na{0, 0}, nb{0, 0}, tv{0, 0};
+  double mx = 0;
+  for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < N; i += (uint64_t)gridDim.x * blockDim.x) {
+    auto x = a[i];
+    double2 y = b[i];
+    double ar = (double)x.x, ai = (double)x.y;
+    double dr = ar - y.x, di = ai - y.y;
+    double d2 = dr * dr + di * di;
+    two_sum_acc(dd, d2);
+    two_sum_acc(re, y.x * dr + y.y * di);
+    two_sum_acc(im, y.x * di - y.y * dr);
+    two_sum_acc(na, ar * ar + ai * ai);
+    two_sum_acc(nb, y.x * y.x + y.y * y.y);
+    two_sum_acc(tv, fabs(dr * (ar + y.x) + di * (ai + y.y)));
+    mx = fmax(mx, d2);
+  }
+  const DD acc[6] = {dd, re, im, na, nb, tv};
+  for (int k = 0; k < 6; ++k) {
+    block_reduce_store<256>(acc[k], d_part, k * gridDim.x + blockIdx.x);
+    __syncthreads();
+  }
+  __shared__ double mred[8];
+  for (int o = 16; o > 0; o >>= 1) mx = fmax(mx, __shfl_down_sync(0xffffffffu, mx, o));
+  if ((threadIdx.x & 31) == 0) mred[threadIdx.x >> 5] = mx;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double m = mred[0];
+    for (int w = 1; w < 8; ++w) m = fmax(m, mred[w]);
+    d_max[blockIdx.x] = m;
+  }
+}
+
 // Marginal over fixed-bit outcomes: blockIdx.y = outcome over the unique measured bits.
 template <typename R>
 __global__ void __launch_bounds__(256) k_marginal(const typename C2<R>::T* __restrict__ s, uint64_t work, Fixed f0,
@@ -717,6 +758,17 @@ cudaError_t launch_inner(const void* a, const void* b, int precision, int n, dou
   uint64_t N = 1ULL << n;
   if (precision == QG_C64) k_inner<float><<<nblocks, 256, 0, st>>>((const float2*)a, (const float2*)b, N, d_part);
   else k_inner<double><<<nblocks, 256, 0, st>>>((const double2*)a, (const double2*)b, N, d_part);
+  counted();
+  return cudaGetLastError();
+}
+
+cudaError_t launch_compare(const void* a, int precision, const void* b, int n, double* d_part, double* d_max,
+                           int nblocks, cudaStream_t st) {
+  uint64_t N = 1ULL << n;
+  if (precision == QG_C64)
+    k_compare<float><<<nblocks, 256, 0, st>>>((const float2*)a, (const double2*)b, N, d_part, d_max);
+  else
+    k_compare<double><<<nblocks, 256, 0, st>>>((const double2*)a, (const double2*)b, N, d_part, d_max);
   counted();
   return cudaGetLastError();
 }

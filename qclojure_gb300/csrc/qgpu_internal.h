@@ -238,6 +238,9 @@ cudaError_t launch_expect_1q(const void* s, int precision, int n, int bit, const
                              int nblocks, cudaStream_t st);
 cudaError_t launch_inner(const void* a, const void* b, int precision, int n, double* d_part, int nblocks,
                          cudaStream_t st);
+// a: complex64 or complex128, b: complex128; partials 6 x nblocks double-doubles, maxima nblocks
+cudaError_t launch_compare(const void* a, int precision, const void* b, int n, double* d_part, double* d_max,
+                           int nblocks, cudaStream_t st);
 // Marginal probabilities over measured bits: per outcome FP64 (sum, comp) and u64 quantised totals.
 cudaError_t launch_marginal_host(const void* s, int precision, int n, const int* h_bits, const int* d_bits, int m,
                                  int nbx, double* d_pm, unsigned long long* d_qm, cudaStream_t st);

@@ -433,6 +433,43 @@ static int st_inner(State* a, State* b, double* re, double* im, std::string* err
   return fetch_dd(a, a->d_part + 2 * a->nblocks, a->nblocks, im, err);
 }
 
+// out[0] = max_i |a_i - b_i|, out[1] = 1 - |<b|a>|^2 / (<a|a><b|b>), out[2] = total variation
+// distance of the outcome distributions, 1/2 sum_i | |a_i|^2 - |b_i|^2 |.
+static int st_compare(State* a, State* b, double* out, std::string* err) {
+  if (a->n != b->n || b->prec != QG_C128) {
+    *err = "the reference state must be complex128 of the same size";
+    return QG_ERR_INVALID_ARG;
+  }
+  CK(cudaStreamSynchronize(b->stream), "sync");
+  const int nb = a->nblocks;
+  double* d_buf = nullptr;
+  CK(cudaMallocAsync((void**)&d_buf, sizeof(double) * 13 * nb, a->stream), "alloc partials");
+  int rc = QG_OK;
+  double v[6] = {0, 0, 0, 0, 0, 0};
+  std::vector<double> mx(nb);
+  if (launch_compare(a->d, a->prec, b->d, a->n, d_buf, d_buf + 12 * nb, nb, a->stream) != cudaSuccess) {
+    *err = "compare launch failed";
+    rc = QG_ERR_DEVICE;
+  }
+  for (int k = 0; k < 6 && rc == QG_OK; ++k) rc = fetch_dd(a, d_buf + 2 * k * nb, nb, &v[k], err);
+  if (rc == QG_OK &&
+      (cudaMemcpyAsync(mx.data(), d_buf + 12 * nb, sizeof(double) * nb, cudaMemcpyDeviceToHost, a->stream) !=
+           cudaSuccess ||
+       cudaStreamSynchronize(a->stream) != cudaSuccess)) {
+    *err = "D2H maxima";
+    rc = QG_ERR_DEVICE;
+  }
+  cudaFreeAsync(d_buf, a->stream);
+  if (rc != QG_OK) return rc;
+  double m = 0;
+  for (double x : mx) m = std::max(m, x);
+  const double dd = v[0], zr = v[1], zi = v[2], na = v[3], nbn = v[4], tv = v[5];
+  out[0] = std::sqrt(m);
+  out[1] = (na > 0 && nbn > 0) ? (nbn * dd - (zr * zr + zi * zi)) / (na * nbn) : 1.0;
+  out[2] = 0.5 * tv;
+  return QG_OK;
+}
+
 static int st_sample(State* s, uint64_t shots, uint64_t seed, std::vector<uint64_t>* outcomes, std::string* err) {
   size_t scratch = sampler_scratch_bytes(s->n, shots);
   void* d_scratch = nullptr;
@@ -1890,6 +1927,14 @@ int qg_state_inner(void* a, void* b, double* re, double* im) {
   cudaSetDevice(s->ctx->device);
   std::string err;
   return state_err(s, st_inner(s, (State*)b, re, im, &err), err);
+}
+
+int qg_state_compare(void* state, void* reference, double* out3) {
+  if (!state || !reference || !out3) return QG_ERR_INVALID_ARG;
+  State* s = (State*)state;
+  cudaSetDevice(s->ctx->device);
+  std::string err;
+  return state_err(s, st_compare(s, (State*)reference, out3, &err), err);
 }
 
 int qg_state_measure(void* state, const int32_t* qubits, int32_t count, uint64_t seed, uint64_t* outcome_out,

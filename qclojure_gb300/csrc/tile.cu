@@ -403,35 +403,45 @@ __device__ __forceinline__ void swap_regs(typename P::Reg (&r)[kRegs], uint32_t 
   }
 }
 
-// dense 2^dk block applied in shared memory (exact policies only)
+// dense 2^dk block applied in shared memory (exact policies only). Each thread forms
+// output amplitudes as row sums over the block's 2^dk inputs, visiting the columns in
+// Gray-code order so that each step flips one tile bit of the input index. complex128
+// multiplies in FP64 with the entries as doubles; complex64 in FP32 with the entries
+// stored as float pairs.
 template <class P>
 __device__ void dense_smem(unsigned char* buf, const KOp& op, const double* dense, const TileGeo& g) {
   using V = typename P::Reg;
+  using R = decltype(V{}.x);
   constexpr int E = P::kElem;
   const int dk = (int)op.tmask, D = 1 << dk;
-  const double* M = dense + 2 * (int64_t)op.tval;
-  int dbits[5];
-#pragma unroll
-  for (int j = 0; j < 5; ++j) dbits[j] = (op.rmr >> (4 * j)) & 15;
+  const uint32_t dbits = op.rmr;  // 4 bits per block bit
   constexpr int kMaxItems = 16;
   V out[kMaxItems];
   int cnt = 0;
   for (int idx = threadIdx.x; idx < g.K; idx += g.T, ++cnt) {
     const int grp = idx >> dk, row = idx & (D - 1);
-    uint32_t lg = grp;
+    uint32_t lc = grp;
     for (int j = 0; j < dk; ++j) {
-      const int b = dbits[j];
-      lg = ((lg >> b) << (b + 1)) | (lg & ((1u << b) - 1));
+      const int b = (dbits >> (4 * j)) & 15;
+      lc = ((lc >> b) << (b + 1)) | (lc & ((1u << b) - 1));
     }
-    double ar = 0, ai = 0;
-    for (int col = 0; col < D; ++col) {
-      uint32_t lc = lg;
-      for (int j = 0; j < dk; ++j)
-        if ((col >> j) & 1) lc |= 1u << dbits[j];
+    R ar = 0, ai = 0;
+    for (int i = 0; i < D; ++i) {
+      if (i) lc ^= 1u << ((dbits >> (4 * (__ffs(i) - 1))) & 15);
+      const int e = row * D + (i ^ (i >> 1));
+      R mr, mi;
+      if constexpr (sizeof(R) == 8) {
+        const double2 m = __ldg(reinterpret_cast<const double2*>(dense) + op.tval + e);
+        mr = m.x;
+        mi = m.y;
+      } else {
+        const float2 m = __ldg(reinterpret_cast<const float2*>(dense) + op.tval + e);
+        mr = m.x;
+        mi = m.y;
+      }
       const V x = P::load_work(buf, swz<E>(lc));
-      const double mr = M[2 * (row * D + col)], mi = M[2 * (row * D + col) + 1];
-      ar = fma(mr, (double)x.x, fma(-mi, (double)x.y, ar));
-      ai = fma(mr, (double)x.y, fma(mi, (double)x.x, ai));
+      ar = fma(mr, x.x, fma(-mi, x.y, ar));
+      ai = fma(mr, x.y, fma(mi, x.x, ai));
     }
     V y;
     y.x = ar;
@@ -444,11 +454,11 @@ __device__ void dense_smem(unsigned char* buf, const KOp& op, const double* dens
     const int grp = idx >> dk, row = idx & (D - 1);
     uint32_t lg = grp;
     for (int j = 0; j < dk; ++j) {
-      const int b = dbits[j];
+      const int b = (dbits >> (4 * j)) & 15;
       lg = ((lg >> b) << (b + 1)) | (lg & ((1u << b) - 1));
     }
     for (int j = 0; j < dk; ++j)
-      if ((row >> j) & 1) lg |= 1u << dbits[j];
+      if ((row >> j) & 1) lg |= 1u << ((dbits >> (4 * j)) & 15);
     P::store_work(buf, swz<E>(lg), out[cnt]);
   }
   __syncthreads();

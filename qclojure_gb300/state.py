@@ -161,6 +161,14 @@ class DeviceState:
         self._ck(self.lib.qg_state_inner(self.h, other.h, C.byref(re), C.byref(im)))
         return complex(re.value, im.value)
 
+    def compare(self, reference: "DeviceState") -> dict:
+        """Distance from a complex128 state of the same size: the largest amplitude
+        difference, 1 - fidelity and the total variation distance of the outcome
+        distributions."""
+        out = (C.c_double * 3)()
+        self._ck(self.lib.qg_state_compare(self.h, reference.h, out))
+        return {"max_abs_diff": out[0], "one_minus_fidelity": out[1], "tvd": out[2]}
+
     def measure(self, qubits: list[int], seed: int) -> tuple[int, float]:
         arr = (C.c_int32 * len(qubits))(*qubits)
         o, p = C.c_uint64(), C.c_double()

@@ -133,6 +133,22 @@ def test_dense_fusion_c128(states, oracle, gpu_ctx, n, k):
     assert np.max(np.abs(got - ref)) <= 1e-12  # tolerance: FMA inside the 2^k x 2^k block product
 
 
+@pytest.mark.parametrize("k", [1, 3, 5])
+@pytest.mark.parametrize("n", [6, 15])
+def test_dense_fusion_c64(states, oracle, n, k):
+    """complex64 dense blocks multiply in FP32 (entries stored as float pairs)."""
+    from qclojure_gb300 import workloads
+    from qclojure_gb300.state import Context
+
+    c = workloads.layered_circuit(n, 10, seed=20 + k)
+    ref = oracle.run(c)
+    with Context(fusion="dense", fusion_width=k) as ctx:
+        with ctx.state(n, "c64") as st:
+            st.apply(c, fusion="dense")
+            got = st.download()
+    assert np.max(np.abs(got - ref)) <= 2e-5  # FP32 rounding of the block entries and sums
+
+
 @pytest.mark.parametrize("n", [4, 12, 16])
 @pytest.mark.parametrize("fusion", ["plain", "tiled"])
 def test_layered_c64(states, oracle, n, fusion):
@@ -251,6 +267,51 @@ def test_norm_and_inner(states, gpu_ctx, oracle):
         b.apply(c2)
         assert abs(a.norm2() - 1.0) <= 1e-13
         assert abs(a.inner(b) - oracle.inner(r1, r2)) <= 1e-12
+
+
+def _compare_numpy(a, r):
+    d = a.astype(np.complex128) - r
+    na, nr = np.vdot(a, a).real, np.vdot(r, r).real
+    z = np.vdot(r, d)
+    return {"max_abs_diff": np.max(np.abs(d)),
+            "one_minus_fidelity": (nr * np.vdot(d, d).real - abs(z) ** 2) / (na * nr),
+            "tvd": 0.5 * np.sum(np.abs(np.abs(a.astype(np.complex128)) ** 2 - np.abs(r) ** 2))}
+
+
+def test_state_compare(gpu_ctx, gpu_ctx_df, oracle):
+    """qg_state_compare against numpy on the downloaded states: two unrelated states, a
+    double-float and a complex64 run against the exact run of one circuit, identical states."""
+    from qclojure_gb300 import workloads
+
+    n = 13
+    c1 = workloads.layered_circuit(n, 12, seed=5)
+    c2 = workloads.layered_circuit(n, 12, seed=6)
+    with gpu_ctx.state(n) as x1, gpu_ctx.state(n) as x2, gpu_ctx_df.state(n) as f1, \
+            gpu_ctx.state(n, "c64") as s1:
+        x1.apply(c1)
+        x2.apply(c2)
+        f1.apply(c1)
+        s1.apply(c1)
+        r1 = x1.download()
+        assert np.array_equal(r1, oracle.run(c1))
+        far = x2.compare(x1)
+        want = _compare_numpy(x2.download(), r1)
+        assert want["one_minus_fidelity"] > 0.5
+        assert far["max_abs_diff"] == pytest.approx(want["max_abs_diff"], rel=1e-12)
+        assert far["one_minus_fidelity"] == pytest.approx(1 - abs(oracle.inner(r1, x2.download())) ** 2, rel=1e-10)
+        assert far["tvd"] == pytest.approx(want["tvd"], rel=1e-10)
+        for st, lo, hi in ((f1, 1e-17, 1e-12), (s1, 1e-9, 1e-4)):
+            got = st.compare(x1)
+            want = _compare_numpy(st.download(), r1)
+            assert lo <= got["max_abs_diff"] <= hi
+            assert got["max_abs_diff"] == pytest.approx(want["max_abs_diff"], rel=1e-12)
+            assert got["tvd"] == pytest.approx(want["tvd"], rel=1e-8)
+            assert got["one_minus_fidelity"] == pytest.approx(want["one_minus_fidelity"], rel=1e-6, abs=1e-28)
+            assert 0 <= got["one_minus_fidelity"] <= got["max_abs_diff"] ** 2 * 2 ** n
+        same = x1.compare(x1)
+        assert same == {"max_abs_diff": 0.0, "one_minus_fidelity": 0.0, "tvd": 0.0}
+        with pytest.raises(Exception):
+            x1.compare(s1)
 
 
 @pytest.mark.parametrize("fusion", ["plain", "tiled"])
