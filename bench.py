@@ -499,6 +499,27 @@ def main():
                                 "block_pass_gbs": bpp / (mean_k / 1e3) / 1e9 if tiles else None}
             dense[dprec] = rows
         line["dense_blocks"] = dense
+
+        # noisy trajectories (the hardware simulator's shot loop): the 10-qubit, 20-layer
+        # recipe with depolarizing noise on every gate type and readout errors, as batched
+        # device trajectories; shots with equal Kraus choices share one state
+        from qclojure_gb300.hardware import run_trajectories
+
+        noisy_c = workloads.layered_circuit(10, 20, args.seed + rank)
+        noisy = {"workload": "layered-10x20 (300 gates), depolarizing on every gate, readout 1%/2%"}
+        for label, p1, p2 in (("realistic", 0.001, 0.01), ("heavy", 0.02, 0.05)):
+            gn = {g: {"noise-type": "depolarizing", "noise-strength": p1} for g in workloads.LAYER_GATES}
+            gn["cnot"] = {"noise-type": "depolarizing", "noise-strength": p2}
+            nm = {"gate-noise": gn, "readout-error": {"prob-0-to-1": 0.01, "prob-1-to-0": 0.02}}
+            shots = 100_000
+            run_trajectories(ctx, noisy_c, nm, 1000, seed=1, max_trajectories=0)  # warm-up
+            t0 = time.perf_counter()
+            run = run_trajectories(ctx, noisy_c, nm, shots, seed=2, max_trajectories=0)
+            dt = time.perf_counter() - t0
+            noisy[label] = {"depolarizing": [p1, p2], "shots": shots, "shots_per_s": shots / dt, "ms": dt * 1e3,
+                            "device_ms": run["stats"]["device-ms"], "distinct_states": run["stats"]["distinct-states"],
+                            "noise_sites": run["stats"]["noise-sites"], "batches": run["stats"]["batches"]}
+        line["noisy_trajectories"] = noisy
         # batched parameter sweep: 1024 QAOA MaxCut circuits (p=3, n uniform over 12..24 even),
         # one launch per pass over all states of a size, replayed from CUDA graphs
         from qclojure_gb300.sweep import Sweep

@@ -110,6 +110,9 @@ enum {
   QG_OP_U = 70,               /* explicit 2x2 matrix m on q[0], applied like a 1-qubit gate */
   QG_OP_CU = 71,              /* explicit 2x2 matrix m on q[1], control q[0] (transposed, as the reference) */
   QG_OP_RZZ = 72,             /* exp(-i angle/2 Z(q0) Z(q1)); a diagonal extension for QAOA cost layers */
+  QG_OP_KRAUS = 73,           /* explicit 2x2 operator m on q[0], applied as a general matrix whatever its
+                                 entries and without renormalisation (noisy trajectories renormalise once,
+                                 after the last operation) */
   QG_OP_I = 80                /* identity: the reference dispatch has no case for it and fails */
 };
 
@@ -361,6 +364,67 @@ int qg_sweep_run(void* sweep, const int32_t* term_offsets, const double* coeffic
 /* Copy circuit c's final state (complex128) to the host. */
 int qg_sweep_state(void* sweep, int32_t c, double* host_c128);
 int qg_sweep_destroy(void* sweep);
+
+/* ---- noisy trajectories ----------------------------------------------------------
+   The hardware simulator's shot loop (adapter/backend/hardware_simulator.clj:84-193):
+   every shot runs the circuit from |0...0>, applying after each operation that has a
+   gate-noise entry one Kraus operator of that entry's channel on the operation's
+   :target (noise.clj:53-102); the operator is drawn with the probabilities
+   max_ij |K_ij|^2 of the channel's operators (channel.clj:194-232) and the state is
+   renormalised (channel.clj:127-171). The shot then samples one outcome from its final
+   state and applies readout noise with correlations (noise.clj:107-202). Shots run as
+   batched trajectories: the noise draws depend only on (seed, shot, site), so every
+   trajectory shares one compiled program and differs only in its Kraus matrices. */
+enum {
+  QG_NOISE_NONE = 0,               /* noise type the reference ignores (noise.clj:101)    */
+  QG_NOISE_DEPOLARIZING = 1,       /* {sqrt(1-p) I, sqrt(p/3) X, Y, Z}, channel.clj:40-63 */
+  QG_NOISE_AMPLITUDE_DAMPING = 2,  /* {[[1,0],[0,sqrt(1-g)]], [[0,sqrt g],[0,0]]}, :65-84 */
+  QG_NOISE_PHASE_DAMPING = 3,      /* {[[1,0],[0,sqrt(1-g)]], [[0,0],[0,sqrt g]]}, :86-104 */
+  QG_NOISE_COHERENT = 4            /* one rotation operator, channel.clj:106-125           */
+};
+enum { QG_NOISE_HAS_T1 = 1, QG_NOISE_HAS_T2 = 2, QG_NOISE_HAS_GATE_TIME = 4 };
+typedef struct qg_gate_noise {
+  int32_t noise_type;      /* QG_NOISE_*                                                  */
+  int32_t present;         /* QG_NOISE_HAS_* bits for t1_us, t2_us, gate_time_ns          */
+  double strength;         /* :noise-strength (the reference's default is 0.01)           */
+  double t1_us, t2_us;     /* :t1-time, :t2-time (microseconds)                           */
+  double gate_time_ns;     /* :gate-time (nanoseconds)                                    */
+  double coherent_angle;   /* :coherent-error :rotation-angle                             */
+  int32_t coherent_axis;   /* :rotation-axis 0 = :x, 1 = :y, 2 = :z                       */
+  int32_t pad;
+} qg_gate_noise;
+typedef struct qg_noise_model {
+  int32_t num_entries;            /* gate-noise entries                                    */
+  int32_t has_readout;            /* :readout-error present                                */
+  const qg_gate_noise* entries;
+  const int32_t* op_entry;        /* per circuit operation: its entry (looked up by the
+                                     operation's :operation-type), or -1 for none          */
+  const int32_t* op_target;       /* per circuit operation: (get-in op [:operation-params
+                                     :target] 0), the qubit the noise acts on              */
+  double prob_0_to_1, prob_1_to_0;
+  int32_t num_correlations;       /* :correlated-errors {source {target factor}} as triples */
+  int32_t pad;
+  const int32_t* corr_source;
+  const int32_t* corr_target;
+  const double* corr_factor;
+} qg_noise_model;
+typedef struct qg_noisy_stats {
+  double device_ms;        /* device time: state set-up, passes, renormalisation, sampling */
+  double total_ms;         /* wall time of the call                                       */
+  int32_t batches;         /* device batches of trajectories                              */
+  int32_t batch_size;      /* trajectories per batch                                      */
+  int64_t noise_sites;     /* Kraus operators per trajectory                              */
+  int64_t passes;          /* tiled HBM passes per batch                                  */
+  int64_t distinct_states; /* states simulated: shots with equal Kraus choices share one  */
+} qg_noisy_stats;
+/* Run `shots` trajectories of `circuit` (no mid-circuit measurements) in `precision`
+   (complex128 with the context's arithmetic, or complex64). outcomes[s] is the basis
+   index read in shot s after readout noise (qubit q <-> bit n-1-q). trajectories, if not
+   NULL, receives the first min(shots, max_trajectories) final states, renormalised, as
+   complex128 (2 * 2^n doubles each); final_state, if not NULL, the last shot's. */
+int qg_noisy_run(void* ctx, const qg_circuit* circuit, const qg_noise_model* noise, uint64_t shots, uint64_t seed,
+                 int32_t precision, int32_t max_trajectories, uint64_t* outcomes, double* trajectories,
+                 double* final_state, qg_noisy_stats* stats);
 
 /* ---- measurement (no counterpart in the reference) ----------------------------
    qg_state_profile applies a circuit like qg_state_apply and records a CUDA event

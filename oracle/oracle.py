@@ -6,6 +6,7 @@ CPU-baseline / reference arm of bench.py, never by the product package.
 from __future__ import annotations
 
 import ctypes as C
+import math
 import sys
 from pathlib import Path
 
@@ -45,6 +46,8 @@ def lib():
         L.or_draw64.argtypes = [C.c_uint64, C.c_uint64, C.c_uint32]
         L.or_draw64.restype = C.c_uint64
         L.or_refalgo_rows.argtypes = [DP, C.c_int, DP, C.c_int, C.c_uint64, C.c_uint64, DP]
+        L.or_sample_one.argtypes = [DP, C.c_int, C.c_uint64, C.c_uint64, C.c_uint32]
+        L.or_sample_one.restype = C.c_uint64
         _lib = L
     return _lib
 
@@ -138,3 +141,149 @@ def refalgo_rows(x: np.ndarray, gate2x2, target: int, row0: int, nrows: int) -> 
     lib().or_refalgo_rows(_dp(np.ascontiguousarray(x)), n, _dp(g), target, C.c_uint64(row0), C.c_uint64(nrows),
                           _dp(y))
     return y
+
+
+# ---------------------------------------------------------------------------
+# Noisy trajectories (adapter/backend/hardware_simulator.clj:84-193). Each shot
+# restated as the reference runs it: the operation, then, if its :operation-type has
+# a gate-noise entry, one Kraus operator of that channel on its :target chosen by the
+# draw (seed, shot, 0x40000000 + site), applied and renormalised (QG_OP_KRAUS of
+# qgo.c); one outcome drawn with (seed, shot, 2); readout noise with one draw per
+# qubit (seed, shot, 0x20000000 + qubit).
+# ---------------------------------------------------------------------------
+_KRAUS_STREAM, _READOUT_STREAM, _MEASURE_STREAM = 0x40000000, 0x20000000, 2
+
+
+def _key(k) -> str:
+    s = str(k)
+    return s[1:] if s.startswith(":") else s
+
+
+def _uniform(seed: int, index: int, stream: int) -> float:
+    return (lib().or_draw64(C.c_uint64(seed), C.c_uint64(index), C.c_uint32(stream)) >> 11) * 2.0 ** -53
+
+
+def kraus_channel(cfg: dict) -> list[np.ndarray] | None:
+    """The Kraus operators apply-gate-noise builds (noise.clj:73-99, channel.clj:40-125,
+    :234-250); None for a noise type it ignores. Raises ValueError where the reference's
+    preconditions fail."""
+    t = _key(cfg.get("noise-type"))
+    strength = cfg.get("noise-strength", 0.01)
+    t1, t2, gt = cfg.get("t1-time"), cfg.get("t2-time"), cfg.get("gate-time")
+
+    def deco(a, b, g):
+        if not (a > 0 and b > 0 and g > 0):
+            raise ValueError("decoherence parameters must be positive")
+        us = g / 1000.0
+        return 1.0 - math.exp(-(us / a)), 1.0 - math.exp(-(us / b))
+
+    if t == "depolarizing":
+        p = strength
+        if not (0 <= p <= 1) or p > 0.75:
+            raise ValueError("depolarizing probability out of range")
+        a, b = math.sqrt(1.0 - p), math.sqrt(p / 3.0)
+        return [np.array([[a, 0], [0, a]], complex), np.array([[0, b], [b, 0]], complex),
+                np.array([[0, -1j * b], [1j * b, 0]], complex), np.array([[b, 0], [0, -b]], complex)]
+    if t in ("amplitude-damping", "phase-damping"):
+        g = strength
+        if t == "amplitude-damping" and t1 is not None and gt is not None:
+            g = deco(t1, t2 if t2 is not None else t1, gt)[0]
+        if t == "phase-damping" and t2 is not None and gt is not None:
+            g = deco(t1 if t1 is not None else t2, t2, gt)[1]
+        if not (0 <= g <= 1):
+            raise ValueError("damping parameter out of range")
+        k0 = np.array([[1, 0], [0, math.sqrt(1.0 - g)]], complex)
+        k1 = (np.array([[0, math.sqrt(g)], [0, 0]], complex) if t == "amplitude-damping"
+              else np.array([[0, 0], [0, math.sqrt(g)]], complex))
+        return [k0, k1]
+    if t == "coherent":
+        ce = cfg.get("coherent-error") or {"rotation-angle": 0.01, "rotation-axis": "z"}
+        th, ax = ce["rotation-angle"], _key(ce["rotation-axis"])
+        c, s_ = math.cos(th / 2.0), math.sin(th / 2.0)
+        if ax == "x":
+            return [np.array([[c, -s_], [s_, c]], complex)]
+        if ax == "y":
+            return [np.array([[c, s_], [-s_, c]], complex)]
+        if ax == "z":
+            return [np.array([[math.cos(th), 0], [0, math.cos(-th)]], complex)]
+        raise ValueError("rotation axis")
+    return None
+
+
+def choose_kraus(ops: list[np.ndarray], u: float) -> int:
+    """apply-quantum-channel (channel.clj:194-232): probabilities max_ij |K_ij|^2."""
+    if len(ops) == 1:
+        return 0
+    probs = [max(z.real * z.real + z.imag * z.imag for z in m.ravel()) for m in ops]
+    cum = 0.0
+    for i, p in enumerate(probs):
+        nc = cum + p
+        if u < nc or i >= len(ops) - 1:
+            return i
+        cum = nc
+    return len(ops) - 1
+
+
+def readout_noise(outcome: int, n: int, readout: dict | None, seed: int, shot: int) -> int:
+    """calculate-final-bitstring (noise.clj:107-160)."""
+    if not readout:
+        return outcome
+    corr = {int(a): {int(b): f for b, f in (row or {}).items()}
+            for a, row in (readout.get("correlated-errors") or {}).items()}
+    bits = outcome
+    hist: list[int] = []
+    for q in range(n):
+        b = n - 1 - q
+        bit = (bits >> b) & 1
+        base = readout["prob-1-to-0"] if bit else readout["prob-0-to-1"]
+        f = 1.0
+        if corr and hist:
+            for src in hist:
+                if q in corr.get(src, {}):
+                    f *= corr[src][q]
+        eff = min(1.0, max(0.0, base * f))
+        if _uniform(seed, shot, _READOUT_STREAM + q) < eff:
+            bits ^= 1 << b
+            hist.append(q)
+    return bits
+
+
+def noisy_shots(circuit: dict, noise_model: dict | None, shots: int, seed: int):
+    """(outcomes after readout noise, final states) of `shots` noisy shots."""
+    nm = noise_model or {}
+    gate_noise = {_key(k): v for k, v in (nm.get("gate-noise") or {}).items()}
+    n = circuit["num-qubits"]
+    chans = {}
+    outs, states = [], []
+    for shot in range(shots):
+        s = zero_state(n)
+        site = 0
+        for op in circuit["operations"]:
+            enc = encode({"num-qubits": n, "operations": [op]})
+            rc = lib().or_run_circuit(_dp(s), n, enc.array, enc.count, C.c_uint64(seed))
+            if rc:
+                raise ValueError("oracle rejected an operation")
+            name = _key(op.get("operation-type"))
+            cfg = gate_noise.get(name)
+            if cfg is None:
+                continue
+            if name not in chans:
+                chans[name] = kraus_channel(cfg)
+            ops = chans[name]
+            if ops is None:
+                continue
+            k = choose_kraus(ops, _uniform(seed, shot, _KRAUS_STREAM + site)) if len(ops) > 1 else 0
+            site += 1
+            kop = A.QgOp()
+            kop.opcode = A.OP["kraus"]
+            kop.nq = 1
+            kop.q[0] = int((op.get("operation-params") or {}).get("target", 0) or 0)
+            for j, z in enumerate(ops[k].ravel()):
+                kop.m[2 * j], kop.m[2 * j + 1] = z.real, z.imag
+            rc = lib().or_run_circuit(_dp(s), n, C.pointer(kop), 1, C.c_uint64(seed))
+            if rc:
+                raise ValueError("oracle rejected a Kraus operator")
+        o = int(lib().or_sample_one(_dp(s), n, C.c_uint64(seed), C.c_uint64(shot), C.c_uint32(_MEASURE_STREAM)))
+        outs.append(readout_noise(o, n, nm.get("readout-error"), seed, shot))
+        states.append(s)
+    return np.array(outs, np.uint64), np.array(states)

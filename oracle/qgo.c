@@ -35,6 +35,10 @@
  *    probabilities quantised to 2^-62, so CPU and GPU agree on the same seed.
  *  - Pauli expectation Re<psi|P|psi>, char i of the string on qubit i
  *    (domain/observables.clj:216-251, domain/hamiltonian.clj:82-114).
+ *  - QG_OP_KRAUS (noisy trajectories): the operator's 2x2 matrix on its qubit
+ *    (apply-matrix-to-amplitude, domain/channel.clj:127-146), then normalize-state
+ *    (state.clj:524-551): every amplitude times 1/norm when norm > 1e-12
+ *    (apply-single-qubit-kraus-operator, domain/channel.clj:148-192).
  */
 #include <math.h>
 #include <stdint.h>
@@ -258,6 +262,20 @@ int or_apply_op(double* s, int n, const qg_op* op, uint64_t seed, uint64_t* meas
       for (int k = 0; k < 4; ++k) g[k] = mk(op->m[2 * k], op->m[2 * k + 1]);
       apply_1q(s, n, op->q[0], g);
       return ORC_OK;
+    case QG_OP_KRAUS: {
+      if (!check_q(n, op->q[0])) return ORC_ERR;
+      for (int k = 0; k < 4; ++k) g[k] = mk(op->m[2 * k], op->m[2 * k + 1]);
+      apply_1q(s, n, op->q[0], g);
+      uint64_t N = 1ULL << n;
+      double acc = 0.0;
+      for (uint64_t i = 0; i < N; ++i) acc += s[2 * i] * s[2 * i] + s[2 * i + 1] * s[2 * i + 1];
+      double norm = sqrt(acc);
+      if (norm > 0 && norm > 1e-12) {
+        double inv = 1.0 / norm;
+        for (uint64_t i = 0; i < 2 * N; ++i) s[i] *= inv;
+      }
+      return ORC_OK;
+    }
     case QG_OP_CNOT: case QG_OP_CZ: case QG_OP_CY: case QG_OP_CRX: case QG_OP_CRY: case QG_OP_CRZ:
     case QG_OP_RYDBERG_CZ: case QG_OP_CU: {
       int c = op->q[0], t = op->q[1];
@@ -389,6 +407,21 @@ int or_sample(const double* s, int n, uint64_t shots, uint64_t seed, uint64_t* o
   }
   free(C);
   return 0;
+}
+
+/* One outcome of a normalised state for the draw (seed, index, stream): the first i
+   whose cumulative quantised probability exceeds floor(r64 T / 2^64) (measure-state,
+   state.clj:869-913, with the sampler's integer prefix sums). */
+uint64_t or_sample_one(const double* s, int n, uint64_t seed, uint64_t index, uint32_t stream) {
+  uint64_t N = 1ULL << n, T = 0;
+  for (uint64_t i = 0; i < N; ++i) T += or_quantize(s[2 * i] * s[2 * i] + s[2 * i + 1] * s[2 * i + 1]);
+  if (T == 0) return 0;
+  uint64_t u = mulhi64(or_draw64(seed, index, stream), T), c = 0;
+  for (uint64_t i = 0; i < N; ++i) {
+    c += or_quantize(s[2 * i] * s[2 * i] + s[2 * i + 1] * s[2 * i + 1]);
+    if (c > u) return i;
+  }
+  return N - 1;
 }
 
 /* Re<psi|P|psi> with the explicit Pauli action (observables.clj:216-251) */

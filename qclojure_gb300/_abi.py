@@ -59,8 +59,13 @@ OP = dict(
     cnot=20, cz=21, crx=22, cry=23, crz=24, cy=25, swap=26, iswap=27, toffoli=28, fredkin=29,
     rydberg_cz=40, rydberg_cphase=41, rydberg_blockade=42,
     global_rx=50, global_ry=51, global_rz=52, global_h=53, global_x=54, global_y=55, global_z=56,
-    measure=60, u=70, cu=71, rzz=72, i=80,
+    measure=60, u=70, cu=71, rzz=72, kraus=73, i=80,
 )
+
+# noise channels of qg_noisy_run
+QG_NOISE_NONE, QG_NOISE_DEPOLARIZING, QG_NOISE_AMPLITUDE_DAMPING, QG_NOISE_PHASE_DAMPING, QG_NOISE_COHERENT = range(5)
+NOISE_TYPES = {"depolarizing": 1, "amplitude-damping": 2, "phase-damping": 3, "coherent": 4}
+QG_NOISE_HAS_T1, QG_NOISE_HAS_T2, QG_NOISE_HAS_GATE_TIME = 1, 2, 4
 
 # result flags
 QG_RES_MEASUREMENTS = 1 << 0
@@ -128,6 +133,27 @@ class QgSweepStats(C.Structure):
                 ("state_bytes", C.c_uint64)]
 
 
+class QgGateNoise(C.Structure):
+    _fields_ = [("noise_type", C.c_int32), ("present", C.c_int32), ("strength", C.c_double),
+                ("t1_us", C.c_double), ("t2_us", C.c_double), ("gate_time_ns", C.c_double),
+                ("coherent_angle", C.c_double), ("coherent_axis", C.c_int32), ("pad", C.c_int32)]
+
+
+class QgNoiseModel(C.Structure):
+    _fields_ = [("num_entries", C.c_int32), ("has_readout", C.c_int32), ("entries", C.POINTER(QgGateNoise)),
+                ("op_entry", C.POINTER(C.c_int32)), ("op_target", C.POINTER(C.c_int32)),
+                ("prob_0_to_1", C.c_double), ("prob_1_to_0", C.c_double),
+                ("num_correlations", C.c_int32), ("pad", C.c_int32),
+                ("corr_source", C.POINTER(C.c_int32)), ("corr_target", C.POINTER(C.c_int32)),
+                ("corr_factor", C.POINTER(C.c_double))]
+
+
+class QgNoisyStats(C.Structure):
+    _fields_ = [("device_ms", C.c_double), ("total_ms", C.c_double), ("batches", C.c_int32),
+                ("batch_size", C.c_int32), ("noise_sites", C.c_int64), ("passes", C.c_int64),
+                ("distinct_states", C.c_int64)]
+
+
 P = C.c_void_p
 U64 = C.c_uint64
 I32 = C.c_int32
@@ -181,6 +207,8 @@ SIGNATURES = {
     "qg_state_norm2": ([P, DP], C.c_int),
     "qg_state_inner": ([P, P, DP, DP], C.c_int),
     "qg_state_compare": ([P, P, DP], C.c_int),
+    "qg_noisy_run": ([P, C.POINTER(QgCircuit), C.POINTER(QgNoiseModel), U64, U64, I32, I32, U64P, DP, DP,
+                      C.POINTER(QgNoisyStats)], C.c_int),
     "qg_state_measure": ([P, I32P, I32, U64, U64P, DP], C.c_int),
     "qg_state_device_ptr": ([P, C.POINTER(P), C.POINTER(P)], C.c_int),
     "qg_state_synchronize": ([P], C.c_int),

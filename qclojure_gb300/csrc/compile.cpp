@@ -159,6 +159,7 @@ int lower_circuit(const qg_circuit* c, std::vector<GOp>* gops, std::vector<std::
     return QG_ERR_INVALID_ARG;
   }
   auto inrange = [n](int q) { return q >= 0 && q < n; };
+  int32_t kraus_sites = 0;
   for (int k = 0; k < c->num_ops; ++k) {
     const qg_op& op = c->ops[k];
     const int oc = op.opcode;
@@ -180,6 +181,18 @@ int lower_circuit(const qg_circuit* c, std::vector<GOp>* gops, std::vector<std::
         if (oc == QG_OP_U) std::memcpy(m, op.m, sizeof(m));
         else gate_matrix(oc, op.angle, m);
         push(gops, classify(m, bitof(n, q), 0));
+      } break;
+      case QG_OP_KRAUS: {  // general matrix, tagged with its ordinal so the noisy runner can patch it
+        int q = op.q[0];
+        if (!inrange(q)) return qerr("Assert failed: (< qubit-index (:num-qubits state))");
+        GOp g;
+        std::memset(&g, 0, sizeof(g));
+        g.kind = OK_U2;
+        g.cls = U2_GENERAL;
+        g.t = bitof(n, q);
+        std::memcpy(g.m, op.m, sizeof(g.m));
+        g.tag = ++kraus_sites;
+        gops->push_back(g);
       } break;
       case QG_OP_CNOT: case QG_OP_CZ: case QG_OP_CY: case QG_OP_CRX: case QG_OP_CRY: case QG_OP_CRZ:
       case QG_OP_RYDBERG_CZ: case QG_OP_CU: {
@@ -450,6 +463,7 @@ TOp localize(const GOp& g, const int* lpos /* abs bit -> local or -1 */, int n) 
   t.flags = g.flags;
   t.dk = g.dk;
   t.doff = g.doff;
+  t.tag = (uint32_t)g.tag;
   std::memcpy(t.m, g.m, sizeof(t.m));
   auto split = [&](uint64_t mask, uint32_t* lm, uint64_t* gm) {
     *lm = 0;
@@ -550,6 +564,15 @@ void split_coeffs(TOp* t) {
     t->mf[8 + q] = (float)(t->m[q] - (double)hi);
   }
 }
+
+}  // namespace
+
+void set_op_matrix(TOp* t, const double m[8]) {
+  std::memcpy(t->m, m, sizeof(t->m));
+  split_coeffs(t);
+}
+
+namespace {
 
 // Insert OK_LAYOUT ops: consecutive ops whose non-diagonal bits fit in three
 // register bits form a group; the register positions are written into the ops.

@@ -762,6 +762,114 @@ cudaError_t launch_inner(const void* a, const void* b, int precision, int n, dou
   return cudaGetLastError();
 }
 
+// ---------------------------------------------------------------------------
+// Noisy trajectories: end of a shot. The Kraus operators were applied without
+// renormalisation, so each distinct trajectory state is first scaled by 1 / ||a||
+// (state.clj:524-551: every amplitude times (/ 1.0 norm)), one CTA per state. Then
+// every shot draws one outcome from its state the way the shot sampler draws:
+// quantised probabilities q_i = floor(p_i 2^62), their integer total T,
+// u = floor(r64 T / 2^64) and the first i whose inclusive prefix sum exceeds u, one
+// CTA per shot. Each thread owns a contiguous chunk of the state; the chunk sums are
+// scanned in shared memory and the chunk that holds u is walked by its thread.
+// ---------------------------------------------------------------------------
+template <typename R>
+__global__ void __launch_bounds__(256) k_traj_normalise(void* const* __restrict__ states, int n,
+                                                        double* __restrict__ norm2) {
+  using T = typename C2<R>::T;
+  T* s = reinterpret_cast<T*>(states[blockIdx.x]);
+  const uint64_t N = 1ULL << n;
+  const uint64_t chunk = (N + blockDim.x - 1) / blockDim.x;
+  const uint64_t lo = min(N, (uint64_t)threadIdx.x * chunk), hi = min(N, lo + chunk);
+  __shared__ DD red[8];
+  __shared__ double scale_sh;
+  DD acc{0, 0};
+  for (uint64_t i = lo; i < hi; ++i) two_sum_acc(acc, p_of<R>(s[i]));
+  for (int o = 16; o > 0; o >>= 1) {
+    DD w;
+    w.s = __shfl_down_sync(0xffffffffu, acc.s, o);
+    w.c = __shfl_down_sync(0xffffffffu, acc.c, o);
+    acc = dd_add(acc, w);
+  }
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = acc;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    DD t = red[0];
+    for (int w = 1; w < (int)(blockDim.x >> 5); ++w) t = dd_add(t, red[w]);
+    const double nn = t.s + t.c;
+    norm2[blockIdx.x] = nn;
+    scale_sh = nn > 0 ? 1.0 / sqrt(nn) : 0.0;
+  }
+  __syncthreads();
+  const double sc = scale_sh;
+  for (uint64_t i = lo; i < hi; ++i) {
+    T a = s[i];
+    a.x = (R)((double)a.x * sc);
+    a.y = (R)((double)a.y * sc);
+    s[i] = a;
+  }
+}
+
+template <typename R>
+__global__ void __launch_bounds__(256) k_traj_sample(void* const* __restrict__ states,
+                                                     const int32_t* __restrict__ state_of, int n, int shift,
+                                                     uint64_t seed, uint64_t traj0, uint32_t stream,
+                                                     uint64_t* __restrict__ out) {
+  using T = typename C2<R>::T;
+  const T* s = reinterpret_cast<const T*>(states[state_of[blockIdx.x]]);
+  const uint64_t N = 1ULL << n;
+  const uint64_t chunk = (N + blockDim.x - 1) / blockDim.x;
+  const uint64_t lo = min(N, (uint64_t)threadIdx.x * chunk), hi = min(N, lo + chunk);
+  __shared__ unsigned long long pre[256];
+  unsigned long long q = 0;
+  for (uint64_t i = lo; i < hi; ++i) q += quant(p_of<R>(s[i]));
+  pre[threadIdx.x] = q;
+  __syncthreads();
+  for (unsigned o = 1; o < blockDim.x; o <<= 1) {  // inclusive scan of the chunk sums
+    const unsigned long long add = threadIdx.x >= o ? pre[threadIdx.x - o] : 0ULL;
+    __syncthreads();
+    pre[threadIdx.x] += add;
+    __syncthreads();
+  }
+  const unsigned long long total = pre[blockDim.x - 1];
+  if (total == 0) {
+    if (threadIdx.x == 0) out[blockIdx.x] = 0;
+    return;
+  }
+  const unsigned long long u = __umul64hi(draw64(seed, traj0 + blockIdx.x, stream), total);
+  const unsigned long long before = pre[threadIdx.x] - q;
+  if (u >= before && u < pre[threadIdx.x]) {
+    unsigned long long c = before;
+    for (uint64_t i = lo; i < hi; ++i) {
+      c += quant(p_of<R>(s[i]));
+      if (c > u) {
+        out[blockIdx.x] = i >> shift;
+        break;
+      }
+    }
+  }
+}
+
+cudaError_t launch_traj_normalise(int precision, void* const* d_states, int nstates, int n, double* d_norm2,
+                                  cudaStream_t st) {
+  if (nstates < 1) return cudaSuccess;
+  if (precision == QG_C64) k_traj_normalise<float><<<nstates, 256, 0, st>>>(d_states, n, d_norm2);
+  else k_traj_normalise<double><<<nstates, 256, 0, st>>>(d_states, n, d_norm2);
+  counted();
+  return cudaGetLastError();
+}
+
+cudaError_t launch_traj_sample(int precision, void* const* d_states, const int32_t* d_state_of, int nshots, int n,
+                               int shift, uint64_t seed, uint64_t traj0, uint32_t stream, uint64_t* d_out,
+                               cudaStream_t st) {
+  if (nshots < 1) return cudaSuccess;
+  if (precision == QG_C64)
+    k_traj_sample<float><<<nshots, 256, 0, st>>>(d_states, d_state_of, n, shift, seed, traj0, stream, d_out);
+  else
+    k_traj_sample<double><<<nshots, 256, 0, st>>>(d_states, d_state_of, n, shift, seed, traj0, stream, d_out);
+  counted();
+  return cudaGetLastError();
+}
+
 cudaError_t launch_compare(const void* a, int precision, const void* b, int n, double* d_part, double* d_max,
                            int nblocks, cudaStream_t st) {
   uint64_t N = 1ULL << n;

@@ -59,7 +59,7 @@ struct GOp {
   uint64_t val;
   double m[8];
   int32_t dbits[5];
-  int32_t pad;
+  int32_t tag;      // 1 + ordinal of the QG_OP_KRAUS operation it came from, 0 otherwise
   int64_t doff;     // offset (in complex entries) of a dense block in the pass's matrix buffer
 };
 
@@ -77,7 +77,7 @@ struct TOp {
   uint32_t lcmask;   // local control mask
   uint32_t lmask;    // local part of mask
   uint32_t lval;     // local part of val
-  uint32_t pad0;
+  uint32_t tag;      // GOp::tag
   uint64_t gcmask;   // non-local control bits (absolute)
   uint64_t gmask;    // non-local part of mask (absolute)
   uint64_t gval;     // non-local part of val (absolute)
@@ -175,6 +175,13 @@ struct TileJobRec {
 cudaError_t launch_tile_jobs(int precision, int arithmetic, int n, const TileJobRec* d_jobs, int njobs,
                              const void* d_kops, const int32_t* d_pass_nops, cudaStream_t st);
 size_t kop_record_bytes();
+// Context services (runtime.cpp) for the noisy-trajectory runner (noisy.cpp).
+int ctx_device_of(void* ctx);
+int ctx_arithmetic_of(void* ctx);
+void ctx_report_error(void* ctx, const std::string& msg);
+int ctx_compile_tiled(void* ctx, const qg_circuit* c, int precision, Program* prog, std::string* err);
+// Set the 2x2 matrix of a tiled op (and its float-pair split for the float policies).
+void set_op_matrix(TOp* t, const double m[8]);
 // ---------------------------------------------------------------------------
 // Specialised pass kernels (pass_kernels.cpp): every tiled pass of a program
 // (complex64, or complex128 double-float) compiled by NVRTC into its own
@@ -214,6 +221,15 @@ int diag_max_groups();
 size_t diag_state_bytes();
 void fill_diag_state(void* out, uint64_t zoff, int ngroups, const int* gcount, const int* nid);
 cudaError_t launch_batch_zero(void* slab, int precision, int n, int nstates, cudaStream_t st);
+// Noisy trajectories: one CTA per state renormalises it in place and records its
+// squared norm before renormalisation; one CTA per shot draws an outcome of state
+// d_state_of[shot] (draw64(seed, traj0 + shot, stream)), shifted right by `shift`
+// (states padded with idle low qubits).
+cudaError_t launch_traj_normalise(int precision, void* const* d_states, int nstates, int n, double* d_norm2,
+                                  cudaStream_t st);
+cudaError_t launch_traj_sample(int precision, void* const* d_states, const int32_t* d_state_of, int nshots, int n,
+                               int shift, uint64_t seed, uint64_t traj0, uint32_t stream, uint64_t* d_out,
+                               cudaStream_t st);
 int diag_max_terms_per_group();
 uint32_t diag_qmask(uint64_t z);  // bit q: parity of q & bits 8..11 of z
 cudaError_t launch_diag_expect(void* const* d_states, int precision, int n, const void* d_diag, const uint64_t* d_z,

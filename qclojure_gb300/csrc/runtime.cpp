@@ -631,6 +631,17 @@ static void set_ctx_error(Ctx* c, const std::string& e) {
   c->last_error = e;
 }
 
+// ---------------------------------------------------------------------------
+// Context services for the noisy-trajectory runner (noisy.cpp)
+// ---------------------------------------------------------------------------
+int ctx_device_of(void* ctx) { return ((Ctx*)ctx)->device; }
+int ctx_arithmetic_of(void* ctx) { return ((Ctx*)ctx)->cfg.arithmetic; }
+void ctx_report_error(void* ctx, const std::string& msg) { set_ctx_error((Ctx*)ctx, msg); }
+int ctx_compile_tiled(void* ctx, const qg_circuit* c, int precision, Program* prog, std::string* err) {
+  Ctx* cx = (Ctx*)ctx;
+  return compile_program(c, precision, QG_FUSE_TILED, cx->cfg.fuse_k, cx->cfg.arithmetic, prog, err, true);
+}
+
 static size_t job_bytes(int n, int prec) {
   size_t st = amp_bytes(prec) << n;
   return st + st / 4 + (64ULL << 20);  // state + sampler/probability scratch headroom
