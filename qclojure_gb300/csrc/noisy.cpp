@@ -22,6 +22,7 @@
 #include <cmath>
 #include <cstring>
 #include <string>
+#include <thread>
 #include <unordered_map>
 #include <vector>
 
@@ -182,6 +183,24 @@ struct Site {
   int pass;    // tiled pass holding its op
   int64_t at;  // index of its op within the pass
 };
+
+// Run body(begin, end) over [0, count) on the host's cores.
+template <class F>
+void parallel_for(uint64_t count, uint64_t grain, F body) {
+  const unsigned hw = std::max(1u, std::thread::hardware_concurrency());
+  const uint64_t parts = std::min<uint64_t>(hw, std::max<uint64_t>(1, count / std::max<uint64_t>(1, grain)));
+  if (parts <= 1) {
+    body(0, count);
+    return;
+  }
+  std::vector<std::thread> th;
+  const uint64_t per = (count + parts - 1) / parts;
+  for (uint64_t t = 0; t < parts; ++t) {
+    const uint64_t b = t * per, e = std::min(count, b + per);
+    if (b < e) th.emplace_back(body, b, e);
+  }
+  for (auto& x : th) x.join();
+}
 
 double ms_between(std::chrono::steady_clock::time_point a) {
   return std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - a).count();
@@ -398,14 +417,19 @@ extern "C" int qg_noisy_run(void* ctx, const qg_circuit* circuit, const qg_noise
     // Kraus choices of every shot, and the distinct choice vectors
     reps.clear();
     seen.clear();
-    for (uint64_t m = 0; m < nb; ++m) {
-      uint8_t* cv = choices.data() + m * S;
-      for (size_t s = 0; s < S; ++s) {
-        const Channel& ch = chans[sites[s].entry];
-        cv[s] = (uint8_t)(ch.ops.size() > 1
-                              ? choose(ch, uniform01(draw64(seed, base + m, kStreamKraus + (uint32_t)s)))
-                              : 0);
+    parallel_for(nb, 256, [&](uint64_t b, uint64_t e) {
+      for (uint64_t m = b; m < e; ++m) {
+        uint8_t* cv = choices.data() + m * S;
+        for (size_t s = 0; s < S; ++s) {
+          const Channel& ch = chans[sites[s].entry];
+          cv[s] = (uint8_t)(ch.ops.size() > 1
+                                ? choose(ch, uniform01(draw64(seed, base + m, kStreamKraus + (uint32_t)s)))
+                                : 0);
+        }
       }
+    });
+    for (uint64_t m = 0; m < nb; ++m) {
+      const uint8_t* cv = choices.data() + m * S;
       auto it = seen.emplace(std::string((const char*)cv, S), (int32_t)reps.size());
       if (it.second) reps.push_back(m);
       state_of[m] = it.first->second;
@@ -423,18 +447,21 @@ extern "C" int qg_noisy_run(void* ctx, const qg_circuit* circuit, const qg_noise
       }
     }
     // op records of the distinct states: pass-major, states contiguous within a pass
-    for (uint64_t u = 0; u < U; ++u) {
-      const uint8_t* cv = choices.data() + reps[u] * S;
-      for (size_t p = 0; p < P; ++p) {
-        unsigned char* dst = h_kops + rec * (size_t)(rec_off[p] * (int64_t)U + (int64_t)u * nops[p]);
-        std::memcpy(dst, tmpl.data() + rec * (size_t)rec_off[p], rec * (size_t)nops[p]);
+    parallel_for(U, 64, [&](uint64_t b, uint64_t e) {
+      for (uint64_t u = b; u < e; ++u) {
+        const uint8_t* cv = choices.data() + reps[u] * S;
+        for (size_t p = 0; p < P; ++p) {
+          unsigned char* dst = h_kops + rec * (size_t)(rec_off[p] * (int64_t)U + (int64_t)u * nops[p]);
+          std::memcpy(dst, tmpl.data() + rec * (size_t)rec_off[p], rec * (size_t)nops[p]);
+        }
+        for (size_t s = 0; s < S; ++s) {
+          const Site& si = sites[s];
+          unsigned char* dst =
+              h_kops + rec * (size_t)(rec_off[si.pass] * (int64_t)U + (int64_t)u * nops[si.pass] + si.at);
+          std::memcpy(dst, variants[s].data() + rec * (size_t)cv[s], rec);
+        }
       }
-      for (size_t s = 0; s < S; ++s) {
-        const Site& si = sites[s];
-        unsigned char* dst = h_kops + rec * (size_t)(rec_off[si.pass] * (int64_t)U + (int64_t)u * nops[si.pass] + si.at);
-        std::memcpy(dst, variants[s].data() + rec * (size_t)cv[s], rec);
-      }
-    }
+    });
     ok = cuda_check(cudaEventRecord(e0, st), "event") &&
          cuda_check(cudaMemcpyAsync(d_kops, h_kops, rec * (size_t)R * U, cudaMemcpyHostToDevice, st), "H2D records") &&
          cuda_check(cudaMemcpyAsync(d_state_of, state_of.data(), sizeof(int32_t) * nb, cudaMemcpyHostToDevice, st),
@@ -468,9 +495,11 @@ extern "C" int qg_noisy_run(void* ctx, const qg_circuit* circuit, const qg_noise
         err = "State is not properly normalized (trajectory " + std::to_string(base + m) + ")";
         break;
       }
-      outcomes[base + m] = apply_readout(h_out[m], n, ro, seed, base + m);
     }
     if (result != QG_OK) break;
+    parallel_for(nb, 1024, [&](uint64_t b, uint64_t e) {
+      for (uint64_t m = b; m < e; ++m) outcomes[base + m] = apply_readout(h_out[m], n, ro, seed, base + m);
+    });
     // final states: the first max_trajectories shots, and the last shot
     const uint64_t N = 1ULL << n, Nr = 1ULL << n_run;
     for (uint64_t m = 0; m < nb; ++m) {
