@@ -520,6 +520,36 @@ def main():
                             "device_ms": run["stats"]["device-ms"], "distinct_states": run["stats"]["distinct-states"],
                             "noise_sites": run["stats"]["noise-sites"], "batches": run["stats"]["batches"]}
         line["noisy_trajectories"] = noisy
+
+        # variational loop client: Adam with parameter-shift gradients on QAOA MaxCut
+        # (20 qubits, p = 3, 6 parameters): each step is one sweep of 13 circuits (the new
+        # point and its 12 shifted points); beside it the same step as 13 separate circuits
+        try:
+            from qclojure_gb300 import variational as V
+
+            vw = workloads.qaoa_maxcut(20, 3, 17)
+            vf = lambda prm: V.qaoa_maxcut_circuit(20, vw["edges"], prm)  # noqa: E731
+            vp0 = [x for pair in zip(vw["gammas"], vw["betas"]) for x in pair]
+            vobj = V.BatchedObjective(ctx, vw["hamiltonian"], vf)
+            V.adam_optimization(vobj, vp0, {"learning-rate": 0.02, "max-iterations": 3, "tolerance": 0})  # warm-up
+            t0 = time.perf_counter()
+            vres = V.adam_optimization(vobj, vp0, {"learning-rate": 0.02, "max-iterations": 21, "tolerance": 0})
+            vdt = time.perf_counter() - t0
+            vobj.close()
+            steps = len(vres["convergence-history"])
+            hterms = [(t["coefficient"], t["pauli-string"]) for t in vw["hamiltonian"]]
+            t0 = time.perf_counter()
+            for prm in [vp0] + V.shifted_points(vp0, V.DEFAULT_SHIFT):
+                with ctx.state(20, "c128") as s1:
+                    s1.apply(vf(prm))
+                    s1.hamiltonian(hterms)
+            plain_step = time.perf_counter() - t0
+            line["variational"] = {"workload": "Adam, QAOA MaxCut n=20 p=3 (6 parameters), parameter-shift gradients",
+                                   "steps": steps, "steps_per_s": steps / vdt, "circuits_per_step": 13,
+                                   "energy_first_last": [vres["convergence-history"][0], vres["convergence-history"][-1]],
+                                   "plain_step_ms": plain_step * 1e3, "batched_step_ms": vdt / steps * 1e3}
+        except Exception as e:  # the line must still print
+            line["variational"] = {"error": f"{type(e).__name__}: {e}"}
         # batched parameter sweep: 1024 QAOA MaxCut circuits (p=3, n uniform over 12..24 even),
         # one launch per pass over all states of a size, replayed from CUDA graphs
         from qclojure_gb300.sweep import Sweep
