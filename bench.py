@@ -550,6 +550,21 @@ def main():
                                    "plain_step_ms": plain_step * 1e3, "batched_step_ms": vdt / steps * 1e3}
         except Exception as e:  # the line must still print
             line["variational"] = {"error": f"{type(e).__name__}: {e}"}
+
+        # OpenQASM ingestion (host): the 40 random layers of the workload (1800 gates)
+        # emitted as OpenQASM 3 and parsed back, then submitted as a job
+        from qclojure_gb300 import qasm as Q
+
+        qc = workloads.layered_circuit(n, args.depth, args.seed + rank)
+        t0 = time.perf_counter()
+        qtext = Q.circuit_to_qasm3(qc)
+        t1 = time.perf_counter()
+        parsed = Q.qasm3_to_circuit(qtext)
+        t2 = time.perf_counter()
+        line["qasm"] = {"workload": f"layered-{n}x{args.depth} as OpenQASM 3 ({len(qc['operations'])} gates, "
+                                    f"{len(qtext)} bytes)", "emit_ms": (t1 - t0) * 1e3, "parse_ms": (t2 - t1) * 1e3,
+                        "gates_per_s": len(qc["operations"]) / (t2 - t1),
+                        "round_trip_equal": parsed["operations"] == qc["operations"]}
         # batched parameter sweep: 1024 QAOA MaxCut circuits (p=3, n uniform over 12..24 even),
         # one launch per pass over all states of a size, replayed from CUDA graphs
         from qclojure_gb300.sweep import Sweep
