@@ -565,6 +565,16 @@ def main():
                                     f"{len(qtext)} bytes)", "emit_ms": (t1 - t0) * 1e3, "parse_ms": (t2 - t1) * 1e3,
                         "gates_per_s": len(qc["operations"]) / (t2 - t1),
                         "round_trip_equal": parsed["operations"] == qc["operations"]}
+
+        # gate and qubit optimisation stages of the hardware pipeline (host), on the workload
+        from qclojure_gb300 import optimization as OPT
+
+        t0 = time.perf_counter()
+        optr = OPT.optimize(circ)
+        line["optimization"] = {"workload": f"layered-{n}x{args.depth}+qft{n} ({gates} gates)",
+                                "ms": (time.perf_counter() - t0) * 1e3,
+                                "gates_after": len(optr["circuit"]["operations"]),
+                                "qubits_after": optr["circuit"]["num-qubits"]}
         # batched parameter sweep: 1024 QAOA MaxCut circuits (p=3, n uniform over 12..24 even),
         # one launch per pass over all states of a size, replayed from CUDA graphs
         from qclojure_gb300.sweep import Sweep

@@ -309,10 +309,17 @@ class HardwareSimulator:
         job_id = f"job_{next(self._ids)}_{int(time.time() * 1000)}"
         job = {"id": job_id, "circuit": circuit, "options": dict(options or {}), "device": self._current,
                "status": "queued", "result": None, "created-at": time.time() * 1000, "completed-at": None}
-        if not circuit.get("operations"):
-            # the hardware optimisation of submit-circuit rejects empty circuits
+        # submit-circuit runs the hardware optimisation pipeline and executes the original
+        # circuit: the pipeline only decides whether the job fails (hardware_simulator.clj:300-330)
+        from .optimization import OptimizationError, optimize
+
+        opts = dict(options or {})
+        try:
+            optimize(circuit, {"optimize-gates?": opts.get("optimize-gates?", True),
+                               "optimize-qubits?": opts.get("optimize-qubits?", True)})
+        except OptimizationError as e:
             job.update({"status": "failed", "completed-at": time.time() * 1000,
-                        "result": {"job-status": "failed", "error-message": "Circuit has no operations"}})
+                        "result": {"job-status": "failed", "error-message": str(e)}})
             with self._lock:
                 self._jobs[job_id] = job
             return job_id
