@@ -341,7 +341,10 @@ class HardwareSimulator:
                 if job["status"] != "queued":
                     continue
                 job["status"] = "running"
-            res = execute_circuit(job["circuit"], job["device"], job["options"], ctx=self._ctx)
+            try:
+                res = execute_circuit(job["circuit"], job["device"], job["options"], ctx=self._ctx)
+            except Exception as e:  # a job that raises fails; the worker keeps serving
+                res = {"job-status": "failed", "error-message": f"{type(e).__name__}: {e}"}
             with self._cv:
                 job["result"] = res
                 job["status"] = res["job-status"]
