@@ -251,6 +251,25 @@ def serving_leg(num_jobs=100, rates=(100, 1000, 5000), seed=11):
 
 
 # ---------------------------------------------------------------------------
+def max_over_ranks(ms: float, dist=None, device: str = "cpu") -> float:
+    """The slowest rank's time: every rank runs its own replica (no data exchange), and
+    the job is done when the last one is."""
+    if dist is None:
+        return ms
+    import torch
+
+    t = torch.tensor([ms], device=device, dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    dist.barrier()
+    return float(t.item())
+
+
+def whole_job_rate(world: int, units_per_rank: float, ms_per_step: float) -> float:
+    """Units processed by all replicas per second (weak scaling: fixed work per rank)."""
+    return world * units_per_rank / (ms_per_step / 1e3)
+
+
+# ---------------------------------------------------------------------------
 def run_reference(args):
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
@@ -351,13 +370,9 @@ def main():
     ck = clocks.stop()
     torch.cuda.synchronize()
     elapsed_ms = e0.elapsed_time(e1)
-    if dist:
-        t = torch.tensor([elapsed_ms], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        elapsed_ms = float(t.item())
-        dist.barrier()
+    elapsed_ms = max_over_ranks(elapsed_ms, dist, "cuda")
     ms_per_step = elapsed_ms / args.steps
-    value = world * gates * N / (ms_per_step / 1e3)
+    value = whole_job_rate(world, gates * N, ms_per_step)
 
     # per-pass timing (separate, untimed run) for the roofline of the dominant kernel
     enc = encode(circ)
