@@ -265,7 +265,10 @@ class HardwareSimulator:
 
         self.config = config or {"max-qubits": 16}
         self._devices = list(devices or [])
-        noiseless = {"id": "noiseless", "name": "Noiseless device", "noise-model": {}}
+        from .circuit import NATIVE_SIMULATOR_GATE_SET
+
+        noiseless = {"id": "noiseless", "name": "Noiseless device", "noise-model": {},
+                     "native-gates": set(NATIVE_SIMULATOR_GATE_SET)}
         if device is not None:
             self._devices.append(device)
         self._current = device or (self._devices[0] if self._devices else noiseless)
@@ -315,8 +318,11 @@ class HardwareSimulator:
 
         opts = dict(options or {})
         try:
-            optimize(circuit, {"optimize-gates?": opts.get("optimize-gates?", True),
-                               "optimize-qubits?": opts.get("optimize-qubits?", True)})
+            optimize(circuit, self._current, {
+                "optimize-gates?": opts.get("optimize-gates?", True),
+                "optimize-qubits?": opts.get("optimize-qubits?", True),
+                "transform-operations?": opts.get("transform-operations?", True),
+                "max-iterations": opts.get("max-iterations", 100)})
         except OptimizationError as e:
             job.update({"status": "failed", "completed-at": time.time() * 1000,
                         "result": {"job-status": "failed", "error-message": str(e)}})

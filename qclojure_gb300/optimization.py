@@ -1,8 +1,9 @@
 """The first stages of the reference's hardware optimisation pipeline on the host.
 
 application/hardware_optimization.clj:42-109 runs gate optimisation, qubit
-optimisation, error correction, topology routing and gate decomposition. The first
-two are restated here, as the reference defines them:
+optimisation, error correction, topology routing and gate decomposition. Gate
+optimisation, qubit optimisation and gate decomposition are restated here, as the
+reference defines them:
 
 * `optimize_gates` (domain/gate_optimization.clj:776-860): repeat until nothing
   changes: cancel S/S†, T/T† and self-inverse pairs that meet with no gate between them
@@ -12,6 +13,10 @@ two are restated here, as the reference defines them:
   A circuit optimised to nothing is an error ("Optimization resulted in an empty circuit").
 * `optimize_qubit_usage` (domain/qubit_optimization.clj:104-150): renumber the qubits
   that operations use to 0..k-1 and shrink the register.
+* `transform_circuit` (domain/circuit_transformation.clj:21-74 with
+  gate_decomposition.clj): decompose operations the device does not support through
+  the operation catalog's decomposition entries, one at a time, at most
+  :max-iterations (100) steps ("Maximum iterations reached during circuit transformation").
 
 The hardware simulator calls the pipeline on submission and runs the original
 circuit (hardware_simulator.clj:300-330): the pipeline only decides whether a job
@@ -256,9 +261,159 @@ def optimize_qubit_usage(circuit: dict, options: dict | None = None) -> tuple[di
     return out, mapping
 
 
-def optimize(circuit: dict, options: dict | None = None) -> dict:
-    """The pipeline's first stages (hardware_optimization.clj:42-109 steps 1-2)."""
+# ---------------------------------------------------------------------------
+# Gate decomposition (domain/gate_decomposition.clj, with the decomposition entries of
+# the operation catalog, domain/operation_registry.clj:53-370)
+# ---------------------------------------------------------------------------
+_PI = math.pi
+# vector steps are tuples (gate, specs...), keyword steps plain strings
+CATALOG_DECOMPOSITIONS = {
+    "x": {"universal": ["ry"], "parametric-fn": lambda _: [("ry", _PI)], "rz-only": ["rz", "h", "rz", "h"]},
+    "y": {"universal": ["s", "x", "s-dag"],
+          "parametric-fn": lambda _: [("rz", _PI / 2), ("ry", _PI), ("rz", _PI / -2)],
+          "t-basis": ["t", "t", "x", "t", "t", "t", "t"]},
+    "z": {"universal": ["t", "t", "t", "t"], "parametric-fn": lambda _: [("rz", _PI)], "s-basis": ["s", "s"]},
+    "i": {"universal": [], "parametric-fn": lambda _: [], "nop": True},
+    "h": None,
+    "s": {"universal": ["t", "t"], "parametric-fn": lambda _: [("rz", _PI / 2)]},
+    "s-dag": {"universal": ["t-dag", "t-dag"], "parametric-fn": lambda _: [("rz", _PI / -2)]},
+    "t": None,
+    "t-dag": {"parametric-fn": lambda _: [("rz", _PI / -4)]},
+    "rx": {"universal-fn": lambda th: [("h",), ("rz", th), ("h",)],
+           "ry-rz-fn": lambda th: [("ry", _PI / 2), ("rz", th), ("ry", _PI / -2)]},
+    "ry": {"universal-fn": lambda th: [("rx", _PI / 2), ("rz", th), ("rx", _PI / -2)]},
+    "rz": None,
+    "phase": ["rz"],
+    "cnot": None,
+    "cz": {"cnot-h": [("h", "target"), ("cnot", "control", "target"), ("h", "target")]},
+    "cy": {"cnot-s": [("s-dag", "target"), ("cnot", "control", "target"), ("s", "target")]},
+    "swap": {"cnot": [("cnot", "target1", "target2"), ("cnot", "target2", "target1"), ("cnot", "target1", "target2")]},
+    "iswap": {"cnot-s": [("s", "target1"), ("s", "target2"), ("h", "target1"), ("cnot", "target1", "target2"),
+                         ("cnot", "target2", "target1"), ("h", "target2")]},
+    "crx": ["cnot", "rx"], "cry": ["cnot", "ry"], "crz": ["cnot", "rz"],
+    "toffoli": {"cnot-t": [("h", "target"), ("cnot", "control2", "target"), ("t-dag", "target"),
+                           ("cnot", "control1", "target"), ("t", "target"), ("cnot", "control2", "target"),
+                           ("t-dag", "target"), ("cnot", "control1", "target"), ("t", "control2"), ("t", "target"),
+                           ("cnot", "control1", "control2"), ("h", "target"), ("t", "control1"),
+                           ("t-dag", "control2"), ("cnot", "control1", "control2")]},
+    "fredkin": {"cnot-toffoli": [("cnot", "target2", "target1"), ("toffoli", "control", "target1", "target2"),
+                                 ("cnot", "target2", "target1")]},
+    "rydberg-cz": {"standard": ["cz"]},
+    "rydberg-cphase": {"standard-fn": lambda phi: [("crz", phi)]},
+    "rydberg-blockade": None,
+    **{g: {"single-qubit-fn": None} for g in ("global-rx", "global-ry", "global-rz", "global-h", "global-x",
+                                               "global-y", "global-z")},
+    "measure": None,
+}
+_SELECT = ("target", "control", "control1", "control2", "target1", "target2")
+
+
+def _select(params: dict) -> dict:
+    return {k: params[k] for k in _SELECT if k in params}
+
+
+def _step_op(step, params: dict) -> dict:
+    if isinstance(step, tuple):
+        g, specs = step[0], step[1:]
+        if g in ("rz", "rx", "ry") and len(specs) == 1 and isinstance(specs[0], (int, float)):
+            p = {"target": params.get("target"), "angle": specs[0]}
+        elif g == "cnot":
+            if len(specs) < 2:
+                raise OptimizationError("decomposition step without operands")
+            p = {"control": params.get(specs[0]), "target": params.get(specs[1])}
+        elif g in ("h", "x", "y", "z", "s", "s-dag", "t", "t-dag"):
+            p = {"target": params.get(specs[0])} if specs else {"target": params.get("target")}
+        else:
+            p = _select(params)
+        return {"operation-type": g, "operation-params": p}
+    return {"operation-type": step, "operation-params": _select(params)}
+
+
+def decompose_operation(op: dict, supported) -> list:
+    """decompose-operation (gate_decomposition.clj:50-234)."""
+    g = op.get("operation-type")
+    params = op.get("operation-params") or {}
+    sup = supported if supported is not None else frozenset()
+    if g in sup:
+        return [op]
+    decs = CATALOG_DECOMPOSITIONS.get(g)
+    if decs is None:
+        if g == "t" and "rz" in sup and "t" not in sup:
+            return [{"operation-type": "rz", "operation-params": {**params, "angle": math.pi / 4}}]
+        return [op]
+    get = (lambda k: decs.get(k)) if isinstance(decs, dict) else (lambda k: None)
+    angle = params.get("angle")  # Clojure truthiness: any number, 0.0 included, is true
+    if angle is not None and get("parametric-fn"):
+        steps = get("parametric-fn")(angle)
+    elif get("parametric-fn") and angle is None and "rz" in sup:
+        steps = get("parametric-fn")(None)
+    elif angle is not None and get("universal-fn"):
+        steps = get("universal-fn")(angle)
+    elif supported is not None:
+        steps = ((get("cnot") or get("cnot-h") or get("cnot-t") or get("cnot-s")) if "cnot" in sup else None) \
+            or get("universal") or (decs if isinstance(decs, list) else None)
+    else:
+        steps = get("universal")
+    if steps is None:
+        return [op]
+    return [_step_op(st, params) for st in steps]
+
+
+def transform_operations(ops: list, supported, max_iterations: int = 100) -> list:
+    """transform-operations (gate_decomposition.clj:236-289): replace the first
+    operation needing decomposition until none is left; an operation type that does not
+    decompose is left as it is."""
+    sup = supported if supported is not None else frozenset()
+    cur, processed = list(ops), set()
+    for _ in range(max_iterations):
+        idx = next((i for i, o in enumerate(cur)
+                    if o.get("operation-type") not in processed and o.get("operation-type") not in sup), None)
+        if idx is None:
+            return cur
+        op = cur[idx]
+        idx = cur.index(op)
+        dec = decompose_operation(op, supported)
+        if dec == [op]:
+            processed.add(op.get("operation-type"))
+        cur = cur[:idx] + dec + cur[idx + 1:]
+    raise OptimizationError("Maximum iterations reached during circuit transformation")
+
+
+def transform_circuit(circuit: dict, device: dict | None = None, options: dict | None = None) -> dict:
+    """transform-circuit (circuit_transformation.clj:21-74)."""
     o = options or {}
+    if not o.get("transform-operations?", True):
+        return {"circuit": circuit}
+    d = device or {}
+    supported = d.get("supported-operations", d.get("native-gates"))
+    ops = list(circuit.get("operations") or [])
+    new = transform_operations(ops, supported, o.get("max-iterations", 100)) \
+        if o.get("transform-unsupported?", True) else ops
+    sup = supported if supported is not None else frozenset()
+    seen = []
+    for x in new:
+        t = x.get("operation-type")
+        if t not in seen:
+            seen.append(t)
+    return {"circuit": {**circuit, "operations": new}, "transformed-operation-count": len(new) - len(ops),
+            "unsupported-operations": [t for t in seen if t not in sup]}
+
+
+def optimize(circuit: dict, device: dict | None = None, options: dict | None = None) -> dict:
+    """The pipeline of hardware_optimization.clj:42-109 without error correction and
+    topology routing: gate optimisation, qubit optimisation, gate decomposition and the
+    check that every remaining operation is supported."""
+    o = options or {}
+    if o.get("apply-error-correction?") or o.get("optimize-topology?"):
+        raise OptimizationError("error correction and topology routing are not built")
     c = optimize_gates(circuit, o)
     c, mapping = optimize_qubit_usage(c, o)
-    return {"circuit": c, "qubit-mapping": mapping, "pipeline-order": ["gate-cancellation", "qubit-optimization"]}
+    tr = transform_circuit(c, device, o)
+    c = tr["circuit"]
+    d = device or {}
+    supported = d.get("supported-operations", d.get("native-gates")) or frozenset()
+    unsupported = sorted({x.get("operation-type") for x in c["operations"]} - set(supported))
+    return {"circuit": c, "qubit-mapping": mapping, "all-gates-supported?": not unsupported,
+            "final-unsupported-gates": unsupported,
+            "transformed-operation-count": tr.get("transformed-operation-count", 0),
+            "pipeline-order": ["gate-cancellation", "qubit-optimization", "gate-decomposition", "validation"]}

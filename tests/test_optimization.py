@@ -98,3 +98,57 @@ def test_optimised_circuit_same_state_up_to_phase(oracle):
     assert len(opt["operations"]) <= len(c["operations"])
     a, b = oracle.run(c), oracle.run(opt)
     assert abs(abs(np.vdot(a, b)) - 1.0) <= 1e-12
+
+
+def test_transform_circuit_cases():
+    # circuit_transformation_test.clj:25-136
+    c = C(2, g("h", target=0), g("t", target=1), g("cnot", control=0, target=1))
+    r = O.transform_circuit(c, {"supported-operations": {"h", "x", "z", "rz", "cnot"}})
+    assert set(types(r["circuit"])) <= {"h", "x", "z", "rz", "cnot"}
+    assert r["circuit"]["operations"][1] == g("rz", target=1, angle=math.pi / 4)
+    bell = C(2, g("h", target=0), g("cnot", control=0, target=1))
+    r = O.transform_circuit(bell, {"supported-operations": {"h", "cnot"}})
+    assert r["transformed-operation-count"] == 0 and r["unsupported-operations"] == [] and r["circuit"] == bell
+    assert O.transform_circuit(C(1, g("t", target=0)), {"supported-operations": {"h"}},
+                               {"transform-operations?": False})["circuit"] == C(1, g("t", target=0))
+    r = O.transform_circuit(C(1, g("h", target=0)), {"supported-operations": set()})
+    assert r["unsupported-operations"] == ["h"]
+    r = O.transform_circuit(C(1), {"supported-operations": {"h"}})
+    assert r["transformed-operation-count"] == 0 and r["unsupported-operations"] == []
+
+
+def test_decomposition_rules():
+    sup = {"h", "rz", "cnot", "t", "t-dag"}
+    # toffoli: the 15-step CNOT+T form; cz through H-CNOT-H
+    tof = O.decompose_operation(g("toffoli", control1=0, control2=1, target=2), sup)
+    assert len(tof) == 15 and tof[1] == g("cnot", control=1, target=2) and tof[8] == g("t", target=1)
+    assert O.decompose_operation(g("cz", control=0, target=1), sup) == \
+        [g("h", target=1), g("cnot", control=0, target=1), g("h", target=1)]
+    # fixed-angle gates through the parametric form when RZ is supported
+    assert O.decompose_operation(g("s", target=0), sup) == [g("rz", target=0, angle=math.pi / 2)]
+    assert O.decompose_operation(g("x", target=3), sup) == [g("ry", target=3, angle=math.pi)]
+    # rotations through their universal form, keeping the angle
+    assert O.decompose_operation(g("rx", target=0, angle=0.3), sup) == \
+        [g("h", target=0), g("rz", target=0, angle=0.3), g("h", target=0)]
+    # the phase gate's entry is a bare [:rz]: the angle is not carried over
+    assert O.decompose_operation(g("phase", target=0, angle=0.3), sup) == [g("rz", target=0)]
+    # SWAP's steps name target1/target2, which a SWAP operation does not have
+    assert O.decompose_operation(g("swap", qubit1=0, qubit2=1), sup)[0] == g("cnot", control=None, target=None)
+    # an operation without a usable decomposition stays, and is left alone afterwards
+    assert O.decompose_operation(g("h", target=0), {"cnot"}) == [g("h", target=0)]
+    assert O.transform_operations([g("h", target=0)] * 3, {"cnot"}) == [g("h", target=0)] * 3
+
+
+def test_transform_iteration_limit():
+    ops = [g("s", target=q % 4) for q in range(150)]
+    with pytest.raises(O.OptimizationError, match="Maximum iterations"):
+        O.transform_operations(ops, {"h", "rz", "cnot"}, 100)
+    assert len(O.transform_operations(ops[:40], {"h", "rz", "cnot"}, 100)) == 40
+
+
+def test_pipeline_on_submission_shapes():
+    dev = {"native-gates": {"h", "cnot", "rz", "x"}}
+    r = O.optimize(C(3, g("h", target=0), g("t", target=2), g("cnot", control=0, target=2)), dev)
+    assert r["circuit"]["num-qubits"] == 2 and r["all-gates-supported?"] and r["qubit-mapping"] == {0: 0, 2: 1}
+    with pytest.raises(O.OptimizationError):
+        O.optimize(C(1, g("h", target=0), g("h", target=0)), dev)
