@@ -399,6 +399,61 @@ def transform_circuit(circuit: dict, device: dict | None = None, options: dict |
             "unsupported-operations": [t for t in seen if t not in sup]}
 
 
+# ---------------------------------------------------------------------------
+# Reverse qubit mappings (domain/qubit_mapping.clj:19-200)
+# ---------------------------------------------------------------------------
+def compose_mappings(m1: dict | None, m2: dict | None) -> dict | None:
+    """A -> B then B -> C gives A -> C; values missing from m2 pass through."""
+    if m1 is None or m2 is None:
+        return None
+    return {k: m2.get(v, v) for k, v in m1.items()}
+
+
+def invert_simple_mapping(m: dict | None) -> dict | None:
+    return None if m is None else {v: k for k, v in m.items()}
+
+
+def invert_vector_mapping(m: dict | None) -> dict | None:
+    return None if m is None else {p: k for k, vec in m.items() for p in vec}
+
+
+def create_all_reverse_mappings(ctx: dict) -> dict:
+    """create-all-reverse-mappings (qubit_mapping.clj:83-147)."""
+    out = dict(ctx)
+    if ctx.get("qubit-mapping"):
+        out["inverse-qubit-mapping"] = invert_simple_mapping(ctx["qubit-mapping"])
+    l2p = ctx.get("logical-to-physical")
+    if l2p:
+        first = next(iter(l2p.values()))
+        out["physical-to-logical"] = (invert_vector_mapping(l2p) if isinstance(first, (list, tuple))
+                                      else invert_simple_mapping(l2p))
+    if ctx.get("logical-to-ancillas"):
+        out["ancilla-to-logical"] = invert_vector_mapping(ctx["logical-to-ancillas"])
+    return out
+
+
+def map_qubit_to_original(qubit: int, ctx: dict):
+    """map-qubit-to-original (qubit_mapping.clj:149-182): through physical-to-logical
+    (error correction or topology) and then the inverse qubit mapping; None when either
+    is absent, as in the reference."""
+    p2l = ctx.get("physical-to-logical")
+    compacted = p2l.get(qubit) if p2l else None
+    inv = ctx.get("inverse-qubit-mapping")
+    if compacted is None or not inv:
+        return None
+    return inv.get(compacted, compacted)
+
+
+def map_measurements_to_original(measurements: dict, ctx: dict) -> dict:
+    """map-measurements-to-original (qubit_mapping.clj:184-202)."""
+    out = {}
+    for q, v in measurements.items():
+        o = map_qubit_to_original(q, ctx)
+        if o is not None:
+            out[o] = v
+    return out
+
+
 def optimize(circuit: dict, device: dict | None = None, options: dict | None = None) -> dict:
     """The pipeline of hardware_optimization.clj:42-109 without error correction and
     topology routing: gate optimisation, qubit optimisation, gate decomposition and the
@@ -413,7 +468,10 @@ def optimize(circuit: dict, device: dict | None = None, options: dict | None = N
     d = device or {}
     supported = d.get("supported-operations", d.get("native-gates")) or frozenset()
     unsupported = sorted({x.get("operation-type") for x in c["operations"]} - set(supported))
-    return {"circuit": c, "qubit-mapping": mapping, "all-gates-supported?": not unsupported,
+    ctx = create_all_reverse_mappings({"qubit-mapping": mapping})
+    return {"circuit": c, "qubit-mapping": mapping, "inverse-qubit-mapping": ctx.get("inverse-qubit-mapping"),
+            "all-gates-supported?": not unsupported,
             "final-unsupported-gates": unsupported,
             "transformed-operation-count": tr.get("transformed-operation-count", 0),
-            "pipeline-order": ["gate-cancellation", "qubit-optimization", "gate-decomposition", "validation"]}
+            "pipeline-order": ["gate-cancellation", "qubit-optimization", "gate-decomposition", "reverse-mappings",
+                               "validation"]}

@@ -152,3 +152,17 @@ def test_pipeline_on_submission_shapes():
     assert r["circuit"]["num-qubits"] == 2 and r["all-gates-supported?"] and r["qubit-mapping"] == {0: 0, 2: 1}
     with pytest.raises(O.OptimizationError):
         O.optimize(C(1, g("h", target=0), g("h", target=0)), dev)
+
+
+def test_reverse_mappings():
+    # qubit_mapping.clj docstring examples and the lookup chain
+    assert O.compose_mappings({0: 10, 1: 20}, {10: 100, 20: 200}) == {0: 100, 1: 200}
+    assert O.invert_simple_mapping({0: 0, 2: 1, 4: 2}) == {0: 0, 1: 2, 2: 4}
+    assert O.invert_vector_mapping({0: [0, 1, 2], 1: [3, 4, 5]}) == {0: 0, 1: 0, 2: 0, 3: 1, 4: 1, 5: 1}
+    ctx = O.create_all_reverse_mappings({"qubit-mapping": {0: 0, 2: 1}, "logical-to-physical": {0: 5, 1: 7}})
+    assert ctx["inverse-qubit-mapping"] == {0: 0, 1: 2} and ctx["physical-to-logical"] == {5: 0, 7: 1}
+    assert O.map_measurements_to_original({5: 1, 7: 0, 9: 1}, ctx) == {0: 1, 2: 0}
+    only_compaction = O.create_all_reverse_mappings({"qubit-mapping": {0: 0, 2: 1}})
+    assert O.map_qubit_to_original(1, only_compaction) is None  # needs a physical-to-logical step
+    r = O.optimize(C(3, g("h", target=0), g("x", target=2)), {"native-gates": {"h", "x"}})
+    assert r["inverse-qubit-mapping"] == {0: 0, 1: 2}
