@@ -251,6 +251,38 @@ def serving_leg(num_jobs=100, rates=(100, 1000, 5000), seed=11):
 
 
 # ---------------------------------------------------------------------------
+def cpu_statevector_rates(args, rank: int) -> dict:
+    """Beside the reference's algorithm, the best CPU figure: an optimised CPU state
+    vector (oracle/cpu_sv.c: one in-place pass per gate, OpenMP on all host cores,
+    complex128), NOT the reference. Bounded samples of the workload: its first 300 gates
+    at 24 qubits and its first 12 gates at 30 qubits, after one gate that touches the
+    state's pages."""
+    try:
+        import numpy as np
+
+        from oracle import oracle as ORC
+        from qclojure_gb300 import workloads
+
+        lib = ORC.cpu_sv_lib()
+        if lib is None:
+            return {"unavailable": "the CPU state-vector library could not be built"}
+        out = {"label": "not the reference: optimised CPU state vector, all host cores", "threads": int(lib.sv_threads())}
+        for sn, sg in ((24, 300), (30, 12)):
+            ops = workloads.large_circuit(sn, args.depth, args.seed + rank)["operations"][:sg + 1]
+            sv = np.zeros(1 << sn, np.complex128)
+            sv[0] = 1
+            ORC.cpu_sv_run({"num-qubits": sn, "operations": ops[:1]}, sv)
+            t0 = time.perf_counter()
+            ORC.cpu_sv_run({"num-qubits": sn, "operations": ops[1:]}, sv)
+            dt = time.perf_counter() - t0
+            out[f"n{sn}"] = {"gates": sg, "s": dt, "gate_amps_per_s": sg * 2 ** sn / dt}
+            del sv
+        return out
+    except Exception as e:  # the line must still print
+        return {"error": f"{type(e).__name__}: {e}"}
+
+
+# ---------------------------------------------------------------------------
 def max_over_ranks(ms: float, dist=None, device: str = "cpu") -> float:
     """The slowest rank's time: every rank runs its own replica (no data exchange), and
     the job is done when the last one is."""
@@ -677,6 +709,7 @@ def main():
         line["serving"] = serving_leg()
         rate, desc, threads = cpu_reference_rate(n, gates, 8.0)
         line["cpu_baseline"] = {"value": rate, "unit": UNIT, "cores": threads, "kind": "port", "sample": desc}
+        line["cpu_baseline"]["optimised_statevector"] = cpu_statevector_rates(args, rank)
     else:
         st.close()
     ctx.close()

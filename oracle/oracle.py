@@ -287,3 +287,41 @@ def noisy_shots(circuit: dict, noise_model: dict | None, shots: int, seed: int):
         outs.append(readout_noise(o, n, nm.get("readout-error"), seed, shot))
         states.append(s)
     return np.array(outs, np.uint64), np.array(states)
+
+
+# ---------------------------------------------------------------------------
+# The optimised CPU state-vector baseline (oracle/cpu_sv.c): NOT the reference's
+# algorithm; it only gives the benchmark's "best CPU" figure beside the GPU's.
+# ---------------------------------------------------------------------------
+_sv = None
+
+
+def cpu_sv_lib():
+    """libcpusv.so, or None when it could not be built."""
+    global _sv
+    if _sv is None:
+        from oracle.build import build_cpu_sv
+
+        path = build_cpu_sv()
+        if path is None:
+            return None
+        L = C.CDLL(str(path))
+        L.sv_run_circuit.argtypes = [C.POINTER(C.c_double), C.c_int, C.POINTER(A.QgOp), C.c_int]
+        L.sv_run_circuit.restype = C.c_int
+        L.sv_threads.restype = C.c_int
+        _sv = L
+    return _sv
+
+
+def cpu_sv_run(circuit: dict, state: np.ndarray | None = None) -> np.ndarray:
+    """Run a circuit from |0...0> (or in place on `state`) with the CPU baseline."""
+    L = cpu_sv_lib()
+    if L is None:
+        raise RuntimeError("the CPU state-vector baseline could not be built")
+    n = circuit["num-qubits"]
+    s = zero_state(n) if state is None else state
+    enc = encode(circuit)
+    rc = L.sv_run_circuit(_dp(s), n, enc.array, enc.count)
+    if rc:
+        raise ValueError(f"CPU baseline does not implement operation {rc - 1}")
+    return s

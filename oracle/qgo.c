@@ -97,6 +97,17 @@ static void gate_matrix(int opcode, double angle, cpx g[4]) {
   }
 }
 
+/* The matrix of gate_matrix as 8 doubles (re, im of m00 m01 m10 m11), for the CPU
+   state-vector baseline built beside the oracle. */
+void or_gate_matrix8(int opcode, double angle, double m[8]) {
+  cpx g[4];
+  gate_matrix(opcode, angle, g);
+  for (int k = 0; k < 4; ++k) {
+    m[2 * k] = g[k].re;
+    m[2 * k + 1] = g[k].im;
+  }
+}
+
 /* apply-single-qubit-gate (gate.clj:355-395): y_r = g_r0*x_lo + g_r1*x_hi */
 static void apply_1q(double* s, int n, int q, const cpx g[4]) {
   uint64_t N = 1ULL << n, tb = 1ULL << (n - 1 - q);
