@@ -98,3 +98,22 @@ def test_noisy_shots_without_noise_are_ideal(oracle):
     assert np.all(np.abs(states - ref) <= 1e-15)
     assert [int(o) for o in outs] == [int(oracle.lib().or_sample_one(
         oracle._dp(ref), 5, 4, s, 2)) for s in range(20)]
+
+
+def test_shot_statistics_match_the_channel_mixture(oracle):
+    """Over many shots the oracle's outcome frequency matches the mixture its channel
+    defines: sum_k p_k |<0|K_k psi>|^2 / ||K_k psi||^2, then readout flips."""
+    th = 0.7
+    c = {"num-qubits": 1, "operations": [{"operation-type": "ry", "operation-params": {"target": 0, "angle": th}}]}
+    p, p01, p10 = 0.3, 0.05, 0.1
+    nm = {"gate-noise": {"ry": {"noise-type": "depolarizing", "noise-strength": p}},
+          "readout-error": {"prob-0-to-1": p01, "prob-1-to-0": p10}}
+    psi = np.array([math.cos(th / 2), math.sin(th / 2)], complex)
+    probs = [1 - p, p / 3, p / 3, p / 3]
+    mats = [np.eye(2), np.array([[0, 1], [1, 0]]), np.array([[0, -1j], [1j, 0]]), np.diag([1, -1])]
+    p0 = sum(w * abs((m @ psi)[0]) ** 2 / np.vdot(m @ psi, m @ psi).real for w, m in zip(probs, mats))
+    want = p0 * (1 - p01) + (1 - p0) * p10
+    shots = 20000
+    outs, _ = oracle.noisy_shots(c, nm, shots, seed=17)
+    got = float(np.mean(outs == 0))
+    assert abs(got - want) <= 4 * math.sqrt(want * (1 - want) / shots)
