@@ -455,23 +455,31 @@ def map_measurements_to_original(measurements: dict, ctx: dict) -> dict:
 
 
 def optimize(circuit: dict, device: dict | None = None, options: dict | None = None) -> dict:
-    """The pipeline of hardware_optimization.clj:42-109 without error correction and
-    topology routing: gate optimisation, qubit optimisation, gate decomposition and the
-    check that every remaining operation is supported."""
+    """The pipeline of hardware_optimization.clj:42-109 without error correction: gate
+    optimisation, qubit optimisation, topology-aware routing (`topology.py`, when
+    "optimize-topology?"), gate decomposition, reverse mappings and validation. The
+    context threads through the stages as in the reference, including where a stage
+    replaces it (routing on a device with native SWAP) and validation's lookup of the
+    supported operations on the context itself (so every gate type is reported)."""
+    from .topology import topology_aware_transform
+
     o = options or {}
-    if o.get("apply-error-correction?") or o.get("optimize-topology?"):
-        raise OptimizationError("error correction and topology routing are not built")
-    c = optimize_gates(circuit, o)
-    c, mapping = optimize_qubit_usage(c, o)
-    tr = transform_circuit(c, device, o)
-    c = tr["circuit"]
-    d = device or {}
-    supported = d.get("supported-operations", d.get("native-gates")) or frozenset()
-    unsupported = sorted({x.get("operation-type") for x in c["operations"]} - set(supported))
-    ctx = create_all_reverse_mappings({"qubit-mapping": mapping})
-    return {"circuit": c, "qubit-mapping": mapping, "inverse-qubit-mapping": ctx.get("inverse-qubit-mapping"),
-            "all-gates-supported?": not unsupported,
-            "final-unsupported-gates": unsupported,
-            "transformed-operation-count": tr.get("transformed-operation-count", 0),
-            "pipeline-order": ["gate-cancellation", "qubit-optimization", "gate-decomposition", "reverse-mappings",
-                               "validation"]}
+    if o.get("apply-error-correction?"):
+        raise OptimizationError("error correction is not built")
+    ctx: dict = {"circuit": optimize_gates(circuit, o), "device": device, "options": o}
+    c, mapping = optimize_qubit_usage(ctx["circuit"], o)
+    ctx.update({"circuit": c, "qubit-mapping": mapping})
+    ctx = topology_aware_transform(ctx)
+    tr = transform_circuit(ctx["circuit"], ctx.get("device"), ctx.get("options"))
+    ctx = {**ctx, **tr}
+    ctx = create_all_reverse_mappings(ctx)
+    sup = ctx.get("supported-operations") or frozenset()
+    seen = []
+    for x in ctx["circuit"]["operations"]:
+        if x.get("operation-type") not in seen:
+            seen.append(x.get("operation-type"))
+    unsupported = [t for t in seen if t not in sup]
+    ctx.update({"all-gates-supported?": not unsupported, "final-unsupported-gates": unsupported,
+                "pipeline-order": ["gate-cancellation", "qubit-optimization", "error-correction",
+                                   "topology-optimization", "gate-decomposition", "reverse-mappings", "validation"]})
+    return ctx
