@@ -321,6 +321,8 @@ class HardwareSimulator:
             optimize(circuit, self._current, {
                 "optimize-gates?": opts.get("optimize-gates?", True),
                 "optimize-qubits?": opts.get("optimize-qubits?", True),
+                "optimize-topology?": opts.get("optimize-topology?", False),
+                "apply-error-correction?": opts.get("apply-error-correction?", False),
                 "transform-operations?": opts.get("transform-operations?", True),
                 "max-iterations": opts.get("max-iterations", 100)})
         except OptimizationError as e:
