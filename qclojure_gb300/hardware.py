@@ -318,13 +318,13 @@ class HardwareSimulator:
 
         opts = dict(options or {})
         try:
+            # the defaults, then every submitted option over them (`merge`)
             optimize(circuit, self._current, {
                 "optimize-gates?": opts.get("optimize-gates?", True),
                 "optimize-qubits?": opts.get("optimize-qubits?", True),
                 "optimize-topology?": opts.get("optimize-topology?", False),
-                "apply-error-correction?": opts.get("apply-error-correction?", False),
                 "transform-operations?": opts.get("transform-operations?", True),
-                "max-iterations": opts.get("max-iterations", 100)})
+                "max-iterations": opts.get("max-iterations", 100), **opts})
         except OptimizationError as e:
             job.update({"status": "failed", "completed-at": time.time() * 1000,
                         "result": {"job-status": "failed", "error-message": str(e)}})

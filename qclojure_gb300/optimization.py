@@ -1,7 +1,8 @@
-"""The first stages of the reference's hardware optimisation pipeline on the host.
+"""The reference's hardware optimisation pipeline on the host.
 
 application/hardware_optimization.clj:42-109 runs gate optimisation, qubit
-optimisation, error correction, topology routing and gate decomposition. Gate
+optimisation, error correction, topology routing and gate decomposition. Error
+correction lives in `error_correction.py` and routing in `topology.py`; gate
 optimisation, qubit optimisation and gate decomposition are restated here, as the
 reference defines them:
 
@@ -455,20 +456,21 @@ def map_measurements_to_original(measurements: dict, ctx: dict) -> dict:
 
 
 def optimize(circuit: dict, device: dict | None = None, options: dict | None = None) -> dict:
-    """The pipeline of hardware_optimization.clj:42-109 without error correction: gate
-    optimisation, qubit optimisation, topology-aware routing (`topology.py`, when
-    "optimize-topology?"), gate decomposition, reverse mappings and validation. The
+    """The pipeline of hardware_optimization.clj:42-109: gate optimisation, qubit
+    optimisation, error correction (`error_correction.py`, when "apply-error-correction?"),
+    topology-aware routing (`topology.py`, when "optimize-topology?"), gate decomposition,
+    reverse mappings and validation. The
     context threads through the stages as in the reference, including where a stage
     replaces it (routing on a device with native SWAP) and validation's lookup of the
     supported operations on the context itself (so every gate type is reported)."""
+    from .error_correction import apply_error_correction
     from .topology import topology_aware_transform
 
     o = options or {}
-    if o.get("apply-error-correction?"):
-        raise OptimizationError("error correction is not built")
     ctx: dict = {"circuit": optimize_gates(circuit, o), "device": device, "options": o}
     c, mapping = optimize_qubit_usage(ctx["circuit"], o)
     ctx.update({"circuit": c, "qubit-mapping": mapping})
+    ctx = apply_error_correction(ctx)
     ctx = topology_aware_transform(ctx)
     tr = transform_circuit(ctx["circuit"], ctx.get("device"), ctx.get("options"))
     ctx = {**ctx, **tr}

@@ -76,3 +76,15 @@ def test_cancel_and_not_found(sim):
     assert sim.job_result("fake-job-id")["job-status"] == "not-found"
     assert sim.backend_info()["backend-type"] == "hardware-simulator" and sim.available()
     assert sim.select_device("dev")["id"] == "dev"
+
+
+def test_submission_runs_error_correction(sim):
+    """Every submitted option reaches the pipeline (`merge` over its defaults): error
+    correction encodes the circuit there, the original circuit runs, and an unknown code
+    fails the job."""
+    ok = sim.submit_circuit(_bell(), {"shots": 5, "apply-error-correction?": True, "error-correction-code": "shor"})
+    bad = sim.submit_circuit(_bell(), {"apply-error-correction?": True, "error-correction-code": "nope"})
+    r = sim.job_result(bad)
+    assert r["job-status"] == "failed" and "Unknown error correction code" in r["error-message"]
+    sim.gate.set()
+    assert sim.wait(ok, 10) == "completed" and sim.calls == [_bell()]
