@@ -26,6 +26,7 @@ table per builder) and produce the reference's operation lists gate for gate.
 from __future__ import annotations
 
 from . import circuit as C
+from .clj import hash_long, map_order
 from .optimization import OptimizationError
 
 
@@ -408,43 +409,10 @@ def translate_operation_to_physical(op: dict, logical_to_physical: dict) -> list
     return [op]
 
 
-def _clj_hash_long(x: int) -> int:
-    """Clojure's hash of a long (Murmur3 hashLong with seed 0), as an unsigned 32-bit value."""
-    if x == 0:
-        return 0
-    M = 0xFFFFFFFF
-
-    def rotl(v, r):
-        return ((v << r) | (v >> (32 - r))) & M
-
-    def mix_k1(k):
-        return (rotl((k * 0xCC9E2D51) & M, 15) * 0x1B873593) & M
-
-    def mix_h1(h, k):
-        return (rotl(h ^ k, 13) * 5 + 0xE6546B64) & M
-
-    x &= 0xFFFFFFFFFFFFFFFF
-    h = mix_h1(mix_h1(0, mix_k1(x & M)), mix_k1(x >> 32))
-    h ^= 8
-    h ^= h >> 16
-    h = (h * 0x85EBCA6B) & M
-    h ^= h >> 13
-    h = (h * 0xC2B2AE35) & M
-    return h ^ (h >> 16)
-
-
 def clj_map_key_order(keys: list[int]) -> list[int]:
     """The order in which a Clojure map built by `into {}` from these integer keys yields
-    them: insertion order up to 8 entries (an array map), else the hash map's trie order,
-    which visits keys by the 5-bit digits of their hash, lowest digit first."""
-    if len(keys) <= 8:
-        return list(keys)
-
-    def digits(k):
-        h = _clj_hash_long(k)
-        return tuple((h >> s) & 31 for s in range(0, 32, 5))
-
-    return sorted(keys, key=digits)
+    them (insertion order up to 8 entries, else the hash trie's order)."""
+    return map_order(keys, hash_long)
 
 
 def inject_syndrome_measurements(circuit: dict, code_key: str, logical_to_physical: dict,

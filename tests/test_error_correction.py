@@ -7,6 +7,7 @@ import pytest
 
 from qclojure_gb300 import circuit as C
 from qclojure_gb300 import error_correction as E
+from qclojure_gb300.clj import hash_long
 from qclojure_gb300.optimization import optimize
 
 SIZES = {"bit-flip": (3, 2), "shor": (9, 8), "steane": (7, 6), "five-qubit": (5, 4)}
@@ -208,7 +209,7 @@ def test_syndrome_order_beyond_eight_logical_qubits():
     """A map of more than eight logical qubits yields them in the Clojure hash map's order
     (for 0..9: 0 7 1 4 6 3 2 9 5 8), and the syndrome measurements follow it."""
     assert E.clj_map_key_order(list(range(10))) == [0, 7, 1, 4, 6, 3, 2, 9, 5, 8]
-    assert E._clj_hash_long(1) == 1392991556
+    assert hash_long(1) == 1392991556
     out = E.apply_error_correction({"circuit": C.create_circuit(10), "options": {"apply-error-correction?": True}})
     ms = [o["operation-params"]["measurement-qubits"] for o in out["circuit"]["operations"]
           if o["operation-type"] == "measure"]
