@@ -11,8 +11,9 @@ energies reduced on the device, and new angles only rewrite the op records of th
 sweep kept from the previous step.
 
 The optimisers follow optimization.clj's loops (adam-optimization :309-365,
-gradient-descent-optimization :367-420) step for step: same updates, same
-convergence test, same result maps. The gradient at each new point is computed in
+gradient-descent-optimization :367-420, spsa-optimization :463-567) step for step:
+same updates, same convergence test, same result maps. The adaptive-shift gradients
+(:181-262) evaluate every candidate shift in one batch. The gradient at each new point is computed in
 the same batch as the point's energy; when the loop stops there, that gradient is the
 `final-gradient`, and the extra evaluations are not counted.
 """
@@ -178,6 +179,111 @@ def gradient_descent_optimization(objective, initial_parameters: Sequence[float]
             return {"success": True, "optimal-parameters": list(params), "optimal-energy": new_energy,
                     "iterations": it, "function-evaluations": it * nparam * 2, "convergence-history": energies,
                     "final-gradient": list(used), "reason": "converged"}
+        it += 1
+
+
+ADAPTIVE_SHIFTS = (math.pi / 2, math.pi / 4, math.pi / 8, math.pi / 16)
+
+
+def adaptive_parameter_shift_gradient(objective, params: Sequence[float], param_types: Sequence[str]) -> np.ndarray:
+    """adaptive-parameter-shift-gradient (optimization.clj:181-205): shift π/4 for an
+    "amplitude" parameter and π/2 for any other type, all 2N evaluations in one batch.
+    Parameters pair with types by position; the shorter list sets the gradient's length."""
+    n = min(len(params), len(param_types))
+    shifts = [math.pi / 4 if param_types[i] == "amplitude" else math.pi / 2 for i in range(n)]
+    pts = []
+    for i in range(n):
+        plus, minus = list(params), list(params)
+        plus[i] += shifts[i]
+        minus[i] -= shifts[i]
+        pts += [plus, minus]
+    e = objective.energies(pts) if pts else np.zeros(0)
+    return np.array([(1.0 / (2.0 * math.sin(shifts[i]))) * (e[2 * i] - e[2 * i + 1]) for i in range(n)])
+
+
+def _max_key_abs(values: Sequence[float]) -> int:
+    """Index `(apply max-key #(Math/abs %) values)` picks: of two, the first only when
+    strictly larger; after that, a later value whenever it is at least as large."""
+    best = 0
+    if len(values) > 1:
+        best = 0 if abs(values[0]) > abs(values[1]) else 1
+        for k in range(2, len(values)):
+            if abs(values[k]) >= abs(values[best]):
+                best = k
+    return best
+
+
+def adaptive_shift_gradient(objective, params: Sequence[float], options: dict | None = None) -> np.ndarray:
+    """calculate-adaptive-shift-gradient with select-best-shift (optimization.clj:207-262):
+    per parameter, the parameter-shift gradient at the candidate shift whose gradient is
+    largest in magnitude. All 2·N·S evaluations (S candidate shifts, default π/2, π/4,
+    π/8, π/16) run as one batch; the gradient at the chosen shift is the one already
+    evaluated, as the objective is deterministic."""
+    shifts = list((options or {}).get("candidate-shifts", ADAPTIVE_SHIFTS))
+    n = len(params)
+    if n == 0 or not shifts:
+        return np.zeros(0)
+    e = objective.energies([pt for sh in shifts for pt in shifted_points(params, sh)])
+    per = [gradient_from_energies(e[2 * n * k:2 * n * (k + 1)], sh) for k, sh in enumerate(shifts)]
+    return np.array([per[_max_key_abs([g[i] for g in per])][i] for i in range(n)])
+
+
+def spsa_optimization(objective, initial_parameters: Sequence[float], options: dict | None = None) -> dict:
+    """spsa-optimization (optimization.clj:463-567): gains a_k = a / (A + k)^α and
+    c_k = c / k^γ, a Bernoulli ±1 perturbation Δ of all parameters, the gradient estimate
+    (E(θ + c_k Δ) - E(θ - c_k Δ)) / (2 c_k) · Δ, and the step θ - a_k ĝ; with a blocking
+    size above 1 the last iterates are averaged and the average evaluated. Convergence
+    needs more than 50 iterations and an energy change below the tolerance. The
+    perturbations come from a generator seeded by the "seed" option (the reference draws
+    from an unseeded `rand`). Each iteration is one batch: the new point (and its average)
+    with the next iteration's two perturbed points, which depend only on the new point and
+    the next draws."""
+    o = options or {}
+    a, c = o.get("a", 0.16), o.get("c", 0.1)
+    max_iter = o.get("max-iterations", 1000)
+    big_a = o.get("A", 0.1 * max_iter)
+    alpha, gamma = o.get("alpha", 0.602), o.get("gamma", 0.101)
+    tol = o.get("tolerance", 1e-6)
+    block = o.get("blocking-size", 1)
+    rng = np.random.default_rng(o.get("seed", 0))
+    hyper = {"a": a, "c": c, "A": big_a, "alpha": alpha, "gamma": gamma}
+
+    def probe(params, k):
+        ck = c / math.pow(k, gamma)
+        delta = [-1.0 if rng.random() < 0.5 else 1.0 for _ in params]
+        return ck, delta, [p + ck * d for p, d in zip(params, delta)], [p - ck * d for p, d in zip(params, delta)]
+
+    params = [float(x) for x in initial_parameters]
+    nxt = probe(params, 1)
+    e = objective.energies([params, nxt[2], nxt[3]])
+    prev, ep, em = float(e[0]), float(e[1]), float(e[2])
+    energies, blocked = [prev], [params]
+    it = 0
+    while True:
+        if it >= max_iter:
+            return {"success": False, "optimal-parameters": params, "optimal-energy": prev, "iterations": it,
+                    "function-evaluations": it * 2, "convergence-history": energies,
+                    "spsa-hyperparameters": hyper, "reason": "max-iterations-reached"}
+        k = it + 1
+        ak = a / math.pow(big_a + k, alpha)
+        ck, delta = nxt[0], nxt[1]
+        coef = (ep - em) / (2.0 * ck)
+        new = [p - ak * (coef * d) for p, d in zip(params, delta)]
+        blocked.append(new)
+        recent = blocked[-block:] if block > 0 else []
+        avg = ([sum(col) / len(col) for col in zip(*recent)] if block > 1 else new)
+        nxt = probe(new, k + 1)
+        batch = [new] + ([avg] if block > 1 else []) + [nxt[2], nxt[3]]
+        e = objective.energies(batch)
+        new_e = float(e[0])
+        avg_e = float(e[1]) if block > 1 else new_e
+        ep, em = float(e[-2]), float(e[-1])
+        energies.append(new_e)
+        if it > 50 and abs(prev - avg_e) < tol:
+            return {"success": True, "optimal-parameters": avg, "optimal-energy": avg_e, "iterations": it,
+                    "function-evaluations": it * 2 + (1 if block > 1 else 0), "convergence-history": energies,
+                    "spsa-hyperparameters": {**hyper, "final-ak": ak, "final-ck": ck}, "reason": "converged"}
+        params, prev = new, avg_e
         it += 1
 
 

@@ -131,3 +131,30 @@ def test_finite_difference_option(vctx, oracle):
         assert abs(e - e2) <= 1e-11 and np.max(np.abs(g - g2)) <= 1e-7
     finally:
         gpu.close()
+
+
+def test_adaptive_shift_gradient_and_spsa(vctx, oracle):
+    """The adaptive-shift gradients and the SPSA loop on the device against the same
+    calls on the oracle's energies (same seeded perturbations); 30 iterations stay below
+    SPSA's 50-iteration convergence floor, so both runs take the same exit."""
+    from qclojure_gb300.variational import (BatchedObjective, adaptive_parameter_shift_gradient,
+                                            adaptive_shift_gradient, spsa_optimization)
+
+    n, layers = 6, 1
+    f, h = _hea(n, layers), _ham(n, 11)
+    p = list(np.random.default_rng(6).uniform(-math.pi, math.pi, 2 * n * layers))
+    gpu = BatchedObjective(vctx, h, f)
+    ref = OracleObjective(oracle, h, f)
+    try:
+        g, r = adaptive_shift_gradient(gpu, p), adaptive_shift_gradient(ref, p)
+        assert np.max(np.abs(g - r)) <= 1e-10 * max(1.0, np.max(np.abs(r)))
+        types = ["rotation", "amplitude"] * n
+        g, r = adaptive_parameter_shift_gradient(gpu, p, types), adaptive_parameter_shift_gradient(ref, p, types)
+        assert np.max(np.abs(g - r)) <= 1e-10 * max(1.0, np.max(np.abs(r)))
+        opts = {"max-iterations": 30, "seed": 2, "blocking-size": 3}
+        a, b = spsa_optimization(gpu, p, opts), spsa_optimization(ref, p, opts)
+        assert a["iterations"] == b["iterations"] == 30 and not a["success"] and not b["success"]
+        assert np.max(np.abs(np.array(a["optimal-parameters"]) - b["optimal-parameters"])) <= 1e-8
+        assert np.max(np.abs(np.array(a["convergence-history"]) - b["convergence-history"])) <= 1e-9
+    finally:
+        gpu.close()
