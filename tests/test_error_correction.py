@@ -308,3 +308,19 @@ def test_oracle_steane_and_five_qubit_encoders_leave_the_code_space(oracle):
         s = oracle.run(c, _embed(np.array([0.6, 0.8]), n))
         _, _, p = oracle.measure(s, list(range(size, n)), 7, 0)
         assert p < 0.99
+
+
+def test_stage_then_routing():
+    """The encoded circuit goes on through topology routing on a linear coupling; with no
+    native SWAP each inserted SWAP becomes three CNOTs."""
+    from qclojure_gb300 import topology as T
+
+    c = C.cnot_gate(C.h_gate(C.create_circuit(2), 0), 0, 1)
+    base = {"supported-operations": {"h", "cnot", "x", "z", "measure"}, "coupling": T.linear_coupling(12)}
+    routed = optimize(c, base, {"apply-error-correction?": True, "optimize-topology?": True})
+    native = optimize(c, {**base, "supported-operations": base["supported-operations"] | {"swap"}},
+                      {"apply-error-correction?": True, "optimize-topology?": True})
+    assert routed["swap-count"] == native["swap-count"] > 0
+    assert len(routed["circuit"]["operations"]) == len(native["circuit"]["operations"]) + 2 * native["swap-count"]
+    assert "swap" not in types(routed["circuit"])
+    C.validate_circuit(routed["circuit"])
