@@ -228,8 +228,9 @@ def readout_noise(outcome: int, n: int, readout: dict | None, seed: int, shot: i
     """calculate-final-bitstring (noise.clj:107-160)."""
     if not readout:
         return outcome
-    corr = {int(a): {int(b): f for b, f in (row or {}).items()}
-            for a, row in (readout.get("correlated-errors") or {}).items()}
+    # a row that is not a map (a bare factor) adjusts nothing: `get` on a number is nil
+    corr = {int(a): {int(b): f for b, f in row.items()}
+            for a, row in (readout.get("correlated-errors") or {}).items() if isinstance(row, dict)}
     bits = outcome
     hist: list[int] = []
     for q in range(n):

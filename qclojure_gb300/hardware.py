@@ -85,7 +85,9 @@ class NoiseSpec:
         corr = []
         if ro:
             for src, row in (ro.get("correlated-errors") or {}).items():
-                for dst, f in (row or {}).items():
+                # a row that is not a map (a bare factor) adjusts nothing: `get` on a
+                # number gives nil in noise.clj:134-141
+                for dst, f in (row.items() if isinstance(row, dict) else ()):
                     corr.append((int(src), int(dst), float(f)))
         self.corr_source = (C.c_int32 * max(1, len(corr)))(*[c[0] for c in corr])
         self.corr_target = (C.c_int32 * max(1, len(corr)))(*[c[1] for c in corr])
@@ -401,6 +403,22 @@ class HardwareSimulator:
                 "completed-jobs": sum(s == "completed" for s in st)}
 
 
-def create_hardware_simulator(config: dict | None = None, device: dict | None = None) -> HardwareSimulator:
-    """hardware_simulator.clj:400-418"""
-    return HardwareSimulator(config, device)
+def create_hardware_simulator(config: dict | None = None, device: dict | None = None,
+                              devices: list | None = None) -> HardwareSimulator:
+    """hardware_simulator.clj:400-418. `devices` is the catalogue the simulator starts with
+    (the reference loads its own, simulator-devices.edn, and starts on its first entry:
+    hardware_simulator.clj:39-55); `load_devices` reads that file."""
+    return HardwareSimulator(config, device, devices)
+
+
+def load_devices(path: str) -> list[dict]:
+    """The device maps of an EDN device catalogue such as the reference's
+    resources/simulator-devices.edn, with keyword keys and values as plain strings (the
+    spelling this package uses: "native-gates", "gate-noise", "all-to-all") and sets as
+    frozensets."""
+    from .edn import EdnError, load
+
+    data = load(path)
+    if not isinstance(data, list) or not all(isinstance(d, dict) for d in data):
+        raise EdnError("a device catalogue is a vector of device maps")
+    return data
