@@ -149,3 +149,23 @@ def test_execute_circuit_and_protocol(built):
         assert {"total-jobs", "active-jobs", "completed-jobs"} <= set(q)
     finally:
         sim.close()
+
+
+def test_catalogue_device_noise_matches_oracle(contexts, oracle):
+    """A device read from catalogue EDN, flat correlation rows included, runs its noisy
+    shots as the oracle does."""
+    from qclojure_gb300 import edn
+    from qclojure_gb300.hardware import run_trajectories
+
+    dev = edn.loads("""
+      {:id :catalogue-test
+       :noise-model {:gate-noise {:h {:noise-type :depolarizing :noise-strength 0.02}
+                                  :cnot {:noise-type :amplitude-damping :noise-strength 0.01
+                                         :t1-time 120.0 :t2-time 90.0 :gate-time 300.0}}
+                     :readout-error {:prob-0-to-1 0.05 :prob-1-to-0 0.08
+                                     :correlated-errors {0 1.0 1 1.2 2 0.8}}}}""")
+    c = _bell(3)
+    run = run_trajectories(contexts["exact"], c, dev["noise-model"], 200, seed=17, max_trajectories=200)
+    outs, states = oracle.noisy_shots(c, dev["noise-model"], 200, seed=17)
+    assert np.array_equal(run["outcomes"], outs)
+    assert np.max(np.abs(run["trajectories"] - states)) <= 1e-12
