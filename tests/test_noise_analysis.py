@@ -92,3 +92,11 @@ def test_many_gate_types_follow_the_hash_order():
     assert [t for t, _ in d["dominant-error-sources"]] == list(d["gate-counts"])
     with pytest.raises(ValueError):
         N.estimate_circuit_fidelity({"operations": []}, {})
+
+
+def test_clojure_hashes():
+    """Clojure's `hash` of 1 is 1392991556 and of :a is -2123407586."""
+    from qclojure_gb300.clj import hash_long
+
+    assert hash_long(1) == 1392991556
+    assert hash_keyword("a") - (1 << 32) == -2123407586
