@@ -272,6 +272,11 @@ class HardwareSimulator:
         noiseless = {"id": "noiseless", "name": "Noiseless device", "noise-model": {},
                      "native-gates": set(NATIVE_SIMULATOR_GATE_SET)}
         if device is not None:
+            # create-hardware-simulator normalises a device it is given
+            # (hardware_simulator.clj:409-414, device.clj:57-68)
+            from .device import validate_device
+
+            device = validate_device(device)
             self._devices.append(device)
         self._current = device or (self._devices[0] if self._devices else noiseless)
         self._ctx = Context(precision=self.config.get("precision", "c128"))

@@ -386,7 +386,9 @@ def transform_circuit(circuit: dict, device: dict | None = None, options: dict |
     if not o.get("transform-operations?", True):
         return {"circuit": circuit}
     d = device or {}
-    supported = d.get("supported-operations", d.get("native-gates"))
+    supported = d.get("supported-operations")
+    if supported is None:  # `or`: a nil set falls through to the native gates
+        supported = d.get("native-gates")
     ops = list(circuit.get("operations") or [])
     new = transform_operations(ops, supported, o.get("max-iterations", 100)) \
         if o.get("transform-unsupported?", True) else ops
