@@ -283,6 +283,139 @@ def cpu_statevector_rates(args, rank: int) -> dict:
 
 
 # ---------------------------------------------------------------------------
+CONFIG0 = {"qubits": 10, "depth": 20, "shots": 1024, "seed": 0}
+
+
+def reference_config0(measure_up_to: int = 12, extrapolate_to: int = 16) -> dict:
+    """The reference's algorithm on the plain CPU case, single-threaded as the reference runs
+    a job (one future per job, ideal_simulator.clj:129): the config-0 circuit (10 qubits,
+    depth 20, 300 gates) and 1024 shots, run whole by oracle.refalgo_circuit (a dense
+    Kronecker mat-vec per single-qubit gate, a full probability scan per shot). The same
+    recipe at 8..measure_up_to qubits is measured whole; beyond that the time is
+    extrapolated from the largest measured size by the single-qubit gates' 4^n work and
+    labelled so. A lower bound on the reference's JVM time, which cannot run on this machine."""
+    from oracle import oracle as O
+    from qclojure_gb300 import workloads
+
+    d, shots = CONFIG0["depth"], CONFIG0["shots"]
+    out = {"label": "reference algorithm restated in C (oracle/qgo.c or_refalgo_circuit), 1 thread; "
+                    "a lower bound on the reference's JVM time", "threads": 1,
+           "recipe": f"layered depth {d} + {shots} shots, seed {CONFIG0['seed']}", "by_qubits": {}}
+    last = None
+    for n in range(8, measure_up_to + 1):
+        c = workloads.layered_circuit(n, d, CONFIG0["seed"])
+        t0 = time.perf_counter()
+        O.refalgo_circuit(c, shots, 1)
+        dt = time.perf_counter() - t0
+        g1 = sum(1 for op in c["operations"] if op["operation-type"] != "cnot")
+        out["by_qubits"][str(n)] = {"gates": len(c["operations"]), "s": dt, "measured": True}
+        last = (n, dt, g1)
+    n0, t0s, g10 = last
+    for n in range(measure_up_to + 1, extrapolate_to + 1):
+        g1 = n * d
+        est = t0s * (g1 / g10) * 4.0 ** (n - n0)
+        out["by_qubits"][str(n)] = {"gates": g1 + (n // 2) * d, "s": est, "measured": False,
+                                    "extrapolated_from": n0}
+    out["config0_s"] = out["by_qubits"][str(CONFIG0["qubits"])]["s"]
+    out["config0_circuits_per_s"] = 1.0 / out["config0_s"]
+    return out
+
+
+def gpu_config0(device: int, runs: int = 50) -> dict:
+    """The config-0 job end to end through the job API on the GPU (complex128, final
+    state + probabilities + 1024 shots into host buffers), mean over `runs` jobs."""
+    from qclojure_gb300 import workloads
+    from qclojure_gb300.backend import GpuStateVectorSimulator, execute_circuit
+
+    c = workloads.layered_circuit(CONFIG0["qubits"], CONFIG0["depth"], CONFIG0["seed"])
+    opts = {"result-specs": {"measurements": {"shots": CONFIG0["shots"]}, "probabilities": {}}, "seed": 1}
+    out = {}
+    for arith in ("double-float", "exact"):
+        sim = GpuStateVectorSimulator({"precision": "c128", "fusion": "tiled", "workers": 1, "seed": 1,
+                                       "arithmetic": arith}, device=device)
+        try:
+            for _ in range(3):
+                r = execute_circuit(sim, c, opts, timeout_ms=60_000)
+                sim.free_job(r["job-id"])
+            t0 = time.perf_counter()
+            for _ in range(runs):
+                r = execute_circuit(sim, c, opts, timeout_ms=60_000)
+                assert r["job-status"] == "completed", r
+                sim.free_job(r["job-id"])
+            dt = (time.perf_counter() - t0) / runs
+        finally:
+            sim.close()
+        out[arith.replace("-", "_")] = {"ms_per_job": dt * 1e3, "circuits_per_s": 1.0 / dt}
+    out["path"] = "qg_submit -> qg_wait -> final state, probabilities, 1024 shots (host buffers)"
+    return out
+
+
+def oracle_spot_check_30(ctx, n: int, depth: int, seed: int, device: int) -> dict:
+    """The large-n oracle check: the 30-qubit recipe at reduced depth (`depth` layers + the
+    full QFT) run by the CPU state vector (oracle/cpu_sv.c, bit-identical to the oracle,
+    all host cores), uploaded as a complex128 reference, against the device's double-float
+    result (the benchmarked path) and its exact FP64 result."""
+    import numpy as np
+
+    from oracle import oracle as ORC
+    from qclojure_gb300 import workloads
+
+    if ORC.cpu_sv_lib() is None:
+        return {"unavailable": "the CPU state-vector library could not be built"}
+    c = workloads.layered_circuit(n, depth, seed)
+    c = {"num-qubits": n, "operations": c["operations"] + workloads.qft_ops(n)}
+    sv = np.zeros(1 << n, np.complex128)
+    sv[0] = 1
+    t0 = time.perf_counter()
+    ORC.cpu_sv_run(c, sv)
+    cpu_s = time.perf_counter() - t0
+    out = {"workload": f"layered-{n}x{depth}+qft{n} ({len(c['operations'])} gates)",
+           "oracle": "oracle/cpu_sv.c on the host (bit-identical to oracle/qgo.c)", "cpu_s": cpu_s}
+    from qclojure_gb300.state import Context
+
+    with ctx.state(n, "c128") as ref:
+        ref.upload(sv)
+        del sv
+        with ctx.state(n, "c128") as s:
+            s.set_basis(0)
+            s.apply(c)
+            out["c128_double_float"] = s.compare(ref)
+        with Context(device=device, workers=1, seed=7, arithmetic="exact") as cx:
+            with cx.state(n, "c128") as s:
+                s.set_basis(0)
+                s.apply(c)
+                out["c128_exact"] = s.compare(ref)
+    return out
+
+
+# ---------------------------------------------------------------------------
+def _short(x, digits: int = 4):
+    """Floats to `digits` significant digits, recursively (the summary keys at the line's end)."""
+    if isinstance(x, float):
+        return float(f"{x:.{digits}g}") if math.isfinite(x) else x
+    if isinstance(x, dict):
+        return {k: _short(v, digits) for k, v in x.items()}
+    if isinstance(x, list):
+        return [_short(v, digits) for v in x]
+    return x
+
+
+def order_line(line: dict) -> dict:
+    """The JSON line's key order: the contract's keys, then the long legs, then the
+    headline's evidence (roofline, CPU baselines, end to end, complex64, exact FP64,
+    accuracy) so that the end of the line carries it."""
+    head = ["metric", "value", "unit", "n_gpus", "steps", "warmup", "ms_per_step", "higher_is_better", "scaling",
+            "vs_baseline", "dtype", "data", "gpu_launches", "config", "clocks"]
+    tail = ["cpu_baseline", "e2e", "layer_ms", "hbm_passes_per_step", "roofline", "c64", "exact_fp64",
+            "oracle_30q", "accuracy"]
+    out = {k: line[k] for k in head if k in line}
+    out.update({k: v for k, v in line.items() if k not in out and k not in tail})
+    for k in tail:
+        if k in line:
+            out[k] = _short(line[k]) if k in ("c64", "exact_fp64", "oracle_30q", "accuracy") else line[k]
+    return out
+
+
 def max_over_ranks(ms: float, dist=None, device: str = "cpu") -> float:
     """The slowest rank's time: every rank runs its own replica (no data exchange), and
     the job is done when the last one is."""
@@ -313,10 +446,10 @@ def run_reference(args):
     desc = ""
     threads = os.cpu_count() or 1
     for _ in range(args.warmup):
-        cpu_reference_rate(args.qubits, gates, 1.0)
+        cpu_reference_rate(args.qubits, gates, 0.5)
     t0 = time.perf_counter()
     for _ in range(args.steps):
-        v, desc, threads = cpu_reference_rate(args.qubits, gates, 5.0)
+        v, desc, threads = cpu_reference_rate(args.qubits, gates, 2.5)
         vals.append(v)
     dt = time.perf_counter() - t0
     value = statistics.mean(vals)
@@ -326,10 +459,16 @@ def run_reference(args):
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
         "config": {"workload": f"layered-{args.qubits}x{args.depth}+qft{args.qubits}", "n_qubits": args.qubits,
                    "gates": gates, "precision": "c128"},
-        "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port", "sample": desc},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port", "sample": desc,
+                         "extrapolated": "a sample of one gate's rows scaled to the whole circuit: the "
+                                         "dense algorithm cannot run a 30-qubit gate (2^60 entries)"},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
         "note": "the reference (Clojure/JVM) cannot run here; this times its algorithm restated in C",
     }
+    try:
+        line["cpu_baseline"]["config0"] = reference_config0()
+    except Exception as e:  # the line must still print
+        line["cpu_baseline"]["config0"] = {"error": f"{type(e).__name__}: {e}"}
     print(json.dumps(line), flush=True)
     return 0
 
@@ -427,8 +566,7 @@ def main():
     achieved = pass_bytes / (mean_pass / 1e3) / 1e9 if dom else float("nan")
     # DRAM bytes per tiled pass from an ncu capture of the same kernel on a 26-qubit state
     # (dram__bytes_read.sum + dram__bytes_write.sum = 2.087e9 per c128 launch, 1.012e9 per c64
-    # launch), scaled by the amplitudes processed:
-    # profiles/qgp_pass_c128_doublefloat_layered30x40_qft30.md, profiles/qgp_pass_c64_layered26x12_qft26.md
+    # launch), scaled by the amplitudes processed
     traffic, traffic_src = None, None
     if args.fusion == "tiled":
         traffic = (2.087e9 if args.precision == "c128" else 1.012e9) * 2 ** (n - 26)
@@ -466,7 +604,7 @@ def main():
                      "passes": len(dom),
                      "note": "passes are bound by instruction issue, not HBM: ncu on the same kernel "
                              "(26 qubits) shows 62-65% issue active and 23-29% DRAM throughput for "
-                             "double-float complex128 (profiles/qgp_pass_c128_doublefloat_layered30x40_qft30.md)"},
+                             "double-float complex128"},
         "gpu_launches": int(l1.value - l0.value),
         "clocks": ck,
     }
@@ -525,6 +663,15 @@ def main():
         sx.close()
         ctx_x.close()
         line["accuracy"] = accuracy
+        # the exact FP64 path (every product and sum an IEEE double in the reference's gate
+        # order, interpreted tiled passes) on the same circuit, timed once above
+        line["exact_fp64"] = {"ms_per_step": accuracy["reference_ms"],
+                              "value": gates * N / (accuracy["reference_ms"] / 1e3), "unit": UNIT}
+        # the large-n oracle check: 4 layers + QFT at full width on the host's CPU state vector
+        try:
+            line["oracle_30q"] = oracle_spot_check_30(ctx, n, 4, args.seed + rank, local)
+        except Exception as e:  # the line must still print
+            line["oracle_30q"] = {"error": f"{type(e).__name__}: {e}"}
         # dense fused blocks of k = 1..5 qubits (one HBM pass per block), per-pass bandwidth on
         # the first two layers of the workload; dense blocks compute in FP64 (c128) or FP32 (c64)
         dense_sample = workloads.layered_circuit(n, 2, args.seed + rank)
@@ -710,11 +857,16 @@ def main():
         rate, desc, threads = cpu_reference_rate(n, gates, 8.0)
         line["cpu_baseline"] = {"value": rate, "unit": UNIT, "cores": threads, "kind": "port", "sample": desc}
         line["cpu_baseline"]["optimised_statevector"] = cpu_statevector_rates(args, rank)
+        try:
+            line["cpu_baseline"]["config0"] = {"reference_algorithm": reference_config0(),
+                                               "gpu": gpu_config0(local)}
+        except Exception as e:  # the line must still print
+            line["cpu_baseline"]["config0"] = {"error": f"{type(e).__name__}: {e}"}
     else:
         st.close()
     ctx.close()
     if rank == 0:
-        print(json.dumps(line), flush=True)
+        print(json.dumps(order_line(line)), flush=True)
     if dist:
         dist.destroy_process_group()
     return 0

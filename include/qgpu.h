@@ -306,7 +306,9 @@ int qg_state_sample(void* state, uint64_t shots, uint64_t seed, uint64_t* host_o
    device memory of the state's device holding at least `shots` values; the call
    returns after the outcomes are written (it synchronises the state's stream).
    The first call on a device looks up the array's device address once (with that
-   device current); make that first call before any stream capture begins. Calls that
+   device current); make that first call before any stream capture begins. After a
+   device reset (cudaDeviceReset, or another library destroying the primary context)
+   the next call sees a new context and looks the address up again. Calls that
    overlap on one device (from several host threads) share the array and race:
    serialise them. */
 int qg_state_sample_noalloc(void* state, uint64_t shots, uint64_t seed, uint64_t* device_outcomes);

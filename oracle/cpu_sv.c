@@ -20,18 +20,39 @@
 void or_gate_matrix8(int opcode, double angle, double m[8]);
 
 static inline void cmac2(const double* g, double xr0, double xi0, double xr1, double xi1, double* yr, double* yi) {
-  /* y = g0 x0 + g1 x1 */
-  *yr = g[0] * xr0 - g[1] * xi0 + g[2] * xr1 - g[3] * xi1;
-  *yi = g[0] * xi0 + g[1] * xr0 + g[2] * xi1 + g[3] * xr1;
+  /* y = g0 x0 + g1 x1, rounded like the oracle's cadd(cmul(g0, x0), cmul(g1, x1)) (qgo.c apply_1q):
+     each complex product first, then the two sums */
+  *yr = (g[0] * xr0 - g[1] * xi0) + (g[2] * xr1 - g[3] * xi1);
+  *yi = (g[0] * xi0 + g[1] * xr0) + (g[2] * xi1 + g[3] * xr1);
 }
 
-/* rows r0 = (m00, m01), r1 = (m10, m11) applied to pairs (i0, i0 | tb) where i0 & cmask == cmask */
+/* k with a zero bit inserted at each position of `bits` (ascending, at most 3) */
+static inline uint64_t spread(uint64_t k, const int* bits, int nb) {
+  for (int j = 0; j < nb; ++j) {
+    const uint64_t lo = k & ((1ULL << bits[j]) - 1);
+    k = ((k >> bits[j]) << (bits[j] + 1)) | lo;
+  }
+  return k;
+}
+
+/* rows r0 = (m00, m01), r1 = (m10, m11) applied to pairs (i0, i0 | tb) where i0 & cmask == cmask
+   (cmask: at most one bit); only the pairs that match are visited */
 static void pass_2x2(double* s, int n, int bit, uint64_t cmask, const double r0[4], const double r1[4]) {
-  const uint64_t half = (1ULL << n) >> 1, tb = 1ULL << bit;
+  const uint64_t tb = 1ULL << bit;
+  int bits[2], nb = 0;
+  if (cmask) {
+    const int cb = __builtin_ctzll(cmask);
+    bits[0] = cb < bit ? cb : bit;
+    bits[1] = cb < bit ? bit : cb;
+    nb = 2;
+  } else {
+    bits[0] = bit;
+    nb = 1;
+  }
+  const uint64_t cnt = (1ULL << n) >> nb;
 #pragma omp parallel for schedule(static)
-  for (uint64_t k = 0; k < half; ++k) {
-    const uint64_t i0 = ((k >> bit) << (bit + 1)) | (k & (tb - 1));
-    if ((i0 & cmask) != cmask) continue;
+  for (uint64_t k = 0; k < cnt; ++k) {
+    const uint64_t i0 = spread(k, bits, nb) | cmask;
     const uint64_t i1 = i0 | tb;
     const double xr0 = s[2 * i0], xi0 = s[2 * i0 + 1], xr1 = s[2 * i1], xi1 = s[2 * i1 + 1];
     double yr, yi;
@@ -44,11 +65,17 @@ static void pass_2x2(double* s, int n, int bit, uint64_t cmask, const double r0[
   }
 }
 
+/* amp *= (pr + i pi) where all bits of mask (two bits) are set, like the oracle's
+   cmul(amp, ph) (qgo.c apply_phase_where) */
 static void pass_phase(double* s, int n, uint64_t mask, double pr, double pi) {
-  const uint64_t N = 1ULL << n;
+  int bits[2];
+  bits[0] = __builtin_ctzll(mask);
+  bits[1] = 63 - __builtin_clzll(mask);
+  const int nb = bits[0] == bits[1] ? 1 : 2;
+  const uint64_t cnt = (1ULL << n) >> nb;
 #pragma omp parallel for schedule(static)
-  for (uint64_t i = 0; i < N; ++i) {
-    if ((i & mask) != mask) continue;
+  for (uint64_t k = 0; k < cnt; ++k) {
+    const uint64_t i = spread(k, bits, nb) | mask;
     const double ar = s[2 * i], ai = s[2 * i + 1];
     s[2 * i] = ar * pr - ai * pi;
     s[2 * i + 1] = ar * pi + ai * pr;

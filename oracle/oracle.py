@@ -47,6 +47,9 @@ def lib():
         L.or_draw64.restype = C.c_uint64
         L.or_refalgo_rows.argtypes = [DP, C.c_int, DP, C.c_int, C.c_uint64, C.c_uint64, DP]
         L.or_sample_one.argtypes = [DP, C.c_int, C.c_uint64, C.c_uint64, C.c_uint32]
+        L.or_refalgo_circuit.argtypes = [DP, C.c_int, C.POINTER(A.QgOp), C.c_int, C.c_uint64, C.c_uint64,
+                                         C.POINTER(C.c_uint64)]
+        L.or_refalgo_circuit.restype = C.c_int
         L.or_sample_one.restype = C.c_uint64
         _lib = L
     return _lib
@@ -141,6 +144,21 @@ def refalgo_rows(x: np.ndarray, gate2x2, target: int, row0: int, nrows: int) -> 
     lib().or_refalgo_rows(_dp(np.ascontiguousarray(x)), n, _dp(g), target, C.c_uint64(row0), C.c_uint64(nrows),
                           _dp(y))
     return y
+
+
+def refalgo_circuit(circuit: dict, shots: int, seed: int) -> tuple[np.ndarray, np.ndarray]:
+    """A whole circuit and its shots run by the reference's algorithm (dense Kronecker
+    mat-vec per single-qubit gate, a full probability scan per shot), single-threaded;
+    for timing the reference at the sizes it reaches. Returns (final state, outcomes)."""
+    n = circuit["num-qubits"]
+    s = zero_state(n)
+    enc = encode(circuit)
+    out = np.zeros(max(1, shots), np.uint64)
+    rc = lib().or_refalgo_circuit(_dp(s), n, enc.array, enc.count, C.c_uint64(shots), C.c_uint64(seed),
+                                  out.ctypes.data_as(C.POINTER(C.c_uint64)))
+    if rc:
+        raise ValueError(f"reference algorithm failed ({rc})")
+    return s, out[:shots]
 
 
 # ---------------------------------------------------------------------------

@@ -508,3 +508,56 @@ void or_refalgo_rows(const double* x, int n, const double* g8, int target, uint6
     st(y, r - r0, acc);
   }
 }
+
+/* A whole circuit run the way the reference runs it, for CPU timing of config-0 sized
+ * jobs: every single-qubit gate as the dense Kronecker mat-vec above (gate.clj:346-395,
+ * all 2^n x 2^n entries visited, into a fresh output vector as the reference builds a
+ * new one), every other operation with the O(2^n) loops of or_apply_op (gate.clj:424-486
+ * and the permutation gates); then `shots` shots, each the reference's measure-state
+ * (state.clj:869-913): the full probability vector, its running sums and a scan for the
+ * first cumulative sum >= u, with u drawn from Philox (the reference draws `rand`).
+ * The final state equals or_run_circuit's bit for bit (the dense row adds exact zeros).
+ * Returns 0, 1 + the index of a failing operation, or -1 when the state is not
+ * normalised for sampling. */
+int or_refalgo_circuit(double* s, int n, const qg_op* ops, int nops, uint64_t shots, uint64_t seed,
+                       uint64_t* outcomes) {
+  uint64_t N = 1ULL << n, mc = 0;
+  double* y = (double*)malloc(sizeof(double) * 2 * N);
+  double* cum = (double*)malloc(sizeof(double) * N);
+  if (!y || !cum) { free(y); free(cum); return -1; }
+  for (int k = 0; k < nops; ++k) {
+    const qg_op* op = &ops[k];
+    int oc = op->opcode;
+    int oneq = oc == QG_OP_X || oc == QG_OP_Y || oc == QG_OP_Z || oc == QG_OP_H || oc == QG_OP_S ||
+               oc == QG_OP_SDAG || oc == QG_OP_T || oc == QG_OP_TDAG || oc == QG_OP_RX || oc == QG_OP_RY ||
+               oc == QG_OP_RZ || oc == QG_OP_PHASE;
+    if (oneq) {
+      if (!check_q(n, op->q[0])) { free(y); free(cum); return k + 1; }
+      cpx g[4];
+      double g8[8];
+      gate_matrix(oc, op->angle, g);
+      for (int j = 0; j < 4; ++j) { g8[2 * j] = g[j].re; g8[2 * j + 1] = g[j].im; }
+      or_refalgo_rows(s, n, g8, op->q[0], 0, N, y);
+      memcpy(s, y, sizeof(double) * 2 * N);
+    } else if (or_apply_op(s, n, op, seed, &mc) != ORC_OK) {
+      free(y);
+      free(cum);
+      return k + 1;
+    }
+  }
+  for (uint64_t j = 0; j < shots; ++j) {
+    double tot = 0.0;
+    for (uint64_t i = 0; i < N; ++i) {
+      tot += s[2 * i] * s[2 * i] + s[2 * i + 1] * s[2 * i + 1];
+      cum[i] = tot;
+    }
+    if (fabs(tot - 1.0) > 1e-8) { free(y); free(cum); return -1; }
+    double u = (double)(or_draw64(seed, j, 0u) >> 11) * 0x1.0p-53 * tot;
+    uint64_t c = 0;
+    for (uint64_t i = 0; i < N; ++i) c += cum[i] < u;
+    outcomes[j] = c < N ? c : N - 1;
+  }
+  free(y);
+  free(cum);
+  return 0;
+}

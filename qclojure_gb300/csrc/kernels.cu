@@ -916,8 +916,7 @@ cudaError_t launch_density(const void* s, int precision, int n, double* d_rho, c
 
 size_t sampler_scratch_bytes(int n, uint64_t shots) {
   (void)shots;
-  SampleGeom g = sample_geom(n);
-  return sizeof(unsigned long long) * (g.nchunks + g.nb + (g.nb + 1)) + sizeof(double) * (g.nb + 2) + 256;
+  return sampler_scratch_bytes_at(n);  // the layout of sample_geom(n) below
 }
 
 cudaError_t launch_sample(const void* s, int precision, int n, uint64_t shots, uint64_t seed, void* d_scratch,

@@ -1225,6 +1225,7 @@ std::string pass_structure_key(const Program& prog, bool table) {
 
 std::shared_ptr<const PassKernels> pass_kernels_for(const Program& prog, int prec, int device, std::string* why,
                                                     bool table) {
+  NvtxRange nvtx("qg pass kernels");
   if (device < 0 || device >= 64) {
     *why = "device ordinal out of range";
     return nullptr;

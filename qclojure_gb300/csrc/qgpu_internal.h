@@ -11,7 +11,21 @@
 
 #include "../../include/qgpu.h"
 
+#if !defined(__CUDACC_RTC__)
+#include <nvtx3/nvToolsExt.h>
+#endif
+
 namespace qg {
+
+// A named NVTX range for the lifetime of the object (host code): admission, compile,
+// device launch and result extraction show up as ranges in a timeline profiler. The
+// header-only NVTX library does nothing unless a tool is attached.
+struct NvtxRange {
+  explicit NvtxRange(const char* name) { nvtxRangePushA(name); }
+  ~NvtxRange() { nvtxRangePop(); }
+  NvtxRange(const NvtxRange&) = delete;
+  NvtxRange& operator=(const NvtxRange&) = delete;
+};
 
 // ---------------------------------------------------------------------------
 // Device operation ("gate op") in amplitude-index space. Bit b of the basis
@@ -264,7 +278,18 @@ cudaError_t launch_gather(const void* s, int precision, const uint64_t* d_idx, i
                           cudaStream_t st);
 cudaError_t launch_density(const void* s, int precision, int n, double* d_rho, cudaStream_t st);
 
-// Hierarchical shot sampler. Scratch sized by sampler_scratch_bytes().
+// Hierarchical shot sampler. Scratch sized by sampler_scratch_bytes(); its layout:
+// chunks of min(2^n, 32) amplitudes, blocks of min(chunks, 256) chunks, then one u64
+// sum per chunk, one u64 sum per block, the blocks' exclusive prefixes plus a total,
+// and FP64 per-block sums plus two (compensated total), with 256 bytes of slack.
+constexpr size_t sampler_scratch_bytes_at(int n) {
+  const uint64_t N = 1ULL << n;
+  const uint64_t ch = N < 32 ? N : 32;
+  const uint64_t nch = N / ch;
+  const uint64_t cpb = nch < 256 ? nch : 256;
+  const uint64_t nb = nch / cpb;
+  return sizeof(unsigned long long) * (nch + nb + (nb + 1)) + sizeof(double) * (nb + 2) + 256;
+}
 size_t sampler_scratch_bytes(int n, uint64_t shots);
 cudaError_t launch_sample(const void* s, int precision, int n, uint64_t shots, uint64_t seed, void* d_scratch,
                           uint64_t* d_outcomes, double* d_total, cudaStream_t st);

@@ -372,6 +372,7 @@ static int exec_program(State* s, const Program& prog, uint64_t seed, const std:
 // sweeps batch circuits whose pass structure must not depend on their graphs.
 static int compile_program(const qg_circuit* c, int precision, int fusion, int fuse_k, int arith, Program* prog,
                            std::string* err, bool reorder = true) {
+  NvtxRange nvtx("qg compile");
   // dense fused blocks are evaluated in FP64 (FMA) whatever the arithmetic setting
   prog->arith = (fusion == QG_FUSE_DENSE || arith != QG_ARITH_DOUBLE_FLOAT) ? QG_ARITH_EXACT : QG_ARITH_DOUBLE_FLOAT;
   std::vector<GOp> gops;
@@ -723,7 +724,10 @@ static int run_job(Ctx* c, Job* j, cudaStream_t stream) {
   auto st = std::make_unique<State>();
   rc = init_job_state(c, j, stream, st.get(), &err);
   ExecStats stats;
-  if (rc == QG_OK) rc = exec_program(st.get(), *j->prog, j->seed, &j->cancel, &stats, &err);
+  if (rc == QG_OK) {
+    NvtxRange nvtx("qg launch");
+    rc = exec_program(st.get(), *j->prog, j->seed, &j->cancel, &stats, &err);
+  }
   j->device_ms = stats.device_ms;
   j->passes = stats.passes;
   j->specialised = stats.specialised;
@@ -733,6 +737,7 @@ static int run_job(Ctx* c, Job* j, cudaStream_t stream) {
 // Result extraction on the final state (result.clj:179-457), then keep the state
 // for later reads or release it.
 static int job_results(Ctx* c, Job* j, std::unique_ptr<State> st, cudaStream_t stream, int rc, std::string err) {
+  NvtxRange nvtx("qg extract");
   const SpecCopy& sp = j->spec;
   const uint64_t N = 1ULL << j->n;
   if (rc == QG_OK && (sp.flags & QG_RES_MEASUREMENTS)) {
@@ -1344,6 +1349,7 @@ int qg_ctx_capabilities(void* ctx, int32_t* mq128, int32_t* mq64, uint64_t* hbm_
 
 int qg_submit(void* ctx, const qg_circuit* circuit, const qg_options* options, uint64_t* job_out) {
   if (!ctx) return QG_ERR_INVALID_ARG;
+  NvtxRange nvtx("qg admit");
   return submit_one((Ctx*)ctx, circuit, options, job_out);
 }
 
@@ -1783,6 +1789,7 @@ int qg_state_download(void* state, double* host) {
 
 int qg_state_apply(void* state, const qg_circuit* circuit, int32_t fusion, uint64_t seed, int32_t* passes_out) {
   if (!state || !circuit) return QG_ERR_INVALID_ARG;
+  NvtxRange nvtx("qg apply");
   State* s = (State*)state;
   if (circuit->num_qubits != s->n) {
     set_ctx_error(s->ctx, "circuit and state have mismatched number of qubits");
@@ -2523,6 +2530,7 @@ int qg_sweep_update(void* sweep, const qg_circuit* circuits, int32_t count) {
 int qg_sweep_run(void* sweep, const int32_t* term_offsets, const double* coefficients, const char* pauli_strings,
                  double* energies, qg_sweep_stats* stats) {
   if (!sweep) return QG_ERR_INVALID_ARG;
+  NvtxRange nvtx("qg sweep run");
   Sweep* sw = (Sweep*)sweep;
   cudaSetDevice(sw->ctx->device);
   std::string err;

@@ -1,5 +1,5 @@
-"""Device maps (qclojure_gb300.device), restating domain/device.clj's normalisation and
-queries, and the hardware simulator normalising a device it is given."""
+"""Device normalisation (qclojure_gb300.device, domain/device.clj:50-73) and the hardware
+simulator normalising a device it is given."""
 from qclojure_gb300 import device as D
 
 
@@ -16,23 +16,13 @@ def test_supported_operations_and_validation():
     assert [x["supported-operations"] for x in D.validate_devices([d])] == [v["supported-operations"]]
 
 
-def test_fidelities_and_noise():
-    d = {"performance": {"two-qubit-gate-fidelity": 0.99, "single-qubit-gate-fidelity": 0.999}}
-    assert D.gate_fidelity(d) == 0.99 and D.gate_fidelity({}) is None
-    assert D.estimated_fidelity(d, 3) == 0.99 ** 3
-    assert D.estimated_fidelity(d, 0) is None and D.estimated_fidelity({}, 3) is None
-    assert D.noise_model({}) == {} and D.noise_model({"noise-model": {"a": 1}}) == {"a": 1}
+def test_topology_without_qubit_count_names_the_problem():
+    import pytest
 
-
-def test_circuit_checks_and_comparison():
-    c = {"num-qubits": 2, "operations": [{"operation-type": "h"}, {"operation-type": "cz"},
-                                         {"operation-type": "h"}, {"operation-type": "rx"}]}
-    r = D.validate_circuit({"supported-operations": {"h", "cnot"}}, c)
-    assert r == {"all-gates-supported?": False, "unsupported-gates": ["cz", "rx"]}
-    assert D.validate_circuit({}, c)["unsupported-gates"] == ["h", "cz", "rx"]
-    cmp = D.compare_gate_support({"supported-operations": {"h", "x"}}, {"supported-operations": {"x", "y"}})
-    assert cmp["shared-operations"] == {"x"} and cmp["device1-only"] == {"h"} and cmp["device2-only"] == {"y"}
-    assert cmp["total-unique-operations"] == {"h", "x", "y"}
+    with pytest.raises(ValueError, match="num-qubits"):
+        D.validate_device({"id": "t", "topology": "ring"})
+    with pytest.raises(ValueError, match="num-qubits"):
+        D.validate_device({"id": "t", "topology": "linear", "num-qubits": -1})
 
 
 def test_simulator_normalises_its_device(monkeypatch):

@@ -96,6 +96,54 @@ def test_mix_equals_alone_and_oracle(oracle, precision, arith, tol):
         sim.close()
 
 
+def test_served_c64_stream_tvd_against_oracle(oracle):
+    """The served complex64 contract on a mixed stream that reaches 22 qubits: jobs of
+    n = 8 + Geometric(0.15) qubits plus four of 20-22 qubits, nine in ten asking for shots
+    and the tenth for a Pauli-string expectation, all submitted while earlier ones run.
+    Every served job's outcome distribution is within TVD 1e-5 of the FP64 oracle's, its
+    expectation within 1e-5, and its result equals the same job run alone."""
+    from qclojure_gb300 import workloads
+    from qclojure_gb300.backend import create_simulator
+
+    jobs = _stream(5, count=26, cap=18)
+    rng = np.random.default_rng(77)
+    for i, n in enumerate((20, 21, 22, 20)):
+        c = workloads.layered_circuit(n, int(rng.integers(3, 8)), seed=9000 + i)
+        if i == 3:
+            pauli = "".join("IXYZ"[k] for k in rng.integers(0, 4, n))
+            spec = {"hamiltonian": [{"coefficient": 1.0, "pauli-string": pauli}], "state-vector": True}
+        else:
+            spec = SHOT_SPEC
+        jobs.insert(3 + 6 * i, (c, {"result-specs": spec}))
+    assert max(c["num-qubits"] for c, _ in jobs) >= 20
+    sim = create_simulator({"precision": "c64", "fusion": "tiled", "workers": 4, "seed": 9})
+    try:
+        ids = [sim.submit_circuit(c, o) for c, o in jobs]
+        for j in ids:
+            assert sim.wait(j, 600_000) == "completed"
+        for (c, o), jid in zip(jobs, ids):
+            r = sim.job_result(jid)
+            ref = oracle.run(c)
+            sv = _sv(r)
+            tvd = 0.5 * float(np.abs(np.abs(sv) ** 2 - np.abs(ref) ** 2).sum())
+            assert tvd <= 1e-5, (c["num-qubits"], tvd)
+            res = r["results"]
+            if "hamiltonian-result" in res:
+                p = o["result-specs"]["hamiltonian"][0]["pauli-string"]
+                assert abs(res["hamiltonian-result"]["energy-expectation"] - oracle.pauli_expectation(ref, p)) <= 1e-5
+            a_id = sim.submit_circuit(c, o)  # alone
+            assert sim.wait(a_id, 600_000) == "completed"
+            a = sim.job_result(a_id)
+            assert np.array_equal(sv, _sv(a))
+            if "measurement-results" in res:
+                assert res["measurement-results"]["measurement-outcomes"] == \
+                    a["results"]["measurement-results"]["measurement-outcomes"]
+            sim.free_job(jid)
+            sim.free_job(a_id)
+    finally:
+        sim.close()
+
+
 def test_cancel_small_job_waiting_in_queue():
     """A queued small job can be cancelled; the rest of its batch completes."""
     from qclojure_gb300 import workloads

@@ -99,6 +99,21 @@ def test_refalgo_rows_match_gate(oracle):
     assert np.allclose(y, _kron_gate(n, 2, np.array(g)) @ x, atol=1e-13)
 
 
+def test_refalgo_circuit_is_the_oracle_bit_for_bit(oracle):
+    """The whole-circuit reference algorithm (dense Kronecker row sums, zeros included)
+    leaves the oracle's final state exactly: the row adds exact zeros around the two
+    non-zero products in ascending column order (gate.clj:384-395). Its shots follow the
+    probabilities (state.clj:897-911)."""
+    from qclojure_gb300 import workloads
+
+    for n, depth, seed in ((6, 10, 1), (8, 4, 2)):
+        c = workloads.layered_circuit(n, depth, seed)
+        s, shots = oracle.refalgo_circuit(c, 2000, seed=5)
+        assert np.array_equal(s, oracle.run(c))
+        counts = np.bincount(shots.astype(np.int64), minlength=1 << n) / 2000.0
+        assert 0.5 * np.abs(counts - oracle.probabilities(s)).sum() < 0.12
+
+
 def test_controlled_gate_transpose_quirk(oracle):
     """gate.clj:473-483 applies G^T: controlled RY(t) acts as RY(-t) on the target."""
     th = 0.7

@@ -45,3 +45,19 @@ def test_noalloc_sampler_rejects_states_beyond_its_scratch(gpu_ctx):
             st.sample_noalloc(16, 1, buf.data_ptr())
         assert ei.value.code == QG_ERR_INVALID_ARG
         assert "24 qubits" in str(ei.value)
+
+
+def test_noalloc_sampler_rejects_host_outcome_buffers(gpu_ctx):
+    """The outcome buffer must be device memory of the state's device: a pageable host
+    array (numpy) is refused before any kernel runs."""
+    from qclojure_gb300 import workloads
+    from qclojure_gb300._abi import QG_ERR_INVALID_ARG, QgError
+
+    host = np.zeros(64, np.uint64)
+    with gpu_ctx.state(8, "c128") as st:
+        st.apply(workloads.layered_circuit(8, 2, seed=1), fusion="tiled")
+        with pytest.raises(QgError) as ei:
+            st.sample_noalloc(64, 1, host.ctypes.data)
+        assert ei.value.code == QG_ERR_INVALID_ARG
+        assert "device memory" in str(ei.value)
+    assert not host.any()
