@@ -49,6 +49,8 @@ def parse():
     ap.add_argument("--pass-kernels", choices=["auto", "always", "off"], default="auto",
                     help="specialised per-pass kernels (auto: states of 29 qubits and more)")
     ap.add_argument("--seed", type=int, default=1)
+    ap.add_argument("--no-autotune", action="store_true",
+                    help="keep the default pass-kernel shape instead of timing the candidates first")
     return ap.parse_args()
 
 
@@ -510,6 +512,14 @@ def main():
     N = 1 << n
     lib = A.load_library()
     ctx = Context(device=local, workers=1, seed=7, pass_kernels=args.pass_kernels)
+    # the pass kernels' tile size and launch shape, chosen on the device before timing
+    tuning = {}
+    if not args.no_autotune and args.fusion == "tiled":
+        for tp in ((args.precision, "c64") if args.precision == "c128" and not args.no_extras else (args.precision,)):
+            try:
+                tuning[tp] = ctx.autotune(n, tp)
+            except Exception as e:  # nothing to tune (exact arithmetic, interpreted sizes)
+                tuning[tp] = {"skipped": f"{type(e).__name__}: {e}"}
     st = ctx.state(n, args.precision)
     dptr, sptr = st.device_ptr()
     stream = torch.cuda.ExternalStream(sptr, device=torch.device("cuda", local))
@@ -589,7 +599,9 @@ def main():
         "dtype": "f32x2 double-float (f64 storage)" if args.precision == "c128" else "f32", "data": "synthetic",
         "config": {"workload": f"layered-{n}x{args.depth}+qft{n}", "n_qubits": n, "depth": args.depth,
                    "gates": gates, "precision": args.precision, "fusion": args.fusion,
-                   "parallelism": f"replicas{world}", "l2": "state larger than L2 (no flush needed)"},
+                   "parallelism": f"replicas{world}", "l2": "state larger than L2 (no flush needed)",
+                   "pass_kernel_shape": {k: (v.get("chosen") or v) for k, v in tuning.items()} or "default"},
+        "autotune": tuning,
         "layer_ms": layer_ms,
         "pass_kernels": {"specialised_passes": n_spec, "compile_ms": compile_ms,
                          "note": "NVRTC compile of the per-pass kernels, once per program, before timing"},
@@ -672,8 +684,9 @@ def main():
             line["oracle_30q"] = oracle_spot_check_30(ctx, n, 4, args.seed + rank, local)
         except Exception as e:  # the line must still print
             line["oracle_30q"] = {"error": f"{type(e).__name__}: {e}"}
-        # dense fused blocks of k = 1..5 qubits (one HBM pass per block), per-pass bandwidth on
-        # the first two layers of the workload; dense blocks compute in FP64 (c128) or FP32 (c64)
+        # dense fused blocks of k = 1..5 qubits, per-pass bandwidth on the first two layers of
+        # the workload: complex128 blocks compute in FP64 inside tiled passes; complex64 blocks
+        # run one HBM pass each on the tensor cores (split-TF32, kind 4 in the profile)
         dense_sample = workloads.layered_circuit(n, 2, args.seed + rank)
         dense = {"sample": f"first 2 layers of layered-{n}x{args.depth} ({len(dense_sample['operations'])} gates)"}
         for dprec in (("c128", "c64") if args.precision == "c128" else ("c64",)):
@@ -685,12 +698,14 @@ def main():
                         sk.apply(dense_sample, fusion="dense")  # warm-up
                         sk.set_basis(0)
                         pk_ms, pk_kind = sk.profile(dense_sample, fusion="dense")
-                tiles = [t for t, kk in zip(pk_ms, pk_kind) if kk == 1]
+                tiles = [t for t, kk in zip(pk_ms, pk_kind) if kk in (1, 4)]
+                ntc = sum(1 for kk in pk_kind if kk == 4)
                 bpp = 2 * (16 if dprec == "c128" else 8) * N
                 mean_k = statistics.mean(tiles) if tiles else float("nan")
-                rows[str(k)] = {"passes": len(pk_ms), "block_passes": len(tiles), "total_ms": float(sum(pk_ms)),
-                                "mean_block_pass_ms": mean_k,
-                                "block_pass_gbs": bpp / (mean_k / 1e3) / 1e9 if tiles else None}
+                rows[str(k)] = {"passes": len(pk_ms), "block_passes": len(tiles), "tensor_core_passes": ntc,
+                                "total_ms": float(sum(pk_ms)), "mean_block_pass_ms": mean_k,
+                                "block_pass_gbs": bpp / (mean_k / 1e3) / 1e9 if tiles else None,
+                                "block_pass_frac": bpp / (mean_k / 1e3) / 1e9 / peak if tiles else None}
             dense[dprec] = rows
         line["dense_blocks"] = dense
 

@@ -432,7 +432,7 @@ int qg_noisy_run(void* ctx, const qg_circuit* circuit, const qg_noise_model* noi
    qg_state_profile applies a circuit like qg_state_apply and records a CUDA event
    pair around every HBM pass on the state's stream: pass_ms[i] is the duration of
    pass i and pass_kind[i] its kind (0 plain gate, 1 tiled pass, 2 measurement,
-   3 tiled pass run by its specialised kernel).
+   3 tiled pass run by its specialised kernel, 4 dense block on the tensor cores).
    qg_kernel_launches reports how many kernels this library has launched in the
    process so far. */
 int qg_state_profile(void* state, const qg_circuit* circuit, int32_t fusion, uint64_t seed, float* pass_ms,
@@ -447,6 +447,32 @@ int qg_kernel_launches(uint64_t* count);
 int qg_pass_kernels_build(const qg_circuit* circuit, int32_t precision, int32_t arithmetic, int32_t* kernels_out,
                           double* compile_ms_out, char* err_buf, int64_t err_len);
 int qg_pass_kernels_info(int32_t* available, uint64_t* cache_hits, uint64_t* cache_misses);
+
+/* ---- autotuner (no counterpart in the reference; the reference's hook for gate
+   optimisation is gate_optimization.clj:776-860, which this tiled executor replaces) --
+   The specialised pass kernels apply a pass's gates to tiles of 2^tile_bits amplitudes,
+   each thread holding 2^reg_bits of them, with `buffers` tile buffers in shared memory
+   and the kernels built for ctas_per_sm CTAs per SM. qg_autotune times candidate shapes
+   on a calibration circuit (six layers of the layered recipe and four QFT columns) on a
+   state of num_qubits qubits, keeps the fastest (the default unless another is faster
+   by more than 1 %), records it in the context for programs of that size and precision
+   that run specialised, and reports every candidate with its median device time (ms).
+   It allocates one state of that size while it runs. qg_tuning_set records a shape
+   directly (tile_bits 0: back to the default); qg_tuning_get reports the shape in use.
+   qg_tuning_pick is the choice rule on its own: the index of the fastest valid entry,
+   or default_index when that one is within tie_frac of it (-1: none valid). */
+typedef struct qg_tuning {
+  int32_t tile_bits;    /* local qubits per tile: 11, 12 or 13 */
+  int32_t reg_bits;     /* amplitudes per thread = 2^reg_bits (3 or 4) */
+  int32_t buffers;      /* tile buffers in shared memory (1 or 2) */
+  int32_t ctas_per_sm;  /* CTAs per SM the kernels are built for */
+  double ms;            /* measured device time of the calibration circuit (qg_autotune) */
+} qg_tuning;
+int qg_autotune(void* ctx, int32_t num_qubits, int32_t precision, qg_tuning* chosen, qg_tuning* tried, int32_t cap,
+                int32_t* count_out);
+int qg_tuning_set(void* ctx, int32_t num_qubits, int32_t precision, const qg_tuning* tuning);
+int qg_tuning_get(void* ctx, int32_t num_qubits, int32_t precision, qg_tuning* out);
+int32_t qg_tuning_pick(const double* ms, const int32_t* valid, int32_t count, int32_t default_index, double tie_frac);
 
 #ifdef __cplusplus
 }

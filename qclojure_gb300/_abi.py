@@ -133,6 +133,15 @@ class QgSweepStats(C.Structure):
                 ("state_bytes", C.c_uint64)]
 
 
+class QgTuning(C.Structure):
+    _fields_ = [("tile_bits", C.c_int32), ("reg_bits", C.c_int32), ("buffers", C.c_int32),
+                ("ctas_per_sm", C.c_int32), ("ms", C.c_double)]
+
+    def as_dict(self) -> dict:
+        return {"tile_bits": self.tile_bits, "reg_bits": self.reg_bits, "buffers": self.buffers,
+                "ctas_per_sm": self.ctas_per_sm, "ms": self.ms}
+
+
 class QgGateNoise(C.Structure):
     _fields_ = [("noise_type", C.c_int32), ("present", C.c_int32), ("strength", C.c_double),
                 ("t1_us", C.c_double), ("t2_us", C.c_double), ("gate_time_ns", C.c_double),
@@ -216,6 +225,10 @@ SIGNATURES = {
     "qg_kernel_launches": ([U64P], C.c_int),
     "qg_pass_kernels_build": ([C.POINTER(QgCircuit), I32, I32, I32P, DP, C.c_char_p, I64], C.c_int),
     "qg_pass_kernels_info": ([I32P, U64P, U64P], C.c_int),
+    "qg_autotune": ([P, I32, I32, C.POINTER(QgTuning), C.POINTER(QgTuning), I32, I32P], C.c_int),
+    "qg_tuning_set": ([P, I32, I32, C.POINTER(QgTuning)], C.c_int),
+    "qg_tuning_get": ([P, I32, I32, C.POINTER(QgTuning)], C.c_int),
+    "qg_tuning_pick": ([DP, I32P, I32, I32, C.c_double], I32),
     "qg_sweep_create": ([P, C.POINTER(QgCircuit), I32, I32, I32, C.POINTER(P)], C.c_int),
     "qg_sweep_update": ([P, C.POINTER(QgCircuit), I32], C.c_int),
     "qg_sweep_run": ([P, I32P, DP, C.c_char_p, DP, C.POINTER(QgSweepStats)], C.c_int),
@@ -227,7 +240,7 @@ SIGNATURES = {
 def declared_symbols() -> list[str]:
     """Every function the header declares (used by the export test)."""
     text = HEADER.read_text()
-    return re.findall(r"^int\s+(qg_\w+)\s*\(", text, flags=re.M)
+    return re.findall(r"^(?:int|int32_t)\s+(qg_\w+)\s*\(", text, flags=re.M)
 
 
 class QgError(RuntimeError):

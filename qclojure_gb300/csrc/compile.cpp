@@ -664,11 +664,12 @@ void plan_register_groups(std::vector<TOp>& ops, int k) {
 
 int schedule(int n, int precision, int fusion, int fuse_k, const std::vector<GOp>& gops,
              const std::vector<std::vector<int>>& measures, const std::vector<int>& measure_at, Program* prog,
-             std::string* err, bool reorder) {
+             std::string* err, bool reorder, int tile_bits) {
   prog->n = n;
   prog->steps.clear();
   prog->tops.clear();
   prog->dense.clear();
+  prog->dense_tc.clear();
   prog->hbm_passes = 0;
   size_t mi = 0;
   auto emit_measures_at = [&](size_t gi) {
@@ -695,7 +696,7 @@ int schedule(int n, int precision, int fusion, int fuse_k, const std::vector<GOp
     return QG_OK;
   }
 
-  const int k = tile_bits_for(n, precision);
+  const int k = (tile_bits >= 5 && tile_bits <= kMaxTileBits && tile_bits <= n) ? tile_bits : tile_bits_for(n, precision);
   // bits 0..klow_min-1 stay local in every pass: contiguous 128-byte runs in HBM
   const int klow_min = std::min(k, precision == QG_C64 ? 4 : 3);
   const uint64_t low_mask = (klow_min >= 64) ? ~0ULL : ((1ULL << klow_min) - 1);
@@ -745,7 +746,19 @@ int schedule(int n, int precision, int fusion, int fuse_k, const std::vector<GOp
           mat[2 * (row * D + col) + 1] = v[row].imag();
         }
       }
-      prog->dense.insert(prog->dense.end(), mat.begin(), mat.end());
+      if (precision == QG_C64 && dense_tc_eligible(n, kb)) {
+        // complex64 blocks run on the tensor cores, one HBM pass each
+        std::vector<float> w;
+        int tb[5];
+        const int ke = dense_tc_prepare(n, kb, pos, mat.data(), &w, tb);
+        d.dk = ke;
+        for (int j = 0; j < ke; ++j) d.dbits[j] = tb[j];
+        d.flags = kDenseTcFlag;
+        d.doff = (int64_t)prog->dense_tc.size();
+        prog->dense_tc.insert(prog->dense_tc.end(), w.begin(), w.end());
+      } else {
+        prog->dense.insert(prog->dense.end(), mat.begin(), mat.end());
+      }
       ops.push_back(d);
       orig_index.push_back(gi);
       gi = gj;
@@ -787,6 +800,15 @@ int schedule(int n, int precision, int fusion, int fuse_k, const std::vector<GOp
       continue;
     }
     if (oi >= ops.size()) break;
+    if (ops[oi].kind == OK_DENSE && (ops[oi].flags & kDenseTcFlag)) {  // a tensor-core block is its own pass
+      Step s;
+      s.kind = Step::PLAIN_OP;
+      s.op = ops[oi];
+      prog->steps.push_back(s);
+      prog->hbm_passes += 1;
+      done[oi] = 1;
+      continue;
+    }
     uint64_t L = low_mask;
     size_t begin = oi;
     size_t limit = ops.size();
@@ -804,6 +826,7 @@ int schedule(int n, int precision, int fusion, int fuse_k, const std::vector<GOp
     uint64_t changed = 0, seen = 0;
     for (size_t j = begin; j < limit && members.size() < max_ops; ++j) {
       if (done[j]) continue;
+      if (ops[j].kind == OK_DENSE && (ops[j].flags & kDenseTcFlag)) break;
       const uint64_t tb = touched(ops[j]), r = required_local(ops[j]);
       const bool commutes = (r & seen) == 0 && ((tb & ~r) & changed) == 0;
       if (commutes && __builtin_popcountll(L | r) <= k) {

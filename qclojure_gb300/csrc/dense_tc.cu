@@ -1,0 +1,508 @@
+// Dense fused blocks on the tensor cores (complex64, one HBM pass per block).
+//
+// The gate fuser (compile.cpp, fusion "dense") multiplies a run of gates on at most
+// five qubits into one 2^k x 2^k complex block. Applied with FP32 FMAs, a block of
+// k = 4 or 5 qubits costs 8 * 2^k flops per amplitude against 16 bytes of HBM traffic,
+// which puts it on the FMA pipe, not HBM. Here the block runs on the 5th-generation
+// tensor cores instead (tcgen05.mma, kind::tf32, accumulators in tensor memory):
+//
+//   * A tile is 4096 amplitudes: every combination of the block's k target bits and
+//     the lowest 12 - k other bits. Its HBM footprint is a few contiguous runs of at
+//     least 1 KiB (all bits below the highest column bit belong to the tile), moved by
+//     the bulk-copy engine (cp.async.bulk, mbarrier completion) into a staging buffer,
+//     three tiles deep, and written back from it the same way.
+//   * The block is a real GEMM. Column c of the tile (the non-target bits, 128 per
+//     MMA) is a row of the A operand holding its 2^k amplitudes as 2^(k+1) reals
+//     (re, im interleaved); the B operand is the real form of the block,
+//     W[(r,o),(j,i)] = [[Ur, -Ui], [Ui, Ur]], so D[c, 2r+o] is output amplitude (r, c).
+//     Both operands are K-major in shared memory with the 128-byte swizzle.
+//   * Precision: every operand is split into a TF32 high part and a TF32 low part
+//     (hi = round(x), lo = round(x - hi)); D = Ahi Bhi + Alo Bhi + Ahi Blo accumulates
+//     in FP32 in tensor memory, about the accuracy of FP32 arithmetic (3xTF32).
+//   * Blocks of fewer than four qubits are widened to four on the host (the identity on
+//     the lowest other bits), so the kernel handles k = 4 and k = 5.
+//
+// Every wait on an mbarrier is bounded (about a second of wall time); on a timeout the
+// kernel records an error code, lets its bulk copies drain, frees its tensor memory and
+// returns, and the host reports the error.
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <cstring>
+#include <vector>
+
+#include "qgpu_internal.h"
+
+namespace qg {
+namespace {
+
+constexpr int kTileBits = 12;           // 4096 amplitudes (32 KiB of complex64) per tile
+constexpr int kTileAmps = 1 << kTileBits;
+constexpr int kThreads = 256;
+constexpr int kStages = 3;              // staging buffers (bulk loads in flight)
+constexpr int kStageBytes = kTileAmps * 8;
+constexpr int kAHalfBytes = 32768;      // one of A hi / A lo: 128 x 64 TF32 (k = 5) or 256 x 32 (k = 4)
+constexpr int kBHalfBytes = 16384;      // one of B hi / B lo at k = 5 (64 x 64 TF32)
+constexpr int kTmemCols = 64;
+
+struct DenseTcParams {
+  float2* state;
+  const float* w;        // B hi then B lo, already in the swizzled K-major layout (2 * bbytes)
+  int* err;              // set to a nonzero code when a wait gives up
+  uint64_t ntiles;
+  int k;                 // 4 or 5
+  int bbytes;            // bytes of one of B hi / B lo
+  // tile-local index bit t (0..11) <-> absolute bit tbit[t]; target or column bit
+  int tbit[kTileBits];
+  int tgt_of[kTileBits];   // position within j of tile bit t, or -1
+  int col_of[kTileBits];   // position within c of tile bit t, or -1
+  int runbits;             // the lowest runbits tile bits are bits 0..runbits-1
+  // tile index -> base amplitude: runs of the non-tile bits
+  int nruns;
+  int run_src[64], run_dst[64], run_len[64];
+};
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes)
+               : "memory");
+}
+__device__ __forceinline__ uint64_t global_ns() {
+  uint64_t t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+// Wait for the phase of `parity` to complete; false after about a second.
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
+  const uint32_t a = smem_u32(bar);
+  uint64_t t0 = 0;
+  for (uint32_t it = 0;; ++it) {
+    uint32_t done;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+        : "=r"(done)
+        : "r"(a), "r"(parity)
+        : "memory");
+    if (done) return true;
+    if ((it & 1023u) == 0) {
+      const uint64_t now = global_ns();
+      if (t0 == 0) t0 = now;
+      else if (now - t0 > 1000000000ull) return false;
+    }
+  }
+}
+__device__ __forceinline__ void bulk_g2s(void* dst, const void* src, uint32_t bytes, uint64_t* bar) {
+  asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                   smem_u32(dst)),
+               "l"(src), "r"(bytes), "r"(smem_u32(bar))
+               : "memory");
+}
+__device__ __forceinline__ void bulk_s2g(void* dst, const void* src, uint32_t bytes) {
+  asm volatile("cp.async.bulk.global.shared::cta.bulk_group [%0], [%1], %2;" ::"l"(dst), "r"(smem_u32(src)),
+               "r"(bytes)
+               : "memory");
+}
+__device__ __forceinline__ void bulk_commit() { asm volatile("cp.async.bulk.commit_group;" ::: "memory"); }
+__device__ __forceinline__ void bulk_wait_read_all() { asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory"); }
+__device__ __forceinline__ void bulk_wait_all() { asm volatile("cp.async.bulk.wait_group 0;" ::: "memory"); }
+__device__ __forceinline__ void fence_proxy_async() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
+__device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
+
+// Shared-memory matrix descriptor: K-major, 128-byte swizzle, 8-row groups 1024 bytes
+// apart (stride byte offset), leading byte offset unused (16), descriptor version 1.
+__device__ __forceinline__ uint64_t smem_desc(uint32_t addr) {
+  uint64_t d = 0;
+  d |= (uint64_t)((addr & 0x3FFFFu) >> 4);
+  d |= (uint64_t)(16u >> 4) << 16;
+  d |= (uint64_t)(1024u >> 4) << 32;
+  d |= (uint64_t)1 << 46;
+  d |= (uint64_t)2 << 61;
+  return d;
+}
+// Instruction descriptor of kind::tf32: FP32 accumulator, TF32 A and B, both K-major,
+// M = 128, N = n.
+__host__ __device__ constexpr uint32_t idesc_tf32(int n) {
+  return (1u << 4) | (2u << 7) | (2u << 10) | ((uint32_t)(n >> 3) << 17) | ((uint32_t)(128 >> 4) << 24);
+}
+__device__ __forceinline__ void mma_tf32(uint32_t d_tmem, uint64_t a, uint64_t b, uint32_t idesc, uint32_t acc) {
+  asm volatile(
+      "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+      " tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n}\n" ::"r"(d_tmem),
+      "l"(a), "l"(b), "r"(idesc), "r"(acc)
+      : "memory");
+}
+__device__ __forceinline__ void mma_commit(uint64_t* bar) {
+  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(smem_u32(bar))
+               : "memory");
+}
+__device__ __forceinline__ void tmem_ld32(uint32_t taddr, float* v) {
+  uint32_t r[32];
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
+      "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+        "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]),
+        "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]),
+        "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
+      : "r"(taddr));
+  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+  for (int i = 0; i < 32; ++i) v[i] = __uint_as_float(r[i]);
+}
+__device__ __forceinline__ float to_tf32(float x) {
+  uint32_t r;
+  asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(r) : "f"(x));
+  return __uint_as_float(r);
+}
+
+// Byte offset of element (row, kk) of a K-major operand with `rows` rows (a multiple
+// of 8) in 128-byte swizzled atoms: K-atoms of 32 TF32 values are separate regions of
+// rows x 128 bytes; inside one, 8-row groups are 1024 bytes apart and the 16-byte chunk
+// index is XORed with the row's position in its group.
+__host__ __device__ __forceinline__ uint32_t kmajor_off(int rows, int row, int kk) {
+  const int atom = kk >> 5, kin = kk & 31;
+  return (uint32_t)(atom * rows * 128 + (row >> 3) * 1024 + (row & 7) * 128 + ((((kin >> 2) ^ (row & 7)) << 4)) +
+                    ((kin & 3) << 2));
+}
+
+__device__ __forceinline__ uint64_t tile_base(const DenseTcParams& p, uint64_t t) {
+  uint64_t b = 0;
+  for (int r = 0; r < p.nruns; ++r) b |= ((t >> p.run_src[r]) & ((1ull << p.run_len[r]) - 1)) << p.run_dst[r];
+  return b;
+}
+
+__global__ void __launch_bounds__(kThreads, 1) k_dense_tc(const __grid_constant__ DenseTcParams p) {
+  extern __shared__ __align__(1024) unsigned char smem_raw[];
+  // 1024-aligned regions: A hi, A lo (also the epilogue's transposition buffer), B hi, B lo, staging
+  unsigned char* base = (unsigned char*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
+  unsigned char* a_hi = base;
+  unsigned char* a_lo = a_hi + kAHalfBytes;
+  unsigned char* b_hi = a_lo + kAHalfBytes;
+  unsigned char* b_lo = b_hi + kBHalfBytes;
+  unsigned char* stage = b_lo + kBHalfBytes;
+  uint64_t* full = reinterpret_cast<uint64_t*>(stage + kStages * kStageBytes);
+  uint64_t* mma_bar = full + kStages;
+  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(mma_bar + 1);
+  uint16_t* j_of = reinterpret_cast<uint16_t*>(tmem_slot + 2);     // tile index -> j (4096)
+  uint16_t* c_of = j_of + kTileAmps;                                // tile index -> c (4096)
+
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int k = p.k;
+  const int D = 1 << k;                    // target combinations
+  const int Kp = 2 * D;                    // reals per column (K of the GEMM)
+  const int Np = Kp;                       // reals per output column (N of the GEMM)
+  const int G = (k == 4) ? 2 : 1;          // 128-column MMA blocks per tile
+  const int Mrows = 128 * G;               // columns of a tile
+  const uint32_t idesc = idesc_tf32(Np);
+
+  for (int i = tid; i < kTileAmps; i += kThreads) {
+    int j = 0, c = 0;
+    for (int t = 0; t < kTileBits; ++t) {
+      const int bit = (i >> t) & 1;
+      if (p.tgt_of[t] >= 0) j |= bit << p.tgt_of[t];
+      else c |= bit << p.col_of[t];
+    }
+    j_of[i] = (uint16_t)j;
+    c_of[i] = (uint16_t)c;
+  }
+  // the block's real form, hi and lo, already laid out by the host
+  for (int i = tid * 4; i < p.bbytes / 4; i += kThreads * 4) {
+    *reinterpret_cast<float4*>(b_hi + 4 * i) = *reinterpret_cast<const float4*>(p.w + i);
+    *reinterpret_cast<float4*>(b_lo + 4 * i) = *reinterpret_cast<const float4*>(p.w + p.bbytes / 4 + i);
+  }
+  if (tid == 0) {
+    for (int s = 0; s < kStages; ++s) mbar_init(&full[s], 1);
+    mbar_init(mma_bar, 1);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tmem_slot)),
+                 "r"(kTmemCols)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+  }
+  fence_proxy_async();
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem = *tmem_slot;
+
+  const uint64_t t_begin = p.ntiles * blockIdx.x / gridDim.x, t_end = p.ntiles * (blockIdx.x + 1) / gridDim.x;
+  const uint64_t count = t_end - t_begin;
+  const int nrun = 1 << (kTileBits - p.runbits);
+  const uint32_t run_bytes = (uint32_t)(8u << p.runbits);
+
+  // thread 0: bulk-load this CTA's tile number r (tile t_begin + r) into buffer r % kStages
+  auto issue_load = [&](uint64_t r) {
+    const int s = (int)(r % kStages);
+    uint64_t* bar = &full[s];
+    mbar_expect_tx(bar, (uint32_t)kStageBytes);
+    const uint64_t tb = tile_base(p, t_begin + r);
+    for (int q = 0; q < nrun; ++q) {
+      uint64_t off = 0;
+      for (int b = p.runbits; b < kTileBits; ++b)
+        if ((q >> (b - p.runbits)) & 1) off |= 1ull << p.tbit[b];
+      bulk_g2s(stage + s * kStageBytes + (size_t)q * run_bytes, p.state + tb + off, run_bytes, bar);
+    }
+  };
+  uint64_t issued = 0;  // loads issued (thread 0's count)
+  if (tid == 0) {
+    for (; issued < 2 && issued < count; ++issued) issue_load(issued);
+  }
+
+  bool failed = false;
+  uint64_t r = 0;
+  for (; r < count; ++r) {
+    const int s = (int)(r % kStages);
+    bool ok = mbar_wait(&full[s], (uint32_t)(r / kStages) & 1u);
+    if (__syncthreads_or(!ok)) {
+      failed = true;
+      break;
+    }
+    // staging (address order) -> A hi / A lo (column rows, K-major, swizzled)
+    const float2* st = reinterpret_cast<const float2*>(stage + s * kStageBytes);
+    for (int i = tid; i < kTileAmps; i += kThreads) {
+      const float2 x = st[i];
+      const int j = j_of[i], c = c_of[i];
+      const float hr = to_tf32(x.x), hi_ = to_tf32(x.y);
+      const float lr = to_tf32(x.x - hr), li = to_tf32(x.y - hi_);
+      const uint32_t off = kmajor_off(Mrows, c, 2 * j);
+      *reinterpret_cast<float2*>(a_hi + off) = make_float2(hr, hi_);
+      *reinterpret_cast<float2*>(a_lo + off) = make_float2(lr, li);
+    }
+    fence_proxy_async();
+    tc_fence_before();
+    __syncthreads();
+    if (tid == 0) {
+      tc_fence_after();
+      const uint32_t ah = smem_u32(a_hi), al = smem_u32(a_lo), bh = smem_u32(b_hi), bl = smem_u32(b_lo);
+      uint32_t acc = 0;
+      for (int step = 0; step < Kp / 8; ++step) {
+        const int atom = step >> 2;
+        const uint32_t kin = (uint32_t)(step & 3) * 32u;
+        const uint32_t boff = (uint32_t)(atom * Np * 128) + kin;
+        for (int g = 0; g < G; ++g) {
+          const uint32_t aoff = (uint32_t)(atom * Mrows * 128 + g * 128 * 128) + kin;
+          const uint32_t d = tmem + (uint32_t)(g * Np);
+          mma_tf32(d, smem_desc(ah + aoff), smem_desc(bh + boff), idesc, acc);
+          mma_tf32(d, smem_desc(al + aoff), smem_desc(bh + boff), idesc, 1);
+          mma_tf32(d, smem_desc(ah + aoff), smem_desc(bl + boff), idesc, 1);
+        }
+        acc = 1;
+      }
+      mma_commit(mma_bar);
+      // the buffer of tile r - 1 is free once its store has read it: load tile r + 2 there
+      bulk_wait_read_all();
+      if (issued < count && issued == r + 2) issue_load(issued++);
+    }
+    ok = mbar_wait(mma_bar, (uint32_t)r & 1u);
+    if (__syncthreads_or(!ok)) {
+      failed = true;
+      break;
+    }
+    tc_fence_after();
+    // accumulators -> out[c][n'] (pitch Np + 1 floats), in the A region
+    {
+      float v[32];
+      const int quarter = warp & 3, half = warp >> 2;
+      tmem_ld32(tmem + ((uint32_t)(32 * quarter) << 16) + (uint32_t)(half * 32), v);
+      float* out = reinterpret_cast<float*>(a_hi);
+      const int row = 32 * quarter + lane;
+      const int c = (G == 2 ? half * 128 : 0) + row;
+      const int n0 = (G == 2) ? 0 : half * 32;
+#pragma unroll
+      for (int q = 0; q < 32; ++q) out[c * (Np + 1) + n0 + q] = v[q];
+    }
+    tc_fence_before();
+    __syncthreads();
+    {
+      const float* out = reinterpret_cast<const float*>(a_hi);
+      float2* so = reinterpret_cast<float2*>(stage + s * kStageBytes);
+      for (int i = tid; i < kTileAmps; i += kThreads) {
+        const int j = j_of[i], c = c_of[i];
+        so[i] = make_float2(out[c * (Np + 1) + 2 * j], out[c * (Np + 1) + 2 * j + 1]);
+      }
+    }
+    fence_proxy_async();
+    __syncthreads();
+    if (tid == 0) {
+      const uint64_t tb = tile_base(p, t_begin + r);
+      for (int q = 0; q < nrun; ++q) {
+        uint64_t off = 0;
+        for (int b = p.runbits; b < kTileBits; ++b)
+          if ((q >> (b - p.runbits)) & 1) off |= 1ull << p.tbit[b];
+        bulk_s2g(p.state + tb + off, stage + s * kStageBytes + (size_t)q * run_bytes, run_bytes);
+      }
+      bulk_commit();
+    }
+  }
+  if (failed && tid == 0) {
+    // let the loads still in flight land (bounded) before the shared memory goes away
+    for (uint64_t q = r; q < issued; ++q) mbar_wait(&full[q % kStages], (uint32_t)(q / kStages) & 1u);
+  }
+  if (failed && tid == 0) atomicExch(p.err, 1);
+  if (tid == 0) bulk_wait_all();
+  tc_fence_before();
+  __syncthreads();
+  if (warp == 0) {
+    tc_fence_after();
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(kTmemCols) : "memory");
+  }
+}
+
+size_t dense_tc_smem_bytes() {
+  return 1024 + 2 * kAHalfBytes + 2 * kBHalfBytes + kStages * kStageBytes + (kStages + 1) * 8 + 8 +
+         2 * kTileAmps * sizeof(uint16_t);
+}
+
+}  // namespace
+
+bool dense_tc_eligible(int n, int dk) { return dk >= 1 && dk <= 5 && n >= kTileBits; }
+
+// The block's real form for the kernel: a 2^k x 2^k complex block (row-major, (re, im)
+// per entry; bit b of a row or column index is absolute bit pos[b]) widened to
+// k_eff = max(k, 4) target bits with the identity on the lowest other bits, then
+// W[(r,o),(j,i)] = [[Ur, -Ui], [Ui, Ur]] split into TF32 hi and lo parts and laid out
+// K-major with the 128-byte swizzle (N = K = 2^(k_eff+1) rows and columns).
+// Returns the widened target bits in tbits_out (ascending) and the floats in w_out.
+int dense_tc_prepare(int n, int dk, const int* pos, const double* mat, std::vector<float>* w_out, int* tbits_out) {
+  int tb[5], ke = dk;
+  for (int i = 0; i < dk; ++i) tb[i] = pos[i];
+  // widen with the lowest bits not already targets
+  uint64_t used = 0;
+  for (int i = 0; i < dk; ++i) used |= 1ull << pos[i];
+  std::vector<int> extra;
+  for (int b = 0; b < n && ke + (int)extra.size() < 4; ++b)
+    if (!(used & (1ull << b))) extra.push_back(b);
+  for (int b : extra) tb[ke++] = b;
+  // sort the widened bits; perm[i] = index in the sorted order of original slot i
+  int order[5];
+  for (int i = 0; i < ke; ++i) order[i] = i;
+  for (int i = 0; i < ke; ++i)
+    for (int j = i + 1; j < ke; ++j)
+      if (tb[order[j]] < tb[order[i]]) std::swap(order[i], order[j]);
+  int sorted_pos_of_slot[5];
+  for (int r = 0; r < ke; ++r) sorted_pos_of_slot[order[r]] = r;
+  for (int r = 0; r < ke; ++r) tbits_out[r] = tb[order[r]];
+  const int De = 1 << ke, D = 1 << dk;
+  // widened complex block in sorted-bit indexing
+  std::vector<double> U(2 * (size_t)De * De, 0.0);
+  auto remap = [&](int idx_slots) {  // index over slots (0..dk-1 original, then extras) -> sorted index
+    int out = 0;
+    for (int sl = 0; sl < ke; ++sl)
+      if ((idx_slots >> sl) & 1) out |= 1 << sorted_pos_of_slot[sl];
+    return out;
+  };
+  for (int ex = 0; ex < (1 << (ke - dk)); ++ex)
+    for (int r = 0; r < D; ++r)
+      for (int c = 0; c < D; ++c) {
+        const int R = remap(r | (ex << dk)), C = remap(c | (ex << dk));
+        U[2 * ((size_t)R * De + C)] = mat[2 * ((size_t)r * D + c)];
+        U[2 * ((size_t)R * De + C) + 1] = mat[2 * ((size_t)r * D + c) + 1];
+      }
+  const int K = 2 * De, N = K;
+  const int bytes = N * K * 4;
+  w_out->assign((size_t)2 * bytes / 4, 0.0f);
+  float* whi = w_out->data();
+  float* wlo = whi + bytes / 4;
+  for (int r = 0; r < De; ++r)
+    for (int o = 0; o < 2; ++o)
+      for (int j = 0; j < De; ++j)
+        for (int i = 0; i < 2; ++i) {
+          const double ur = U[2 * ((size_t)r * De + j)], ui = U[2 * ((size_t)r * De + j) + 1];
+          const double w = (o == 0) ? (i == 0 ? ur : -ui) : (i == 0 ? ui : ur);
+          // TF32: 10 explicit mantissa bits, round to nearest (ties away) on the host
+          auto tf32 = [](double x) {
+            float f = (float)x;
+            uint32_t u;
+            std::memcpy(&u, &f, 4);
+            if ((u & 0x7f800000u) != 0x7f800000u) u = (u + 0x1000u) & 0xffffe000u;
+            std::memcpy(&f, &u, 4);
+            return f;
+          };
+          const float h = tf32(w);
+          const float l = tf32(w - (double)h);
+          const uint32_t off = kmajor_off(N, 2 * r + o, 2 * j + i) / 4;
+          whi[off] = h;
+          wlo[off] = l;
+        }
+  return ke;
+}
+
+cudaError_t launch_dense_tc(void* state, int n, int ke, const int* tbits, const float* d_w, int* d_err,
+                            cudaStream_t st) {
+  if (ke != 4 && ke != 5) return cudaErrorInvalidValue;
+  DenseTcParams p;
+  std::memset(&p, 0, sizeof(p));
+  p.state = (float2*)state;
+  p.w = d_w;
+  p.err = d_err;
+  p.k = ke;
+  p.bbytes = (2 << ke) * (2 << ke) * 4;
+  p.ntiles = 1ull << (n - kTileBits);
+  // tile bits: the targets and the lowest 12 - k other bits
+  uint64_t tmask = 0;
+  for (int i = 0; i < ke; ++i) tmask |= 1ull << tbits[i];
+  uint64_t cols = 0;
+  int nc = 0;
+  for (int b = 0; b < n && nc < kTileBits - ke; ++b)
+    if (!(tmask & (1ull << b))) {
+      cols |= 1ull << b;
+      ++nc;
+    }
+  const uint64_t all = tmask | cols;
+  int t = 0, jn = 0, cn = 0;
+  for (int b = 0; b < n; ++b)
+    if (all & (1ull << b)) {
+      p.tbit[t] = b;
+      p.tgt_of[t] = (tmask >> b) & 1 ? jn++ : -1;
+      p.col_of[t] = (cols >> b) & 1 ? cn++ : -1;
+      ++t;
+    }
+  int rb = 0;
+  while (rb < kTileBits && p.tbit[rb] == rb) ++rb;
+  p.runbits = rb;
+  if (rb < 1) return cudaErrorInvalidValue;  // the lowest bit always belongs to the tile
+  // runs of the remaining bits (tile index bit -> absolute bit)
+  int src = 0;
+  p.nruns = 0;
+  for (int b = 0; b < n;) {
+    if (all & (1ull << b)) {
+      ++b;
+      continue;
+    }
+    const int dst = b;
+    int len = 0;
+    while (b < n && !(all & (1ull << b))) {
+      ++b;
+      ++len;
+    }
+    p.run_src[p.nruns] = src;
+    p.run_dst[p.nruns] = dst;
+    p.run_len[p.nruns] = len;
+    ++p.nruns;
+    src += len;
+  }
+  static bool attr_set[64] = {};
+  int dev = 0;
+  cudaGetDevice(&dev);
+  const size_t smem = dense_tc_smem_bytes();
+  if (dev >= 0 && dev < 64 && !attr_set[dev]) {
+    cudaError_t e = cudaFuncSetAttribute(k_dense_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    attr_set[dev] = true;
+  }
+  int sms = kSMCount;
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  const uint64_t grid = p.ntiles < (uint64_t)sms ? p.ntiles : (uint64_t)sms;
+  k_dense_tc<<<(unsigned)grid, kThreads, smem, st>>>(p);
+  count_launch(1);
+  return cudaGetLastError();
+}
+
+}  // namespace qg

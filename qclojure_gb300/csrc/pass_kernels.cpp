@@ -285,14 +285,20 @@ Shape shape_for(int prec) {
   if (prec == QG_C128) return Shape{3, 2, 1};
   return Shape{4, 2, 2};
 }
+// A program's own shape (set by the autotuner, qg_tuning) or the precision's default.
+Shape shape_of(const Program& prog, int prec) {
+  if (prog.rbits > 0 && prog.bufs > 0 && prog.ctas > 0) return Shape{prog.rbits, prog.bufs, prog.ctas};
+  return shape_for(prec);
+}
 
 class PassGen {
  public:
   // table = true: the matrix entries are read from a per-state table in shared
   // memory (cs[16 * op + q], op numbered in the pass's own op order) instead of
   // literals, so one kernel serves every state of a parameter sweep.
-  PassGen(std::ostringstream& o, const PassDesc& pd, const TOp* ops, int nops, int prec, int io, bool table = false)
-      : out_(o), pd_(pd), df_(prec == QG_C128), io_(io), tab_(table), sh_(shape_for(prec)) {
+  PassGen(std::ostringstream& o, const PassDesc& pd, const TOp* ops, int nops, int prec, int io, bool table,
+          Shape sh)
+      : out_(o), pd_(pd), df_(prec == QG_C128), io_(io), tab_(table), sh_(sh) {
     std::vector<TOp> tagged(ops, ops + nops);
     for (int i = 0; i < nops; ++i) {
       tagged[i].pad1 = i;  // the op's row in the coefficient table
@@ -1038,6 +1044,7 @@ cudaError_t fill_root_table(cudaLibrary_t lib) {
 }
 
 struct Compiled : PassKernels {
+  Shape sh{0, 0, 0};                 // the kernels' launch shape
   std::vector<cudaLibrary_t> libs;
   std::vector<cudaKernel_t> kernel;  // per program step (nullptr: interpreted)
   std::vector<int> smem;             // dynamic shared memory per step
@@ -1104,11 +1111,13 @@ bool generate_units(const Program& prog, int prec, std::vector<Unit>* units, std
   size_t total = 0;
   for (size_t i = 0; i < prog.steps.size(); ++i) {
     const Step& st = prog.steps[i];
-    if (st.kind != Step::TILE_PASS || st.pass.k != 12) continue;
+    const Shape sh = shape_of(prog, prec);
+    // a full tile of at least 2^11 amplitudes, a warp or more of threads
+    if (st.kind != Step::TILE_PASS || st.pass.k < 11 || st.pass.k - sh.rbits < 5) continue;
     const TOp* ops = prog.tops.data() + st.pass.op_begin;
     const int nops = (int)(st.pass.op_end - st.pass.op_begin);
     std::ostringstream o;
-    PassGen g(o, st.pass, ops, nops, prec, tile_pass_io(prog, i), table);
+    PassGen g(o, st.pass, ops, nops, prec, tile_pass_io(prog, i), table, sh);
     if (!g.supported()) continue;
     g.emit((int)i);
     pieces.emplace_back((int)i, o.str());
@@ -1231,7 +1240,10 @@ std::shared_ptr<const PassKernels> pass_kernels_for(const Program& prog, int pre
     return nullptr;
   }
   // generating the source for every run of a cached program would cost more than a lookup
-  const std::string key = std::to_string(prec) + ":" + pass_structure_key(prog, table);
+  const Shape shape = shape_of(prog, prec);
+  const std::string key = std::to_string(prec) + ":" + std::to_string(shape.rbits) + "/" +
+                          std::to_string(shape.bufs) + "/" + std::to_string(shape.ctas) + ":" +
+                          pass_structure_key(prog, table);
   {
     std::lock_guard<std::mutex> lk(g_mu);
     if (std::shared_ptr<Compiled>* hit = g_cache[device].find(key)) {
@@ -1251,6 +1263,7 @@ std::shared_ptr<const PassKernels> pass_kernels_for(const Program& prog, int pre
   const auto t0 = std::chrono::steady_clock::now();
   if (!compile_units(units, why)) return remember_failure();
   auto c = std::make_shared<Compiled>();
+  c->sh = shape;
   c->kernel.assign(prog.steps.size(), nullptr);
   c->smem.assign(prog.steps.size(), 0);
   const int E = prec == QG_C128 ? 16 : 8;
@@ -1275,7 +1288,7 @@ std::shared_ptr<const PassKernels> pass_kernels_for(const Program& prog, int pre
         *why = "pass kernel " + name + " missing";
         return nullptr;
       }
-      const Shape sh = shape_for(prec);
+      const Shape sh = shape;
       const PassDesc& pd = prog.steps[s].pass;
       const int smem = sh.bufs * (1 << pd.k) * E + (table ? 16 * 4 * (int)(pd.op_end - pd.op_begin) : 0);
       e = cudaKernelSetAttributeForDevice(k, cudaFuncAttributeMaxDynamicSharedMemorySize, smem, device);
@@ -1305,7 +1318,8 @@ cudaError_t launch_pass_kernel(const PassKernels& pk, size_t step, int n, const 
   const Compiled& c = static_cast<const Compiled&>(pk);
   if (step >= c.kernel.size() || !c.kernel[step]) return cudaErrorInvalidValue;
   const uint64_t ntiles = 1ULL << (n - pd.k);
-  const Shape sh = shape_for(prec);
+  const Shape sh = c.sh;
+  (void)prec;
   uint64_t grid = (uint64_t)kSMCount * sh.ctas;
   if (grid > ntiles) grid = ntiles;
   unsigned long long nt = ntiles;
@@ -1323,7 +1337,8 @@ cudaError_t launch_pass_kernel_batch(const PassKernels& pk, size_t step, int n, 
   const Compiled& c = static_cast<const Compiled&>(pk);
   if (step >= c.kernel.size() || !c.kernel[step] || nstates < 1) return cudaErrorInvalidValue;
   const uint64_t ntiles = 1ULL << (n - pd.k);
-  const Shape sh = shape_for(prec);
+  const Shape sh = c.sh;
+  (void)prec;
   uint64_t grid = (uint64_t)kSMCount * sh.ctas;
   if (grid > ntiles * (uint64_t)nstates) grid = ntiles * (uint64_t)nstates;
   unsigned long long nt = ntiles;
@@ -1363,7 +1378,7 @@ void pass_coefficients(const Program& prog, size_t step, int prec, float* out) {
   if (!parity) return;
   std::vector<TOp> tagged(ops, ops + nops);
   for (int i = 0; i < nops; ++i) tagged[i].pad1 = i;
-  const std::vector<TOp> plan = plan_layouts(tagged.data(), nops, pd.k, shape_for(prec).rbits, true);
+  const std::vector<TOp> plan = plan_layouts(tagged.data(), nops, pd.k, shape_of(prog, prec).rbits, true);
   auto put = [&](float* at, std::complex<double> v) {
     if (prec == QG_C128) {
       const float rh = (float)v.real(), ih = (float)v.imag();

@@ -136,8 +136,11 @@ struct Program {
   std::vector<Step> steps;
   std::vector<TOp> tops;             // all tile ops, referenced by PassDesc ranges
   std::vector<double> dense;         // dense block matrices (re, im interleaved)
+  std::vector<float> dense_tc;       // tensor-core blocks: TF32 hi / lo operands (dense_tc_prepare)
   int hbm_passes = 0;
   int arith = QG_ARITH_EXACT;        // complex128 arithmetic of the tiled passes
+  // shape of the specialised pass kernels (qg_tuning); 0: the precision's default
+  int32_t rbits = 0, bufs = 0, ctas = 0;
 };
 
 // Compile a reference-level circuit into GOps (returns QG_OK or an error code;
@@ -151,9 +154,10 @@ constexpr int kFactorNone = 0, kFactorRotations = 1;
 void factor_global_phases(std::vector<GOp>* gops, std::vector<int>* measure_at, int rotations);
 // Schedule GOps into passes for the given fusion mode; reorder lets commuting ops
 // overtake each other to fill passes (tolerance-held policies only).
+// tile_bits: local qubits per tile (0: tile_bits_for(n, precision)).
 int schedule(int n, int precision, int fusion, int fuse_k, const std::vector<GOp>& gops,
              const std::vector<std::vector<int>>& measures, const std::vector<int>& measure_at,
-             Program* prog, std::string* err, bool reorder);
+             Program* prog, std::string* err, bool reorder, int tile_bits = 0);
 
 // ---------------------------------------------------------------------------
 // Kernel launchers (kernels.cu). All return cudaError_t from the launch.
@@ -298,6 +302,17 @@ cudaError_t launch_sample(const void* s, int precision, int n, uint64_t shots, u
 // address for `device` (which must be current), resolved once per device, and its size.
 constexpr int kNoAllocSampleMaxQubits = 24;
 cudaError_t noalloc_sample_scratch(int device, void** ptr, size_t* bytes);
+
+// Dense blocks on the tensor cores (dense_tc.cu, complex64). A block of dk <= 5 qubits
+// of an n >= 12 qubit state qualifies; dense_tc_prepare widens it to ke = max(dk, 4)
+// target bits (tbits_out, ascending), lays out its TF32 operands (w_out) and returns
+// ke; launch_dense_tc applies it in one HBM pass and sets *d_err when a bounded wait
+// inside the kernel gives up.
+constexpr int kDenseTcFlag = 1;  // GOp::flags of an OK_DENSE op run by launch_dense_tc
+bool dense_tc_eligible(int n, int dk);
+int dense_tc_prepare(int n, int dk, const int* pos, const double* mat, std::vector<float>* w_out, int* tbits_out);
+cudaError_t launch_dense_tc(void* state, int n, int ke, const int* tbits, const float* d_w, int* d_err,
+                            cudaStream_t st);
 
 int reduce_blocks_for(int n);
 unsigned long long kernel_launch_count();

@@ -301,6 +301,16 @@ static int exec_program(State* s, const Program& prog, uint64_t seed, const std:
                        s->stream),
        "H2D dense");
   }
+  float* d_tc = nullptr;  // tensor-core block operands, then one int: the kernels' error word
+  int* d_tc_err = nullptr;
+  if (!prog.dense_tc.empty()) {
+    const size_t wb = sizeof(float) * prog.dense_tc.size(), wb_al = (wb + 255) / 256 * 256;
+    CK(cudaMallocAsync((void**)&d_tc, wb_al + 256, s->stream), "alloc dense tc");
+    CK(cudaMemcpyAsync(d_tc, prog.dense_tc.data(), wb, cudaMemcpyHostToDevice, s->stream), "H2D dense tc");
+    d_tc_err = (int*)((char*)d_tc + wb_al);
+    CK(cudaMemsetAsync(d_tc_err, 0, sizeof(int), s->stream), "clear dense tc error");
+    CK(cudaStreamSynchronize(s->stream), "sync");  // the program's host vector may go away
+  }
   cudaEvent_t e0, e1;
   CK(cudaEventCreate(&e0), "event");
   CK(cudaEventCreate(&e1), "event");
@@ -323,7 +333,10 @@ static int exec_program(State* s, const Program& prog, uint64_t seed, const std:
     const Step& st = prog.steps[i];
     if (profile) cudaEventRecord(evs[i], s->stream);
     cudaError_t e = cudaSuccess;
-    if (st.kind == Step::PLAIN_OP) {
+    if (st.kind == Step::PLAIN_OP && st.op.kind == OK_DENSE && (st.op.flags & kDenseTcFlag)) {
+      e = launch_dense_tc(s->d, s->n, st.op.dk, st.op.dbits, d_tc + st.op.doff, d_tc_err, s->stream);
+      if (profile) spec_step[i] = 2;
+    } else if (st.kind == Step::PLAIN_OP) {
       e = launch_plain_op(s->d, s->prec, s->n, st.op, s->stream);
     } else if (st.kind == Step::TILE_PASS) {
       if (pk && pass_kernel_ready(*pk, i)) {
@@ -355,9 +368,19 @@ static int exec_program(State* s, const Program& prog, uint64_t seed, const std:
       if (rc == QG_OK) cudaEventElapsedTime(&t, evs[i], evs[i + 1]);
       stats->pass_ms->push_back(t);
       const Step::Kind k = prog.steps[i].kind;
-      stats->pass_kind->push_back(k == Step::PLAIN_OP ? 0 : k == Step::TILE_PASS ? (spec_step[i] ? 3 : 1) : 2);
+      stats->pass_kind->push_back(k == Step::PLAIN_OP ? (spec_step[i] == 2 ? 4 : 0)
+                                  : k == Step::TILE_PASS ? (spec_step[i] ? 3 : 1) : 2);
     }
     for (auto& ev : evs) cudaEventDestroy(ev);
+  }
+  if (d_tc) {
+    int tc_err = 0;
+    if (cudaMemcpyAsync(&tc_err, d_tc_err, sizeof(int), cudaMemcpyDeviceToHost, s->stream) == cudaSuccess &&
+        cudaStreamSynchronize(s->stream) == cudaSuccess && tc_err != 0 && rc == QG_OK) {
+      *err = "dense block kernel: a bounded wait gave up (tensor-core pass did not complete)";
+      rc = QG_ERR_DEVICE;
+    }
+    cudaFreeAsync(d_tc, s->stream);
   }
   if (d_dense) cudaFreeAsync(d_dense, s->stream);
   if (d_kops) cudaFreeAsync(d_kops, s->stream);
@@ -371,8 +394,13 @@ static int exec_program(State* s, const Program& prog, uint64_t seed, const std:
 // reorder = false keeps passes in circuit order even for tolerance-held policies:
 // sweeps batch circuits whose pass structure must not depend on their graphs.
 static int compile_program(const qg_circuit* c, int precision, int fusion, int fuse_k, int arith, Program* prog,
-                           std::string* err, bool reorder = true) {
+                           std::string* err, bool reorder = true, const qg_tuning* tune = nullptr) {
   NvtxRange nvtx("qg compile");
+  if (tune) {
+    prog->rbits = tune->reg_bits;
+    prog->bufs = tune->buffers;
+    prog->ctas = tune->ctas_per_sm;
+  }
   // dense fused blocks are evaluated in FP64 (FMA) whatever the arithmetic setting
   prog->arith = (fusion == QG_FUSE_DENSE || arith != QG_ARITH_DOUBLE_FLOAT) ? QG_ARITH_EXACT : QG_ARITH_DOUBLE_FLOAT;
   std::vector<GOp> gops;
@@ -384,7 +412,7 @@ static int compile_program(const qg_circuit* c, int precision, int fusion, int f
   if (fusion == QG_FUSE_TILED && tolerance_held)
     factor_global_phases(&gops, &measure_at, reorder ? kFactorRotations : kFactorNone);
   return schedule(c->num_qubits, precision, fusion, fuse_k, gops, measures, measure_at, prog, err,
-                  reorder && fusion == QG_FUSE_TILED && tolerance_held);
+                  reorder && fusion == QG_FUSE_TILED && tolerance_held, tune ? tune->tile_bits : 0);
 }
 
 // ---------------------------------------------------------------------------
@@ -614,7 +642,29 @@ struct Ctx {
   int sm_count = 0;
   std::string last_error;
   std::mutex err_mu;
+  // pass-kernel shapes chosen by qg_autotune / qg_tuning_set, per (qubits, precision)
+  std::mutex tune_mu;
+  std::map<std::pair<int, int>, qg_tuning> tunings;
 };
+
+// True when programs of this kind run as specialised pass kernels (the condition
+// maybe_pass_kernels applies at run time), so a tuned shape applies to them.
+static bool will_specialise(const Ctx* c, int n, int prec, int arith, int fusion) {
+  if (fusion != QG_FUSE_TILED) return false;
+  if (prec == QG_C128 && arith != QG_ARITH_DOUBLE_FLOAT) return false;
+  const int mode = c->cfg.pass_kernels;
+  if (mode == QG_PASS_KERNELS_OFF) return false;
+  return mode == QG_PASS_KERNELS_ALWAYS || n >= kPassKernelMinQubits;
+}
+// The tuned shape for programs of this kind, if one was chosen (copied into *out).
+static const qg_tuning* tuning_for(Ctx* c, int n, int prec, int arith, int fusion, qg_tuning* out) {
+  if (!c || !will_specialise(c, n, prec, arith, fusion)) return nullptr;
+  std::lock_guard<std::mutex> lk(c->tune_mu);
+  auto it = c->tunings.find({n, prec});
+  if (it == c->tunings.end()) return nullptr;
+  *out = it->second;
+  return out;
+}
 
 static std::shared_ptr<const PassKernels> maybe_pass_kernels(const State* s, const Program& prog) {
   const Ctx* c = s->ctx;
@@ -683,7 +733,9 @@ static bool make_room(Ctx* c, size_t need) {
 static int compile_job(Ctx* c, Job* j, std::string* err) {
   auto prog = std::make_unique<Program>();
   qg_circuit circ{j->n, (int32_t)j->ops.size(), j->ops.data()};
-  const int rc = compile_program(&circ, j->precision, j->fusion, c->cfg.fuse_k, j->arith, prog.get(), err);
+  qg_tuning tu;
+  const qg_tuning* tune = tuning_for(c, j->n, j->precision, j->arith, j->fusion, &tu);
+  const int rc = compile_program(&circ, j->precision, j->fusion, c->cfg.fuse_k, j->arith, prog.get(), err, true, tune);
   if (rc == QG_OK) j->prog = std::move(prog);
   return rc;
 }
@@ -1798,7 +1850,10 @@ int qg_state_apply(void* state, const qg_circuit* circuit, int32_t fusion, uint6
   cudaSetDevice(s->ctx->device);
   std::string err;
   Program prog;
-  int rc = compile_program(circuit, s->prec, fusion, s->ctx->cfg.fuse_k, s->ctx->cfg.arithmetic, &prog, &err);
+  qg_tuning tu;
+  const qg_tuning* tune = tuning_for(s->ctx, s->n, s->prec, s->ctx->cfg.arithmetic, fusion, &tu);
+  int rc = compile_program(circuit, s->prec, fusion, s->ctx->cfg.fuse_k, s->ctx->cfg.arithmetic, &prog, &err, true,
+                           tune);
   if (rc != QG_OK) return state_err(s, rc, err);
   ExecStats st;
   rc = exec_program(s, prog, seed, nullptr, &st, &err);
@@ -1817,7 +1872,10 @@ int qg_state_prepare(void* state, const qg_circuit* circuit, int32_t fusion, dou
   cudaSetDevice(s->ctx->device);
   std::string err;
   Program prog;
-  int rc = compile_program(circuit, s->prec, fusion, s->ctx->cfg.fuse_k, s->ctx->cfg.arithmetic, &prog, &err);
+  qg_tuning tu;
+  const qg_tuning* tune = tuning_for(s->ctx, s->n, s->prec, s->ctx->cfg.arithmetic, fusion, &tu);
+  int rc = compile_program(circuit, s->prec, fusion, s->ctx->cfg.fuse_k, s->ctx->cfg.arithmetic, &prog, &err, true,
+                           tune);
   if (rc != QG_OK) return state_err(s, rc, err);
   const auto t0 = Clock::now();
   auto pk = maybe_pass_kernels(s, prog);
@@ -1991,7 +2049,10 @@ int qg_state_profile(void* state, const qg_circuit* circuit, int32_t fusion, uin
   cudaSetDevice(s->ctx->device);
   std::string err;
   Program prog;
-  int rc = compile_program(circuit, s->prec, fusion, s->ctx->cfg.fuse_k, s->ctx->cfg.arithmetic, &prog, &err);
+  qg_tuning tu;
+  const qg_tuning* tune = tuning_for(s->ctx, s->n, s->prec, s->ctx->cfg.arithmetic, fusion, &tu);
+  int rc = compile_program(circuit, s->prec, fusion, s->ctx->cfg.fuse_k, s->ctx->cfg.arithmetic, &prog, &err, true,
+                           tune);
   if (rc != QG_OK) return state_err(s, rc, err);
   std::vector<float> ms;
   std::vector<int> kinds;
@@ -2039,6 +2100,203 @@ int qg_pass_kernels_info(int32_t* available, uint64_t* cache_hits, uint64_t* cac
   pass_kernel_cache_stats(&h, &m);
   if (cache_hits) *cache_hits = h;
   if (cache_misses) *cache_misses = m;
+  return QG_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Autotuner: the specialised pass kernels' tile size and launch shape per
+// (qubits, precision), chosen from measured device time on a calibration circuit.
+// ---------------------------------------------------------------------------
+int32_t qg_tuning_pick(const double* ms, const int32_t* valid, int32_t count, int32_t default_index,
+                       double tie_frac) {
+  if (!ms || !valid || count < 1) return -1;
+  int best = -1;
+  for (int i = 0; i < count; ++i)
+    if (valid[i] && ms[i] > 0 && (best < 0 || ms[i] < ms[best])) best = i;
+  if (best < 0) return -1;
+  // the default shape stays unless another one is faster by more than tie_frac
+  if (default_index >= 0 && default_index < count && valid[default_index] && ms[default_index] > 0 &&
+      ms[default_index] <= ms[best] * (1.0 + (tie_frac > 0 ? tie_frac : 0)))
+    return default_index;
+  return best;
+}
+
+static bool tuning_valid(const qg_tuning& t, int n, int prec) {
+  const int E = prec == QG_C128 ? 16 : 8;
+  if (t.tile_bits < 11 || t.tile_bits > kMaxTileBits || t.tile_bits > n) return false;
+  if (t.reg_bits < 3 || t.reg_bits > 4 || t.tile_bits - t.reg_bits < 5 || t.tile_bits - t.reg_bits > 10) return false;
+  if (t.buffers < 1 || t.buffers > 2 || t.ctas_per_sm < 1 || t.ctas_per_sm > 8) return false;
+  const long smem = (long)t.buffers * (1L << t.tile_bits) * E;
+  return smem <= 227L * 1024 && smem * t.ctas_per_sm <= 228L * 1024;
+}
+
+int qg_tuning_set(void* ctx, int32_t n, int32_t precision, const qg_tuning* t) {
+  if (!ctx || !t || n < 1 || n > QG_MAX_QUBITS || (precision != QG_C128 && precision != QG_C64))
+    return QG_ERR_INVALID_ARG;
+  Ctx* c = (Ctx*)ctx;
+  std::lock_guard<std::mutex> lk(c->tune_mu);
+  if (t->tile_bits == 0) {  // back to the default shape
+    c->tunings.erase({n, precision});
+    return QG_OK;
+  }
+  if (!tuning_valid(*t, n, precision)) return QG_ERR_INVALID_ARG;
+  c->tunings[{n, precision}] = *t;
+  return QG_OK;
+}
+
+int qg_tuning_get(void* ctx, int32_t n, int32_t precision, qg_tuning* out) {
+  if (!ctx || !out) return QG_ERR_INVALID_ARG;
+  Ctx* c = (Ctx*)ctx;
+  std::lock_guard<std::mutex> lk(c->tune_mu);
+  auto it = c->tunings.find({n, precision});
+  if (it != c->tunings.end()) {
+    *out = it->second;
+    return QG_OK;
+  }
+  std::memset(out, 0, sizeof(*out));
+  out->tile_bits = std::min(12, (int)n);
+  out->reg_bits = precision == QG_C128 ? 3 : 4;
+  out->buffers = 2;
+  out->ctas_per_sm = precision == QG_C128 ? 1 : 2;
+  return QG_OK;
+}
+
+// The calibration circuit: `depth` layers of the layered recipe (one gate from
+// {H,X,Y,Z,S,T,RX,RY,RZ} per qubit, CNOTs on a random matching) and the first four
+// columns of a QFT (H and controlled phases pi/2^k), from a fixed seed.
+static std::vector<qg_op> calibration_ops(int n, int depth) {
+  std::vector<qg_op> ops;
+  uint64_t x = 0x9E3779B97F4A7C15ull;
+  auto rnd = [&]() {
+    x ^= x << 13;
+    x ^= x >> 7;
+    x ^= x << 17;
+    return x;
+  };
+  const int gates[9] = {QG_OP_H, QG_OP_X, QG_OP_Y, QG_OP_Z, QG_OP_S, QG_OP_T, QG_OP_RX, QG_OP_RY, QG_OP_RZ};
+  auto op1 = [&](int code, int q, double a) {
+    qg_op o;
+    std::memset(&o, 0, sizeof(o));
+    o.opcode = (uint16_t)code;
+    o.nq = 1;
+    o.q[0] = (uint32_t)q;
+    o.angle = a;
+    ops.push_back(o);
+  };
+  auto op2 = [&](int code, int a, int b, double ang) {
+    qg_op o;
+    std::memset(&o, 0, sizeof(o));
+    o.opcode = (uint16_t)code;
+    o.nq = 2;
+    o.q[0] = (uint32_t)a;
+    o.q[1] = (uint32_t)b;
+    o.angle = ang;
+    ops.push_back(o);
+  };
+  std::vector<int> perm(n);
+  for (int d = 0; d < depth; ++d) {
+    for (int q = 0; q < n; ++q) op1(gates[rnd() % 9], q, (double)(rnd() % 100000) * 6.283185307179586e-5);
+    for (int q = 0; q < n; ++q) perm[q] = q;
+    for (int q = n - 1; q > 0; --q) std::swap(perm[q], perm[rnd() % (q + 1)]);
+    for (int q = 0; q + 1 < n; q += 2) op2(QG_OP_CNOT, perm[q], perm[q + 1], 0.0);
+  }
+  for (int j = 0; j < std::min(4, n); ++j) {
+    op1(QG_OP_H, j, 0.0);
+    for (int k = j + 1; k < n; ++k) op2(QG_OP_RYDBERG_CPHASE, k, j, 3.141592653589793 / (double)(1ull << (k - j)));
+  }
+  return ops;
+}
+
+int qg_autotune(void* ctx, int32_t n, int32_t precision, qg_tuning* chosen, qg_tuning* tried, int32_t cap,
+                int32_t* count_out) {
+  if (!ctx || !chosen || n < 11 || n > QG_MAX_QUBITS || (precision != QG_C128 && precision != QG_C64))
+    return QG_ERR_INVALID_ARG;
+  Ctx* c = (Ctx*)ctx;
+  NvtxRange nvtx("qg autotune");
+  if (const char* why = pass_kernels_unavailable()) {
+    set_ctx_error(c, std::string("autotune: ") + why);
+    return QG_ERR_UNSUPPORTED;
+  }
+  const int arith = c->cfg.arithmetic;
+  if (precision == QG_C128 && arith != QG_ARITH_DOUBLE_FLOAT) {
+    set_ctx_error(c, "autotune: complex128 exact arithmetic runs interpreted (nothing to tune)");
+    return QG_ERR_UNSUPPORTED;
+  }
+  if (!will_specialise(c, n, precision, arith, QG_FUSE_TILED)) {
+    set_ctx_error(c, "autotune: states of " + std::to_string(n) +
+                         " qubits run interpreted under this context's pass-kernel policy (nothing to tune)");
+    return QG_ERR_UNSUPPORTED;
+  }
+  // candidates: the default first (tile bits, register bits, buffers, CTAs per SM)
+  std::vector<qg_tuning> cand;
+  auto add = [&](int k, int r, int b, int ct) {
+    qg_tuning t;
+    std::memset(&t, 0, sizeof(t));
+    t.tile_bits = k;
+    t.reg_bits = r;
+    t.buffers = b;
+    t.ctas_per_sm = ct;
+    if (tuning_valid(t, n, precision)) cand.push_back(t);
+  };
+  if (precision == QG_C128) {
+    add(12, 3, 2, 1);
+    add(11, 3, 2, 2);
+    add(12, 3, 1, 1);
+    add(11, 3, 1, 2);
+  } else {
+    add(12, 4, 2, 2);
+    add(11, 4, 2, 4);
+    add(13, 4, 2, 1);
+    add(12, 4, 1, 2);
+  }
+  cudaSetDevice(c->device);
+  std::vector<qg_op> ops = calibration_ops(n, 6);
+  qg_circuit circ{n, (int32_t)ops.size(), ops.data()};
+  void* sh = nullptr;
+  int rc = qg_state_create(ctx, n, precision, &sh);
+  if (rc != QG_OK) return rc;
+  State* s = (State*)sh;
+  std::vector<double> ms(cand.size(), 0.0);
+  std::vector<int32_t> ok(cand.size(), 0);
+  std::string err;
+  for (size_t i = 0; i < cand.size(); ++i) {
+    Program prog;
+    rc = compile_program(&circ, precision, QG_FUSE_TILED, c->cfg.fuse_k, arith, &prog, &err, true, &cand[i]);
+    if (rc != QG_OK) break;
+    std::string why;
+    auto pk = pass_kernels_for(prog, precision, c->device, &why);
+    if (!pk) continue;  // this shape did not compile: not a candidate
+    // one warm-up run, then the median of three
+    std::vector<double> runs;
+    for (int r = 0; r < 4 && rc == QG_OK; ++r) {
+      ExecStats st;
+      rc = exec_program(s, prog, 0, nullptr, &st, &err);
+      if (r > 0) runs.push_back(st.device_ms);
+    }
+    if (rc != QG_OK) break;
+    std::sort(runs.begin(), runs.end());
+    ms[i] = runs[runs.size() / 2];
+    ok[i] = 1;
+    cand[i].ms = ms[i];
+  }
+  qg_state_destroy(sh);
+  if (rc != QG_OK) {
+    set_ctx_error(c, "autotune: " + err);
+    return rc;
+  }
+  const int pick = qg_tuning_pick(ms.data(), ok.data(), (int32_t)cand.size(), 0, 0.01);
+  if (pick < 0) {
+    set_ctx_error(c, "autotune: no candidate shape compiled");
+    return QG_ERR_UNSUPPORTED;
+  }
+  *chosen = cand[pick];
+  {
+    std::lock_guard<std::mutex> lk(c->tune_mu);
+    c->tunings[{n, precision}] = cand[pick];
+  }
+  if (count_out) *count_out = (int32_t)cand.size();
+  if (tried)
+    for (int i = 0; i < (int)cand.size() && i < cap; ++i) tried[i] = cand[i];
   return QG_OK;
 }
 

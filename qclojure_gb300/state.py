@@ -48,6 +48,26 @@ class Context:
     def state(self, num_qubits: int, precision: str = "c128") -> "DeviceState":
         return DeviceState(self, num_qubits, precision)
 
+    def autotune(self, num_qubits: int, precision: str = "c128") -> dict:
+        """Time candidate pass-kernel shapes on a calibration circuit of num_qubits and keep
+        the fastest for this context (qg_autotune); returns the choice and every candidate."""
+        chosen = A.QgTuning()
+        tried = (A.QgTuning * 16)()
+        count = C.c_int32()
+        _check(self.lib.qg_autotune(self.ctx, num_qubits, PRECISIONS[precision], C.byref(chosen), tried, 16,
+                                    C.byref(count)), self.lib, self.ctx)
+        return {"chosen": chosen.as_dict(), "candidates": [tried[i].as_dict() for i in range(count.value)]}
+
+    def tuning(self, num_qubits: int, precision: str = "c128") -> dict:
+        t = A.QgTuning()
+        _check(self.lib.qg_tuning_get(self.ctx, num_qubits, PRECISIONS[precision], C.byref(t)), self.lib, self.ctx)
+        return t.as_dict()
+
+    def set_tuning(self, num_qubits: int, precision: str, tile_bits: int, reg_bits: int = 0, buffers: int = 0,
+                   ctas_per_sm: int = 0) -> None:
+        t = A.QgTuning(tile_bits, reg_bits, buffers, ctas_per_sm, 0.0)
+        _check(self.lib.qg_tuning_set(self.ctx, num_qubits, PRECISIONS[precision], C.byref(t)), self.lib, self.ctx)
+
 
 class DeviceState:
     def __init__(self, ctx: Context, num_qubits: int, precision: str = "c128"):
@@ -102,7 +122,7 @@ class DeviceState:
     def profile(self, circuit: dict, fusion: str = "tiled", seed: int = 0) -> tuple[np.ndarray, np.ndarray]:
         """Apply like apply() and return per-pass device times (ms) and kinds
         (0 plain gate, 1 tiled pass, 2 measurement, 3 tiled pass run by its
-        specialised kernel)."""
+        specialised kernel, 4 dense block on the tensor cores)."""
         enc = encode(circuit)
         cap = 1 << 16
         ms = (C.c_float * cap)()

@@ -80,3 +80,24 @@ def test_missing_library_fails_loudly(tmp_path):
 
     with pytest.raises(RuntimeError):
         A.load_library(tmp_path / "libqgpu.so")
+
+
+def test_tuning_pick_rule(built):
+    """qg_tuning_pick: the fastest valid candidate, unless the default is within the tie
+    fraction of it; invalid or unmeasured entries never win (fake timings, no GPU)."""
+    from qclojure_gb300 import _abi as A
+
+    lib = A.load_library()
+
+    def pick(ms, valid, default=0, tie=0.01):
+        n = len(ms)
+        return lib.qg_tuning_pick((C.c_double * n)(*ms), (C.c_int32 * n)(*valid), n, default, tie)
+
+    assert pick([10.0, 8.0, 9.0], [1, 1, 1]) == 1
+    assert pick([10.0, 9.95, 9.0], [1, 1, 0]) == 0          # within 1 %: keep the default
+    assert pick([10.0, 9.0, 9.5], [1, 1, 1], tie=0.2) == 0  # a wider tie band keeps it too
+    assert pick([10.0, 4.0, 9.0], [1, 0, 1]) == 2           # the fastest one did not compile
+    assert pick([0.0, 7.0], [1, 1]) == 1                    # no measurement is no candidate
+    assert pick([5.0, 7.0], [0, 0]) == -1
+    assert pick([12.0, 11.0], [1, 1], default=-1) == 1
+
