@@ -473,6 +473,17 @@ int qg_autotune(void* ctx, int32_t num_qubits, int32_t precision, qg_tuning* cho
 int qg_tuning_set(void* ctx, int32_t num_qubits, int32_t precision, const qg_tuning* tuning);
 int qg_tuning_get(void* ctx, int32_t num_qubits, int32_t precision, qg_tuning* out);
 int32_t qg_tuning_pick(const double* ms, const int32_t* valid, int32_t count, int32_t default_index, double tie_frac);
+/* qg_autotune_crossover (no counterpart in the reference) measures from which state size
+   a circuit that runs once gains from its specialised kernels: for 20, 22, ..., 30 qubits
+   it runs a calibration circuit of `layers` layers interpreted, compiles its kernels cold
+   and runs it specialised. The crossover is the smallest size from which compile wall
+   time plus the specialised run beats the interpreted run at every larger size; the
+   context then specialises states of at least that many qubits under
+   QG_PASS_KERNELS_AUTO (29 until measured). table receives up to cap rows of
+   (qubits, interpreted ms, compile ms, specialised ms). Call it before submitting work:
+   it allocates one state of each size in turn. */
+int qg_autotune_crossover(void* ctx, int32_t precision, int32_t layers, int32_t* min_qubits_out, double* table,
+                          int32_t cap, int32_t* count_out);
 
 #ifdef __cplusplus
 }

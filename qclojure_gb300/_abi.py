@@ -229,6 +229,7 @@ SIGNATURES = {
     "qg_tuning_set": ([P, I32, I32, C.POINTER(QgTuning)], C.c_int),
     "qg_tuning_get": ([P, I32, I32, C.POINTER(QgTuning)], C.c_int),
     "qg_tuning_pick": ([DP, I32P, I32, I32, C.c_double], I32),
+    "qg_autotune_crossover": ([P, I32, I32, I32P, DP, I32, I32P], C.c_int),
     "qg_sweep_create": ([P, C.POINTER(QgCircuit), I32, I32, I32, C.POINTER(P)], C.c_int),
     "qg_sweep_update": ([P, C.POINTER(QgCircuit), I32], C.c_int),
     "qg_sweep_run": ([P, I32P, DP, C.c_char_p, DP, C.POINTER(QgSweepStats)], C.c_int),

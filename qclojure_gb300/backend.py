@@ -141,6 +141,14 @@ class GpuStateVectorSimulator:
             self._lib.qg_ctx_destroy(self._ctx)
             self._ctx = None
 
+    def autotune_crossover(self, precision: str = "c64", layers: int = 100) -> dict:
+        """Measure from which state size a one-off job of `layers` layers gains from compiling its
+        pass kernels, and specialise jobs from there on (qg_autotune_crossover). Call it before
+        submitting work."""
+        from .state import Context
+
+        return Context.autotune_crossover(_CtxView(self._lib, self._ctx), precision, layers)
+
     def __del__(self):
         try:
             self.close()
@@ -627,3 +635,10 @@ def group_pauli_terms_by_measurement_basis(terms: list[dict]) -> dict:
             basis = "Y"
         out.setdefault(basis, []).append(t)
     return out
+
+
+class _CtxView:
+    """The (library, context) pair a Context method needs, for a simulator's own context."""
+
+    def __init__(self, lib, ctx):
+        self.lib, self.ctx = lib, ctx

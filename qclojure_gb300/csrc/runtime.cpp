@@ -15,6 +15,7 @@
 #include <condition_variable>
 #include <cstring>
 #include <deque>
+#include <array>
 #include <map>
 #include <memory>
 #include <mutex>
@@ -274,18 +275,25 @@ static int do_measure(State* s, const std::vector<int>& qubits, uint64_t seed, u
 // (in parallel over the host cores); an interpreted 29-qubit double-float pass
 // takes about 13 ms on the device, so from here on even a circuit that runs once
 // gains, while smaller one-off jobs (the serving stream) would lose.
+// qg_autotune_crossover measures the crossover for a context and replaces it.
 constexpr int kPassKernelMinQubits = 29;
 
 static std::shared_ptr<const PassKernels> maybe_pass_kernels(const State* s, const Program& prog);
+static std::shared_ptr<const PassKernels> forced_pass_kernels(const State* s, const Program& prog);
 
+// specialise: -1 the context's policy (maybe_pass_kernels), 0 never, 1 always.
 static int exec_program(State* s, const Program& prog, uint64_t seed, const std::atomic<bool>* cancel,
-                        ExecStats* stats, std::string* err) {
+                        ExecStats* stats, std::string* err, int specialise = -1) {
   double* d_dense = nullptr;
   void* d_kops = nullptr;
   std::shared_ptr<const PassKernels> pk;
   {
     const auto t0 = Clock::now();
-    pk = maybe_pass_kernels(s, prog);
+    if (specialise < 0) {
+      pk = maybe_pass_kernels(s, prog);
+    } else if (specialise > 0) {
+      pk = forced_pass_kernels(s, prog);
+    }
     if (stats) stats->compile_ms = ms_since(t0);
   }
   if (!prog.tops.empty()) {
@@ -645,6 +653,9 @@ struct Ctx {
   // pass-kernel shapes chosen by qg_autotune / qg_tuning_set, per (qubits, precision)
   std::mutex tune_mu;
   std::map<std::pair<int, int>, qg_tuning> tunings;
+  // smallest state that runs specialised under QG_PASS_KERNELS_AUTO, per precision
+  // (kPassKernelMinQubits until qg_autotune_crossover measures it)
+  std::atomic<int> spec_min_qubits[2] = {{kPassKernelMinQubits}, {kPassKernelMinQubits}};
 };
 
 // True when programs of this kind run as specialised pass kernels (the condition
@@ -654,7 +665,7 @@ static bool will_specialise(const Ctx* c, int n, int prec, int arith, int fusion
   if (prec == QG_C128 && arith != QG_ARITH_DOUBLE_FLOAT) return false;
   const int mode = c->cfg.pass_kernels;
   if (mode == QG_PASS_KERNELS_OFF) return false;
-  return mode == QG_PASS_KERNELS_ALWAYS || n >= kPassKernelMinQubits;
+  return mode == QG_PASS_KERNELS_ALWAYS || n >= c->spec_min_qubits[prec == QG_C64 ? 1 : 0].load();
 }
 // The tuned shape for programs of this kind, if one was chosen (copied into *out).
 static const qg_tuning* tuning_for(Ctx* c, int n, int prec, int arith, int fusion, qg_tuning* out) {
@@ -672,9 +683,17 @@ static std::shared_ptr<const PassKernels> maybe_pass_kernels(const State* s, con
   if (s->prec == QG_C128 && prog.arith != QG_ARITH_DOUBLE_FLOAT) return nullptr;
   const int mode = c->cfg.pass_kernels;
   if (mode == QG_PASS_KERNELS_OFF) return nullptr;
-  if (mode != QG_PASS_KERNELS_ALWAYS && s->n < kPassKernelMinQubits) return nullptr;
+  if (mode != QG_PASS_KERNELS_ALWAYS && s->n < c->spec_min_qubits[s->prec == QG_C64 ? 1 : 0].load()) return nullptr;
   std::string why;
   return pass_kernels_for(prog, s->prec, c->device, &why);
+}
+
+// The program's pass kernels whatever the context's policy (nullptr when none compile).
+static std::shared_ptr<const PassKernels> forced_pass_kernels(const State* s, const Program& prog) {
+  if (!s->ctx || prog.tops.empty()) return nullptr;
+  if (s->prec == QG_C128 && prog.arith != QG_ARITH_DOUBLE_FLOAT) return nullptr;
+  std::string why;
+  return pass_kernels_for(prog, s->prec, s->ctx->device, &why);
 }
 
 static void set_ctx_error(Ctx* c, const std::string& e) {
@@ -2297,6 +2316,93 @@ int qg_autotune(void* ctx, int32_t n, int32_t precision, qg_tuning* chosen, qg_t
   if (count_out) *count_out = (int32_t)cand.size();
   if (tried)
     for (int i = 0; i < (int)cand.size() && i < cap; ++i) tried[i] = cand[i];
+  return QG_OK;
+}
+
+// The specialisation crossover for one-off circuits: for each state size, a fresh
+// calibration job of `layers` layers (never seen before, so its kernels compile cold)
+// runs interpreted and specialised; the crossover is the smallest size from which
+// compile wall time + specialised run beats the interpreted run at every larger size
+// measured. Under QG_PASS_KERNELS_AUTO the context then specialises from there on.
+int qg_autotune_crossover(void* ctx, int32_t precision, int32_t layers, int32_t* min_qubits_out, double* table,
+                          int32_t cap, int32_t* count_out) {
+  if (!ctx || !min_qubits_out || layers < 1 || (precision != QG_C128 && precision != QG_C64))
+    return QG_ERR_INVALID_ARG;
+  Ctx* c = (Ctx*)ctx;
+  NvtxRange nvtx("qg autotune crossover");
+  if (const char* why = pass_kernels_unavailable()) {
+    set_ctx_error(c, std::string("autotune crossover: ") + why);
+    return QG_ERR_UNSUPPORTED;
+  }
+  const int arith = c->cfg.arithmetic;
+  if (precision == QG_C128 && arith != QG_ARITH_DOUBLE_FLOAT) {
+    set_ctx_error(c, "autotune crossover: complex128 exact arithmetic runs interpreted");
+    return QG_ERR_UNSUPPORTED;
+  }
+  static std::atomic<int> salt{0};
+  cudaSetDevice(c->device);
+  const int sizes[] = {20, 22, 24, 26, 28, 30};
+  std::vector<std::array<double, 4>> rows;
+  std::string err;
+  int rc = QG_OK;
+  for (int n : sizes) {
+    if (n > QG_MAX_QUBITS) break;
+    std::vector<qg_op> ops = calibration_ops(n, layers);
+    // a distinct angle per call: the program is new to the kernel cache
+    const int sl = salt.fetch_add(1);
+    for (qg_op& o : ops)
+      if (o.opcode == QG_OP_RX || o.opcode == QG_OP_RY || o.opcode == QG_OP_RZ) {
+        o.angle += 1e-9 * (double)(sl + 1);
+        break;
+      }
+    qg_circuit circ{n, (int32_t)ops.size(), ops.data()};
+    void* sh = nullptr;
+    rc = qg_state_create(ctx, n, precision, &sh);
+    if (rc != QG_OK) break;
+    State* s = (State*)sh;
+    Program prog;
+    rc = compile_program(&circ, precision, QG_FUSE_TILED, c->cfg.fuse_k, arith, &prog, &err);
+    double interp = 0, spec = 0, comp = 0;
+    if (rc == QG_OK) {
+      // interpreted, then a cold compile, then specialised (the kernels just compiled)
+      ExecStats st;
+      rc = exec_program(s, prog, 0, nullptr, &st, &err, 0);
+      interp = st.device_ms;
+      if (rc == QG_OK) {
+        std::string why;
+        const auto t0 = Clock::now();
+        auto pk = pass_kernels_for(prog, precision, c->device, &why);
+        comp = ms_since(t0);
+        if (!pk) {
+          err = "pass kernels: " + why;
+          rc = QG_ERR_UNSUPPORTED;
+        } else {
+          ExecStats st2;
+          rc = exec_program(s, prog, 0, nullptr, &st2, &err, 1);
+          spec = st2.device_ms;
+        }
+      }
+    }
+    qg_state_destroy(sh);
+    if (rc != QG_OK) break;
+    rows.push_back({(double)n, interp, comp, spec});
+  }
+  if (rc != QG_OK) {
+    set_ctx_error(c, "autotune crossover: " + err);
+    return rc;
+  }
+  // from the largest size down, as long as compiling and running specialised wins
+  int cross = rows.empty() ? kPassKernelMinQubits : (int)rows.back()[0] + 1;
+  for (int i = (int)rows.size() - 1; i >= 0; --i) {
+    if (rows[i][2] + rows[i][3] < rows[i][1]) cross = (int)rows[i][0];
+    else break;
+  }
+  c->spec_min_qubits[precision == QG_C64 ? 1 : 0].store(cross);
+  *min_qubits_out = cross;
+  if (count_out) *count_out = (int32_t)rows.size();
+  if (table)
+    for (int i = 0; i < (int)rows.size() && i < cap; ++i)
+      for (int q = 0; q < 4; ++q) table[4 * i + q] = rows[i][q];
   return QG_OK;
 }
 

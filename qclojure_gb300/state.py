@@ -58,6 +58,17 @@ class Context:
                                     C.byref(count)), self.lib, self.ctx)
         return {"chosen": chosen.as_dict(), "candidates": [tried[i].as_dict() for i in range(count.value)]}
 
+    def autotune_crossover(self, precision: str = "c64", layers: int = 100) -> dict:
+        """Measure from which size a one-off circuit of `layers` layers gains from compiling its
+        kernels (qg_autotune_crossover); the context specialises from there on."""
+        mq, cnt = C.c_int32(), C.c_int32()
+        tab = (C.c_double * 32)()
+        _check(self.lib.qg_autotune_crossover(self.ctx, PRECISIONS[precision], layers, C.byref(mq), tab, 8,
+                                              C.byref(cnt)), self.lib, self.ctx)
+        rows = [{"qubits": int(tab[4 * i]), "interpreted_ms": tab[4 * i + 1], "compile_ms": tab[4 * i + 2],
+                 "specialised_ms": tab[4 * i + 3]} for i in range(cnt.value)]
+        return {"min_qubits": mq.value, "rows": rows}
+
     def tuning(self, num_qubits: int, precision: str = "c128") -> dict:
         t = A.QgTuning()
         _check(self.lib.qg_tuning_get(self.ctx, num_qubits, PRECISIONS[precision], C.byref(t)), self.lib, self.ctx)

@@ -50,3 +50,35 @@ def test_tuning_set_refuses_impossible_shapes():
         assert ctx.tuning(20, "c128")["tile_bits"] == 11
         ctx.set_tuning(20, "c128", 0)
         assert ctx.tuning(20, "c128")["tile_bits"] == 12
+
+
+def test_crossover_sets_the_specialisation_size(oracle):
+    """qg_autotune_crossover measures interpreted vs compile + specialised time per size and
+    the context then specialises from the crossover on; results stay within tolerance."""
+    import ctypes as C
+
+    from qclojure_gb300 import _abi as A
+    from qclojure_gb300 import workloads
+    from qclojure_gb300.backend import create_simulator
+
+    sim = create_simulator({"precision": "c64", "fusion": "tiled", "workers": 2, "seed": 1})
+    try:
+        res = sim.autotune_crossover("c64", 30)
+        rows = res["rows"]
+        assert [r["qubits"] for r in rows] == [20, 22, 24, 26, 28, 30]
+        assert all(r["interpreted_ms"] > 0 and r["specialised_ms"] > 0 and r["compile_ms"] > 0 for r in rows)
+        m = res["min_qubits"]
+        assert 20 <= m <= 31
+        gains = [r["compile_ms"] + r["specialised_ms"] < r["interpreted_ms"] for r in rows]
+        assert all(g for r, g in zip(rows, gains) if r["qubits"] >= m)
+        n = 20 if m > 20 else m  # a job below (or at) the crossover
+        c = workloads.layered_circuit(n, 4, seed=2)
+        jid = sim.submit_circuit(c, {"result-specs": {"state-vector": True}})
+        assert sim.wait(jid, 300_000) == "completed"
+        info = A.QgJobInfo()
+        sim._lib.qg_job_details(sim._ctx, C.c_uint64(sim._jid(jid)), C.byref(info))
+        assert (info.specialised_passes > 0) == (n >= m)
+        sv = np.asarray(sim.job_result(jid)["results"]["final-state"]["state-vector"])
+        assert np.max(np.abs(sv - oracle.run(c))) <= 2e-5
+    finally:
+        sim.close()
