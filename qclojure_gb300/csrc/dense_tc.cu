@@ -188,8 +188,6 @@ __global__ void __launch_bounds__(kThreads, 1) k_dense_tc(const __grid_constant_
   uint64_t* full = reinterpret_cast<uint64_t*>(stage + kStages * kStageBytes);
   uint64_t* mma_bar = full + kStages;
   uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(mma_bar + 1);
-  uint16_t* j_of = reinterpret_cast<uint16_t*>(tmem_slot + 2);     // tile index -> j (4096)
-  uint16_t* c_of = j_of + kTileAmps;                                // tile index -> c (4096)
 
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const int k = p.k;
@@ -200,15 +198,21 @@ __global__ void __launch_bounds__(kThreads, 1) k_dense_tc(const __grid_constant_
   const int Mrows = 128 * G;               // columns of a tile
   const uint32_t idesc = idesc_tf32(Np);
 
-  for (int i = tid; i < kTileAmps; i += kThreads) {
+  // this thread's 16 tile positions (i = tid + q * kThreads) map to the same places in
+  // every tile: A operand byte offsets and epilogue buffer indices, computed once
+  constexpr int PER = kTileAmps / kThreads;
+  uint32_t a_off[PER], o_off[PER];
+#pragma unroll
+  for (int q = 0; q < PER; ++q) {
+    const int i = tid + q * kThreads;
     int j = 0, c = 0;
     for (int t = 0; t < kTileBits; ++t) {
       const int bit = (i >> t) & 1;
       if (p.tgt_of[t] >= 0) j |= bit << p.tgt_of[t];
       else c |= bit << p.col_of[t];
     }
-    j_of[i] = (uint16_t)j;
-    c_of[i] = (uint16_t)c;
+    a_off[q] = kmajor_off(Mrows, c, 2 * j);
+    o_off[q] = (uint32_t)(c * (Np + 1) + 2 * j);
   }
   // the block's real form, hi and lo, already laid out by the host
   for (int i = tid * 4; i < p.bbytes / 4; i += kThreads * 4) {
@@ -234,24 +238,25 @@ __global__ void __launch_bounds__(kThreads, 1) k_dense_tc(const __grid_constant_
 
   const uint64_t t_begin = p.ntiles * blockIdx.x / gridDim.x, t_end = p.ntiles * (blockIdx.x + 1) / gridDim.x;
   const uint64_t count = t_end - t_begin;
-  const int nrun = 1 << (kTileBits - p.runbits);
+  const int nrun = 1 << (kTileBits - p.runbits);  // at most 32: runs are at least 2^7 amplitudes
   const uint32_t run_bytes = (uint32_t)(8u << p.runbits);
+  // warp 0, lane q < nrun: the amplitude offset of run q inside a tile (the same for every tile)
+  uint64_t run_off = 0;
+  if (warp == 0 && lane < nrun)
+    for (int b = p.runbits; b < kTileBits; ++b)
+      if ((lane >> (b - p.runbits)) & 1) run_off |= 1ull << p.tbit[b];
 
-  // thread 0: bulk-load this CTA's tile number r (tile t_begin + r) into buffer r % kStages
+  // warp 0: bulk-load this CTA's tile number r into buffer r % kStages, one run per lane
   auto issue_load = [&](uint64_t r) {
     const int s = (int)(r % kStages);
-    uint64_t* bar = &full[s];
-    mbar_expect_tx(bar, (uint32_t)kStageBytes);
+    if (lane == 0) mbar_expect_tx(&full[s], (uint32_t)kStageBytes);
+    __syncwarp();
     const uint64_t tb = tile_base(p, t_begin + r);
-    for (int q = 0; q < nrun; ++q) {
-      uint64_t off = 0;
-      for (int b = p.runbits; b < kTileBits; ++b)
-        if ((q >> (b - p.runbits)) & 1) off |= 1ull << p.tbit[b];
-      bulk_g2s(stage + s * kStageBytes + (size_t)q * run_bytes, p.state + tb + off, run_bytes, bar);
-    }
+    if (lane < nrun) bulk_g2s(stage + s * kStageBytes + (size_t)lane * run_bytes, p.state + tb + run_off, run_bytes,
+                              &full[s]);
   };
-  uint64_t issued = 0;  // loads issued (thread 0's count)
-  if (tid == 0) {
+  uint64_t issued = 0;  // loads issued (warp 0's count)
+  if (warp == 0) {
     for (; issued < 2 && issued < count; ++issued) issue_load(issued);
   }
 
@@ -265,39 +270,43 @@ __global__ void __launch_bounds__(kThreads, 1) k_dense_tc(const __grid_constant_
       break;
     }
     // staging (address order) -> A hi / A lo (column rows, K-major, swizzled)
-    const float2* st = reinterpret_cast<const float2*>(stage + s * kStageBytes);
-    for (int i = tid; i < kTileAmps; i += kThreads) {
-      const float2 x = st[i];
-      const int j = j_of[i], c = c_of[i];
-      const float hr = to_tf32(x.x), hi_ = to_tf32(x.y);
-      const float lr = to_tf32(x.x - hr), li = to_tf32(x.y - hi_);
-      const uint32_t off = kmajor_off(Mrows, c, 2 * j);
-      *reinterpret_cast<float2*>(a_hi + off) = make_float2(hr, hi_);
-      *reinterpret_cast<float2*>(a_lo + off) = make_float2(lr, li);
+    {
+      const float2* st = reinterpret_cast<const float2*>(stage + s * kStageBytes);
+#pragma unroll
+      for (int q = 0; q < PER; ++q) {
+        const float2 x = st[tid + q * kThreads];
+        const float hr = to_tf32(x.x), hi_ = to_tf32(x.y);
+        const float lr = to_tf32(x.x - hr), li = to_tf32(x.y - hi_);
+        *reinterpret_cast<float2*>(a_hi + a_off[q]) = make_float2(hr, hi_);
+        *reinterpret_cast<float2*>(a_lo + a_off[q]) = make_float2(lr, li);
+      }
     }
     fence_proxy_async();
     tc_fence_before();
     __syncthreads();
-    if (tid == 0) {
-      tc_fence_after();
-      const uint32_t ah = smem_u32(a_hi), al = smem_u32(a_lo), bh = smem_u32(b_hi), bl = smem_u32(b_lo);
-      uint32_t acc = 0;
-      for (int step = 0; step < Kp / 8; ++step) {
-        const int atom = step >> 2;
-        const uint32_t kin = (uint32_t)(step & 3) * 32u;
-        const uint32_t boff = (uint32_t)(atom * Np * 128) + kin;
-        for (int g = 0; g < G; ++g) {
-          const uint32_t aoff = (uint32_t)(atom * Mrows * 128 + g * 128 * 128) + kin;
-          const uint32_t d = tmem + (uint32_t)(g * Np);
-          mma_tf32(d, smem_desc(ah + aoff), smem_desc(bh + boff), idesc, acc);
-          mma_tf32(d, smem_desc(al + aoff), smem_desc(bh + boff), idesc, 1);
-          mma_tf32(d, smem_desc(ah + aoff), smem_desc(bl + boff), idesc, 1);
+    if (warp == 0) {
+      if (lane == 0) {
+        tc_fence_after();
+        const uint32_t ah = smem_u32(a_hi), al = smem_u32(a_lo), bh = smem_u32(b_hi), bl = smem_u32(b_lo);
+        uint32_t acc = 0;
+        for (int step = 0; step < Kp / 8; ++step) {
+          const int atom = step >> 2;
+          const uint32_t kin = (uint32_t)(step & 3) * 32u;
+          const uint32_t boff = (uint32_t)(atom * Np * 128) + kin;
+          for (int g = 0; g < G; ++g) {
+            const uint32_t aoff = (uint32_t)(atom * Mrows * 128 + g * 128 * 128) + kin;
+            const uint32_t d = tmem + (uint32_t)(g * Np);
+            mma_tf32(d, smem_desc(ah + aoff), smem_desc(bh + boff), idesc, acc);
+            mma_tf32(d, smem_desc(al + aoff), smem_desc(bh + boff), idesc, 1);
+            mma_tf32(d, smem_desc(ah + aoff), smem_desc(bl + boff), idesc, 1);
+          }
+          acc = 1;
         }
-        acc = 1;
+        mma_commit(mma_bar);
       }
-      mma_commit(mma_bar);
-      // the buffer of tile r - 1 is free once its store has read it: load tile r + 2 there
+      // the buffer of tile r - 1 is free once its stores have read it: load tile r + 2 there
       bulk_wait_read_all();
+      __syncwarp();
       if (issued < count && issued == r + 2) issue_load(issued++);
     }
     ok = mbar_wait(mma_bar, (uint32_t)r & 1u);
@@ -323,21 +332,14 @@ __global__ void __launch_bounds__(kThreads, 1) k_dense_tc(const __grid_constant_
     {
       const float* out = reinterpret_cast<const float*>(a_hi);
       float2* so = reinterpret_cast<float2*>(stage + s * kStageBytes);
-      for (int i = tid; i < kTileAmps; i += kThreads) {
-        const int j = j_of[i], c = c_of[i];
-        so[i] = make_float2(out[c * (Np + 1) + 2 * j], out[c * (Np + 1) + 2 * j + 1]);
-      }
+#pragma unroll
+      for (int q = 0; q < PER; ++q) so[tid + q * kThreads] = make_float2(out[o_off[q]], out[o_off[q] + 1]);
     }
     fence_proxy_async();
     __syncthreads();
-    if (tid == 0) {
+    if (warp == 0) {
       const uint64_t tb = tile_base(p, t_begin + r);
-      for (int q = 0; q < nrun; ++q) {
-        uint64_t off = 0;
-        for (int b = p.runbits; b < kTileBits; ++b)
-          if ((q >> (b - p.runbits)) & 1) off |= 1ull << p.tbit[b];
-        bulk_s2g(p.state + tb + off, stage + s * kStageBytes + (size_t)q * run_bytes, run_bytes);
-      }
+      if (lane < nrun) bulk_s2g(p.state + tb + run_off, stage + s * kStageBytes + (size_t)lane * run_bytes, run_bytes);
       bulk_commit();
     }
   }
@@ -346,6 +348,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_dense_tc(const __grid_constant_
     for (uint64_t q = r; q < issued; ++q) mbar_wait(&full[q % kStages], (uint32_t)(q / kStages) & 1u);
   }
   if (failed && tid == 0) atomicExch(p.err, 1);
+  if (warp == 0) bulk_wait_all();
   if (tid == 0) bulk_wait_all();
   tc_fence_before();
   __syncthreads();
@@ -356,8 +359,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_dense_tc(const __grid_constant_
 }
 
 size_t dense_tc_smem_bytes() {
-  return 1024 + 2 * kAHalfBytes + 2 * kBHalfBytes + kStages * kStageBytes + (kStages + 1) * 8 + 8 +
-         2 * kTileAmps * sizeof(uint16_t);
+  return 1024 + 2 * kAHalfBytes + 2 * kBHalfBytes + kStages * kStageBytes + (kStages + 1) * 8 + 8;
 }
 
 }  // namespace
