@@ -317,11 +317,13 @@ class PassGen {
   // false: the pass holds an op the generator does not specialise
   bool supported() const { return !unsupported_; }
 
-  void emit(int id) {
+  // ns_name: the namespace of the pass's P (default s<id> / p<id>); kernel = false emits
+  // only the namespace (the level kernels of a sweep call several passes' bodies)
+  void emit(int id, const std::string& ns_name = std::string(), bool kernel = true) {
     const int E = df_ ? 16 : 8;
     uint64_t lm = 0;
     for (int j = 0; j < pd_.k; ++j) lm |= 1ULL << pd_.lbits[j];
-    const std::string ns = (tab_ ? "s" : "p") + std::to_string(id);
+    const std::string ns = ns_name.empty() ? (tab_ ? "s" : "p") + std::to_string(id) : ns_name;
     body();  // into o_; tables it needs go to pre_
     out_ << "namespace " << ns << " {\n" << pre_.str() << "struct P {\n";
     out_ << "  static constexpr int E = " << E << ", K_BITS = " << pd_.k << ", KLOW = " << pd_.klow
@@ -342,6 +344,7 @@ class PassGen {
     out_ << "    using namespace qgp;\n    const unsigned tid = threadIdx.x;\n    (void)base; (void)tid; (void)cs;\n";
     out_ << o_.str();
     out_ << "  }\n};\n}  // namespace " << ns << "\n";
+    if (!kernel) return;
     out_ << "extern \"C\" __global__ void __launch_bounds__(" << ((1 << pd_.k) >> sh_.rbits) << ", " << sh_.ctas
          << ") ";
     if (tab_)
@@ -1304,6 +1307,162 @@ std::shared_ptr<const PassKernels> pass_kernels_for(const Program& prog, int pre
   std::lock_guard<std::mutex> lk(g_mu);
   ++g_cache_misses;
   return g_cache[device].insert(key, c);
+}
+
+// ---------------------------------------------------------------------------
+// Sweep level kernels: for a sweep of several sizes, level l runs the l-th pass of
+// every group (qubit count) that has one, in one launch over all the groups' items
+// (qgl_<l>, a GroupLevel descriptor per group). The bodies are the table-form pass
+// bodies of each group; groups must share the tile size and the kernel shape.
+// ---------------------------------------------------------------------------
+struct LevelKernels : PassKernels {
+  Shape sh{0, 0, 0};
+  int threads = 0;                            // threads per CTA (tile / registers per thread)
+  std::vector<cudaLibrary_t> libs;
+  std::vector<cudaKernel_t> kernel;           // per level
+  std::vector<int> smem;                      // per level
+  std::vector<std::vector<int>> groups;       // per level: the groups it runs, in descriptor order
+  double compile_ms = 0;
+  ~LevelKernels() {
+    for (cudaLibrary_t l : libs) cudaLibraryUnload(l);
+  }
+};
+
+std::shared_ptr<const PassKernels> level_kernels_for(const std::vector<const Program*>& progs,
+                                                     const std::vector<std::vector<int>>& pass_steps, int prec,
+                                                     int device, std::string* why) {
+  NvtxRange nvtx("qg level kernels");
+  if (progs.empty() || progs.size() != pass_steps.size()) {
+    *why = "no groups";
+    return nullptr;
+  }
+  const Shape sh = shape_of(*progs[0], prec);
+  const int E = prec == QG_C128 ? 16 : 8;
+  int K = -1;
+  size_t levels = 0;
+  for (size_t g = 0; g < progs.size(); ++g) {
+    if (prec == QG_C128 && progs[g]->arith != QG_ARITH_DOUBLE_FLOAT) {
+      *why = "complex128 exact arithmetic runs interpreted";
+      return nullptr;
+    }
+    for (int st : pass_steps[g]) {
+      const int k = progs[g]->steps[st].pass.k;
+      if (K < 0) K = k;
+      if (k != K) {
+        *why = "groups with different tile sizes";
+        return nullptr;
+      }
+    }
+    levels = std::max(levels, pass_steps[g].size());
+  }
+  if (K < 11 || K - sh.rbits < 5 || levels == 0) {
+    *why = "no pass to specialise";
+    return nullptr;
+  }
+  auto lk = std::make_shared<LevelKernels>();
+  lk->sh = sh;
+  lk->threads = (1 << K) >> sh.rbits;
+  lk->groups.resize(levels);
+  lk->smem.assign(levels, 0);
+  // generate: one piece per level holding its groups' bodies and the level kernel
+  std::vector<std::pair<int, std::string>> pieces;
+  for (size_t l = 0; l < levels; ++l) {
+    std::ostringstream o;
+    std::vector<std::string> names;
+    for (size_t g = 0; g < progs.size(); ++g) {
+      if (l >= pass_steps[g].size()) continue;
+      const Program& pr = *progs[g];
+      const int st = pass_steps[g][l];
+      const PassDesc& pd = pr.steps[st].pass;
+      const TOp* ops = pr.tops.data() + pd.op_begin;
+      const int nops = (int)(pd.op_end - pd.op_begin);
+      const std::string ns = "g" + std::to_string(g) + "l" + std::to_string(l);
+      PassGen gen(o, pd, ops, nops, prec, tile_pass_io(pr, (size_t)st), true, sh);
+      if (!gen.supported()) {
+        *why = "a sweep pass the generator does not specialise";
+        return nullptr;
+      }
+      gen.emit(st, ns, false);
+      names.push_back(ns);
+      lk->groups[l].push_back((int)g);
+      lk->smem[l] = std::max(lk->smem[l], sh.bufs * (1 << K) * E + 16 * 4 * nops);
+    }
+    o << "extern \"C\" __global__ void __launch_bounds__(" << ((1 << K) >> sh.rbits) << ", " << sh.ctas << ") qgl_"
+      << l << "(const qgp::GroupLevel* __restrict__ gl, unsigned long long total) {\n"
+      << "  const qgp::u64 w0 = total * blockIdx.x / gridDim.x, w1 = total * (blockIdx.x + 1) / gridDim.x;\n";
+    for (size_t q = 0; q < names.size(); ++q)
+      o << "  qgp::run_group_share<" << names[q] << "::P>(gl[" << q << "], w0, w1);\n";
+    o << "}\n\n";
+    pieces.emplace_back((int)l, o.str());
+  }
+  // units: levels dealt largest first, one unit per host thread
+  const unsigned hw = std::max(1u, std::thread::hardware_concurrency());
+  const size_t nunits = std::min<size_t>(pieces.size(), std::min(hw, 32u));
+  std::vector<Unit> units(nunits);
+  std::vector<size_t> load(nunits, 0), order(pieces.size());
+  for (size_t i = 0; i < order.size(); ++i) order[i] = i;
+  std::sort(order.begin(), order.end(),
+            [&](size_t a, size_t b) { return pieces[a].second.size() > pieces[b].second.size(); });
+  for (Unit& u : units) u.src = "#include \"pass_prelude.cuh\"\n\n";
+  for (size_t i : order) {
+    const size_t u = std::min_element(load.begin(), load.end()) - load.begin();
+    units[u].src += pieces[i].second;
+    units[u].steps.push_back(pieces[i].first);
+    load[u] += pieces[i].second.size() * (1 + pieces[i].second.size() / 16384);
+  }
+  const auto t0 = std::chrono::steady_clock::now();
+  if (!compile_units(units, why)) return nullptr;
+  lk->kernel.assign(levels, nullptr);
+  for (Unit& u : units) {
+    cudaLibrary_t lib = nullptr;
+    cudaError_t e = cudaLibraryLoadData(&lib, u.cubin.data(), nullptr, nullptr, 0, nullptr, nullptr, 0);
+    if (e != cudaSuccess) {
+      *why = std::string("loading level kernels: ") + cudaGetErrorString(e);
+      return nullptr;
+    }
+    lk->libs.push_back(lib);
+    e = fill_root_table(lib);
+    if (e != cudaSuccess) {
+      *why = std::string("level kernel tables: ") + cudaGetErrorString(e);
+      return nullptr;
+    }
+    for (int l : u.steps) {
+      cudaKernel_t k = nullptr;
+      const std::string name = "qgl_" + std::to_string(l);
+      e = cudaLibraryGetKernel(&k, lib, name.c_str());
+      if (e == cudaSuccess)
+        e = cudaKernelSetAttributeForDevice(k, cudaFuncAttributeMaxDynamicSharedMemorySize, lk->smem[l], device);
+      if (e != cudaSuccess) {
+        *why = "level kernel " + name + ": " + cudaGetErrorString(e);
+        return nullptr;
+      }
+      lk->kernel[l] = k;
+    }
+  }
+  lk->compile_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+  return lk;
+}
+
+int level_count(const PassKernels& lk) { return (int)static_cast<const LevelKernels&>(lk).kernel.size(); }
+const std::vector<int>& level_groups(const PassKernels& lk, int level) {
+  return static_cast<const LevelKernels&>(lk).groups[(size_t)level];
+}
+double level_kernels_compile_ms(const PassKernels& lk) { return static_cast<const LevelKernels&>(lk).compile_ms; }
+
+cudaError_t launch_level_kernel(const PassKernels& lkb, int level, const GroupLevelDesc* d_desc, uint64_t total,
+                                cudaStream_t st) {
+  const LevelKernels& lk = static_cast<const LevelKernels&>(lkb);
+  if (level < 0 || level >= (int)lk.kernel.size() || !lk.kernel[(size_t)level] || total == 0)
+    return cudaErrorInvalidValue;
+  uint64_t grid = (uint64_t)kSMCount * lk.sh.ctas;
+  if (grid > total) grid = total;
+  const GroupLevelDesc* dp = d_desc;
+  unsigned long long tt = total;
+  void* args[2] = {&dp, &tt};
+  cudaError_t e = cudaLaunchKernel((const void*)lk.kernel[(size_t)level], dim3((unsigned)grid),
+                                   dim3((unsigned)lk.threads), args, (size_t)lk.smem[(size_t)level], st);
+  count_launch(1);
+  return e;
 }
 
 bool pass_kernel_ready(const PassKernels& pk, size_t step) {

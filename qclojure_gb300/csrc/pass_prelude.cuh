@@ -416,12 +416,13 @@ __device__ __forceinline__ void run_pass(unsigned char* __restrict__ state, u64 
 }
 
 // The same pass over many states of one structure (a parameter sweep): work
-// items are (state, tile) pairs; a CTA walks a contiguous range of them and,
-// whenever it reaches a new state, stages that state's matrix entries (ncoef
+// items are (state, tile) pairs; a CTA walks a contiguous range [w0, w1) of them
+// and, whenever it reaches a new state, stages that state's matrix entries (ncoef
 // floats at coefs + state * ncoef) into shared memory after the tile buffers.
 template <class P>
-__device__ __forceinline__ void run_pass_batch(unsigned char* const* __restrict__ states,
-                                               const float* __restrict__ coefs, int ncoef, u64 ntiles, int nstates) {
+__device__ __forceinline__ void run_pass_range(unsigned char* const* __restrict__ states,
+                                               const float* __restrict__ coefs, int ncoef, u64 ntiles, u64 w0,
+                                               u64 w1) {
   constexpr int E = P::E, K = 1 << P::K_BITS, T = K >> P::R_BITS, PER = 16 / E, CPT = (K * E / 16) / T;
   extern __shared__ __align__(128) unsigned char smem[];
   float* cs = reinterpret_cast<float*>(smem + P::BUFS * K * E);
@@ -433,8 +434,6 @@ __device__ __forceinline__ void run_pass_batch(unsigned char* const* __restrict_
     goff[i] = ((u64)(l & ((1 << P::KLOW) - 1)) | P::hioff(l >> P::KLOW)) * E;
     soff[i] = (unsigned)swz<E>(l) * E;
   }
-  const u64 W = ntiles * (u64)nstates;
-  const u64 w0 = W * blockIdx.x / gridDim.x, w1 = W * (blockIdx.x + 1) / gridDim.x;
   for (u64 w = w0; w < w1;) {
     const int si = (int)(w / ntiles);
     const u64 t0 = w - (u64)si * ntiles;
@@ -474,6 +473,30 @@ __device__ __forceinline__ void run_pass_batch(unsigned char* const* __restrict_
     }
     w += t1 - t0;
   }
+}
+
+// One launch per pass over all states of a group: CTA b takes its share of the items.
+template <class P>
+__device__ __forceinline__ void run_pass_batch(unsigned char* const* __restrict__ states,
+                                               const float* __restrict__ coefs, int ncoef, u64 ntiles, int nstates) {
+  const u64 W = ntiles * (u64)nstates;
+  run_pass_range<P>(states, coefs, ncoef, ntiles, W * blockIdx.x / gridDim.x, W * (blockIdx.x + 1) / gridDim.x);
+}
+
+// Sweeps of several sizes: one launch per pass level runs the pass of that level of
+// every group (qubit count) that has one. The items of the groups are laid end to end
+// (group g owns [item0, item0 + items)); each CTA takes an equal share of all of them
+// and runs, group by group, the part of its share that falls in each group's range.
+struct GroupLevel {
+  unsigned char* const* states;
+  const float* coefs;  // this pass's rows: ncoef floats per state
+  int ncoef, nstates;
+  u64 ntiles, item0, items;
+};
+template <class P>
+__device__ __forceinline__ void run_group_share(const GroupLevel& d, u64 w0, u64 w1) {
+  const u64 a = w0 > d.item0 ? w0 : d.item0, b = w1 < d.item0 + d.items ? w1 : d.item0 + d.items;
+  if (a < b) run_pass_range<P>(d.states, d.coefs, d.ncoef, d.ntiles, a - d.item0, b - d.item0);
 }
 
 }  // namespace qgp

@@ -223,6 +223,25 @@ cudaError_t launch_pass_kernel_batch(const PassKernels& pk, size_t step, int n, 
                                      void* const* d_states, int nstates, const float* d_coefs, int prec,
                                      cudaStream_t st);
 void pass_coefficients(const Program& prog, size_t step, int prec, float* out);
+// Sweep level kernels (pass_kernels.cpp): level l runs pass pass_steps[g][l] of every
+// group g that has one, in one launch over all those groups' (state, tile) items. The
+// descriptor array of a level lists its groups in level_groups order; each group's
+// items are [item0, item0 + items) with items = ntiles * nstates. Layout shared with
+// the device (qgp::GroupLevel).
+struct GroupLevelDesc {
+  void* const* states;
+  const float* coefs;
+  int32_t ncoef, nstates;
+  uint64_t ntiles, item0, items;
+};
+std::shared_ptr<const PassKernels> level_kernels_for(const std::vector<const Program*>& progs,
+                                                     const std::vector<std::vector<int>>& pass_steps, int prec,
+                                                     int device, std::string* why);
+int level_count(const PassKernels& lk);
+const std::vector<int>& level_groups(const PassKernels& lk, int level);
+double level_kernels_compile_ms(const PassKernels& lk);
+cudaError_t launch_level_kernel(const PassKernels& lk, int level, const GroupLevelDesc* d_desc, uint64_t total,
+                                cudaStream_t st);
 bool pass_kernel_ready(const PassKernels& pk, size_t step);
 double pass_kernels_compile_ms(const PassKernels& pk);
 cudaError_t launch_pass_kernel(const PassKernels& pk, size_t step, int n, const PassDesc& pd, void* state, int prec,
@@ -239,6 +258,15 @@ int diag_max_groups();
 size_t diag_state_bytes();
 void fill_diag_state(void* out, uint64_t zoff, int ngroups, const int* gcount, const int* nid);
 cudaError_t launch_batch_zero(void* slab, int precision, int n, int nstates, cudaStream_t st);
+// every state of up to kMaxZeroGroups slabs to |0...0> in one launch
+constexpr int kMaxZeroGroups = 16;
+struct MultiZero {
+  void* slab[kMaxZeroGroups];
+  uint64_t per[kMaxZeroGroups];  // amplitudes per state
+  int32_t nstates[kMaxZeroGroups];
+  int32_t ngroups;
+};
+cudaError_t launch_multi_zero(const MultiZero& z, int precision, cudaStream_t st);
 // Noisy trajectories: one CTA per state renormalises it in place and records its
 // squared norm before renormalisation; one CTA per shot draws an outcome of state
 // d_state_of[shot] (draw64(seed, traj0 + shot, stream)), shifted right by `shift`

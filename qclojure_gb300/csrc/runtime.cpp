@@ -2455,6 +2455,14 @@ struct Sweep {
   cudaStream_t stream = nullptr;
   int count = 0;
   std::vector<SweepGroup> groups;
+  // level kernels: one launch per pass level over every group in lk_groups (sizes
+  // side by side), after one launch that sets all their states to |0...0>
+  std::shared_ptr<const PassKernels> lk;
+  std::vector<int> lk_groups;              // sweep groups run by the level kernels
+  std::vector<char> in_level;              // per group: run by the level kernels
+  GroupLevelDesc* d_levels = nullptr;      // descriptors of every level, level after level
+  cudaGraphExec_t lk_exec = nullptr;
+  int lk_launches = 0;
   std::vector<std::pair<int, int>> where;  // circuit -> (group, member)
   uint64_t bytes = 0;
   // the term arrays the energy tables were built from
@@ -2570,7 +2578,87 @@ static cudaError_t launch_group_passes(Sweep* sw, SweepGroup& g) {
   return e;
 }
 
+// Level kernels over the batched groups that have table-form kernels: their states are
+// set to |0...0> in one launch and pass level l of all of them runs in one launch
+// (qgl_<l>), the whole captured in one graph. A sweep of one group keeps its own graph.
+static void setup_level_kernels(Sweep* sw) {
+  std::vector<int> cand;
+  for (size_t gi = 0; gi < sw->groups.size(); ++gi) {
+    const SweepGroup& g = sw->groups[gi];
+    if (g.batched && g.pk && g.d_coefs && !g.pass_steps.empty()) cand.push_back((int)gi);
+  }
+  sw->in_level.assign(sw->groups.size(), 0);
+  if (cand.size() < 2 || cand.size() > (size_t)kMaxZeroGroups) return;
+  std::vector<const Program*> progs;
+  std::vector<std::vector<int>> steps;
+  for (int gi : cand) {
+    progs.push_back(&sw->groups[gi].progs[0]);
+    steps.push_back(sw->groups[gi].pass_steps);
+  }
+  std::string why;
+  auto lk = level_kernels_for(progs, steps, sw->prec, sw->ctx->device, &why);
+  if (!lk) return;
+  const int L = level_count(*lk);
+  std::vector<GroupLevelDesc> desc;
+  std::vector<size_t> off(L);
+  std::vector<uint64_t> total(L, 0);
+  for (int l = 0; l < L; ++l) {
+    off[l] = desc.size();
+    for (int q : level_groups(*lk, l)) {
+      const SweepGroup& g = sw->groups[cand[q]];
+      const PassDesc& pd = g.progs[0].steps[g.pass_steps[l]].pass;
+      GroupLevelDesc d;
+      d.states = g.d_states;
+      d.coefs = g.d_coefs + g.coef_off[l];
+      d.ncoef = 16 * g.pass_nops[l];
+      d.nstates = (int32_t)g.members.size();
+      d.ntiles = 1ULL << (g.n - pd.k);
+      d.item0 = total[l];
+      d.items = d.ntiles * (uint64_t)d.nstates;
+      total[l] += d.items;
+      desc.push_back(d);
+    }
+  }
+  if (cudaMallocAsync((void**)&sw->d_levels, sizeof(GroupLevelDesc) * desc.size(), sw->stream) != cudaSuccess ||
+      cudaMemcpyAsync(sw->d_levels, desc.data(), sizeof(GroupLevelDesc) * desc.size(), cudaMemcpyHostToDevice,
+                      sw->stream) != cudaSuccess ||
+      cudaStreamSynchronize(sw->stream) != cudaSuccess) {
+    cudaGetLastError();
+    return;
+  }
+  MultiZero z;
+  std::memset(&z, 0, sizeof(z));
+  for (int gi : cand) {
+    const SweepGroup& g = sw->groups[gi];
+    z.slab[z.ngroups] = g.slab;
+    z.per[z.ngroups] = 1ULL << g.n;
+    z.nstates[z.ngroups] = (int32_t)g.members.size();
+    ++z.ngroups;
+  }
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  if (cudaStreamBeginCapture(sw->stream, cudaStreamCaptureModeThreadLocal) != cudaSuccess) {
+    cudaGetLastError();
+    return;
+  }
+  cudaError_t le = launch_multi_zero(z, sw->prec, sw->stream);
+  for (int l = 0; l < L && le == cudaSuccess; ++l) le = launch_level_kernel(*lk, l, sw->d_levels + off[l], total[l], sw->stream);
+  cudaError_t ce = cudaStreamEndCapture(sw->stream, &graph);
+  count_launch(-(1 + L));  // captured launches do not run here; replays count them
+  if (le == cudaSuccess && ce == cudaSuccess && graph && cudaGraphInstantiate(&exec, graph, 0) == cudaSuccess) {
+    sw->lk = lk;
+    sw->lk_exec = exec;
+    sw->lk_launches = 1 + L;
+    sw->lk_groups = cand;
+    for (int gi : cand) sw->in_level[gi] = 1;
+  }
+  if (graph) cudaGraphDestroy(graph);
+  cudaGetLastError();
+}
+
 static void sweep_free(Sweep* sw) {
+  if (sw->lk_exec) cudaGraphExecDestroy(sw->lk_exec);
+  if (sw->d_levels) cudaFreeAsync(sw->d_levels, sw->stream);
   for (auto& g : sw->groups) {
     if (g.exec) cudaGraphExecDestroy(g.exec);
     for (auto& v : g.views) {
@@ -2844,6 +2932,7 @@ int qg_sweep_create(void* ctx, const qg_circuit* circuits, int32_t count, int32_
       count_launch(-g.launches);  // captured launches do not run here; replays count them
     }
   }
+  setup_level_kernels(sw);
   if (cudaStreamSynchronize(sw->stream) != cudaSuccess) {
     sweep_free(sw);
     return QG_ERR_DEVICE;
@@ -2905,7 +2994,16 @@ int qg_sweep_run(void* sweep, const int32_t* term_offsets, const double* coeffic
   cudaEventRecord(e0, sw->stream);
   int launches = 0, graphs = 0;
   int rc = QG_OK;
-  for (auto& g : sw->groups) {
+  if (sw->lk_exec) {
+    cudaError_t e = cudaGraphLaunch(sw->lk_exec, sw->stream);
+    if (e != cudaSuccess) rc = cuda_fail(&err, e, "sweep level kernels");
+    launches += sw->lk_launches;
+    graphs += 1;
+    count_launch(sw->lk_launches);
+  }
+  for (size_t gi = 0; gi < sw->groups.size() && rc == QG_OK; ++gi) {
+    SweepGroup& g = sw->groups[gi];
+    if (!sw->in_level.empty() && sw->in_level[gi]) continue;
     if (g.batched) {
       cudaError_t e = g.exec ? cudaGraphLaunch(g.exec, sw->stream) : launch_group_passes(sw, g);
       if (e != cudaSuccess) {

@@ -137,7 +137,39 @@ __global__ void k_diag_reduce(const double* __restrict__ partial, uint64_t chunk
   energies[s] = e;
 }
 
+// Several slabs at once (one launch for every group of a sweep): slab g holds
+// nstates[g] states of per[g] amplitudes; items are laid end to end.
+template <typename V>
+__global__ void k_multi_zero(const MultiZero z) {
+  uint64_t total = 0;
+  for (int g = 0; g < z.ngroups; ++g) total += z.per[g] * (uint64_t)z.nstates[g];
+  for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < total; i += (uint64_t)gridDim.x * blockDim.x) {
+    uint64_t j = i;
+    int g = 0;
+    while (g + 1 < z.ngroups && j >= z.per[g] * (uint64_t)z.nstates[g]) {
+      j -= z.per[g] * (uint64_t)z.nstates[g];
+      ++g;
+    }
+    V v;
+    v.x = (j % z.per[g]) == 0 ? 1 : 0;
+    v.y = 0;
+    reinterpret_cast<V*>(z.slab[g])[j] = v;
+  }
+}
+
 }  // namespace
+
+cudaError_t launch_multi_zero(const MultiZero& z, int precision, cudaStream_t st) {
+  if (z.ngroups < 1 || z.ngroups > kMaxZeroGroups) return cudaErrorInvalidValue;
+  uint64_t total = 0;
+  for (int g = 0; g < z.ngroups; ++g) total += z.per[g] * (uint64_t)z.nstates[g];
+  uint64_t grid = (total + 255) / 256;
+  if (grid > (uint64_t)kSMs * 8) grid = (uint64_t)kSMs * 8;
+  if (precision == QG_C64) k_multi_zero<float2><<<(unsigned)grid, 256, 0, st>>>(z);
+  else k_multi_zero<double2><<<(unsigned)grid, 256, 0, st>>>(z);
+  count_launch(1);
+  return cudaGetLastError();
+}
 
 int diag_max_groups() { return kMaxGroups; }
 size_t diag_state_bytes() { return sizeof(DiagState); }

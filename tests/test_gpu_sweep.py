@@ -32,7 +32,13 @@ def test_qaoa_sweep_energies(gpu_ctx, oracle, precision, arith, tol):
     with Sweep(gpu_ctx, circs, precision=precision, arithmetic=arith) as sw:
         en, st = sw.run([c["hamiltonian"] for c in circs])
         distinct = len({c["num-qubits"] for c in circs})
-        assert st["groups"] == distinct and st["graphs"] == distinct
+        assert st["groups"] == distinct
+        if precision == "c64" or arith == "double-float":
+            # table-form kernels: every size runs in one graph, one launch per pass level
+            # (plus one that zeroes all states), not one graph per size
+            assert st["graphs"] == 1, st
+        else:
+            assert st["graphs"] == distinct
         for c, e in zip(circs, en):
             ref = _energy(oracle, c)
             assert abs(e - ref) <= tol * max(1.0, abs(ref)), (e, ref)
