@@ -201,7 +201,14 @@ typedef struct qg_config {
   uint64_t seed;                  /* default seed                                        */
   int32_t arithmetic;             /* QG_ARITH_* for complex128 tiled passes              */
   int32_t pass_kernels;           /* QG_PASS_KERNELS_*                                   */
+  int32_t small_job_loop;         /* QG_JOB_LOOP_*: how jobs of 5..12 qubits run         */
+  int32_t reserved0;
 } qg_config;
+
+/* Jobs of 5..12 qubits (the whole state is one tile) run one CTA per job. AUTO / ON:
+   a device-resident loop per qubit count claims them as they are published (no launch
+   per job or batch); OFF: a host batcher groups ready jobs into one launch. */
+enum { QG_JOB_LOOP_AUTO = 0, QG_JOB_LOOP_ON = 1, QG_JOB_LOOP_OFF = 2 };
 
 typedef struct qg_queue_info {    /* queue-status (ideal_simulator.clj:165-176) + device fields */
   int64_t total_jobs, queued, running, completed, failed, cancelled;
@@ -246,6 +253,15 @@ int qg_wait(void* ctx, uint64_t job, int64_t timeout_ms, int32_t* status_out);
 int qg_cancel(void* ctx, uint64_t job, int32_t* outcome);
 /* queue-status (ideal_simulator.clj:165-176). */
 int qg_queue_status(void* ctx, qg_queue_info* out);
+/* qg_job_loop_info has no counterpart in the reference: the device-resident small-job
+   loops of the context. loops: qubit counts that have one; running: loop kernels still
+   resident; launches: loop kernels started (a loop leaves after a few milliseconds
+   without work and starts again when a job arrives); jobs: jobs served by the loops. */
+typedef struct qg_loop_info {
+  int32_t loops, running;
+  uint64_t launches, jobs;
+} qg_loop_info;
+int qg_job_loop_info(void* ctx, qg_loop_info* out);
 int qg_job_details(void* ctx, uint64_t job, qg_job_info* out);
 /* job-result pieces (result.clj:179-497). Buffers are caller-owned. */
 int qg_result_counts(void* ctx, uint64_t job, uint64_t* outcomes, uint64_t* counts, int64_t cap, int64_t* n_out);

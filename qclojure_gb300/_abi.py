@@ -109,7 +109,15 @@ class QgOptions(C.Structure):
 class QgConfig(C.Structure):
     _fields_ = [("device", C.c_int32), ("precision", C.c_int32), ("fusion", C.c_int32), ("fuse_k", C.c_int32),
                 ("max_qubits", C.c_int32), ("workers", C.c_int32), ("hbm_budget_bytes", C.c_uint64),
-                ("seed", C.c_uint64), ("arithmetic", C.c_int32), ("pass_kernels", C.c_int32)]
+                ("seed", C.c_uint64), ("arithmetic", C.c_int32), ("pass_kernels", C.c_int32),
+                ("small_job_loop", C.c_int32), ("reserved0", C.c_int32)]
+
+
+JOB_LOOP = {"auto": 0, "on": 1, "off": 2}
+
+
+class QgLoopInfo(C.Structure):
+    _fields_ = [("loops", C.c_int32), ("running", C.c_int32), ("launches", C.c_uint64), ("jobs", C.c_uint64)]
 
 
 class QgQueueInfo(C.Structure):
@@ -225,6 +233,7 @@ SIGNATURES = {
     "qg_kernel_launches": ([U64P], C.c_int),
     "qg_pass_kernels_build": ([C.POINTER(QgCircuit), I32, I32, I32P, DP, C.c_char_p, I64], C.c_int),
     "qg_pass_kernels_info": ([I32P, U64P, U64P], C.c_int),
+    "qg_job_loop_info": ([P, C.POINTER(QgLoopInfo)], C.c_int),
     "qg_autotune": ([P, I32, I32, C.POINTER(QgTuning), C.POINTER(QgTuning), I32, I32P], C.c_int),
     "qg_tuning_set": ([P, I32, I32, C.POINTER(QgTuning)], C.c_int),
     "qg_tuning_get": ([P, I32, I32, C.POINTER(QgTuning)], C.c_int),

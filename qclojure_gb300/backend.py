@@ -127,6 +127,7 @@ class GpuStateVectorSimulator:
         cfg.seed = int(self.config.get("seed", 0) or 0) & (2**64 - 1)
         cfg.arithmetic = ARITHMETIC[self.config.get("arithmetic", "double-float")]
         cfg.pass_kernels = A.PASS_KERNELS[self.config.get("pass-kernels", "auto")]
+        cfg.small_job_loop = A.JOB_LOOP[self.config.get("small-job-loop", "auto")]
         ctx = C.c_void_p()
         _check(self._lib.qg_ctx_create(C.byref(cfg), C.byref(ctx)))
         self._ctx = ctx

@@ -190,6 +190,22 @@ struct TileJobRec {
   int32_t npasses;      // passes of the job's program
   int32_t pass_begin;   // index of its first pass in the launch's op-count array
 };
+// Device-resident loop for small jobs (k_job_loop): the host publishes jobs of one qubit
+// count into a ring of slots in mapped host memory and raises *tail; the loop's CTAs
+// claim slots in order (*head, device memory), run each job whole (as k_tile_jobs does)
+// and set the slot's done flag. A CTA that finds no work for idle_ns nanoseconds
+// returns (the bounded wait); the host relaunches the loop when work arrives again.
+struct JobLoopSlot {
+  TileJobRec rec;        // state; op_begin and pass_begin index the two arrays below
+  const void* kops;      // the job's op records (device)
+  const int32_t* pass_nops;
+  int32_t done;          // set to 1 by the device when the job's state is final
+  int32_t pad;
+};
+constexpr int kJobLoopCtas = 8;
+cudaError_t launch_job_loop(int precision, int arithmetic, int n, JobLoopSlot* d_slots, uint32_t cap,
+                            const uint32_t* d_tail, uint32_t* d_head, uint32_t* d_served, uint64_t idle_ns,
+                            cudaStream_t st);
 cudaError_t launch_tile_jobs(int precision, int arithmetic, int n, const TileJobRec* d_jobs, int njobs,
                              const void* d_kops, const int32_t* d_pass_nops, cudaStream_t st);
 size_t kop_record_bytes();

@@ -656,6 +656,13 @@ struct Ctx {
   // smallest state that runs specialised under QG_PASS_KERNELS_AUTO, per precision
   // (kPassKernelMinQubits until qg_autotune_crossover measures it)
   std::atomic<int> spec_min_qubits[2] = {{kPassKernelMinQubits}, {kPassKernelMinQubits}};
+  // device-resident loops of small jobs, per (qubits, precision, arithmetic)
+  std::mutex loop_mu;
+  std::condition_variable loop_cv;
+  std::map<std::tuple<int, int, int>, std::unique_ptr<struct JobLoop>> loops;
+  std::thread loop_poller;
+  bool loop_stop = false;
+  uint64_t loop_jobs = 0;
 };
 
 // True when programs of this kind run as specialised pass kernels (the condition
@@ -964,6 +971,227 @@ static void complete_job(Ctx* c, Job* j, int rc) {
 
 // Workers of the small-job lane compile small jobs and hand them to the batcher,
 // so small jobs never wait behind large ones; the other workers run large jobs.
+// ---------------------------------------------------------------------------
+// Device-resident loops for small jobs (k_job_loop). One loop per (qubits, precision,
+// arithmetic): a ring of slots in mapped host memory that the host fills in order and
+// publishes by raising the tail; the loop's CTAs claim slots in that order, run each
+// job whole in shared memory and set the slot's done flag; a poller thread extracts
+// the results of finished jobs. A loop kernel returns after kLoopIdleNs without work
+// (its only waits are these polls) and is started again when the next job arrives;
+// the poller also restarts one that left while a published job was still unclaimed.
+// ---------------------------------------------------------------------------
+constexpr uint32_t kLoopSlots = 256;
+constexpr uint64_t kLoopIdleNs = 3000000;  // 3 ms
+
+struct JobLoop {
+  int n = 0, prec = 0, arith = 0;
+  void* host = nullptr;  // pinned, mapped: kLoopSlots slots, then the tail word
+  JobLoopSlot* h_slots = nullptr;
+  JobLoopSlot* d_slots = nullptr;
+  uint32_t* h_tail = nullptr;
+  uint32_t* d_tail = nullptr;
+  uint32_t* d_head = nullptr;    // device: claimed count, then the served count
+  cudaStream_t stream = nullptr;
+  cudaEvent_t done = nullptr;    // recorded after the latest loop launch
+  bool launched = false;
+  uint32_t published = 0;
+  uint64_t launches = 0;
+  int since_launch = 0;          // jobs published to the running loop kernel
+  int outstanding = 0;
+  std::vector<std::shared_ptr<Job>> job;      // per slot (null: free)
+  std::vector<std::unique_ptr<State>> state;  // per slot
+  std::vector<void*> buf;                     // per slot: op records, then per-pass op counts
+};
+
+static bool loops_enabled(const Ctx* c) { return c->cfg.small_job_loop != QG_JOB_LOOP_OFF; }
+
+// Caller holds loop_mu.
+static JobLoop* get_loop(Ctx* c, int n, int prec, int arith, std::string* err) {
+  auto key = std::make_tuple(n, prec, arith);
+  auto it = c->loops.find(key);
+  if (it != c->loops.end()) return it->second.get();
+  auto L = std::make_unique<JobLoop>();
+  L->n = n;
+  L->prec = prec;
+  L->arith = arith;
+  const size_t bytes = sizeof(JobLoopSlot) * kLoopSlots + 64;
+  cudaError_t e = cudaHostAlloc(&L->host, bytes, cudaHostAllocMapped | cudaHostAllocPortable);
+  void* dhost = nullptr;
+  if (e == cudaSuccess) e = cudaHostGetDevicePointer(&dhost, L->host, 0);
+  if (e == cudaSuccess) e = cudaMalloc((void**)&L->d_head, 2 * sizeof(uint32_t));
+  if (e == cudaSuccess) e = cudaMemset(L->d_head, 0, 2 * sizeof(uint32_t));
+  if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&L->stream, cudaStreamNonBlocking);
+  if (e == cudaSuccess) e = cudaEventCreateWithFlags(&L->done, cudaEventDisableTiming);
+  if (e != cudaSuccess) {
+    cuda_fail(err, e, "small-job loop setup");
+    if (L->host) cudaFreeHost(L->host);
+    if (L->d_head) cudaFree(L->d_head);
+    return nullptr;
+  }
+  std::memset(L->host, 0, bytes);
+  L->h_slots = (JobLoopSlot*)L->host;
+  L->d_slots = (JobLoopSlot*)dhost;
+  L->h_tail = (uint32_t*)((char*)L->host + sizeof(JobLoopSlot) * kLoopSlots);
+  L->d_tail = (uint32_t*)((char*)dhost + sizeof(JobLoopSlot) * kLoopSlots);
+  L->job.resize(kLoopSlots);
+  L->state.resize(kLoopSlots);
+  L->buf.assign(kLoopSlots, nullptr);
+  JobLoop* raw = L.get();
+  c->loops[key] = std::move(L);
+  return raw;
+}
+
+// Caller holds loop_mu.
+static cudaError_t start_loop(JobLoop* L) {
+  cudaError_t e = launch_job_loop(L->prec, L->arith, L->n, L->d_slots, kLoopSlots, L->d_tail, L->d_head,
+                                  L->d_head + 1, kLoopIdleNs, L->stream);
+  if (e == cudaSuccess) e = cudaEventRecord(L->done, L->stream);
+  if (e == cudaSuccess) {
+    L->launched = true;
+    ++L->launches;
+    L->since_launch = 0;
+  }
+  return e;
+}
+
+// Publish a compiled small job to its loop: its state and op records go to the device
+// first (on the lane's stream), then the slot is filled and the tail raised.
+static int loop_submit(Ctx* c, const std::shared_ptr<Job>& j, cudaStream_t stream, std::string* err) {
+  NvtxRange nvtx("qg loop publish");
+  auto st = std::make_unique<State>();
+  int rc = init_job_state(c, j.get(), stream, st.get(), err);
+  if (rc != QG_OK) return rc;
+  const Program& pr = *j->prog;
+  const size_t rec = kop_record_bytes();
+  std::vector<int32_t> nops;
+  for (const Step& s : pr.steps) nops.push_back((int32_t)(s.pass.op_end - s.pass.op_begin));
+  const size_t b_ops = rec * std::max<size_t>(pr.tops.size(), 1);
+  std::vector<unsigned char> host(b_ops + sizeof(int32_t) * std::max<size_t>(nops.size(), 1), 0);
+  encode_kops(j->precision, pr.arith, pr.tops.data(), (int64_t)pr.tops.size(), host.data());
+  if (!nops.empty()) std::memcpy(host.data() + b_ops, nops.data(), sizeof(int32_t) * nops.size());
+  void* d = nullptr;
+  CK(cudaMallocAsync(&d, host.size(), stream), "small-job records");
+  cudaError_t e = cudaMemcpyAsync(d, host.data(), host.size(), cudaMemcpyHostToDevice, stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(stream);
+  if (e != cudaSuccess) {
+    cudaFreeAsync(d, stream);
+    return cuda_fail(err, e, "small-job records");
+  }
+  std::unique_lock<std::mutex> lk(c->loop_mu);
+  JobLoop* L = get_loop(c, j->n, j->precision, pr.arith, err);
+  if (!L) {
+    cudaFreeAsync(d, stream);
+    return QG_ERR_DEVICE;
+  }
+  const uint32_t idx = L->published;
+  const uint32_t slot = idx % kLoopSlots;
+  c->loop_cv.wait(lk, [&] { return !L->job[slot]; });
+  JobLoopSlot& sl = L->h_slots[slot];
+  sl.rec.state = st->d;
+  sl.rec.op_begin = 0;
+  sl.rec.npasses = (int32_t)nops.size();
+  sl.rec.pass_begin = 0;
+  sl.kops = d;
+  sl.pass_nops = (const int32_t*)((unsigned char*)d + b_ops);
+  *(volatile int32_t*)&sl.done = 0;
+  L->job[slot] = j;
+  L->state[slot] = std::move(st);
+  L->buf[slot] = d;
+  ++L->outstanding;
+  std::atomic_thread_fence(std::memory_order_seq_cst);  // the slot before the tail
+  *(volatile uint32_t*)L->h_tail = idx + 1;
+  L->published = idx + 1;
+  std::atomic_thread_fence(std::memory_order_seq_cst);
+  if (!L->launched || cudaEventQuery(L->done) == cudaSuccess) {
+    e = start_loop(L);
+    if (e != cudaSuccess) {
+      // unpublish is not possible once the tail moved; the poller retries the start
+      cuda_fail(err, e, "small-job loop launch");
+    }
+  }
+  j->batched_with = ++L->since_launch;
+  lk.unlock();
+  c->loop_cv.notify_all();
+  return QG_OK;
+}
+
+// Collect finished loop jobs, extract their results, restart loops that left while a
+// published job was unclaimed. Runs until the context stops and no job is outstanding.
+static void loop_poller_loop(Ctx* c) {
+  cudaSetDevice(c->device);
+  cudaStream_t stream;
+  cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking);
+  struct Finished {
+    std::shared_ptr<Job> job;
+    std::unique_ptr<State> state;
+    void* buf;
+  };
+  for (;;) {
+    std::vector<Finished> fin;
+    {
+      std::unique_lock<std::mutex> lk(c->loop_mu);
+      int outstanding = 0;
+      for (auto& kv : c->loops) {
+        JobLoop* L = kv.second.get();
+        if (L->outstanding == 0) continue;
+        for (uint32_t sidx = 0; sidx < kLoopSlots; ++sidx) {
+          if (!L->job[sidx]) continue;
+          if (*(volatile int32_t*)&L->h_slots[sidx].done == 1) {
+            std::atomic_thread_fence(std::memory_order_acquire);
+            fin.push_back({std::move(L->job[sidx]), std::move(L->state[sidx]), L->buf[sidx]});
+            L->job[sidx].reset();
+            L->buf[sidx] = nullptr;
+            --L->outstanding;
+          }
+        }
+        // a loop that left (idle budget) while a published job was still unclaimed
+        if (L->outstanding > 0 && L->launched && cudaEventQuery(L->done) == cudaSuccess) {
+          bool pending = false;
+          for (uint32_t sidx = 0; sidx < kLoopSlots && !pending; ++sidx)
+            pending = L->job[sidx] && *(volatile int32_t*)&L->h_slots[sidx].done == 0;
+          if (pending) start_loop(L);
+        }
+        outstanding += L->outstanding;
+      }
+      if (fin.empty()) {
+        if (c->loop_stop && outstanding == 0) break;
+        c->loop_cv.wait_for(lk, std::chrono::microseconds(50));
+        continue;
+      }
+      c->loop_jobs += fin.size();
+    }
+    c->loop_cv.notify_all();  // slots are free again
+    for (Finished& f : fin) {
+      cudaFreeAsync(f.buf, stream);
+      Job* j = f.job.get();
+      j->passes = j->prog->hbm_passes;
+      const int rc = job_results(c, j, std::move(f.state), stream, QG_OK, std::string());
+      complete_job(c, j, rc);
+    }
+  }
+  cudaStreamSynchronize(stream);
+  cudaStreamDestroy(stream);
+}
+
+static void loops_shutdown(Ctx* c) {
+  {
+    std::lock_guard<std::mutex> g(c->loop_mu);
+    c->loop_stop = true;
+  }
+  c->loop_cv.notify_all();
+  if (c->loop_poller.joinable()) c->loop_poller.join();
+  for (auto& kv : c->loops) {
+    JobLoop* L = kv.second.get();
+    cudaStreamSynchronize(L->stream);  // a loop kernel leaves within its idle budget
+    cudaEventDestroy(L->done);
+    cudaStreamDestroy(L->stream);
+    cudaFree(L->d_head);
+    cudaFreeHost(L->host);
+  }
+  c->loops.clear();
+}
+
+
 static void worker_loop(Ctx* c, bool small_lane) {
   cudaSetDevice(c->device);
   cudaStream_t stream;
@@ -1034,7 +1262,22 @@ static void worker_loop(Ctx* c, bool small_lane) {
         // compile here (the lane's workers compile in parallel) and hand the job to the batcher
         std::string err;
         rc = compile_job(c, j.get(), &err);
-        const bool batch = rc == QG_OK && small_job(j.get());
+        const bool small = rc == QG_OK && small_job(j.get());
+        if (small && loops_enabled(c)) {
+          // a device-resident loop claims it; the poller completes it
+          rc = loop_submit(c, j, stream, &err);
+          {
+            std::lock_guard<std::mutex> g(c->mu);
+            --c->compiling;
+          }
+          c->ready_cv.notify_all();
+          if (rc == QG_OK) continue;
+          j->error_code = rc;
+          j->error = err;
+          complete_job(c, j.get(), rc);
+          continue;
+        }
+        const bool batch = small;
         {
           std::lock_guard<std::mutex> g(c->mu);
           if (batch) c->ready.push_back(j);
@@ -1323,6 +1566,24 @@ using namespace qg;
 // ===========================================================================
 extern "C" {
 
+int qg_job_loop_info(void* ctx, qg_loop_info* out) {
+  if (!ctx || !out) return QG_ERR_INVALID_ARG;
+  Ctx* c = (Ctx*)ctx;
+  cudaSetDevice(c->device);
+  std::lock_guard<std::mutex> g(c->loop_mu);
+  std::memset(out, 0, sizeof(*out));
+  for (auto& kv : c->loops) {
+    JobLoop* L = kv.second.get();
+    ++out->loops;
+    if (L->launched && cudaEventQuery(L->done) == cudaErrorNotReady) ++out->running;
+    out->launches += L->launches;
+  }
+  cudaGetLastError();
+  out->jobs = c->loop_jobs;
+  return QG_OK;
+}
+
+
 int qg_abi_version(void) { return QG_ABI_VERSION; }
 
 int qg_device_count(int32_t* count) {
@@ -1370,6 +1631,7 @@ int qg_ctx_create(const qg_config* cfg, void** ctx_out) {
   for (int w = 0; w < c->cfg.workers; ++w) c->workers.emplace_back(worker_loop, c, false);
   for (int w = 0; w < kSmallLaneWorkers; ++w) c->workers.emplace_back(worker_loop, c, true);
   c->batcher = std::thread(batcher_loop, c);
+  c->loop_poller = std::thread(loop_poller_loop, c);
   *ctx_out = c;
   return QG_OK;
 }
@@ -1391,6 +1653,7 @@ int qg_ctx_destroy(void* ctx) {
   c->ready_cv.notify_all();
   if (c->batcher.joinable()) c->batcher.join();
   cudaSetDevice(c->device);
+  loops_shutdown(c);
   for (auto& kv : c->jobs)
     if (kv.second->state) {
       State* s = kv.second->state.get();

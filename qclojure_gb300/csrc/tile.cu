@@ -736,6 +736,126 @@ __global__ void __launch_bounds__(512, 1) k_tile_jobs(int n, const TileJobRec* _
   }
 }
 
+// The same per-job work as k_tile_jobs, served by a resident loop: each CTA claims the
+// next published slot (slots in publication order), runs the job, then marks the slot
+// done. The polls of the ring are the loop's only waits; when none finds work for
+// idle_ns the CTA returns (and *served counts the jobs it ran), so a loop never spins
+// beyond that budget.
+__device__ __forceinline__ uint32_t ld_acquire_sys(const uint32_t* p) {
+  uint32_t v;
+  asm volatile("ld.acquire.sys.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+__device__ __forceinline__ void st_release_sys(int32_t* p, int32_t v) {
+  asm volatile("st.release.sys.global.s32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+__device__ __forceinline__ uint64_t now_ns() {
+  uint64_t t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+template <class P>
+__global__ void __launch_bounds__(512, 1) k_job_loop(int n, JobLoopSlot* slots, uint32_t cap,
+                                                     const uint32_t* tail, uint32_t* head, uint32_t* served,
+                                                     uint64_t idle_ns) {
+  constexpr int E = P::kElem;
+  extern __shared__ __align__(128) unsigned char smem[];
+  __shared__ long long s_claim;
+  __shared__ JobLoopSlot s_slot;
+  TileGeo g;
+  g.k = n;
+  g.K = 1 << n;
+  g.klow = n;
+  g.T = blockDim.x;
+  unsigned char* tile = smem;
+  KOp* sops = reinterpret_cast<KOp*>(smem + (size_t)g.K * E);
+  uint64_t* hioff = reinterpret_cast<uint64_t*>(sops + kMaxKOps);
+  if (threadIdx.x == 0) hioff[0] = 0;  // every bit is local
+  __syncthreads();
+  CopyPlan<E> cp;
+  cp.init(hioff, g);
+  uint64_t last = now_ns();
+  uint32_t ran = 0;
+  for (;;) {
+    if (threadIdx.x == 0) {
+      long long claim = -1;
+      for (;;) {
+        const uint32_t t = ld_acquire_sys(tail);
+        const uint32_t h = *reinterpret_cast<volatile uint32_t*>(head);
+        if (h >= t) break;
+        if (atomicCAS(head, h, h + 1) == h) {
+          claim = h;
+          break;
+        }
+      }
+      if (claim >= 0) {
+        // the slot was written before the host raised tail (the acquire above orders these reads)
+        const volatile JobLoopSlot* vs = slots + (claim % cap);
+        s_slot.rec.state = vs->rec.state;
+        s_slot.rec.op_begin = vs->rec.op_begin;
+        s_slot.rec.npasses = vs->rec.npasses;
+        s_slot.rec.pass_begin = vs->rec.pass_begin;
+        s_slot.kops = vs->kops;
+        s_slot.pass_nops = vs->pass_nops;
+        last = now_ns();
+      } else if (now_ns() - last > idle_ns) {
+        claim = -2;  // nothing published for idle_ns: leave
+      } else {
+        __nanosleep(2000);
+      }
+      s_claim = claim;
+    }
+    __syncthreads();
+    const long long claim = s_claim;
+    __syncthreads();
+    if (claim == -2) break;
+    if (claim < 0) continue;
+    const TileJobRec jr = s_slot.rec;
+    const KOp* kops = reinterpret_cast<const KOp*>(s_slot.kops);
+    const int32_t* pass_nops = s_slot.pass_nops;
+    unsigned char* state = reinterpret_cast<unsigned char*>(jr.state);
+    cp.load(tile, state);
+    cp_commit();
+    cp_wait<0>();
+    __syncthreads();
+    if constexpr (P::kInPairs) {  // IEEE doubles -> float pairs, each thread its own slots
+      for (int l = threadIdx.x; l < g.K; l += g.T) {
+        const int q = swz<E>(l);
+        const dfc v = load_dfc(reinterpret_cast<const double2*>(tile)[q]);
+        reinterpret_cast<float4*>(tile)[q] = make_float4(v.rh, v.rl, v.ih, v.il);
+      }
+    }
+    int64_t ob = jr.op_begin;
+    for (int p = 0; p < jr.npasses; ++p) {
+      const int nops = pass_nops[jr.pass_begin + p];
+      __syncthreads();  // the previous pass's readers of sops are done
+      const uint4* src = reinterpret_cast<const uint4*>(kops + ob);
+      uint4* dst = reinterpret_cast<uint4*>(sops);
+      const int words = nops * (int)(sizeof(KOp) / 16);
+      for (int q = threadIdx.x; q < words; q += g.T) dst[q] = src[q];
+      __syncthreads();
+      run_ops<P>(tile, sops, nops, nullptr, 0, g);  // ends with a barrier
+      ob += nops;
+    }
+    if constexpr (P::kOutPairs) {  // float pairs -> IEEE doubles
+      for (int l = threadIdx.x; l < g.K; l += g.T) {
+        const int q = swz<E>(l);
+        const float4 v = reinterpret_cast<const float4*>(tile)[q];
+        reinterpret_cast<double2*>(tile)[q] = store_dfc(dfc{v.x, v.y, v.z, v.w});
+      }
+      __syncthreads();
+    }
+    cp.store(tile, state);
+    __syncthreads();  // every thread's stores are issued; the tile buffer is free
+    if (threadIdx.x == 0) {
+      __threadfence_system();  // the state's stores are visible before the flag
+      st_release_sys(&slots[claim % cap].done, 1);
+      ++ran;
+    }
+  }
+  if (threadIdx.x == 0 && ran) atomicAdd(served, ran);
+}
+
 // Host: translate TOps into the compact records of policy P.
 template <class P>
 void build_kops(KOp* out, const TOp* ops, int64_t nops) {
@@ -872,6 +992,31 @@ cudaError_t launch_jobs_t(int n, const TileJobRec* d_jobs, int njobs, const KOp*
   k_tile_jobs<P><<<(unsigned)njobs, threads, smem, st>>>(n, d_jobs, njobs, d_kops, d_pass_nops);
   count_launch(1);
   return cudaGetLastError();
+}
+
+template <class P>
+cudaError_t launch_loop_t(int n, JobLoopSlot* d_slots, uint32_t cap, const uint32_t* d_tail, uint32_t* d_head,
+                          uint32_t* d_served, uint64_t idle_ns, cudaStream_t st) {
+  constexpr int E = P::kElem;
+  const int K = 1 << n;
+  const int threads = K / kRegs;
+  if (n < 5 || n > kMaxSmallJobQubits || cap < 1) return cudaErrorInvalidValue;
+  const size_t smem = (size_t)K * E + sizeof(KOp) * kMaxKOps + 16;
+  cudaError_t e = cudaFuncSetAttribute(k_job_loop<P>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       (int)((size_t(64) << 10) + sizeof(KOp) * kMaxKOps + 16));
+  if (e != cudaSuccess) return e;
+  k_job_loop<P><<<kJobLoopCtas, threads, smem, st>>>(n, d_slots, cap, d_tail, d_head, d_served, idle_ns);
+  count_launch(1);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_job_loop(int precision, int arithmetic, int n, JobLoopSlot* d_slots, uint32_t cap,
+                            const uint32_t* d_tail, uint32_t* d_head, uint32_t* d_served, uint64_t idle_ns,
+                            cudaStream_t st) {
+  if (precision == QG_C64) return launch_loop_t<PolF>(n, d_slots, cap, d_tail, d_head, d_served, idle_ns, st);
+  if (arithmetic == QG_ARITH_DOUBLE_FLOAT)
+    return launch_loop_t<PolDFT<3>>(n, d_slots, cap, d_tail, d_head, d_served, idle_ns, st);
+  return launch_loop_t<PolD>(n, d_slots, cap, d_tail, d_head, d_served, idle_ns, st);
 }
 
 cudaError_t launch_tile_jobs(int precision, int arithmetic, int n, const TileJobRec* d_jobs, int njobs,

@@ -26,7 +26,7 @@ def test_struct_layouts_match_header(built):
 
     assert C.sizeof(A.QgOp) == 4 + 4 + 40 + 8 + 64
     assert C.sizeof(A.QgCircuit) == 16
-    assert C.sizeof(A.QgConfig) == 6 * 4 + 2 * 8 + 2 * 4
+    assert C.sizeof(A.QgConfig) == 6 * 4 + 2 * 8 + 4 * 4
     src = r'''
 #include <stdio.h>
 #include "qgpu.h"

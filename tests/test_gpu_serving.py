@@ -144,6 +144,69 @@ def test_served_c64_stream_tvd_against_oracle(oracle):
         sim.close()
 
 
+def test_resident_loop_idles_out_and_restarts():
+    """Small jobs run in a device-resident loop per qubit count. Its only waits are polls of
+    the job ring, bounded by an idle budget: with nothing published (the tail word nothing
+    raises) every loop kernel returns by itself within milliseconds, and the next job
+    starts the loop again. The host reads the loops' state through qg_job_loop_info."""
+    import ctypes as C
+    import time
+
+    from qclojure_gb300 import _abi as A
+    from qclojure_gb300 import workloads
+    from qclojure_gb300.backend import create_simulator
+
+    sim = create_simulator({"precision": "c64", "fusion": "tiled", "workers": 2, "seed": 2,
+                            "small-job-loop": "on"})
+
+    def info():
+        i = A.QgLoopInfo()
+        assert sim._lib.qg_job_loop_info(sim._ctx, C.byref(i)) == 0
+        return i
+
+    try:
+        ids = [sim.submit_circuit(workloads.layered_circuit(n, 4, seed=n), {}) for n in (8, 8, 10, 10, 10)]
+        for j in ids:
+            assert sim.wait(j, 60_000) == "completed"
+        first = info()
+        assert first.loops == 2 and first.launches >= 2 and first.jobs == 5
+        deadline = time.time() + 2.0
+        while info().running and time.time() < deadline:
+            time.sleep(0.01)
+        assert info().running == 0, "a loop kernel did not leave after its idle budget"
+        j = sim.submit_circuit(workloads.layered_circuit(10, 3, seed=99), {})
+        assert sim.wait(j, 60_000) == "completed"
+        after = info()
+        assert after.launches > first.launches and after.jobs == 6
+    finally:
+        sim.close()
+
+
+@pytest.mark.parametrize("precision,arith", [("c64", "exact"), ("c128", "double-float"), ("c128", "exact")])
+def test_resident_loop_equals_batcher(precision, arith):
+    """The resident loop and the host batcher run the same op records per job: identical
+    final states and shot outcomes."""
+    from qclojure_gb300.backend import create_simulator
+
+    jobs = [(c, o) for c, o in _stream(7, count=24, cap=12) if c["num-qubits"] <= 12]
+    out = {}
+    for mode in ("on", "off"):
+        sim = create_simulator({"precision": precision, "fusion": "tiled", "workers": 2, "seed": 3,
+                                "arithmetic": arith, "small-job-loop": mode})
+        try:
+            ids = [sim.submit_circuit(c, o) for c, o in jobs]
+            res = []
+            for j in ids:
+                assert sim.wait(j, 120_000) == "completed"
+                r = sim.job_result(j)
+                res.append((_sv(r), r["results"].get("measurement-results", {}).get("measurement-outcomes")))
+            out[mode] = res
+        finally:
+            sim.close()
+    for (a, sa), (b, sb) in zip(out["on"], out["off"]):
+        assert np.array_equal(a, b) and sa == sb
+
+
 def test_cancel_small_job_waiting_in_queue():
     """A queued small job can be cancelled; the rest of its batch completes."""
     from qclojure_gb300 import workloads
