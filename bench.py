@@ -524,7 +524,7 @@ def main():
     if not args.no_autotune and args.fusion == "tiled":
         for tp in ((args.precision, "c64") if args.precision == "c128" and not args.no_extras else (args.precision,)):
             try:
-                tuning[tp] = ctx.autotune(n, tp)
+                tuning[tp] = ctx.autotune(n, tp, circ)  # timed on the workload itself
             except Exception as e:  # nothing to tune (exact arithmetic, interpreted sizes)
                 tuning[tp] = {"skipped": f"{type(e).__name__}: {e}"}
     st = ctx.state(n, args.precision)

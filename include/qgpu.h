@@ -469,8 +469,8 @@ int qg_pass_kernels_info(int32_t* available, uint64_t* cache_hits, uint64_t* cac
    The specialised pass kernels apply a pass's gates to tiles of 2^tile_bits amplitudes,
    each thread holding 2^reg_bits of them, with `buffers` tile buffers in shared memory
    and the kernels built for ctas_per_sm CTAs per SM. qg_autotune times candidate shapes
-   on a calibration circuit (six layers of the layered recipe and four QFT columns) on a
-   state of num_qubits qubits, keeps the fastest (the default unless another is faster
+   on a calibration circuit (the caller's workload, or when null six layers of the
+   layered recipe and four QFT columns) on a state of num_qubits qubits, keeps the fastest (the default unless another is faster
    by more than 1 %), records it in the context for programs of that size and precision
    that run specialised, and reports every candidate with its median device time (ms).
    It allocates one state of that size while it runs. qg_tuning_set records a shape
@@ -484,8 +484,8 @@ typedef struct qg_tuning {
   int32_t ctas_per_sm;  /* CTAs per SM the kernels are built for */
   double ms;            /* measured device time of the calibration circuit (qg_autotune) */
 } qg_tuning;
-int qg_autotune(void* ctx, int32_t num_qubits, int32_t precision, qg_tuning* chosen, qg_tuning* tried, int32_t cap,
-                int32_t* count_out);
+int qg_autotune(void* ctx, int32_t num_qubits, int32_t precision, const qg_circuit* calibration, qg_tuning* chosen,
+                qg_tuning* tried, int32_t cap, int32_t* count_out);
 int qg_tuning_set(void* ctx, int32_t num_qubits, int32_t precision, const qg_tuning* tuning);
 int qg_tuning_get(void* ctx, int32_t num_qubits, int32_t precision, qg_tuning* out);
 int32_t qg_tuning_pick(const double* ms, const int32_t* valid, int32_t count, int32_t default_index, double tie_frac);

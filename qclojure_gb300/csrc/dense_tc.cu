@@ -176,6 +176,7 @@ __device__ __forceinline__ uint64_t tile_base(const DenseTcParams& p, uint64_t t
   return b;
 }
 
+template <int KB>
 __global__ void __launch_bounds__(kThreads, 1) k_dense_tc(const __grid_constant__ DenseTcParams p) {
   extern __shared__ __align__(1024) unsigned char smem_raw[];
   // 1024-aligned regions: A hi, A lo (also the epilogue's transposition buffer), B hi, B lo, staging
@@ -190,13 +191,12 @@ __global__ void __launch_bounds__(kThreads, 1) k_dense_tc(const __grid_constant_
   uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(mma_bar + 1);
 
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-  const int k = p.k;
-  const int D = 1 << k;                    // target combinations
-  const int Kp = 2 * D;                    // reals per column (K of the GEMM)
-  const int Np = Kp;                       // reals per output column (N of the GEMM)
-  const int G = (k == 4) ? 2 : 1;          // 128-column MMA blocks per tile
-  const int Mrows = 128 * G;               // columns of a tile
-  const uint32_t idesc = idesc_tf32(Np);
+  constexpr int D = 1 << KB;               // target combinations
+  constexpr int Kp = 2 * D;                // reals per column (K of the GEMM)
+  constexpr int Np = Kp;                   // reals per output column (N of the GEMM)
+  constexpr int G = (KB == 4) ? 2 : 1;     // 128-column MMA blocks per tile
+  constexpr int Mrows = 128 * G;           // columns of a tile
+  constexpr uint32_t idesc = idesc_tf32(Np);
 
   // this thread's 16 tile positions (i = tid + q * kThreads) map to the same places in
   // every tile: A operand byte offsets and epilogue buffer indices, computed once
@@ -235,6 +235,8 @@ __global__ void __launch_bounds__(kThreads, 1) k_dense_tc(const __grid_constant_
   __syncthreads();
   tc_fence_after();
   const uint32_t tmem = *tmem_slot;
+  const uint64_t dah = smem_desc(smem_u32(a_hi)), dal = smem_desc(smem_u32(a_lo));
+  const uint64_t dbh = smem_desc(smem_u32(b_hi)), dbl = smem_desc(smem_u32(b_lo));
 
   const uint64_t t_begin = p.ntiles * blockIdx.x / gridDim.x, t_end = p.ntiles * (blockIdx.x + 1) / gridDim.x;
   const uint64_t count = t_end - t_begin;
@@ -287,20 +289,21 @@ __global__ void __launch_bounds__(kThreads, 1) k_dense_tc(const __grid_constant_
     if (warp == 0) {
       if (lane == 0) {
         tc_fence_after();
-        const uint32_t ah = smem_u32(a_hi), al = smem_u32(a_lo), bh = smem_u32(b_hi), bl = smem_u32(b_lo);
-        uint32_t acc = 0;
+        // descriptors differ only in their start address field (address / 16), so each
+        // MMA's descriptor is a base descriptor plus a constant offset
+#pragma unroll
         for (int step = 0; step < Kp / 8; ++step) {
           const int atom = step >> 2;
           const uint32_t kin = (uint32_t)(step & 3) * 32u;
-          const uint32_t boff = (uint32_t)(atom * Np * 128) + kin;
+          const uint64_t boff = ((uint32_t)(atom * Np * 128) + kin) >> 4;
+#pragma unroll
           for (int g = 0; g < G; ++g) {
-            const uint32_t aoff = (uint32_t)(atom * Mrows * 128 + g * 128 * 128) + kin;
+            const uint64_t aoff = ((uint32_t)(atom * Mrows * 128 + g * 128 * 128) + kin) >> 4;
             const uint32_t d = tmem + (uint32_t)(g * Np);
-            mma_tf32(d, smem_desc(ah + aoff), smem_desc(bh + boff), idesc, acc);
-            mma_tf32(d, smem_desc(al + aoff), smem_desc(bh + boff), idesc, 1);
-            mma_tf32(d, smem_desc(ah + aoff), smem_desc(bl + boff), idesc, 1);
+            mma_tf32(d, dah + aoff, dbh + boff, idesc, step > 0 ? 1u : 0u);
+            mma_tf32(d, dal + aoff, dbh + boff, idesc, 1);
+            mma_tf32(d, dah + aoff, dbl + boff, idesc, 1);
           }
-          acc = 1;
         }
         mma_commit(mma_bar);
       }
@@ -495,14 +498,17 @@ cudaError_t launch_dense_tc(void* state, int n, int ke, const int* tbits, const 
   cudaGetDevice(&dev);
   const size_t smem = dense_tc_smem_bytes();
   if (dev >= 0 && dev < 64 && !attr_set[dev]) {
-    cudaError_t e = cudaFuncSetAttribute(k_dense_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    cudaError_t e = cudaFuncSetAttribute(k_dense_tc<4>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e == cudaSuccess)
+      e = cudaFuncSetAttribute(k_dense_tc<5>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
     attr_set[dev] = true;
   }
   int sms = kSMCount;
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
   const uint64_t grid = p.ntiles < (uint64_t)sms ? p.ntiles : (uint64_t)sms;
-  k_dense_tc<<<(unsigned)grid, kThreads, smem, st>>>(p);
+  if (ke == 4) k_dense_tc<4><<<(unsigned)grid, kThreads, smem, st>>>(p);
+  else k_dense_tc<5><<<(unsigned)grid, kThreads, smem, st>>>(p);
   count_launch(1);
   return cudaGetLastError();
 }

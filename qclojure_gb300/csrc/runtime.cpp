@@ -2489,8 +2489,8 @@ static std::vector<qg_op> calibration_ops(int n, int depth) {
   return ops;
 }
 
-int qg_autotune(void* ctx, int32_t n, int32_t precision, qg_tuning* chosen, qg_tuning* tried, int32_t cap,
-                int32_t* count_out) {
+int qg_autotune(void* ctx, int32_t n, int32_t precision, const qg_circuit* calibration, qg_tuning* chosen,
+                qg_tuning* tried, int32_t cap, int32_t* count_out) {
   if (!ctx || !chosen || n < 11 || n > QG_MAX_QUBITS || (precision != QG_C128 && precision != QG_C64))
     return QG_ERR_INVALID_ARG;
   Ctx* c = (Ctx*)ctx;
@@ -2531,9 +2531,13 @@ int qg_autotune(void* ctx, int32_t n, int32_t precision, qg_tuning* chosen, qg_t
     add(13, 4, 2, 1);
     add(12, 4, 1, 2);
   }
+  if (calibration && calibration->num_qubits != n) {
+    set_ctx_error(c, "autotune: the calibration circuit has a different number of qubits");
+    return QG_ERR_INVALID_ARG;
+  }
   cudaSetDevice(c->device);
   std::vector<qg_op> ops = calibration_ops(n, 6);
-  qg_circuit circ{n, (int32_t)ops.size(), ops.data()};
+  qg_circuit circ = calibration ? *calibration : qg_circuit{n, (int32_t)ops.size(), ops.data()};
   void* sh = nullptr;
   int rc = qg_state_create(ctx, n, precision, &sh);
   if (rc != QG_OK) return rc;

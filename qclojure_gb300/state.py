@@ -48,14 +48,16 @@ class Context:
     def state(self, num_qubits: int, precision: str = "c128") -> "DeviceState":
         return DeviceState(self, num_qubits, precision)
 
-    def autotune(self, num_qubits: int, precision: str = "c128") -> dict:
-        """Time candidate pass-kernel shapes on a calibration circuit of num_qubits and keep
-        the fastest for this context (qg_autotune); returns the choice and every candidate."""
+    def autotune(self, num_qubits: int, precision: str = "c128", circuit: dict | None = None) -> dict:
+        """Time candidate pass-kernel shapes on a calibration circuit of num_qubits (the given
+        workload, or the library's own) and keep the fastest for this context (qg_autotune);
+        returns the choice and every candidate."""
         chosen = A.QgTuning()
         tried = (A.QgTuning * 16)()
         count = C.c_int32()
-        _check(self.lib.qg_autotune(self.ctx, num_qubits, PRECISIONS[precision], C.byref(chosen), tried, 16,
-                                    C.byref(count)), self.lib, self.ctx)
+        enc = encode(circuit) if circuit is not None else None
+        _check(self.lib.qg_autotune(self.ctx, num_qubits, PRECISIONS[precision], enc.ref() if enc else None,
+                                    C.byref(chosen), tried, 16, C.byref(count)), self.lib, self.ctx)
         return {"chosen": chosen.as_dict(), "candidates": [tried[i].as_dict() for i in range(count.value)]}
 
     def autotune_crossover(self, precision: str = "c64", layers: int = 100) -> dict:
