@@ -51,6 +51,9 @@ def parse():
     ap.add_argument("--seed", type=int, default=1)
     ap.add_argument("--no-autotune", action="store_true",
                     help="keep the default pass-kernel shape instead of timing the candidates first")
+    ap.add_argument("--shape", default=None,
+                    help="pass-kernel shape tile_bits,reg_bits,buffers,ctas_per_sm for the main precision "
+                         "(set directly, no autotuning; for profiling a chosen shape)")
     return ap.parse_args()
 
 
@@ -521,7 +524,11 @@ def main():
     ctx = Context(device=local, workers=1, seed=7, pass_kernels=args.pass_kernels)
     # the pass kernels' tile size and launch shape, chosen on the device before timing
     tuning = {}
-    if not args.no_autotune and args.fusion == "tiled":
+    if args.shape:
+        kb, rb, bf, ct = (int(x) for x in args.shape.split(","))
+        ctx.set_tuning(n, args.precision, kb, rb, bf, ct)
+        tuning[args.precision] = {"chosen": ctx.tuning(n, args.precision), "set": "--shape"}
+    elif not args.no_autotune and args.fusion == "tiled":
         for tp in ((args.precision, "c64") if args.precision == "c128" and not args.no_extras else (args.precision,)):
             try:
                 tuning[tp] = ctx.autotune(n, tp, circ)  # timed on the workload itself
