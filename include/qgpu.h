@@ -152,7 +152,9 @@ enum {
   QG_RES_AMPLITUDES = 1 << 5,     /* :amplitudes    {:basis-states}                 */
   QG_RES_STATE_VECTOR = 1 << 6,   /* :state-vector  true                            */
   QG_RES_DENSITY_MATRIX = 1 << 7, /* :density-matrix true (n <= 14)                 */
-  QG_RES_FIDELITY = 1 << 8        /* :fidelity      {:references}                   */
+  QG_RES_FIDELITY = 1 << 8,       /* :fidelity      {:references}                   */
+  QG_RES_ACCURACY = 1 << 9        /* no reference counterpart: distance of the result from
+                                     the exact FP64 run of the same circuit             */
 };
 
 typedef struct qg_result_spec {
@@ -274,6 +276,12 @@ int qg_result_expectations(void* ctx, uint64_t job, double* expectation, double*
 int qg_result_hamiltonian(void* ctx, uint64_t job, double* energy, double* term_values, int64_t cap);
 int qg_result_fidelities(void* ctx, uint64_t job, double* out, int64_t cap);
 int qg_result_density_matrix(void* ctx, uint64_t job, double* out_c128, int64_t cap_entries);
+/* QG_RES_ACCURACY (no counterpart in the reference): the job's final state against the
+   same circuit run again in complex128 with exact FP64 arithmetic in the reference's gate
+   order (the path that equals the reference's simulator bit for bit): out3 = largest
+   amplitude difference, 1 - fidelity, total variation distance of the outcome
+   probabilities. Costs one more run and a complex128 state of the job's size. */
+int qg_result_accuracy(void* ctx, uint64_t job, double* out3);
 int qg_last_error(void* ctx, uint64_t job, char* buf, int64_t len);
 /* Releases a job and its device state (cleanup-completed-jobs!, ideal_simulator.clj:243-264). */
 int qg_job_free(void* ctx, uint64_t job);

@@ -77,6 +77,7 @@ QG_RES_AMPLITUDES = 1 << 5
 QG_RES_STATE_VECTOR = 1 << 6
 QG_RES_DENSITY_MATRIX = 1 << 7
 QG_RES_FIDELITY = 1 << 8
+QG_RES_ACCURACY = 1 << 9
 
 
 class QgOp(C.Structure):
@@ -201,6 +202,7 @@ SIGNATURES = {
     "qg_result_hamiltonian": ([P, U64, DP, DP, I64], C.c_int),
     "qg_result_fidelities": ([P, U64, DP, I64], C.c_int),
     "qg_result_density_matrix": ([P, U64, DP, I64], C.c_int),
+    "qg_result_accuracy": ([P, C.c_uint64, DP], C.c_int),
     "qg_last_error": ([P, U64, C.c_char_p, I64], C.c_int),
     "qg_job_free": ([P, U64], C.c_int),
     "qg_cleanup_completed": ([P, I64, C.POINTER(I64)], C.c_int),

@@ -279,6 +279,8 @@ class GpuStateVectorSimulator:
             flags |= A.QG_RES_STATE_VECTOR
         if specs.get("density-matrix"):
             flags |= A.QG_RES_DENSITY_MATRIX
+        if specs.get("accuracy"):
+            flags |= A.QG_RES_ACCURACY
         if specs.get("fidelity") is not None:
             flags |= A.QG_RES_FIDELITY
             refs = [_state_vector_of(r) for r in specs["fidelity"].get("references") or []]
@@ -446,6 +448,12 @@ class GpuStateVectorSimulator:
             _check(lib.qg_result_density_matrix(ctx, J, rho.ctypes.data_as(A.DP), C.c_int64(N * N)), lib, ctx)
             res["density-matrix-result"] = {"density-matrix": rho, "num-qubits": n,
                                             "trace-valid": abs(np.trace(rho).real - 1.0) < 1e-10}
+        if info.has_results & A.QG_RES_ACCURACY:
+            acc = (C.c_double * 3)()
+            _check(lib.qg_result_accuracy(ctx, J, acc), lib, ctx)
+            res["accuracy-results"] = {"max-amplitude-error": acc[0], "one-minus-fidelity": acc[1],
+                                       "probability-tvd": acc[2],
+                                       "reference": "complex128, exact FP64 arithmetic in the reference's gate order"}
         if info.has_results & A.QG_RES_FIDELITY:
             refs = specs["fidelity"].get("references") or []
             out = np.zeros(max(1, len(refs)))

@@ -617,6 +617,7 @@ struct Job {
   double energy = 0;
   std::vector<double> fidelities;
   std::vector<double> density;
+  double accuracy[3] = {0, 0, 0};     // QG_RES_ACCURACY: max |d amp|, 1 - F, TVD
   int has = 0;
   std::unique_ptr<State> state;       // final state kept on the device
   bool state_pinned = false;          // requested by :state-vector; never evicted
@@ -917,6 +918,32 @@ static int job_results(Ctx* c, Job* j, std::unique_ptr<State> st, cudaStream_t s
       j->fidelities[k] = std::sqrt(re * re + im * im);
     }
     if (rc == QG_OK) j->has |= QG_RES_FIDELITY;
+  }
+  if (rc == QG_OK && (sp.flags & QG_RES_ACCURACY)) {
+    // the same circuit again: complex128, exact FP64 arithmetic, the reference's gate order
+    NvtxRange nvtx("qg accuracy");
+    Program exact;
+    qg_circuit circ{j->n, (int32_t)j->ops.size(), j->ops.data()};
+    rc = compile_program(&circ, QG_C128, QG_FUSE_TILED, c->cfg.fuse_k, QG_ARITH_EXACT, &exact, &err, false);
+    State ref;
+    ref.ctx = c;
+    if (rc == QG_OK) rc = state_alloc(&ref, j->n, QG_C128, stream, &err);
+    if (rc == QG_OK) {
+      cudaError_t e = launch_set_basis(ref.d, QG_C128, j->n, 0, stream);
+      if (e != cudaSuccess) rc = cuda_fail(&err, e, "accuracy reference zero-state");
+    }
+    if (rc == QG_OK && !j->initial.empty()) rc = upload_c128(&ref, j->initial.data(), &err);
+    ExecStats xs;
+    if (rc == QG_OK) rc = exec_program(&ref, exact, j->seed, nullptr, &xs, &err, 0);
+    double d3[3] = {0, 0, 0};
+    if (rc == QG_OK) rc = st_compare(st.get(), &ref, d3, &err);
+    cudaStreamSynchronize(stream);
+    state_release(&ref);
+    cudaStreamSynchronize(stream);
+    if (rc == QG_OK) {
+      std::memcpy(j->accuracy, d3, sizeof(d3));
+      j->has |= QG_RES_ACCURACY;
+    }
   }
   if (rc == QG_OK && (sp.flags & QG_RES_DENSITY_MATRIX)) {
     if (j->n > 12) {
@@ -1912,6 +1939,16 @@ int qg_result_fidelities(void* ctx, uint64_t job, double* out, int64_t cap) {
   if (!(j->has & QG_RES_FIDELITY)) return QG_ERR_NO_RESULT;
   if (cap < (int64_t)j->fidelities.size()) return QG_ERR_BUFFER_TOO_SMALL;
   if (!j->fidelities.empty()) std::memcpy(out, j->fidelities.data(), sizeof(double) * j->fidelities.size());
+  return QG_OK;
+}
+
+int qg_result_accuracy(void* ctx, uint64_t job, double* out3) {
+  if (!out3) return QG_ERR_INVALID_ARG;
+  std::shared_ptr<Job> j;
+  int rc = completed_job(ctx, job, &j);
+  if (rc != QG_OK) return rc;
+  if (!(j->has & QG_RES_ACCURACY)) return QG_ERR_NO_RESULT;
+  std::memcpy(out3, j->accuracy, sizeof(j->accuracy));
   return QG_OK;
 }
 
