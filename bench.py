@@ -822,10 +822,14 @@ def main():
                 for _ in range(reps):
                     en, sst = sw.run(hams)
                 dt = (time.perf_counter() - t0) / reps
+                pass_gbs = sst["pass-bytes"] / (sst["device-ms"] / 1e3) / 1e9
                 qaoa[prec] = {"circuits_per_s": len(qc_list) / dt, "ms_per_sweep": dt * 1e3,
                               "device_ms": sst["device-ms"], "energy_ms": sst["expect-ms"],
                               "launches": sst["launches"], "graphs": sst["graphs"],
-                              "state_gib": sst["state-bytes"] / 2**30}
+                              "state_gib": sst["state-bytes"] / 2**30,
+                              "roofline": {"bound": "hbm", "achieved": pass_gbs, "peak": peak, "unit": "GB/s",
+                                           "frac": pass_gbs / peak, "pass_bytes": sst["pass-bytes"],
+                                           "kernel": "qgl_<level> (sweep level kernels, all sizes per launch)"}}
         # plain per-circuit complex128 (one HBM pass per gate, one job at a time) on a sample
         sample = qc_list[:48]
         t0 = time.perf_counter()
@@ -843,6 +847,13 @@ def main():
 
         st.close()
         sim = create_simulator({"precision": args.precision, "fusion": args.fusion, "workers": 1, "seed": 5})
+        if tuning.get(args.precision, {}).get("chosen"):  # the same kernel shape as the device-timed run
+            ch = tuning[args.precision]["chosen"]
+            from qclojure_gb300.state import Context as _C
+            from qclojure_gb300.backend import _CtxView
+
+            _C.set_tuning(_CtxView(sim._lib, sim._ctx), n, args.precision, ch["tile_bits"], ch["reg_bits"],
+                          ch["buffers"], ch["ctas_per_sm"])
         opts = {"result-specs": {"measurements": {"shots": 1024}}}
         execute_circuit(sim, circ, opts, timeout_ms=600_000)
         t0 = time.perf_counter()

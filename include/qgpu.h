@@ -373,6 +373,9 @@ typedef struct qg_sweep_stats {
   int32_t graphs;         /* groups replayed from a CUDA graph                    */
   int32_t specialised;    /* groups whose passes run as specialised kernels       */
   uint64_t state_bytes;   /* HBM held by the sweep's states                       */
+  uint64_t pass_bytes;    /* algorithmic HBM bytes of one run's gate passes: one read
+                             and one write of every amplitude per pass, plus the write
+                             that zeroes each state                                  */
 } qg_sweep_stats;
 
 /* Compile circuits (no mid-circuit measurement), allocate their states, capture graphs. */

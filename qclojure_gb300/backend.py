@@ -142,6 +142,13 @@ class GpuStateVectorSimulator:
             self._lib.qg_ctx_destroy(self._ctx)
             self._ctx = None
 
+    def autotune(self, num_qubits: int, precision: str = "c128", circuit: dict | None = None) -> dict:
+        """Choose the pass-kernel shape for jobs of this size and precision from measured
+        device time (qg_autotune; `circuit`: the workload to time, else the library's own)."""
+        from .state import Context
+
+        return Context.autotune(_CtxView(self._lib, self._ctx), num_qubits, precision, circuit)
+
     def autotune_crossover(self, precision: str = "c64", layers: int = 100) -> dict:
         """Measure from which state size a one-off job of `layers` layers gains from compiling its
         pass kernels, and specialise jobs from there on (qg_autotune_crossover). Call it before

@@ -3349,6 +3349,15 @@ int qg_sweep_run(void* sweep, const int32_t* term_offsets, const double* coeffic
     for (auto& g : sw->groups) spec += g.pk ? 1 : 0;
     stats->specialised = spec;
     stats->state_bytes = sw->bytes;
+    uint64_t pb = 0;
+    for (auto& g : sw->groups) {
+      const uint64_t per = (uint64_t)amp_bytes(sw->prec) << g.n;
+      uint64_t passes = 0;
+      for (size_t m = 0; m < g.progs.size(); ++m)
+        passes += g.batched ? g.pass_steps.size() : (uint64_t)g.progs[m].hbm_passes;
+      pb += per * (2 * passes + g.progs.size());  // passes read and write; the zeroing writes
+    }
+    stats->pass_bytes = pb;
   }
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);

@@ -68,7 +68,8 @@ class Sweep:
     @staticmethod
     def _stats(s) -> dict:
         return {"device-ms": s.device_ms, "expect-ms": s.expect_ms, "groups": s.groups, "launches": s.launches,
-                "graphs": s.graphs, "specialised": s.specialised, "state-bytes": s.state_bytes}
+                "graphs": s.graphs, "specialised": s.specialised, "state-bytes": s.state_bytes,
+                "pass-bytes": s.pass_bytes}
 
     def state(self, c: int) -> np.ndarray:
         out = np.empty(1 << self.n[c], np.complex128)
