@@ -827,9 +827,11 @@ def main():
                               "device_ms": sst["device-ms"], "energy_ms": sst["expect-ms"],
                               "launches": sst["launches"], "graphs": sst["graphs"],
                               "state_gib": sst["state-bytes"] / 2**30,
+                              "level_graph_ms": sst["level-graph-ms"], "size_graphs_ms": sst["size-graphs-ms"],
                               "roofline": {"bound": "hbm", "achieved": pass_gbs, "peak": peak, "unit": "GB/s",
                                            "frac": pass_gbs / peak, "pass_bytes": sst["pass-bytes"],
-                                           "kernel": "qgl_<level> (sweep level kernels, all sizes per launch)"}}
+                                           "kernel": "qgl_<level> (sweep level kernels, all sizes per launch)"
+                                           if sst["graphs"] == 1 else "qgs_<pass> (table-form pass kernels per size)"}}
         # plain per-circuit complex128 (one HBM pass per gate, one job at a time) on a sample
         sample = qc_list[:48]
         t0 = time.perf_counter()

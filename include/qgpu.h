@@ -376,6 +376,10 @@ typedef struct qg_sweep_stats {
   uint64_t pass_bytes;    /* algorithmic HBM bytes of one run's gate passes: one read
                              and one write of every amplitude per pass, plus the write
                              that zeroes each state                                  */
+  double level_graph_ms;  /* measured when the sweep was created: all sizes through
+                             one launch per pass level (0: not built)                */
+  double size_graphs_ms;  /* the same passes as one graph per size; the sweep runs
+                             the faster of the two                                   */
 } qg_sweep_stats;
 
 /* Compile circuits (no mid-circuit measurement), allocate their states, capture graphs. */

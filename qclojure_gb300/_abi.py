@@ -139,7 +139,8 @@ class QgJobInfo(C.Structure):
 class QgSweepStats(C.Structure):
     _fields_ = [("device_ms", C.c_double), ("expect_ms", C.c_double), ("groups", C.c_int32),
                 ("launches", C.c_int32), ("graphs", C.c_int32), ("specialised", C.c_int32),
-                ("state_bytes", C.c_uint64), ("pass_bytes", C.c_uint64)]
+                ("state_bytes", C.c_uint64), ("pass_bytes", C.c_uint64), ("level_graph_ms", C.c_double),
+                ("size_graphs_ms", C.c_double)]
 
 
 class QgTuning(C.Structure):

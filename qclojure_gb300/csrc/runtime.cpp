@@ -2767,6 +2767,7 @@ struct Sweep {
   GroupLevelDesc* d_levels = nullptr;      // descriptors of every level, level after level
   cudaGraphExec_t lk_exec = nullptr;
   int lk_launches = 0;
+  float level_ms = 0, group_ms = 0;        // measured at creation: level graph, per-size graphs
   std::vector<std::pair<int, int>> where;  // circuit -> (group, member)
   uint64_t bytes = 0;
   // the term arrays the energy tables were built from
@@ -2950,12 +2951,48 @@ static void setup_level_kernels(Sweep* sw) {
   cudaError_t ce = cudaStreamEndCapture(sw->stream, &graph);
   count_launch(-(1 + L));  // captured launches do not run here; replays count them
   if (le == cudaSuccess && ce == cudaSuccess && graph && cudaGraphInstantiate(&exec, graph, 0) == cudaSuccess) {
-    sw->lk = lk;
-    sw->lk_exec = exec;
-    sw->lk_launches = 1 + L;
-    sw->lk_groups = cand;
-    for (int gi : cand) sw->in_level[gi] = 1;
+    // keep whichever form runs these groups faster: time both (second replay of each)
+    auto time_ms = [&](auto&& run) {
+      cudaEvent_t a, b;
+      cudaEventCreate(&a);
+      cudaEventCreate(&b);
+      float best = -1.0f;
+      for (int rep = 0; rep < 2; ++rep) {
+        cudaEventRecord(a, sw->stream);
+        const cudaError_t re = run();
+        cudaEventRecord(b, sw->stream);
+        if (re != cudaSuccess || cudaEventSynchronize(b) != cudaSuccess) {
+          best = -1.0f;
+          break;
+        }
+        cudaEventElapsedTime(&best, a, b);
+      }
+      cudaEventDestroy(a);
+      cudaEventDestroy(b);
+      return best;
+    };
+    const float t_level = time_ms([&]() { return cudaGraphLaunch(exec, sw->stream); });
+    const float t_groups = time_ms([&]() {
+      cudaError_t e = cudaSuccess;
+      for (int gi : cand) {
+        SweepGroup& g = sw->groups[gi];
+        e = g.exec ? cudaGraphLaunch(g.exec, sw->stream) : launch_group_passes(sw, g);
+        if (e != cudaSuccess) break;
+      }
+      return e;
+    });
+    sw->level_ms = t_level;
+    sw->group_ms = t_groups;
+    if (t_level > 0 && (t_groups <= 0 || t_level <= t_groups)) {
+      sw->lk = lk;
+      sw->lk_exec = exec;
+      sw->lk_launches = 1 + L;
+      sw->lk_groups = cand;
+      for (int gi : cand) sw->in_level[gi] = 1;
+      exec = nullptr;
+    }
   }
+  if (exec) cudaGraphExecDestroy(exec);
   if (graph) cudaGraphDestroy(graph);
   cudaGetLastError();
 }
@@ -3358,6 +3395,8 @@ int qg_sweep_run(void* sweep, const int32_t* term_offsets, const double* coeffic
       pb += per * (2 * passes + g.progs.size());  // passes read and write; the zeroing writes
     }
     stats->pass_bytes = pb;
+    stats->level_graph_ms = sw->level_ms;
+    stats->size_graphs_ms = sw->group_ms;
   }
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);

@@ -69,7 +69,8 @@ class Sweep:
     def _stats(s) -> dict:
         return {"device-ms": s.device_ms, "expect-ms": s.expect_ms, "groups": s.groups, "launches": s.launches,
                 "graphs": s.graphs, "specialised": s.specialised, "state-bytes": s.state_bytes,
-                "pass-bytes": s.pass_bytes}
+                "pass-bytes": s.pass_bytes, "level-graph-ms": s.level_graph_ms,
+                "size-graphs-ms": s.size_graphs_ms}
 
     def state(self, c: int) -> np.ndarray:
         out = np.empty(1 << self.n[c], np.complex128)

@@ -34,9 +34,11 @@ def test_qaoa_sweep_energies(gpu_ctx, oracle, precision, arith, tol):
         distinct = len({c["num-qubits"] for c in circs})
         assert st["groups"] == distinct
         if precision == "c64" or arith == "double-float":
-            # table-form kernels: every size runs in one graph, one launch per pass level
-            # (plus one that zeroes all states), not one graph per size
-            assert st["graphs"] == 1, st
+            # table-form kernels: every size in one graph, one launch per pass level (plus one
+            # that zeroes all states), or one graph per size, whichever measured faster
+            assert st["level-graph-ms"] > 0 and st["size-graphs-ms"] > 0, st
+            faster_level = st["level-graph-ms"] <= st["size-graphs-ms"]
+            assert st["graphs"] == (1 if faster_level else distinct), st
         else:
             assert st["graphs"] == distinct
         for c, e in zip(circs, en):
