@@ -493,7 +493,7 @@ int qg_pass_kernels_info(int32_t* available, uint64_t* cache_hits, uint64_t* cac
    qg_tuning_pick is the choice rule on its own: the index of the fastest valid entry,
    or default_index when that one is within tie_frac of it (-1: none valid). */
 typedef struct qg_tuning {
-  int32_t tile_bits;    /* local qubits per tile: 11, 12 or 13 */
+  int32_t tile_bits;    /* local qubits per tile: 10 to 13 */
   int32_t reg_bits;     /* amplitudes per thread = 2^reg_bits (3 or 4) */
   int32_t buffers;      /* tile buffers in shared memory (1 or 2) */
   int32_t ctas_per_sm;  /* CTAs per SM the kernels are built for */

@@ -1115,8 +1115,8 @@ bool generate_units(const Program& prog, int prec, std::vector<Unit>* units, std
   for (size_t i = 0; i < prog.steps.size(); ++i) {
     const Step& st = prog.steps[i];
     const Shape sh = shape_of(prog, prec);
-    // a full tile of at least 2^11 amplitudes, a warp or more of threads
-    if (st.kind != Step::TILE_PASS || st.pass.k < 11 || st.pass.k - sh.rbits < 5) continue;
+    // a tile of at least 2^10 amplitudes, a warp or more of threads
+    if (st.kind != Step::TILE_PASS || st.pass.k < 10 || st.pass.k - sh.rbits < 5) continue;
     const TOp* ops = prog.tops.data() + st.pass.op_begin;
     const int nops = (int)(st.pass.op_end - st.pass.op_begin);
     std::ostringstream o;
@@ -1355,7 +1355,7 @@ std::shared_ptr<const PassKernels> level_kernels_for(const std::vector<const Pro
     }
     levels = std::max(levels, pass_steps[g].size());
   }
-  if (K < 11 || K - sh.rbits < 5 || levels == 0) {
+  if (K < 10 || K - sh.rbits < 5 || levels == 0) {
     *why = "no pass to specialise";
     return nullptr;
   }

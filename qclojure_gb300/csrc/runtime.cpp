@@ -2442,7 +2442,7 @@ int32_t qg_tuning_pick(const double* ms, const int32_t* valid, int32_t count, in
 
 static bool tuning_valid(const qg_tuning& t, int n, int prec) {
   const int E = prec == QG_C128 ? 16 : 8;
-  if (t.tile_bits < 11 || t.tile_bits > kMaxTileBits || t.tile_bits > n) return false;
+  if (t.tile_bits < 10 || t.tile_bits > kMaxTileBits || t.tile_bits > n) return false;
   if (t.reg_bits < 3 || t.reg_bits > 4 || t.tile_bits - t.reg_bits < 5 || t.tile_bits - t.reg_bits > 10) return false;
   if (t.buffers < 1 || t.buffers > 2 || t.ctas_per_sm < 1 || t.ctas_per_sm > 8) return false;
   const long smem = (long)t.buffers * (1L << t.tile_bits) * E;
@@ -2562,11 +2562,13 @@ int qg_autotune(void* ctx, int32_t n, int32_t precision, const qg_circuit* calib
     add(11, 3, 2, 2);
     add(12, 3, 1, 1);
     add(11, 3, 1, 2);
+    add(10, 3, 2, 4);
   } else {
     add(12, 4, 2, 2);
     add(11, 4, 2, 4);
     add(13, 4, 2, 1);
     add(12, 4, 1, 2);
+    add(10, 4, 2, 8);
   }
   if (calibration && calibration->num_qubits != n) {
     set_ctx_error(c, "autotune: the calibration circuit has a different number of qubits");
