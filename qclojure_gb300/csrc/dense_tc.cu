@@ -9,8 +9,8 @@
 //   * A tile is 4096 amplitudes: every combination of the block's k target bits and
 //     the lowest 12 - k other bits. Its HBM footprint is a few contiguous runs of at
 //     least 1 KiB (all bits below the highest column bit belong to the tile), moved by
-//     the bulk-copy engine (cp.async.bulk, mbarrier completion) into a staging buffer,
-//     three tiles deep, and written back from it the same way.
+//     the bulk-copy engine (cp.async.bulk, mbarrier completion) into one of two staging
+//     buffers, and written back from registers by the epilogue warps.
 //   * The block is a real GEMM. Column c of the tile (the non-target bits, 128 per
 //     MMA) is a row of the A operand holding its 2^k amplitudes as 2^(k+1) reals
 //     (re, im interleaved); the B operand is the real form of the block,
@@ -39,7 +39,6 @@ namespace {
 constexpr int kTileBits = 12;           // 4096 amplitudes (32 KiB of complex64) per tile
 constexpr int kTileAmps = 1 << kTileBits;
 constexpr int kThreads = 256;
-constexpr int kStages = 3;              // staging buffers (bulk loads in flight)
 constexpr int kStageBytes = kTileAmps * 8;
 constexpr int kAHalfBytes = 32768;      // one of A hi / A lo: 128 x 64 TF32 (k = 5) or 256 x 32 (k = 4)
 constexpr int kBHalfBytes = 16384;      // one of B hi / B lo at k = 5 (64 x 64 TF32)
@@ -76,39 +75,23 @@ __device__ __forceinline__ uint64_t global_ns() {
   asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
   return t;
 }
-// Wait for the phase of `parity` to complete; false after about a second.
-__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
-  const uint32_t a = smem_u32(bar);
-  uint64_t t0 = 0;
-  for (uint32_t it = 0;; ++it) {
-    uint32_t done;
-    asm volatile(
-        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
-        : "=r"(done)
-        : "r"(a), "r"(parity)
-        : "memory");
-    if (done) return true;
-    if ((it & 1023u) == 0) {
-      const uint64_t now = global_ns();
-      if (t0 == 0) t0 = now;
-      else if (now - t0 > 1000000000ull) return false;
-    }
-  }
-}
 __device__ __forceinline__ void bulk_g2s(void* dst, const void* src, uint32_t bytes, uint64_t* bar) {
   asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
                    smem_u32(dst)),
                "l"(src), "r"(bytes), "r"(smem_u32(bar))
                : "memory");
 }
-__device__ __forceinline__ void bulk_s2g(void* dst, const void* src, uint32_t bytes) {
-  asm volatile("cp.async.bulk.global.shared::cta.bulk_group [%0], [%1], %2;" ::"l"(dst), "r"(smem_u32(src)),
-               "r"(bytes)
-               : "memory");
+// Named barrier `id` over `count` threads that also ANDs a flag across them: every
+// thread gets the same answer, so a group leaves a loop together.
+__device__ __forceinline__ bool bar_and(int id, int count, bool v) {
+  uint32_t r;
+  asm volatile(
+      "{\n .reg .pred p, q;\n setp.ne.u32 q, %2, 0;\n bar.red.and.pred p, %1, %3, q;\n selp.u32 %0, 1, 0, p;\n}\n"
+      : "=r"(r)
+      : "r"(id), "r"((uint32_t)v), "r"(count)
+      : "memory");
+  return r != 0;
 }
-__device__ __forceinline__ void bulk_commit() { asm volatile("cp.async.bulk.commit_group;" ::: "memory"); }
-__device__ __forceinline__ void bulk_wait_read_all() { asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory"); }
-__device__ __forceinline__ void bulk_wait_all() { asm volatile("cp.async.bulk.wait_group 0;" ::: "memory"); }
 __device__ __forceinline__ void fence_proxy_async() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
 __device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
 __device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
@@ -176,57 +159,70 @@ __device__ __forceinline__ uint64_t tile_base(const DenseTcParams& p, uint64_t t
   return b;
 }
 
+// The tile's work is a pipeline over two groups of four warps, so the phases of
+// consecutive tiles overlap:
+//   transform warps (0-3): wait for tile r's bulk load, split it into A hi / A lo of
+//     buffer r % 2 (once the MMAs of tile r - 2 have read that buffer), then warp 0
+//     issues tile r's MMAs into tensor-memory buffer r % 2 (once the epilogue of tile
+//     r - 2 has read it) and the bulk load of tile r + 2 into the staging buffer tile r
+//     has just left;
+//   epilogue warps (4-7): wait for tile r's MMAs, read its accumulators and store the
+//     amplitudes straight to HBM (lane c holds column c: consecutive lanes write
+//     consecutive amplitudes when the low index bits are column bits), then release
+//     the tensor-memory buffer.
+// Waits are on mbarriers, each bounded; a group that gives up raises a shared abort
+// flag, which ends the other group's waits at once.
 template <int KB>
 __global__ void __launch_bounds__(kThreads, 1) k_dense_tc(const __grid_constant__ DenseTcParams p) {
   extern __shared__ __align__(1024) unsigned char smem_raw[];
-  // 1024-aligned regions: A hi, A lo (also the epilogue's transposition buffer), B hi, B lo, staging
-  unsigned char* base = (unsigned char*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
-  unsigned char* a_hi = base;
-  unsigned char* a_lo = a_hi + kAHalfBytes;
-  unsigned char* b_hi = a_lo + kAHalfBytes;
-  unsigned char* b_lo = b_hi + kBHalfBytes;
-  unsigned char* stage = b_lo + kBHalfBytes;
-  uint64_t* full = reinterpret_cast<uint64_t*>(stage + kStages * kStageBytes);
-  uint64_t* mma_bar = full + kStages;
-  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(mma_bar + 1);
-
-  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   constexpr int D = 1 << KB;               // target combinations
   constexpr int Kp = 2 * D;                // reals per column (K of the GEMM)
   constexpr int Np = Kp;                   // reals per output column (N of the GEMM)
   constexpr int G = (KB == 4) ? 2 : 1;     // 128-column MMA blocks per tile
   constexpr int Mrows = 128 * G;           // columns of a tile
   constexpr uint32_t idesc = idesc_tf32(Np);
+  constexpr int kGroup = kThreads / 2;     // threads per group
+  constexpr int PER = kTileAmps / kGroup;  // tile positions per transform thread
+  // 1024-aligned regions: A hi / A lo of buffers 0 and 1, B hi, B lo, two staging buffers
+  unsigned char* base = (unsigned char*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
+  unsigned char* a_buf = base;                              // buffer b: hi at 2b, lo at 2b + 1 halves
+  unsigned char* b_hi = a_buf + 4 * kAHalfBytes;
+  unsigned char* b_lo = b_hi + kBHalfBytes;
+  unsigned char* stage = b_lo + kBHalfBytes;
+  uint64_t* full = reinterpret_cast<uint64_t*>(stage + 2 * kStageBytes);  // [2]
+  uint64_t* mma_done = full + 2;                                           // [2]
+  uint64_t* tmem_free = mma_done + 2;                                      // [2]
+  uint64_t* r_off = tmem_free + 2;                                         // [32]
+  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(r_off + 32);
+  volatile int* abort_flag = reinterpret_cast<volatile int*>(tmem_slot + 1);
 
-  // this thread's 16 tile positions (i = tid + q * kThreads) map to the same places in
-  // every tile: A operand byte offsets and epilogue buffer indices, computed once
-  constexpr int PER = kTileAmps / kThreads;
-  uint32_t a_off[PER], o_off[PER];
-#pragma unroll
-  for (int q = 0; q < PER; ++q) {
-    const int i = tid + q * kThreads;
-    int j = 0, c = 0;
-    for (int t = 0; t < kTileBits; ++t) {
-      const int bit = (i >> t) & 1;
-      if (p.tgt_of[t] >= 0) j |= bit << p.tgt_of[t];
-      else c |= bit << p.col_of[t];
-    }
-    a_off[q] = kmajor_off(Mrows, c, 2 * j);
-    o_off[q] = (uint32_t)(c * (Np + 1) + 2 * j);
-  }
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const bool transform = tid < kGroup;
+  const int gtid = transform ? tid : tid - kGroup;
+
   // the block's real form, hi and lo, already laid out by the host
   for (int i = tid * 4; i < p.bbytes / 4; i += kThreads * 4) {
     *reinterpret_cast<float4*>(b_hi + 4 * i) = *reinterpret_cast<const float4*>(p.w + i);
     *reinterpret_cast<float4*>(b_lo + 4 * i) = *reinterpret_cast<const float4*>(p.w + p.bbytes / 4 + i);
   }
+  if (tid < D) {  // amplitude offset of target combination r inside a tile
+    uint64_t o = 0;
+    for (int t = 0; t < kTileBits; ++t)
+      if (p.tgt_of[t] >= 0 && ((tid >> p.tgt_of[t]) & 1)) o |= 1ull << p.tbit[t];
+    r_off[tid] = o;
+  }
   if (tid == 0) {
-    for (int s = 0; s < kStages; ++s) mbar_init(&full[s], 1);
-    mbar_init(mma_bar, 1);
+    for (int q = 0; q < 2; ++q) {
+      mbar_init(&full[q], 1);
+      mbar_init(&mma_done[q], 1);
+      mbar_init(&tmem_free[q], 1);
+    }
+    *abort_flag = 0;
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
   if (warp == 0) {
     asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tmem_slot)),
-                 "r"(kTmemCols)
+                 "r"(2 * kTmemCols)
                  : "memory");
     asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
   }
@@ -235,134 +231,183 @@ __global__ void __launch_bounds__(kThreads, 1) k_dense_tc(const __grid_constant_
   __syncthreads();
   tc_fence_after();
   const uint32_t tmem = *tmem_slot;
-  const uint64_t dah = smem_desc(smem_u32(a_hi)), dal = smem_desc(smem_u32(a_lo));
-  const uint64_t dbh = smem_desc(smem_u32(b_hi)), dbl = smem_desc(smem_u32(b_lo));
 
   const uint64_t t_begin = p.ntiles * blockIdx.x / gridDim.x, t_end = p.ntiles * (blockIdx.x + 1) / gridDim.x;
   const uint64_t count = t_end - t_begin;
-  const int nrun = 1 << (kTileBits - p.runbits);  // at most 32: runs are at least 2^7 amplitudes
-  const uint32_t run_bytes = (uint32_t)(8u << p.runbits);
-  // warp 0, lane q < nrun: the amplitude offset of run q inside a tile (the same for every tile)
-  uint64_t run_off = 0;
-  if (warp == 0 && lane < nrun)
-    for (int b = p.runbits; b < kTileBits; ++b)
-      if ((lane >> (b - p.runbits)) & 1) run_off |= 1ull << p.tbit[b];
-
-  // warp 0: bulk-load this CTA's tile number r into buffer r % kStages, one run per lane
-  auto issue_load = [&](uint64_t r) {
-    const int s = (int)(r % kStages);
-    if (lane == 0) mbar_expect_tx(&full[s], (uint32_t)kStageBytes);
-    __syncwarp();
-    const uint64_t tb = tile_base(p, t_begin + r);
-    if (lane < nrun) bulk_g2s(stage + s * kStageBytes + (size_t)lane * run_bytes, p.state + tb + run_off, run_bytes,
-                              &full[s]);
-  };
-  uint64_t issued = 0;  // loads issued (warp 0's count)
-  if (warp == 0) {
-    for (; issued < 2 && issued < count; ++issued) issue_load(issued);
-  }
-
-  bool failed = false;
-  uint64_t r = 0;
-  for (; r < count; ++r) {
-    const int s = (int)(r % kStages);
-    bool ok = mbar_wait(&full[s], (uint32_t)(r / kStages) & 1u);
-    if (__syncthreads_or(!ok)) {
-      failed = true;
-      break;
-    }
-    // staging (address order) -> A hi / A lo (column rows, K-major, swizzled)
-    {
-      const float2* st = reinterpret_cast<const float2*>(stage + s * kStageBytes);
-#pragma unroll
-      for (int q = 0; q < PER; ++q) {
-        const float2 x = st[tid + q * kThreads];
-        const float hr = to_tf32(x.x), hi_ = to_tf32(x.y);
-        const float lr = to_tf32(x.x - hr), li = to_tf32(x.y - hi_);
-        *reinterpret_cast<float2*>(a_hi + a_off[q]) = make_float2(hr, hi_);
-        *reinterpret_cast<float2*>(a_lo + a_off[q]) = make_float2(lr, li);
+  // a bounded wait that also ends when the other group gave up
+  auto wait = [&](uint64_t* bar, uint32_t parity) {
+    const uint32_t a = smem_u32(bar);
+    uint64_t t0 = 0;
+    for (uint32_t it = 0;; ++it) {
+      uint32_t done;
+      asm volatile(
+          "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+          : "=r"(done)
+          : "r"(a), "r"(parity)
+          : "memory");
+      if (done) return true;
+      if ((it & 255u) == 0) {
+        if (*abort_flag) return false;
+        const uint64_t now = global_ns();
+        if (t0 == 0) t0 = now;
+        else if (now - t0 > 1000000000ull) {
+          *abort_flag = 1;
+          return false;
+        }
       }
     }
-    fence_proxy_async();
-    tc_fence_before();
-    __syncthreads();
-    if (warp == 0) {
-      if (lane == 0) {
-        tc_fence_after();
-        // descriptors differ only in their start address field (address / 16), so each
-        // MMA's descriptor is a base descriptor plus a constant offset
+  };
+
+  if (transform) {
+    // this thread's tile positions i = gtid + q * kGroup map to the same A offsets in every tile
+    uint32_t a_off[PER];
 #pragma unroll
-        for (int step = 0; step < Kp / 8; ++step) {
-          const int atom = step >> 2;
-          const uint32_t kin = (uint32_t)(step & 3) * 32u;
-          const uint64_t boff = ((uint32_t)(atom * Np * 128) + kin) >> 4;
+    for (int q = 0; q < PER; ++q) {
+      const int i = gtid + q * kGroup;
+      int j = 0, c = 0;
+      for (int t = 0; t < kTileBits; ++t) {
+        const int bit = (i >> t) & 1;
+        if (p.tgt_of[t] >= 0) j |= bit << p.tgt_of[t];
+        else c |= bit << p.col_of[t];
+      }
+      a_off[q] = kmajor_off(Mrows, c, 2 * j);
+    }
+    const int nrun = 1 << (kTileBits - p.runbits);  // at most 32: runs are at least 2^7 amplitudes
+    const uint32_t run_bytes = (uint32_t)(8u << p.runbits);
+    uint64_t run_off = 0;
+    if (warp == 0 && lane < nrun)
+      for (int b = p.runbits; b < kTileBits; ++b)
+        if ((lane >> (b - p.runbits)) & 1) run_off |= 1ull << p.tbit[b];
+    auto issue_load = [&](uint64_t r) {  // warp 0: tile r into staging buffer r % 2
+      const int s = (int)(r & 1);
+      if (lane == 0) mbar_expect_tx(&full[s], (uint32_t)kStageBytes);
+      __syncwarp();
+      const uint64_t tb = tile_base(p, t_begin + r);
+      if (lane < nrun)
+        bulk_g2s(stage + s * kStageBytes + (size_t)lane * run_bytes, p.state + tb + run_off, run_bytes, &full[s]);
+    };
+    uint64_t issued = 0, mmas = 0;
+    if (warp == 0)
+      for (; issued < 2 && issued < count; ++issued) issue_load(issued);
+    uint64_t r = 0;
+    for (; r < count; ++r) {
+      const int s = (int)(r & 1), b = (int)(r & 1);
+      bool ok = wait(&full[s], (uint32_t)(r >> 1) & 1u);
+      if (ok && r >= 2) ok = wait(&mma_done[b], (uint32_t)((r - 2) >> 1) & 1u);  // A buffer b is read
+      unsigned char* a_hi = a_buf + (2 * b) * kAHalfBytes;
+      unsigned char* a_lo = a_hi + kAHalfBytes;
+      if (ok) {
+        const float2* st = reinterpret_cast<const float2*>(stage + s * kStageBytes);
 #pragma unroll
-          for (int g = 0; g < G; ++g) {
-            const uint64_t aoff = ((uint32_t)(atom * Mrows * 128 + g * 128 * 128) + kin) >> 4;
-            const uint32_t d = tmem + (uint32_t)(g * Np);
-            mma_tf32(d, dah + aoff, dbh + boff, idesc, step > 0 ? 1u : 0u);
-            mma_tf32(d, dal + aoff, dbh + boff, idesc, 1);
-            mma_tf32(d, dah + aoff, dbl + boff, idesc, 1);
+        for (int q = 0; q < PER; ++q) {
+          const float2 x = st[gtid + q * kGroup];
+          const float hr = to_tf32(x.x), hi_ = to_tf32(x.y);
+          const float lr = to_tf32(x.x - hr), li = to_tf32(x.y - hi_);
+          *reinterpret_cast<float2*>(a_hi + a_off[q]) = make_float2(hr, hi_);
+          *reinterpret_cast<float2*>(a_lo + a_off[q]) = make_float2(lr, li);
+        }
+        fence_proxy_async();
+      }
+      // the whole group goes on only if every thread got here and nothing gave up
+      if (!bar_and(1, kGroup, ok && !*abort_flag)) {
+        *abort_flag = 1;
+        break;
+      }
+      if (warp == 0) {
+        if (lane == 0) {
+          const bool tok = r < 2 || wait(&tmem_free[b], (uint32_t)((r - 2) >> 1) & 1u);  // tensor memory b is read
+          if (tok) {
+            tc_fence_after();
+            const uint64_t dah = smem_desc(smem_u32(a_hi)), dal = smem_desc(smem_u32(a_lo));
+            const uint64_t dbh = smem_desc(smem_u32(b_hi)), dbl = smem_desc(smem_u32(b_lo));
+#pragma unroll
+            for (int step = 0; step < Kp / 8; ++step) {
+              const int atom = step >> 2;
+              const uint32_t kin = (uint32_t)(step & 3) * 32u;
+              const uint64_t boff = ((uint32_t)(atom * Np * 128) + kin) >> 4;
+#pragma unroll
+              for (int g = 0; g < G; ++g) {
+                const uint64_t aoff = ((uint32_t)(atom * Mrows * 128 + g * 128 * 128) + kin) >> 4;
+                const uint32_t d = tmem + (uint32_t)(b * kTmemCols + g * Np);
+                mma_tf32(d, dah + aoff, dbh + boff, idesc, step > 0 ? 1u : 0u);
+                mma_tf32(d, dal + aoff, dbh + boff, idesc, 1);
+                mma_tf32(d, dah + aoff, dbl + boff, idesc, 1);
+              }
+            }
+            mma_commit(&mma_done[b]);
+            ++mmas;
           }
         }
-        mma_commit(mma_bar);
+        __syncwarp();
+        // staging buffer s has been read by every transform thread (the barrier above)
+        if (issued < count && issued == r + 2 && !*abort_flag) issue_load(issued++);
+        __syncwarp();
       }
-      // the buffer of tile r - 1 is free once its stores have read it: load tile r + 2 there
-      bulk_wait_read_all();
-      __syncwarp();
-      if (issued < count && issued == r + 2) issue_load(issued++);
     }
-    ok = mbar_wait(mma_bar, (uint32_t)r & 1u);
-    if (__syncthreads_or(!ok)) {
-      failed = true;
-      break;
+    if (warp == 0 && lane == 0 && *abort_flag) {
+      // nothing of this CTA may still be in flight when it leaves: its loads, its last MMAs
+      const uint64_t t0 = global_ns();
+      auto drain = [&](uint64_t* bar, uint32_t parity) {
+        uint32_t done = 0;
+        while (!done && global_ns() - t0 < 2000000000ull)
+          asm volatile(
+              "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+              " selp.u32 %0, 1, 0, p;\n}\n"
+              : "=r"(done)
+              : "r"(smem_u32(bar)), "r"(parity)
+              : "memory");
+      };
+      for (uint64_t q = r; q < issued; ++q) drain(&full[q & 1], (uint32_t)(q >> 1) & 1u);
+      if (mmas) drain(&mma_done[(mmas - 1) & 1], (uint32_t)((mmas - 1) >> 1) & 1u);
+      atomicExch(p.err, 1);
     }
-    tc_fence_after();
-    // accumulators -> out[c][n'] (pitch Np + 1 floats), in the A region
-    {
-      float v[32];
-      const int quarter = warp & 3, half = warp >> 2;
-      tmem_ld32(tmem + ((uint32_t)(32 * quarter) << 16) + (uint32_t)(half * 32), v);
-      float* out = reinterpret_cast<float*>(a_hi);
-      const int row = 32 * quarter + lane;
-      const int c = (G == 2 ? half * 128 : 0) + row;
-      const int n0 = (G == 2) ? 0 : half * 32;
+  } else {
+    // epilogue: lane row = 32 * (warp - 4) + lane of each 128-column block
+    const int row = 32 * (warp - 4) + lane;
+    uint64_t c_off[2] = {0, 0};
 #pragma unroll
-      for (int q = 0; q < 32; ++q) out[c * (Np + 1) + n0 + q] = v[q];
+    for (int h = 0; h < 2; ++h) {
+      const int c = (G == 2 ? h * 128 : 0) + row;
+      for (int t = 0; t < kTileBits; ++t)
+        if (p.col_of[t] >= 0 && ((c >> p.col_of[t]) & 1)) c_off[h] |= 1ull << p.tbit[t];
     }
-    tc_fence_before();
-    __syncthreads();
-    {
-      const float* out = reinterpret_cast<const float*>(a_hi);
-      float2* so = reinterpret_cast<float2*>(stage + s * kStageBytes);
+    for (uint64_t r = 0; r < count; ++r) {
+      const int b = (int)(r & 1);
+      const bool ok = wait(&mma_done[b], (uint32_t)(r >> 1) & 1u);
+      if (ok) {
+        tc_fence_after();
+        const uint64_t tb = tile_base(p, t_begin + r);
 #pragma unroll
-      for (int q = 0; q < PER; ++q) so[tid + q * kThreads] = make_float2(out[o_off[q]], out[o_off[q] + 1]);
-    }
-    fence_proxy_async();
-    __syncthreads();
-    if (warp == 0) {
-      const uint64_t tb = tile_base(p, t_begin + r);
-      if (lane < nrun) bulk_s2g(p.state + tb + run_off, stage + s * kStageBytes + (size_t)lane * run_bytes, run_bytes);
-      bulk_commit();
+        for (int h = 0; h < 2; ++h) {
+          float v[32];
+          // columns [32h, 32h + 32) of this buffer: block h (k = 4) or outputs 16h..16h+15 (k = 5)
+          tmem_ld32(tmem + ((uint32_t)(32 * (warp - 4)) << 16) + (uint32_t)(b * kTmemCols + 32 * h), v);
+          float2* dst = p.state + tb + (G == 2 ? c_off[h] : c_off[0]);
+          const int r0 = (G == 2) ? 0 : 16 * h;
+#pragma unroll
+          for (int q = 0; q < 16; ++q) dst[r_off[r0 + q]] = make_float2(v[2 * q], v[2 * q + 1]);
+        }
+        tc_fence_before();
+      }
+      if (!bar_and(2, kGroup, ok && !*abort_flag)) {
+        *abort_flag = 1;
+        break;
+      }
+      if (gtid == 0)
+        asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(&tmem_free[b])) : "memory");
     }
   }
-  if (failed && tid == 0) {
-    // let the loads still in flight land (bounded) before the shared memory goes away
-    for (uint64_t q = r; q < issued; ++q) mbar_wait(&full[q % kStages], (uint32_t)(q / kStages) & 1u);
-  }
-  if (failed && tid == 0) atomicExch(p.err, 1);
-  if (warp == 0) bulk_wait_all();
-  if (tid == 0) bulk_wait_all();
   tc_fence_before();
   __syncthreads();
   if (warp == 0) {
     tc_fence_after();
-    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(kTmemCols) : "memory");
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(2 * kTmemCols)
+                 : "memory");
   }
 }
 
 size_t dense_tc_smem_bytes() {
-  return 1024 + 2 * kAHalfBytes + 2 * kBHalfBytes + kStages * kStageBytes + (kStages + 1) * 8 + 8;
+  return 1024 + 4 * kAHalfBytes + 2 * kBHalfBytes + 2 * kStageBytes + 6 * 8 + 32 * 8 + 8 + 8;
 }
 
 }  // namespace
