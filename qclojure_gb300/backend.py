@@ -221,7 +221,7 @@ class GpuStateVectorSimulator:
         meta: dict[str, Any] = {"specs": specs, "circuit": circuit}
         unsupported = [k for k in specs if k not in (
             "measurements", "expectation", "variance", "hamiltonian", "probabilities", "amplitudes",
-            "state-vector", "density-matrix", "fidelity")]
+            "state-vector", "density-matrix", "fidelity", "accuracy")]
         if unsupported:
             raise CircuitError(f"result types not supported by this backend: {unsupported}")
         if specs.get("measurements"):
