@@ -1388,10 +1388,9 @@ std::shared_ptr<const PassKernels> level_kernels_for(const std::vector<const Pro
       lk->smem[l] = std::max(lk->smem[l], sh.bufs * (1 << K) * E + 16 * 4 * nops);
     }
     o << "extern \"C\" __global__ void __launch_bounds__(" << ((1 << K) >> sh.rbits) << ", " << sh.ctas << ") qgl_"
-      << l << "(const qgp::GroupLevel* __restrict__ gl, unsigned long long total) {\n"
-      << "  const qgp::u64 w0 = total * blockIdx.x / gridDim.x, w1 = total * (blockIdx.x + 1) / gridDim.x;\n";
+      << l << "(const qgp::GroupLevel* __restrict__ gl, unsigned long long total) {\n  (void)total;\n";
     for (size_t q = 0; q < names.size(); ++q)
-      o << "  qgp::run_group_share<" << names[q] << "::P>(gl[" << q << "], w0, w1);\n";
+      o << "  qgp::run_group_share<" << names[q] << "::P>(gl[" << q << "]);\n";
     o << "}\n\n";
     pieces.emplace_back((int)l, o.str());
   }

@@ -484,9 +484,10 @@ __device__ __forceinline__ void run_pass_batch(unsigned char* const* __restrict_
 }
 
 // Sweeps of several sizes: one launch per pass level runs the pass of that level of
-// every group (qubit count) that has one. The items of the groups are laid end to end
-// (group g owns [item0, item0 + items)); each CTA takes an equal share of all of them
-// and runs, group by group, the part of its share that falls in each group's range.
+// every group (qubit count) that has one. Each CTA takes an equal share of every
+// group's (state, tile) items, group after group, as if each group had its own launch
+// of the same grid: a group of many small states spreads its state switches (each one
+// stages that state's coefficients and cannot prefetch across states) over all CTAs.
 struct GroupLevel {
   unsigned char* const* states;
   const float* coefs;  // this pass's rows: ncoef floats per state
@@ -494,9 +495,9 @@ struct GroupLevel {
   u64 ntiles, item0, items;
 };
 template <class P>
-__device__ __forceinline__ void run_group_share(const GroupLevel& d, u64 w0, u64 w1) {
-  const u64 a = w0 > d.item0 ? w0 : d.item0, b = w1 < d.item0 + d.items ? w1 : d.item0 + d.items;
-  if (a < b) run_pass_range<P>(d.states, d.coefs, d.ncoef, d.ntiles, a - d.item0, b - d.item0);
+__device__ __forceinline__ void run_group_share(const GroupLevel& d) {
+  const u64 a = d.items * blockIdx.x / gridDim.x, b = d.items * (blockIdx.x + 1) / gridDim.x;
+  if (a < b) run_pass_range<P>(d.states, d.coefs, d.ncoef, d.ntiles, a, b);
 }
 
 }  // namespace qgp
