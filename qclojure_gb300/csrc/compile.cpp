@@ -756,6 +756,17 @@ int schedule(int n, int precision, int fusion, int fuse_k, const std::vector<GOp
         d.flags = kDenseTcFlag;
         d.doff = (int64_t)prog->dense_tc.size();
         prog->dense_tc.insert(prog->dense_tc.end(), w.begin(), w.end());
+      } else if (precision == QG_C128 && prog->arith == QG_ARITH_DOUBLE_FLOAT) {
+        // double-float blocks: each entry as (re.hi, re.lo, im.hi, im.lo) floats, 16 bytes
+        // like an FP64 entry, so the entry offsets stay the same
+        const size_t at = prog->dense.size();
+        prog->dense.resize(at + mat.size());
+        float* q = reinterpret_cast<float*>(prog->dense.data() + at);
+        for (size_t e = 0; e < mat.size(); ++e) {
+          const float h = (float)mat[e];
+          q[2 * e] = h;
+          q[2 * e + 1] = (float)(mat[e] - (double)h);
+        }
       } else {
         prog->dense.insert(prog->dense.end(), mat.begin(), mat.end());
       }

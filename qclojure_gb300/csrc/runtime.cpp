@@ -409,8 +409,9 @@ static int compile_program(const qg_circuit* c, int precision, int fusion, int f
     prog->bufs = tune->buffers;
     prog->ctas = tune->ctas_per_sm;
   }
-  // dense fused blocks are evaluated in FP64 (FMA) whatever the arithmetic setting
-  prog->arith = (fusion == QG_FUSE_DENSE || arith != QG_ARITH_DOUBLE_FLOAT) ? QG_ARITH_EXACT : QG_ARITH_DOUBLE_FLOAT;
+  // complex128 dense fused blocks follow the arithmetic setting: double-float blocks on
+  // the FP32 pipes, or FP64 (FMA inside the block product) for the exact setting
+  prog->arith = arith == QG_ARITH_DOUBLE_FLOAT ? QG_ARITH_DOUBLE_FLOAT : QG_ARITH_EXACT;
   std::vector<GOp> gops;
   std::vector<std::vector<int>> measures;
   std::vector<int> measure_at;

@@ -53,6 +53,7 @@ struct PolExact {
   using Reg = V;
   static constexpr int kElem = sizeof(V);  // bytes per amplitude in HBM and shared memory
   static constexpr bool kDense = true;     // dense fused blocks supported
+  static constexpr bool kDF = false;
   static constexpr int kCst = sizeof(R) == 8 ? 0 : 1;
   static constexpr bool kInPairs = false, kOutPairs = false;
   struct Cst {
@@ -130,11 +131,14 @@ using PolF = PolExact<float, float2>;
 // first pass of a run converts from IEEE doubles and the last one back, so the
 // passes in between convert nothing.
 // ---------------------------------------------------------------------------
-template <int IO>
+template <int IO, bool DENSE = false>
 struct PolDFT {
   using Reg = dfc;
   static constexpr int kElem = 16;
-  static constexpr bool kDense = false;  // dense fused blocks run with PolD
+  // dense fused blocks in double-float (dense_df), compiled only into the kernels of
+  // programs that hold them
+  static constexpr bool kDense = DENSE;
+  static constexpr bool kDF = true;
   static constexpr bool kInPairs = (IO & 1) != 0, kOutPairs = (IO & 2) != 0;
   static constexpr int kCst = 2;
   struct Cst {
@@ -464,6 +468,52 @@ __device__ void dense_smem(unsigned char* buf, const KOp& op, const double* dens
   __syncthreads();
 }
 
+// A dense 2^dk x 2^dk block in double-float: entries stored as (re.hi, re.lo, im.hi,
+// im.lo) float quads (one 16-byte entry, the same offsets as the FP64 form), each output
+// amplitude the double-float sum of its row's products with the block's columns, taken
+// in the same Gray-code order as dense_smem.
+template <class P>
+__device__ void dense_df(unsigned char* buf, const KOp& op, const double* dense, const TileGeo& g) {
+  const int dk = (int)op.tmask, D = 1 << dk;
+  const uint32_t dbits = op.rmr;  // 4 bits per block bit
+  constexpr int kMaxItems = 16;
+  dfc out[kMaxItems];
+  int cnt = 0;
+  for (int idx = threadIdx.x; idx < g.K; idx += g.T, ++cnt) {
+    const int grp = idx >> dk, row = idx & (D - 1);
+    uint32_t lc = grp;
+    for (int j = 0; j < dk; ++j) {
+      const int b = (dbits >> (4 * j)) & 15;
+      lc = ((lc >> b) << (b + 1)) | (lc & ((1u << b) - 1));
+    }
+    dfc acc{0.f, 0.f, 0.f, 0.f};
+    for (int i = 0; i < D; ++i) {
+      if (i) lc ^= 1u << ((dbits >> (4 * (__ffs(i) - 1))) & 15);
+      const int e = row * D + (i ^ (i >> 1));
+      const float4 m = __ldg(reinterpret_cast<const float4*>(dense) + op.tval + e);
+      const dfc x = P::load_work(buf, swz<16>(lc));
+      const dfc pr = cmul_df(m.x, m.y, m.z, m.w, x);
+      add2(acc.rh, acc.rl, pr.rh, pr.rl, acc.rh, acc.rl);
+      add2(acc.ih, acc.il, pr.ih, pr.il, acc.ih, acc.il);
+    }
+    out[cnt] = acc;
+  }
+  __syncthreads();
+  cnt = 0;
+  for (int idx = threadIdx.x; idx < g.K; idx += g.T, ++cnt) {
+    const int grp = idx >> dk, row = idx & (D - 1);
+    uint32_t lg = grp;
+    for (int j = 0; j < dk; ++j) {
+      const int b = (dbits >> (4 * j)) & 15;
+      lg = ((lg >> b) << (b + 1)) | (lg & ((1u << b) - 1));
+    }
+    for (int j = 0; j < dk; ++j)
+      if ((row >> j) & 1) lg |= 1u << ((dbits >> (4 * j)) & 15);
+    P::store_work(buf, swz<16>(lg), out[cnt]);
+  }
+  __syncthreads();
+}
+
 #define QG_U2_CASES(CLS)                                                                              \
   case KC_U2 + CLS * 4 + 0: u2_regs<P, CLS, 0, false>(r, kcst<P>(op), 0, true); break;               \
   case KC_U2 + CLS * 4 + 1: u2_regs<P, CLS, 1, false>(r, kcst<P>(op), 0, true); break;               \
@@ -524,7 +574,10 @@ __device__ void run_ops(unsigned char* buf, const KOp* __restrict__ sops, int no
         raw = false;
         __syncthreads();
       }
-      if constexpr (P::kDense) dense_smem<P>(buf, op, dense, g);
+      if constexpr (P::kDense) {
+        if constexpr (P::kDF) dense_df<P>(buf, op, dense, g);
+        else dense_smem<P>(buf, op, dense, g);
+      }
       continue;
     }
     bool tc = true;
@@ -1039,10 +1092,10 @@ cudaError_t launch_tile_pass(int precision, int arithmetic, int io, int n, const
   if (precision == QG_C64) return launch_t<PolF>(n, pd, ba, d_dense, st);
   if (arithmetic == QG_ARITH_DOUBLE_FLOAT) {
     switch (io & 3) {
-      case 0: return launch_t<PolDFT<0>>(n, pd, ba, d_dense, st);
-      case 1: return launch_t<PolDFT<1>>(n, pd, ba, d_dense, st);
-      case 2: return launch_t<PolDFT<2>>(n, pd, ba, d_dense, st);
-      default: return launch_t<PolDFT<3>>(n, pd, ba, d_dense, st);
+      case 0: return d_dense ? launch_t<PolDFT<0, true>>(n, pd, ba, d_dense, st) : launch_t<PolDFT<0>>(n, pd, ba, d_dense, st);
+      case 1: return d_dense ? launch_t<PolDFT<1, true>>(n, pd, ba, d_dense, st) : launch_t<PolDFT<1>>(n, pd, ba, d_dense, st);
+      case 2: return d_dense ? launch_t<PolDFT<2, true>>(n, pd, ba, d_dense, st) : launch_t<PolDFT<2>>(n, pd, ba, d_dense, st);
+      default: return d_dense ? launch_t<PolDFT<3, true>>(n, pd, ba, d_dense, st) : launch_t<PolDFT<3>>(n, pd, ba, d_dense, st);
     }
   }
   return launch_t<PolD>(n, pd, ba, d_dense, st);
