@@ -236,6 +236,7 @@ def serving_leg(num_jobs=250, rates=(5, 20, 100, 5000), seed=11, plain_jobs=100)
             cps, lat, nb, mb = replay_trace(sim, trace)
             out["c64_served"][str(r)] = {"circuits_per_s": cps, "p50_ms": pct(lat, 0.5), "p99_ms": pct(lat, 0.99),
                                          "jobs_batched": nb, "largest_batch": mb}
+        out["precompiled_jobs"] = sim.queue_status()["precompiled-jobs"]
     finally:
         sim.close()
     trace = workloads.serving_trace(num_jobs, float(rates[-1]), seed)[:plain_jobs]

@@ -215,7 +215,9 @@ enum { QG_JOB_LOOP_AUTO = 0, QG_JOB_LOOP_ON = 1, QG_JOB_LOOP_OFF = 2 };
 typedef struct qg_queue_info {    /* queue-status (ideal_simulator.clj:165-176) + device fields */
   int64_t total_jobs, queued, running, completed, failed, cancelled;
   uint64_t hbm_free_bytes, hbm_budget_bytes, hbm_in_use_bytes;
-  int32_t workers, reserved;
+  int32_t workers;
+  int32_t precompiled_jobs;       /* queued large jobs whose pass kernels a background
+                                     compile prepared before they ran (no counterpart)  */
 } qg_queue_info;
 
 typedef struct qg_job_info {

@@ -125,7 +125,7 @@ class QgQueueInfo(C.Structure):
     _fields_ = [("total_jobs", C.c_int64), ("queued", C.c_int64), ("running", C.c_int64),
                 ("completed", C.c_int64), ("failed", C.c_int64), ("cancelled", C.c_int64),
                 ("hbm_free_bytes", C.c_uint64), ("hbm_budget_bytes", C.c_uint64), ("hbm_in_use_bytes", C.c_uint64),
-                ("workers", C.c_int32), ("reserved", C.c_int32)]
+                ("workers", C.c_int32), ("precompiled_jobs", C.c_int32)]
 
 
 class QgJobInfo(C.Structure):

@@ -491,7 +491,7 @@ class GpuStateVectorSimulator:
                 "backend-load": (q.hbm_in_use_bytes / q.hbm_budget_bytes) if q.hbm_budget_bytes else 0.0,
                 "estimated-wait-time": 0, "hbm-free-bytes": q.hbm_free_bytes,
                 "hbm-budget-bytes": q.hbm_budget_bytes, "hbm-in-use-bytes": q.hbm_in_use_bytes,
-                "workers": q.workers}
+                "workers": q.workers, "precompiled-jobs": q.precompiled_jobs}
 
     # -- BatchJobBackend -----------------------------------------------------------
     def batch_submit(self, circuits: list[dict], options: dict | None = None) -> str:

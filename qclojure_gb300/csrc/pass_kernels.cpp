@@ -1464,6 +1464,19 @@ cudaError_t launch_level_kernel(const PassKernels& lkb, int level, const GroupLe
   return e;
 }
 
+std::shared_ptr<const PassKernels> pass_kernels_cached(const Program& prog, int prec, int device) {
+  if (device < 0 || device >= 64 || prog.tops.empty()) return nullptr;
+  const Shape shape = shape_of(prog, prec);
+  const std::string key = std::to_string(prec) + ":" + std::to_string(shape.rbits) + "/" +
+                          std::to_string(shape.bufs) + "/" + std::to_string(shape.ctas) + ":" +
+                          pass_structure_key(prog, false);
+  std::lock_guard<std::mutex> lk(g_mu);
+  std::shared_ptr<Compiled>* hit = g_cache[device].find(key);
+  if (!hit || !*hit) return nullptr;
+  ++g_cache_hits;
+  return *hit;
+}
+
 bool pass_kernel_ready(const PassKernels& pk, size_t step) {
   const Compiled& c = static_cast<const Compiled&>(pk);
   return step < c.kernel.size() && c.kernel[step] != nullptr;

@@ -231,6 +231,8 @@ struct PassKernels {
 // sweep group); matrix entries come from per-state coefficient rows.
 std::shared_ptr<const PassKernels> pass_kernels_for(const Program& prog, int prec, int device, std::string* why,
                                                     bool table = false);
+// The program's kernels if an earlier call compiled them (no compile here).
+std::shared_ptr<const PassKernels> pass_kernels_cached(const Program& prog, int prec, int device);
 // Programs with equal keys share table-form kernels (coefficients left out).
 std::string pass_structure_key(const Program& prog, bool table);
 // Launch the table form over nstates states; d_coefs holds nstates rows of

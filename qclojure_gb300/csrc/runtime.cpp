@@ -277,6 +277,12 @@ static int do_measure(State* s, const std::vector<int>& qubits, uint64_t seed, u
 // gains, while smaller one-off jobs (the serving stream) would lose.
 // qg_autotune_crossover measures the crossover for a context and replaces it.
 constexpr int kPassKernelMinQubits = 29;
+// Large jobs below the crossover that wait in the queue get their pass kernels compiled
+// on background host threads meanwhile; a job that starts after its compile finished
+// runs them, one that starts before runs interpreted. Host cores are otherwise idle
+// while the device works through the queue, so the compile costs the job nothing.
+constexpr int kPrecompileMinQubits = 20;
+constexpr int kPrecompileThreads = 2;
 
 static std::shared_ptr<const PassKernels> maybe_pass_kernels(const State* s, const Program& prog);
 static std::shared_ptr<const PassKernels> forced_pass_kernels(const State* s, const Program& prog);
@@ -665,6 +671,13 @@ struct Ctx {
   std::thread loop_poller;
   bool loop_stop = false;
   uint64_t loop_jobs = 0;
+  // background compiles of queued large jobs' pass kernels (precompile_loop)
+  std::mutex pre_mu;
+  std::condition_variable pre_cv;
+  std::deque<std::shared_ptr<Job>> pre_queue;
+  std::vector<std::thread> pre_threads;
+  bool pre_stop = false;
+  uint64_t precompiled = 0;
 };
 
 // True when programs of this kind run as specialised pass kernels (the condition
@@ -692,7 +705,11 @@ static std::shared_ptr<const PassKernels> maybe_pass_kernels(const State* s, con
   if (s->prec == QG_C128 && prog.arith != QG_ARITH_DOUBLE_FLOAT) return nullptr;
   const int mode = c->cfg.pass_kernels;
   if (mode == QG_PASS_KERNELS_OFF) return nullptr;
-  if (mode != QG_PASS_KERNELS_ALWAYS && s->n < c->spec_min_qubits[s->prec == QG_C64 ? 1 : 0].load()) return nullptr;
+  if (mode != QG_PASS_KERNELS_ALWAYS && s->n < c->spec_min_qubits[s->prec == QG_C64 ? 1 : 0].load()) {
+    // below the crossover a one-off program runs interpreted, unless its kernels were
+    // compiled meanwhile (a queued job's background compile, precompile_loop)
+    return s->n >= kPrecompileMinQubits ? pass_kernels_cached(prog, s->prec, c->device) : nullptr;
+  }
   std::string why;
   return pass_kernels_for(prog, s->prec, c->device, &why);
 }
@@ -1557,6 +1574,44 @@ static int prepare_job(Ctx* c, const qg_circuit* circ, const qg_options* opt, st
 }
 
 // Queue prepared jobs in one step (a batch arrives together) and assign their ids.
+// A queued job whose kernels a background compile could have ready by the time it runs.
+static bool precompile_eligible(const Ctx* c, const Job* j) {
+  if (j->n < kPrecompileMinQubits || j->fusion != QG_FUSE_TILED) return false;
+  if (c->cfg.pass_kernels != QG_PASS_KERNELS_AUTO || pass_kernels_unavailable()) return false;
+  if (j->precision == QG_C128 && j->arith != QG_ARITH_DOUBLE_FLOAT) return false;
+  return j->n < c->spec_min_qubits[j->precision == QG_C64 ? 1 : 0].load();  // above it the run compiles anyway
+}
+
+// Background compile of queued large jobs' pass kernels (into the per-device kernel
+// cache); a job already started or finished is skipped.
+static void precompile_loop(Ctx* c) {
+  cudaSetDevice(c->device);
+  for (;;) {
+    std::shared_ptr<Job> j;
+    {
+      std::unique_lock<std::mutex> lk(c->pre_mu);
+      c->pre_cv.wait(lk, [&] { return c->pre_stop || !c->pre_queue.empty(); });
+      if (c->pre_stop) break;
+      j = c->pre_queue.front();
+      c->pre_queue.pop_front();
+    }
+    if (j->status.load() != QG_JOB_QUEUED) continue;
+    NvtxRange nvtx("qg precompile");
+    Program prog;
+    std::string err;
+    qg_circuit circ{j->n, (int32_t)j->ops.size(), j->ops.data()};
+    qg_tuning tu;  // the same program the run will compile (compile_job)
+    const qg_tuning* tune = tuning_for(c, j->n, j->precision, j->arith, j->fusion, &tu);
+    if (compile_program(&circ, j->precision, j->fusion, c->cfg.fuse_k, j->arith, &prog, &err, true, tune) != QG_OK)
+      continue;
+    std::string why;
+    if (pass_kernels_for(prog, j->precision, c->device, &why, false)) {
+      std::lock_guard<std::mutex> lk(c->pre_mu);
+      ++c->precompiled;
+    }
+  }
+}
+
 static void enqueue_jobs(Ctx* c, std::vector<std::shared_ptr<Job>>& js, uint64_t batch, uint64_t* ids_out) {
   const auto now = Clock::now();
   {
@@ -1574,6 +1629,16 @@ static void enqueue_jobs(Ctx* c, std::vector<std::shared_ptr<Job>>& js, uint64_t
     }
   }
   c->cv.notify_all();
+  bool pre = false;
+  {
+    std::lock_guard<std::mutex> g(c->pre_mu);
+    for (auto& j : js)
+      if (precompile_eligible(c, j.get())) {
+        c->pre_queue.push_back(j);
+        pre = true;
+      }
+  }
+  if (pre) c->pre_cv.notify_one();
 }
 
 static int submit_one(Ctx* c, const qg_circuit* circ, const qg_options* opt, uint64_t* id_out) {
@@ -1660,6 +1725,7 @@ int qg_ctx_create(const qg_config* cfg, void** ctx_out) {
   for (int w = 0; w < kSmallLaneWorkers; ++w) c->workers.emplace_back(worker_loop, c, true);
   c->batcher = std::thread(batcher_loop, c);
   c->loop_poller = std::thread(loop_poller_loop, c);
+  for (int t = 0; t < kPrecompileThreads; ++t) c->pre_threads.emplace_back(precompile_loop, c);
   *ctx_out = c;
   return QG_OK;
 }
@@ -1667,6 +1733,12 @@ int qg_ctx_create(const qg_config* cfg, void** ctx_out) {
 int qg_ctx_destroy(void* ctx) {
   if (!ctx) return QG_ERR_INVALID_ARG;
   Ctx* c = (Ctx*)ctx;
+  {
+    std::lock_guard<std::mutex> g(c->pre_mu);
+    c->pre_stop = true;
+  }
+  c->pre_cv.notify_all();
+  for (auto& t : c->pre_threads) t.join();
   {
     std::lock_guard<std::mutex> g(c->mu);
     c->stop = true;
@@ -1790,6 +1862,10 @@ int qg_queue_status(void* ctx, qg_queue_info* out) {
   out->hbm_budget_bytes = c->hbm_budget;
   out->hbm_in_use_bytes = c->hbm_in_use;
   out->workers = (int32_t)c->workers.size();
+  {
+    std::lock_guard<std::mutex> g2(c->pre_mu);
+    out->precompiled_jobs = (int32_t)c->precompiled;
+  }
   return QG_OK;
 }
 
