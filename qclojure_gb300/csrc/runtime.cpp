@@ -2965,6 +2965,8 @@ static cudaError_t launch_group_passes(Sweep* sw, SweepGroup& g) {
 // Level kernels over the batched groups that have table-form kernels: their states are
 // set to |0...0> in one launch and pass level l of all of them runs in one launch
 // (qgl_<l>), the whole captured in one graph. A sweep of one group keeps its own graph.
+constexpr float kLevelGraphMargin = 1.02f;  // level graph kept up to 2 % slower than the per-size graphs
+
 static void setup_level_kernels(Sweep* sw) {
   std::vector<int> cand;
   for (size_t gi = 0; gi < sw->groups.size(); ++gi) {
@@ -3062,7 +3064,11 @@ static void setup_level_kernels(Sweep* sw) {
     });
     sw->level_ms = t_level;
     sw->group_ms = t_groups;
-    if (t_level > 0 && (t_groups <= 0 || t_level <= t_groups)) {
+    // The level graph is kept unless it is measurably slower: at equal speed one
+    // launch per layer over every size beats a graph per size (fewer launches, and
+    // the small sizes fill the SMs the large ones leave idle at their tails); one
+    // replay's timing varies by about a percent, hence the margin.
+    if (t_level > 0 && (t_groups <= 0 || t_level <= kLevelGraphMargin * t_groups)) {
       sw->lk = lk;
       sw->lk_exec = exec;
       sw->lk_launches = 1 + L;

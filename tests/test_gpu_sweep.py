@@ -35,9 +35,10 @@ def test_qaoa_sweep_energies(gpu_ctx, oracle, precision, arith, tol):
         assert st["groups"] == distinct
         if precision == "c64" or arith == "double-float":
             # table-form kernels: every size in one graph, one launch per pass level (plus one
-            # that zeroes all states), or one graph per size, whichever measured faster
+            # that zeroes all states), unless that measured more than 2 % slower than one
+            # graph per size
             assert st["level-graph-ms"] > 0 and st["size-graphs-ms"] > 0, st
-            faster_level = st["level-graph-ms"] <= st["size-graphs-ms"]
+            faster_level = st["level-graph-ms"] <= 1.02 * st["size-graphs-ms"]  # the runtime's margin
             assert st["graphs"] == (1 if faster_level else distinct), st
         else:
             assert st["graphs"] == distinct
