@@ -9,22 +9,26 @@
 //   * A tile is 4096 amplitudes: every combination of the block's k target bits and
 //     the lowest 12 - k other bits. Its HBM footprint is a few contiguous runs of at
 //     least 1 KiB (all bits below the highest column bit belong to the tile), moved by
-//     the bulk-copy engine (cp.async.bulk, mbarrier completion) into one of two staging
-//     buffers, and written back from registers by the epilogue warps.
+//     the bulk-copy engine (cp.async.bulk, mbarrier completion) into one of six staging
+//     buffers in shared memory, and written back from registers by the epilogue warps.
 //   * The block is a real GEMM. Column c of the tile (the non-target bits, 128 per
 //     MMA) is a row of the A operand holding its 2^k amplitudes as 2^(k+1) reals
 //     (re, im interleaved); the B operand is the real form of the block,
 //     W[(r,o),(j,i)] = [[Ur, -Ui], [Ui, Ur]], so D[c, 2r+o] is output amplitude (r, c).
-//     Both operands are K-major in shared memory with the 128-byte swizzle.
+//     A lives in tensor memory (row c on lane c, K along the columns), written by the
+//     transform warps with tcgen05.st; B is K-major in shared memory with the 128-byte
+//     swizzle. Keeping A out of shared memory leaves room for six staging buffers, so
+//     several tiles' loads are in flight while earlier tiles are transformed,
+//     multiplied and stored.
 //   * Precision: every operand is split into a TF32 high part and a TF32 low part
 //     (hi = round(x), lo = round(x - hi)); D = Ahi Bhi + Alo Bhi + Ahi Blo accumulates
 //     in FP32 in tensor memory, about the accuracy of FP32 arithmetic (3xTF32).
 //   * Blocks of fewer than four qubits are widened to four on the host (the identity on
-//     the lowest other bits), so the kernel handles k = 4 and k = 5.
+//     the lowest other bits from bit 5 up), so the kernel handles k = 4 and k = 5.
 //
 // Every wait on an mbarrier is bounded (about a second of wall time); on a timeout the
-// kernel records an error code, lets its bulk copies drain, frees its tensor memory and
-// returns, and the host reports the error.
+// kernel records an error code, lets its bulk copies and MMAs drain, frees its tensor
+// memory and returns, and the host reports the error.
 #include <cuda_runtime.h>
 
 #include <cstdint>
@@ -40,9 +44,14 @@ constexpr int kTileBits = 12;           // 4096 amplitudes (32 KiB of complex64)
 constexpr int kTileAmps = 1 << kTileBits;
 constexpr int kThreads = 256;
 constexpr int kStageBytes = kTileAmps * 8;
-constexpr int kAHalfBytes = 32768;      // one of A hi / A lo: 128 x 64 TF32 (k = 5) or 256 x 32 (k = 4)
+constexpr int kStages = 6;              // staging buffers: tiles whose loads may be in flight
 constexpr int kBHalfBytes = 16384;      // one of B hi / B lo at k = 5 (64 x 64 TF32)
-constexpr int kTmemCols = 64;
+// Tensor memory: two buffers of 256 columns, each A hi at [0, 64), A lo at [64, 128)
+// and the accumulators D at [128, 192) (both k = 4 with two 128-row blocks of 32
+// columns each, and k = 5 with one block of 64 columns).
+constexpr int kTmemBufCols = 256;
+constexpr int kTmemCols = 2 * kTmemBufCols;
+constexpr int kColALo = 64, kColD = 128;
 
 struct DenseTcParams {
   float2* state;
@@ -69,6 +78,15 @@ __device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
 __device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes) {
   asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes)
                : "memory");
+}
+__device__ __forceinline__ bool mbar_test(uint64_t* bar, uint32_t parity) {
+  uint32_t done;
+  asm volatile(
+      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+      : "=r"(done)
+      : "r"(smem_u32(bar)), "r"(parity)
+      : "memory");
+  return done != 0;
 }
 __device__ __forceinline__ uint64_t global_ns() {
   uint64_t t;
@@ -112,11 +130,14 @@ __device__ __forceinline__ uint64_t smem_desc(uint32_t addr) {
 __host__ __device__ constexpr uint32_t idesc_tf32(int n) {
   return (1u << 4) | (2u << 7) | (2u << 10) | ((uint32_t)(n >> 3) << 17) | ((uint32_t)(128 >> 4) << 24);
 }
-__device__ __forceinline__ void mma_tf32(uint32_t d_tmem, uint64_t a, uint64_t b, uint32_t idesc, uint32_t acc) {
+// D (+)= A B with A read from tensor memory (rows on lanes, K along columns) and B
+// from shared memory through its descriptor.
+__device__ __forceinline__ void mma_tf32_ts(uint32_t d_tmem, uint32_t a_tmem, uint64_t b, uint32_t idesc,
+                                            uint32_t acc) {
   asm volatile(
       "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
-      " tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n}\n" ::"r"(d_tmem),
-      "l"(a), "l"(b), "r"(idesc), "r"(acc)
+      " tcgen05.mma.cta_group::1.kind::tf32 [%0], [%1], %2, %3, p;\n}\n" ::"r"(d_tmem),
+      "r"(a_tmem), "l"(b), "r"(idesc), "r"(acc)
       : "memory");
 }
 __device__ __forceinline__ void mma_commit(uint64_t* bar) {
@@ -136,6 +157,15 @@ __device__ __forceinline__ void tmem_ld32(uint32_t taddr, float* v) {
   asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
 #pragma unroll
   for (int i = 0; i < 32; ++i) v[i] = __uint_as_float(r[i]);
+}
+// 16 consecutive columns of this thread's lane (tcgen05.st shape 32x32b)
+__device__ __forceinline__ void tmem_st16(uint32_t taddr, const float* v) {
+  asm volatile(
+      "tcgen05.st.sync.aligned.32x32b.x16.b32 [%0], {%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,%16};" ::"r"(
+          taddr),
+      "f"(v[0]), "f"(v[1]), "f"(v[2]), "f"(v[3]), "f"(v[4]), "f"(v[5]), "f"(v[6]), "f"(v[7]), "f"(v[8]),
+      "f"(v[9]), "f"(v[10]), "f"(v[11]), "f"(v[12]), "f"(v[13]), "f"(v[14]), "f"(v[15])
+      : "memory");
 }
 __device__ __forceinline__ float to_tf32(float x) {
   uint32_t r;
@@ -161,15 +191,16 @@ __device__ __forceinline__ uint64_t tile_base(const DenseTcParams& p, uint64_t t
 
 // The tile's work is a pipeline over two groups of four warps, so the phases of
 // consecutive tiles overlap:
-//   transform warps (0-3): wait for tile r's bulk load, split it into A hi / A lo of
-//     buffer r % 2 (once the MMAs of tile r - 2 have read that buffer), then warp 0
-//     issues tile r's MMAs into tensor-memory buffer r % 2 (once the epilogue of tile
-//     r - 2 has read it) and the bulk load of tile r + 2 into the staging buffer tile r
-//     has just left;
+//   transform warps (0-3): wait for tile r's bulk load (issued up to six tiles ahead),
+//     split each column's amplitudes into TF32 hi / lo and store them as rows of A in
+//     tensor-memory buffer r % 2 (once the MMAs of tile r - 2 have read it); then warp
+//     0 refills the staging buffer tile r has left with tile r + 6 and issues tile r's
+//     MMAs (once the epilogue of tile r - 2 has read that buffer's accumulators);
 //   epilogue warps (4-7): wait for tile r's MMAs, read its accumulators and store the
 //     amplitudes straight to HBM (lane c holds column c: consecutive lanes write
 //     consecutive amplitudes when the low index bits are column bits), then release
 //     the tensor-memory buffer.
+// Warp w of either group reaches tensor-memory lanes 32w .. 32w + 31, the rows it owns.
 // Waits are on mbarriers, each bounded; a group that gives up raises a shared abort
 // flag, which ends the other group's waits at once.
 template <int KB>
@@ -179,26 +210,23 @@ __global__ void __launch_bounds__(kThreads, 1) k_dense_tc(const __grid_constant_
   constexpr int Kp = 2 * D;                // reals per column (K of the GEMM)
   constexpr int Np = Kp;                   // reals per output column (N of the GEMM)
   constexpr int G = (KB == 4) ? 2 : 1;     // 128-column MMA blocks per tile
-  constexpr int Mrows = 128 * G;           // columns of a tile
   constexpr uint32_t idesc = idesc_tf32(Np);
   constexpr int kGroup = kThreads / 2;     // threads per group
-  constexpr int PER = kTileAmps / kGroup;  // tile positions per transform thread
-  // 1024-aligned regions: A hi / A lo of buffers 0 and 1, B hi, B lo, two staging buffers
-  unsigned char* base = (unsigned char*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
-  unsigned char* a_buf = base;                              // buffer b: hi at 2b, lo at 2b + 1 halves
-  unsigned char* b_hi = a_buf + 4 * kAHalfBytes;
+  static_assert(G * Kp == kColALo && 2 * G * Kp == kColD && kColD + G * Np <= kTmemBufCols, "tensor memory map");
+  // 1024-aligned regions: B hi, B lo, the staging buffers, then the barriers and tables
+  unsigned char* base = smem_raw + ((1024u - (smem_u32(smem_raw) & 1023u)) & 1023u);
+  unsigned char* b_hi = base;
   unsigned char* b_lo = b_hi + kBHalfBytes;
   unsigned char* stage = b_lo + kBHalfBytes;
-  uint64_t* full = reinterpret_cast<uint64_t*>(stage + 2 * kStageBytes);  // [2]
-  uint64_t* mma_done = full + 2;                                           // [2]
-  uint64_t* tmem_free = mma_done + 2;                                      // [2]
-  uint64_t* r_off = tmem_free + 2;                                         // [32]
+  uint64_t* full = reinterpret_cast<uint64_t*>(stage + kStages * kStageBytes);  // [kStages]
+  uint64_t* mma_done = full + kStages;                                          // [2]
+  uint64_t* tmem_free = mma_done + 2;                                           // [2]
+  uint64_t* r_off = tmem_free + 2;                                              // [32]
   uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(r_off + 32);
   volatile int* abort_flag = reinterpret_cast<volatile int*>(tmem_slot + 1);
 
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const bool transform = tid < kGroup;
-  const int gtid = transform ? tid : tid - kGroup;
 
   // the block's real form, hi and lo, already laid out by the host
   for (int i = tid * 4; i < p.bbytes / 4; i += kThreads * 4) {
@@ -212,8 +240,8 @@ __global__ void __launch_bounds__(kThreads, 1) k_dense_tc(const __grid_constant_
     r_off[tid] = o;
   }
   if (tid == 0) {
+    for (int q = 0; q < kStages; ++q) mbar_init(&full[q], 1);
     for (int q = 0; q < 2; ++q) {
-      mbar_init(&full[q], 1);
       mbar_init(&mma_done[q], 1);
       mbar_init(&tmem_free[q], 1);
     }
@@ -222,7 +250,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_dense_tc(const __grid_constant_
   }
   if (warp == 0) {
     asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tmem_slot)),
-                 "r"(2 * kTmemCols)
+                 "r"(kTmemCols)
                  : "memory");
     asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
   }
@@ -236,16 +264,9 @@ __global__ void __launch_bounds__(kThreads, 1) k_dense_tc(const __grid_constant_
   const uint64_t count = t_end - t_begin;
   // a bounded wait that also ends when the other group gave up
   auto wait = [&](uint64_t* bar, uint32_t parity) {
-    const uint32_t a = smem_u32(bar);
     uint64_t t0 = 0;
     for (uint32_t it = 0;; ++it) {
-      uint32_t done;
-      asm volatile(
-          "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
-          : "=r"(done)
-          : "r"(a), "r"(parity)
-          : "memory");
-      if (done) return true;
+      if (mbar_test(bar, parity)) return true;
       if ((it & 255u) == 0) {
         if (*abort_flag) return false;
         const uint64_t now = global_ns();
@@ -257,20 +278,26 @@ __global__ void __launch_bounds__(kThreads, 1) k_dense_tc(const __grid_constant_
       }
     }
   };
+  const uint32_t lane_base = (uint32_t)(32 * (warp & 3)) << 16;  // this warp's tensor-memory lanes
 
   if (transform) {
-    // this thread's tile positions i = gtid + q * kGroup map to the same A offsets in every tile
-    uint32_t a_off[PER];
+    // tile positions of this thread's columns c = 128 g + 32 warp + lane, and of the
+    // target combinations j (the same in every tile)
+    uint32_t cpos[G], jpos[D];
 #pragma unroll
-    for (int q = 0; q < PER; ++q) {
-      const int i = gtid + q * kGroup;
-      int j = 0, c = 0;
-      for (int t = 0; t < kTileBits; ++t) {
-        const int bit = (i >> t) & 1;
-        if (p.tgt_of[t] >= 0) j |= bit << p.tgt_of[t];
-        else c |= bit << p.col_of[t];
-      }
-      a_off[q] = kmajor_off(Mrows, c, 2 * j);
+    for (int g = 0; g < G; ++g) {
+      const int c = 128 * g + 32 * warp + lane;
+      uint32_t pos = 0;
+      for (int t = 0; t < kTileBits; ++t)
+        if (p.col_of[t] >= 0 && ((c >> p.col_of[t]) & 1)) pos |= 1u << t;
+      cpos[g] = pos;
+    }
+#pragma unroll
+    for (int j = 0; j < D; ++j) {
+      uint32_t pos = 0;
+      for (int t = 0; t < kTileBits; ++t)
+        if (p.tgt_of[t] >= 0 && ((j >> p.tgt_of[t]) & 1)) pos |= 1u << t;
+      jpos[j] = pos;
     }
     const int nrun = 1 << (kTileBits - p.runbits);  // at most 32: runs are at least 2^7 amplitudes
     const uint32_t run_bytes = (uint32_t)(8u << p.runbits);
@@ -278,8 +305,8 @@ __global__ void __launch_bounds__(kThreads, 1) k_dense_tc(const __grid_constant_
     if (warp == 0 && lane < nrun)
       for (int b = p.runbits; b < kTileBits; ++b)
         if ((lane >> (b - p.runbits)) & 1) run_off |= 1ull << p.tbit[b];
-    auto issue_load = [&](uint64_t r) {  // warp 0: tile r into staging buffer r % 2
-      const int s = (int)(r & 1);
+    auto issue_load = [&](uint64_t r) {  // warp 0: tile r into staging buffer r % kStages
+      const int s = (int)(r % kStages);
       if (lane == 0) mbar_expect_tx(&full[s], (uint32_t)kStageBytes);
       __syncwarp();
       const uint64_t tb = tile_base(p, t_begin + r);
@@ -288,25 +315,36 @@ __global__ void __launch_bounds__(kThreads, 1) k_dense_tc(const __grid_constant_
     };
     uint64_t issued = 0, mmas = 0;
     if (warp == 0)
-      for (; issued < 2 && issued < count; ++issued) issue_load(issued);
+      for (; issued < (uint64_t)kStages && issued < count; ++issued) issue_load(issued);
     uint64_t r = 0;
     for (; r < count; ++r) {
-      const int s = (int)(r & 1), b = (int)(r & 1);
-      bool ok = wait(&full[s], (uint32_t)(r >> 1) & 1u);
+      const int s = (int)(r % kStages), b = (int)(r & 1);
+      bool ok = wait(&full[s], (uint32_t)(r / kStages) & 1u);
       if (ok && r >= 2) ok = wait(&mma_done[b], (uint32_t)((r - 2) >> 1) & 1u);  // A buffer b is read
-      unsigned char* a_hi = a_buf + (2 * b) * kAHalfBytes;
-      unsigned char* a_lo = a_hi + kAHalfBytes;
       if (ok) {
+        tc_fence_after();
         const float2* st = reinterpret_cast<const float2*>(stage + s * kStageBytes);
+        const uint32_t abuf = tmem + lane_base + (uint32_t)(b * kTmemBufCols);
 #pragma unroll
-        for (int q = 0; q < PER; ++q) {
-          const float2 x = st[gtid + q * kGroup];
-          const float hr = to_tf32(x.x), hi_ = to_tf32(x.y);
-          const float lr = to_tf32(x.x - hr), li = to_tf32(x.y - hi_);
-          *reinterpret_cast<float2*>(a_hi + a_off[q]) = make_float2(hr, hi_);
-          *reinterpret_cast<float2*>(a_lo + a_off[q]) = make_float2(lr, li);
+        for (int g = 0; g < G; ++g) {
+#pragma unroll
+          for (int ch = 0; ch < Kp / 16; ++ch) {  // amplitudes j = 8 ch .. 8 ch + 7 of column c
+            float hv[16], lv[16];
+#pragma unroll
+            for (int q = 0; q < 8; ++q) {
+              const float2 x = st[cpos[g] | jpos[8 * ch + q]];
+              const float hr = to_tf32(x.x), hi_ = to_tf32(x.y);
+              hv[2 * q] = hr;
+              hv[2 * q + 1] = hi_;
+              lv[2 * q] = to_tf32(x.x - hr);
+              lv[2 * q + 1] = to_tf32(x.y - hi_);
+            }
+            tmem_st16(abuf + (uint32_t)(g * Kp + 16 * ch), hv);
+            tmem_st16(abuf + (uint32_t)(kColALo + g * Kp + 16 * ch), lv);
+          }
         }
-        fence_proxy_async();
+        asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory");
+        tc_fence_before();
       }
       // the whole group goes on only if every thread got here and nothing gave up
       if (!bar_and(1, kGroup, ok && !*abort_flag)) {
@@ -314,11 +352,14 @@ __global__ void __launch_bounds__(kThreads, 1) k_dense_tc(const __grid_constant_
         break;
       }
       if (warp == 0) {
+        // staging buffer s has been read by every transform thread (the barrier above)
+        if (issued < count && issued == r + kStages) issue_load(issued++);
+        __syncwarp();
         if (lane == 0) {
-          const bool tok = r < 2 || wait(&tmem_free[b], (uint32_t)((r - 2) >> 1) & 1u);  // tensor memory b is read
+          const bool tok = r < 2 || wait(&tmem_free[b], (uint32_t)((r - 2) >> 1) & 1u);  // D of buffer b is read
           if (tok) {
             tc_fence_after();
-            const uint64_t dah = smem_desc(smem_u32(a_hi)), dal = smem_desc(smem_u32(a_lo));
+            const uint32_t buf = tmem + (uint32_t)(b * kTmemBufCols);
             const uint64_t dbh = smem_desc(smem_u32(b_hi)), dbl = smem_desc(smem_u32(b_lo));
 #pragma unroll
             for (int step = 0; step < Kp / 8; ++step) {
@@ -327,11 +368,12 @@ __global__ void __launch_bounds__(kThreads, 1) k_dense_tc(const __grid_constant_
               const uint64_t boff = ((uint32_t)(atom * Np * 128) + kin) >> 4;
 #pragma unroll
               for (int g = 0; g < G; ++g) {
-                const uint64_t aoff = ((uint32_t)(atom * Mrows * 128 + g * 128 * 128) + kin) >> 4;
-                const uint32_t d = tmem + (uint32_t)(b * kTmemCols + g * Np);
-                mma_tf32(d, dah + aoff, dbh + boff, idesc, step > 0 ? 1u : 0u);
-                mma_tf32(d, dal + aoff, dbh + boff, idesc, 1);
-                mma_tf32(d, dah + aoff, dbl + boff, idesc, 1);
+                const uint32_t d = buf + (uint32_t)(kColD + g * Np);
+                const uint32_t ah = buf + (uint32_t)(g * Kp + 8 * step);
+                const uint32_t al = buf + (uint32_t)(kColALo + g * Kp + 8 * step);
+                mma_tf32_ts(d, ah, dbh + boff, idesc, step > 0 ? 1u : 0u);
+                mma_tf32_ts(d, al, dbh + boff, idesc, 1);
+                mma_tf32_ts(d, ah, dbl + boff, idesc, 1);
               }
             }
             mma_commit(&mma_done[b]);
@@ -339,25 +381,16 @@ __global__ void __launch_bounds__(kThreads, 1) k_dense_tc(const __grid_constant_
           }
         }
         __syncwarp();
-        // staging buffer s has been read by every transform thread (the barrier above)
-        if (issued < count && issued == r + 2 && !*abort_flag) issue_load(issued++);
-        __syncwarp();
       }
     }
     if (warp == 0 && lane == 0 && *abort_flag) {
       // nothing of this CTA may still be in flight when it leaves: its loads, its last MMAs
       const uint64_t t0 = global_ns();
       auto drain = [&](uint64_t* bar, uint32_t parity) {
-        uint32_t done = 0;
-        while (!done && global_ns() - t0 < 2000000000ull)
-          asm volatile(
-              "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
-              " selp.u32 %0, 1, 0, p;\n}\n"
-              : "=r"(done)
-              : "r"(smem_u32(bar)), "r"(parity)
-              : "memory");
+        while (!mbar_test(bar, parity) && global_ns() - t0 < 2000000000ull) {
+        }
       };
-      for (uint64_t q = r; q < issued; ++q) drain(&full[q & 1], (uint32_t)(q >> 1) & 1u);
+      for (uint64_t q = r; q < issued; ++q) drain(&full[q % kStages], (uint32_t)(q / kStages) & 1u);
       if (mmas) drain(&mma_done[(mmas - 1) & 1], (uint32_t)((mmas - 1) >> 1) & 1u);
       atomicExch(p.err, 1);
     }
@@ -380,8 +413,8 @@ __global__ void __launch_bounds__(kThreads, 1) k_dense_tc(const __grid_constant_
 #pragma unroll
         for (int h = 0; h < 2; ++h) {
           float v[32];
-          // columns [32h, 32h + 32) of this buffer: block h (k = 4) or outputs 16h..16h+15 (k = 5)
-          tmem_ld32(tmem + ((uint32_t)(32 * (warp - 4)) << 16) + (uint32_t)(b * kTmemCols + 32 * h), v);
+          // columns kColD + [32h, 32h + 32): block h (k = 4) or outputs 16h..16h+15 (k = 5)
+          tmem_ld32(tmem + lane_base + (uint32_t)(b * kTmemBufCols + kColD + 32 * h), v);
           float2* dst = p.state + tb + (G == 2 ? c_off[h] : c_off[0]);
           const int r0 = (G == 2) ? 0 : 16 * h;
 #pragma unroll
@@ -393,7 +426,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_dense_tc(const __grid_constant_
         *abort_flag = 1;
         break;
       }
-      if (gtid == 0)
+      if (tid == kGroup)
         asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(&tmem_free[b])) : "memory");
     }
   }
@@ -401,13 +434,12 @@ __global__ void __launch_bounds__(kThreads, 1) k_dense_tc(const __grid_constant_
   __syncthreads();
   if (warp == 0) {
     tc_fence_after();
-    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(2 * kTmemCols)
-                 : "memory");
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(kTmemCols) : "memory");
   }
 }
 
 size_t dense_tc_smem_bytes() {
-  return 1024 + 4 * kAHalfBytes + 2 * kBHalfBytes + 2 * kStageBytes + 6 * 8 + 32 * 8 + 8 + 8;
+  return 1024 + 2 * kBHalfBytes + kStages * kStageBytes + (kStages + 4) * 8 + 32 * 8 + 8 + 8;
 }
 
 }  // namespace
@@ -416,18 +448,24 @@ bool dense_tc_eligible(int n, int dk) { return dk >= 1 && dk <= 5 && n >= kTileB
 
 // The block's real form for the kernel: a 2^k x 2^k complex block (row-major, (re, im)
 // per entry; bit b of a row or column index is absolute bit pos[b]) widened to
-// k_eff = max(k, 4) target bits with the identity on the lowest other bits, then
+// k_eff = max(k, 4) target bits with the identity on other bits (from bit 5 up), then
 // W[(r,o),(j,i)] = [[Ur, -Ui], [Ui, Ur]] split into TF32 hi and lo parts and laid out
 // K-major with the 128-byte swizzle (N = K = 2^(k_eff+1) rows and columns).
 // Returns the widened target bits in tbits_out (ascending) and the floats in w_out.
 int dense_tc_prepare(int n, int dk, const int* pos, const double* mat, std::vector<float>* w_out, int* tbits_out) {
   int tb[5], ke = dk;
   for (int i = 0; i < dk; ++i) tb[i] = pos[i];
-  // widen with the lowest bits not already targets
+  // widen with the lowest bits from bit 5 up that are not already targets: the tile's
+  // columns then keep index bits 0-4, so the 32 lanes of a warp (32 consecutive columns)
+  // read and write 32 consecutive amplitudes (widening with bits 0-2 put each lane's
+  // column eight amplitudes from the next: bank conflicts on the staging reads and
+  // scattered stores). n >= 12 leaves enough such bits; bits 0-4 are the fallback.
   uint64_t used = 0;
   for (int i = 0; i < dk; ++i) used |= 1ull << pos[i];
   std::vector<int> extra;
-  for (int b = 0; b < n && ke + (int)extra.size() < 4; ++b)
+  for (int b = 5; b < n && ke + (int)extra.size() < 4; ++b)
+    if (!(used & (1ull << b))) extra.push_back(b);
+  for (int b = 0; b < 5 && b < n && ke + (int)extra.size() < 4; ++b)
     if (!(used & (1ull << b))) extra.push_back(b);
   for (int b : extra) tb[ke++] = b;
   // sort the widened bits; perm[i] = index in the sorted order of original slot i

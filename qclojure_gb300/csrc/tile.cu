@@ -471,9 +471,11 @@ __device__ void dense_smem(unsigned char* buf, const KOp& op, const double* dens
 // A dense 2^dk x 2^dk block in double-float: entries stored as (re.hi, re.lo, im.hi,
 // im.lo) float quads (one 16-byte entry, the same offsets as the FP64 form), each output
 // amplitude the double-float sum of its row's products with the block's columns, taken
-// in the same Gray-code order as dense_smem.
+// in the same Gray-code order as dense_smem. `raw`: the tile is still in the format the
+// pass loaded (IEEE doubles unless the previous pass handed over float pairs); the
+// result is always in the float-pair working format.
 template <class P>
-__device__ void dense_df(unsigned char* buf, const KOp& op, const double* dense, const TileGeo& g) {
+__device__ void dense_df(unsigned char* buf, const KOp& op, const double* dense, const TileGeo& g, bool raw) {
   const int dk = (int)op.tmask, D = 1 << dk;
   const uint32_t dbits = op.rmr;  // 4 bits per block bit
   constexpr int kMaxItems = 16;
@@ -491,7 +493,7 @@ __device__ void dense_df(unsigned char* buf, const KOp& op, const double* dense,
       if (i) lc ^= 1u << ((dbits >> (4 * (__ffs(i) - 1))) & 15);
       const int e = row * D + (i ^ (i >> 1));
       const float4 m = __ldg(reinterpret_cast<const float4*>(dense) + op.tval + e);
-      const dfc x = P::load_work(buf, swz<16>(lc));
+      const dfc x = raw ? P::load_raw(buf, swz<16>(lc)) : P::load_work(buf, swz<16>(lc));
       const dfc pr = cmul_df(m.x, m.y, m.z, m.w, x);
       add2(acc.rh, acc.rl, pr.rh, pr.rl, acc.rh, acc.rl);
       add2(acc.ih, acc.il, pr.ih, pr.il, acc.ih, acc.il);
@@ -575,8 +577,12 @@ __device__ void run_ops(unsigned char* buf, const KOp* __restrict__ sops, int no
         __syncthreads();
       }
       if constexpr (P::kDense) {
-        if constexpr (P::kDF) dense_df<P>(buf, op, dense, g);
-        else dense_smem<P>(buf, op, dense, g);
+        if constexpr (P::kDF) {
+          dense_df<P>(buf, op, dense, g, raw);
+          raw = false;
+        } else {
+          dense_smem<P>(buf, op, dense, g);
+        }
       }
       continue;
     }
@@ -633,8 +639,15 @@ __device__ void run_ops(unsigned char* buf, const KOp* __restrict__ sops, int no
   if (in_regs) {
 #pragma unroll
     for (int j = 0; j < kRegs; ++j) P::store_raw(buf, pos[j], r[j]);
+  } else if (!raw) {
+    if constexpr (P::kDF && !P::kOutPairs) {  // a dense block left float pairs: to IEEE doubles
+      for (int l = threadIdx.x; l < g.K; l += g.T) {
+        const int p = swz<E>(l);
+        P::store_raw(buf, p, P::load_work(buf, p));
+      }
+    }
   } else if constexpr (P::kInPairs != P::kOutPairs) {
-    if (raw) {  // no op loaded the tile: convert it in place (each thread its own slots)
+    {  // no op loaded the tile: convert it in place (each thread its own slots)
       for (int l = threadIdx.x; l < g.K; l += g.T) {
         const int p = swz<E>(l);
         P::store_raw(buf, p, P::load_raw(buf, p));
