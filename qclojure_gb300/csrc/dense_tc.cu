@@ -42,7 +42,7 @@ namespace {
 
 constexpr int kTileBits = 12;           // 4096 amplitudes (32 KiB of complex64) per tile
 constexpr int kTileAmps = 1 << kTileBits;
-constexpr int kThreads = 256;
+constexpr int kThreads = 320;           // transform warps 0-3, epilogue 4-7, loads 8, MMA 9
 constexpr int kStageBytes = kTileAmps * 8;
 constexpr int kStages = 6;              // staging buffers: tiles whose loads may be in flight
 constexpr int kBHalfBytes = 16384;      // one of B hi / B lo at k = 5 (64 x 64 TF32)
@@ -98,17 +98,6 @@ __device__ __forceinline__ void bulk_g2s(void* dst, const void* src, uint32_t by
                    smem_u32(dst)),
                "l"(src), "r"(bytes), "r"(smem_u32(bar))
                : "memory");
-}
-// Named barrier `id` over `count` threads that also ANDs a flag across them: every
-// thread gets the same answer, so a group leaves a loop together.
-__device__ __forceinline__ bool bar_and(int id, int count, bool v) {
-  uint32_t r;
-  asm volatile(
-      "{\n .reg .pred p, q;\n setp.ne.u32 q, %2, 0;\n bar.red.and.pred p, %1, %3, q;\n selp.u32 %0, 1, 0, p;\n}\n"
-      : "=r"(r)
-      : "r"(id), "r"((uint32_t)v), "r"(count)
-      : "memory");
-  return r != 0;
 }
 __device__ __forceinline__ void fence_proxy_async() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
 __device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
@@ -189,20 +178,26 @@ __device__ __forceinline__ uint64_t tile_base(const DenseTcParams& p, uint64_t t
   return b;
 }
 
-// The tile's work is a pipeline over two groups of four warps, so the phases of
-// consecutive tiles overlap:
-//   transform warps (0-3): wait for tile r's bulk load (issued up to six tiles ahead),
-//     split each column's amplitudes into TF32 hi / lo and store them as rows of A in
-//     tensor-memory buffer r % 2 (once the MMAs of tile r - 2 have read it); then warp
-//     0 refills the staging buffer tile r has left with tile r + 6 and issues tile r's
-//     MMAs (once the epilogue of tile r - 2 has read that buffer's accumulators);
-//   epilogue warps (4-7): wait for tile r's MMAs, read its accumulators and store the
-//     amplitudes straight to HBM (lane c holds column c: consecutive lanes write
-//     consecutive amplitudes when the low index bits are column bits), then release
-//     the tensor-memory buffer.
-// Warp w of either group reaches tensor-memory lanes 32w .. 32w + 31, the rows it owns.
-// Waits are on mbarriers, each bounded; a group that gives up raises a shared abort
-// flag, which ends the other group's waits at once.
+// The tile's work is a pipeline over four warp roles, each waiting only for its own
+// inputs, so the phases of consecutive tiles overlap:
+//   load warp (8): refills staging buffer r % 6 with tile r once the transform of tile
+//     r - 6 has read it (mbarrier `empty`), by bulk copies completing on `full`;
+//   transform warps (0-3): wait for tile r's bytes, split each column's amplitudes into
+//     TF32 hi / lo and store them as rows of A in tensor-memory buffer r % 2 (once the
+//     MMAs of tile r - 2 have read it, `mma_done`), then release the staging buffer
+//     (`empty`) and announce A (`a_full`);
+//   MMA warp (9): one thread issues tile r's MMAs into buffer r % 2 once A is there and
+//     the epilogue of tile r - 2 has read that buffer's accumulators (`tmem_free`), and
+//     commits them to `mma_done`;
+//   epilogue warps (4-7): wait for tile r's MMAs, read its accumulators, release the
+//     buffer (`tmem_free`) and store the amplitudes straight to HBM (lane c holds
+//     column c: consecutive lanes write consecutive amplitudes when the low index bits
+//     are column bits).
+// Warp w of the transform or epilogue group reaches tensor-memory lanes 32w .. 32w + 31,
+// the rows it owns. Every wait is bounded; a warp that gives up raises a shared abort
+// flag, which ends every other wait at once, and the load and MMA warps then wait
+// (again bounded) for their copies and MMAs in flight before the CTA frees its tensor
+// memory. Decisions that lead to a warp-collective instruction are made warp-uniform.
 template <int KB>
 __global__ void __launch_bounds__(kThreads, 1) k_dense_tc(const __grid_constant__ DenseTcParams p) {
   extern __shared__ __align__(1024) unsigned char smem_raw[];
@@ -211,7 +206,6 @@ __global__ void __launch_bounds__(kThreads, 1) k_dense_tc(const __grid_constant_
   constexpr int Np = Kp;                   // reals per output column (N of the GEMM)
   constexpr int G = (KB == 4) ? 2 : 1;     // 128-column MMA blocks per tile
   constexpr uint32_t idesc = idesc_tf32(Np);
-  constexpr int kGroup = kThreads / 2;     // threads per group
   static_assert(G * Kp == kColALo && 2 * G * Kp == kColD && kColD + G * Np <= kTmemBufCols, "tensor memory map");
   // 1024-aligned regions: B hi, B lo, the staging buffers, then the barriers and tables
   unsigned char* base = smem_raw + ((1024u - (smem_u32(smem_raw) & 1023u)) & 1023u);
@@ -219,31 +213,42 @@ __global__ void __launch_bounds__(kThreads, 1) k_dense_tc(const __grid_constant_
   unsigned char* b_lo = b_hi + kBHalfBytes;
   unsigned char* stage = b_lo + kBHalfBytes;
   uint64_t* full = reinterpret_cast<uint64_t*>(stage + kStages * kStageBytes);  // [kStages]
-  uint64_t* mma_done = full + kStages;                                          // [2]
+  uint64_t* empty = full + kStages;                                             // [kStages]
+  uint64_t* a_full = empty + kStages;                                           // [2]
+  uint64_t* mma_done = a_full + 2;                                              // [2]
   uint64_t* tmem_free = mma_done + 2;                                           // [2]
   uint64_t* r_off = tmem_free + 2;                                              // [32]
-  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(r_off + 32);
+  uint32_t* jpos = reinterpret_cast<uint32_t*>(r_off + 32);                     // [32]
+  uint32_t* tmem_slot = jpos + 32;
   volatile int* abort_flag = reinterpret_cast<volatile int*>(tmem_slot + 1);
 
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-  const bool transform = tid < kGroup;
 
   // the block's real form, hi and lo, already laid out by the host
   for (int i = tid * 4; i < p.bbytes / 4; i += kThreads * 4) {
     *reinterpret_cast<float4*>(b_hi + 4 * i) = *reinterpret_cast<const float4*>(p.w + i);
     *reinterpret_cast<float4*>(b_lo + 4 * i) = *reinterpret_cast<const float4*>(p.w + p.bbytes / 4 + i);
   }
-  if (tid < D) {  // amplitude offset of target combination r inside a tile
+  if (tid < D) {  // target combination j = tid inside a tile: amplitude offset, tile position
     uint64_t o = 0;
+    uint32_t pos = 0;
     for (int t = 0; t < kTileBits; ++t)
-      if (p.tgt_of[t] >= 0 && ((tid >> p.tgt_of[t]) & 1)) o |= 1ull << p.tbit[t];
+      if (p.tgt_of[t] >= 0 && ((tid >> p.tgt_of[t]) & 1)) {
+        o |= 1ull << p.tbit[t];
+        pos |= 1u << t;
+      }
     r_off[tid] = o;
+    jpos[tid] = pos;
   }
   if (tid == 0) {
-    for (int q = 0; q < kStages; ++q) mbar_init(&full[q], 1);
+    for (int q = 0; q < kStages; ++q) {
+      mbar_init(&full[q], 1);
+      mbar_init(&empty[q], 4);
+    }
     for (int q = 0; q < 2; ++q) {
+      mbar_init(&a_full[q], 4);
       mbar_init(&mma_done[q], 1);
-      mbar_init(&tmem_free[q], 1);
+      mbar_init(&tmem_free[q], 4);
     }
     *abort_flag = 0;
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
@@ -262,7 +267,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_dense_tc(const __grid_constant_
 
   const uint64_t t_begin = p.ntiles * blockIdx.x / gridDim.x, t_end = p.ntiles * (blockIdx.x + 1) / gridDim.x;
   const uint64_t count = t_end - t_begin;
-  // a bounded wait that also ends when the other group gave up
+  // a bounded wait that also ends when another warp gave up
   auto wait = [&](uint64_t* bar, uint32_t parity) {
     uint64_t t0 = 0;
     for (uint32_t it = 0;; ++it) {
@@ -278,12 +283,18 @@ __global__ void __launch_bounds__(kThreads, 1) k_dense_tc(const __grid_constant_
       }
     }
   };
+  // the same wait, made by every lane, agreed across the warp
+  auto wait_warp = [&](uint64_t* bar, uint32_t parity) { return __all_sync(0xffffffffu, wait(bar, parity)) != 0; };
+  auto arrive = [&](uint64_t* bar) {
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
+  };
   const uint32_t lane_base = (uint32_t)(32 * (warp & 3)) << 16;  // this warp's tensor-memory lanes
+  uint64_t issued = 0, mmas = 0;  // load warp: tiles whose copies it issued; MMA thread: tiles committed
 
-  if (transform) {
-    // tile positions of this thread's columns c = 128 g + 32 warp + lane, and of the
-    // target combinations j (the same in every tile)
-    uint32_t cpos[G], jpos[D];
+  if (warp < 4) {
+    // ---- transform: tile positions of this thread's columns c = 128 g + 32 warp + lane
+    // (the same in every tile; those of the target combinations are the table jpos)
+    uint32_t cpos[G];
 #pragma unroll
     for (int g = 0; g < G; ++g) {
       const int c = 128 * g + 32 * warp + lane;
@@ -292,110 +303,40 @@ __global__ void __launch_bounds__(kThreads, 1) k_dense_tc(const __grid_constant_
         if (p.col_of[t] >= 0 && ((c >> p.col_of[t]) & 1)) pos |= 1u << t;
       cpos[g] = pos;
     }
-#pragma unroll
-    for (int j = 0; j < D; ++j) {
-      uint32_t pos = 0;
-      for (int t = 0; t < kTileBits; ++t)
-        if (p.tgt_of[t] >= 0 && ((j >> p.tgt_of[t]) & 1)) pos |= 1u << t;
-      jpos[j] = pos;
-    }
-    const int nrun = 1 << (kTileBits - p.runbits);  // at most 32: runs are at least 2^7 amplitudes
-    const uint32_t run_bytes = (uint32_t)(8u << p.runbits);
-    uint64_t run_off = 0;
-    if (warp == 0 && lane < nrun)
-      for (int b = p.runbits; b < kTileBits; ++b)
-        if ((lane >> (b - p.runbits)) & 1) run_off |= 1ull << p.tbit[b];
-    auto issue_load = [&](uint64_t r) {  // warp 0: tile r into staging buffer r % kStages
-      const int s = (int)(r % kStages);
-      if (lane == 0) mbar_expect_tx(&full[s], (uint32_t)kStageBytes);
-      __syncwarp();
-      const uint64_t tb = tile_base(p, t_begin + r);
-      if (lane < nrun)
-        bulk_g2s(stage + s * kStageBytes + (size_t)lane * run_bytes, p.state + tb + run_off, run_bytes, &full[s]);
-    };
-    uint64_t issued = 0, mmas = 0;
-    if (warp == 0)
-      for (; issued < (uint64_t)kStages && issued < count; ++issued) issue_load(issued);
-    uint64_t r = 0;
-    for (; r < count; ++r) {
+    for (uint64_t r = 0; r < count; ++r) {
       const int s = (int)(r % kStages), b = (int)(r & 1);
-      bool ok = wait(&full[s], (uint32_t)(r / kStages) & 1u);
-      if (ok && r >= 2) ok = wait(&mma_done[b], (uint32_t)((r - 2) >> 1) & 1u);  // A buffer b is read
-      if (ok) {
-        tc_fence_after();
-        const float2* st = reinterpret_cast<const float2*>(stage + s * kStageBytes);
-        const uint32_t abuf = tmem + lane_base + (uint32_t)(b * kTmemBufCols);
+      if (!wait_warp(&full[s], (uint32_t)(r / kStages) & 1u)) break;
+      if (r >= 2 && !wait_warp(&mma_done[b], (uint32_t)((r - 2) >> 1) & 1u)) break;  // A buffer b is read
+      tc_fence_after();
+      const float2* st = reinterpret_cast<const float2*>(stage + s * kStageBytes);
+      const uint32_t abuf = tmem + lane_base + (uint32_t)(b * kTmemBufCols);
 #pragma unroll
-        for (int g = 0; g < G; ++g) {
+      for (int g = 0; g < G; ++g) {
 #pragma unroll
-          for (int ch = 0; ch < Kp / 16; ++ch) {  // amplitudes j = 8 ch .. 8 ch + 7 of column c
-            float hv[16], lv[16];
+        for (int ch = 0; ch < Kp / 16; ++ch) {  // amplitudes j = 8 ch .. 8 ch + 7 of column c
+          float hv[16], lv[16];
 #pragma unroll
-            for (int q = 0; q < 8; ++q) {
-              const float2 x = st[cpos[g] | jpos[8 * ch + q]];
-              const float hr = to_tf32(x.x), hi_ = to_tf32(x.y);
-              hv[2 * q] = hr;
-              hv[2 * q + 1] = hi_;
-              lv[2 * q] = to_tf32(x.x - hr);
-              lv[2 * q + 1] = to_tf32(x.y - hi_);
-            }
-            tmem_st16(abuf + (uint32_t)(g * Kp + 16 * ch), hv);
-            tmem_st16(abuf + (uint32_t)(kColALo + g * Kp + 16 * ch), lv);
+          for (int q = 0; q < 8; ++q) {
+            const float2 x = st[cpos[g] | jpos[8 * ch + q]];
+            const float hr = to_tf32(x.x), hi_ = to_tf32(x.y);
+            hv[2 * q] = hr;
+            hv[2 * q + 1] = hi_;
+            lv[2 * q] = to_tf32(x.x - hr);
+            lv[2 * q + 1] = to_tf32(x.y - hi_);
           }
+          tmem_st16(abuf + (uint32_t)(g * Kp + 16 * ch), hv);
+          tmem_st16(abuf + (uint32_t)(kColALo + g * Kp + 16 * ch), lv);
         }
-        asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory");
-        tc_fence_before();
       }
-      // the whole group goes on only if every thread got here and nothing gave up
-      if (!bar_and(1, kGroup, ok && !*abort_flag)) {
-        *abort_flag = 1;
-        break;
-      }
-      if (warp == 0) {
-        // staging buffer s has been read by every transform thread (the barrier above)
-        if (issued < count && issued == r + kStages) issue_load(issued++);
-        __syncwarp();
-        if (lane == 0) {
-          const bool tok = r < 2 || wait(&tmem_free[b], (uint32_t)((r - 2) >> 1) & 1u);  // D of buffer b is read
-          if (tok) {
-            tc_fence_after();
-            const uint32_t buf = tmem + (uint32_t)(b * kTmemBufCols);
-            const uint64_t dbh = smem_desc(smem_u32(b_hi)), dbl = smem_desc(smem_u32(b_lo));
-#pragma unroll
-            for (int step = 0; step < Kp / 8; ++step) {
-              const int atom = step >> 2;
-              const uint32_t kin = (uint32_t)(step & 3) * 32u;
-              const uint64_t boff = ((uint32_t)(atom * Np * 128) + kin) >> 4;
-#pragma unroll
-              for (int g = 0; g < G; ++g) {
-                const uint32_t d = buf + (uint32_t)(kColD + g * Np);
-                const uint32_t ah = buf + (uint32_t)(g * Kp + 8 * step);
-                const uint32_t al = buf + (uint32_t)(kColALo + g * Kp + 8 * step);
-                mma_tf32_ts(d, ah, dbh + boff, idesc, step > 0 ? 1u : 0u);
-                mma_tf32_ts(d, al, dbh + boff, idesc, 1);
-                mma_tf32_ts(d, ah, dbl + boff, idesc, 1);
-              }
-            }
-            mma_commit(&mma_done[b]);
-            ++mmas;
-          }
-        }
-        __syncwarp();
-      }
+      __syncwarp();
+      if (lane == 0) arrive(&empty[s]);  // this warp's reads of the staging buffer are done
+      asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory");
+      tc_fence_before();
+      __syncwarp();
+      if (lane == 0) arrive(&a_full[b]);
     }
-    if (warp == 0 && lane == 0 && *abort_flag) {
-      // nothing of this CTA may still be in flight when it leaves: its loads, its last MMAs
-      const uint64_t t0 = global_ns();
-      auto drain = [&](uint64_t* bar, uint32_t parity) {
-        while (!mbar_test(bar, parity) && global_ns() - t0 < 2000000000ull) {
-        }
-      };
-      for (uint64_t q = r; q < issued; ++q) drain(&full[q % kStages], (uint32_t)(q / kStages) & 1u);
-      if (mmas) drain(&mma_done[(mmas - 1) & 1], (uint32_t)((mmas - 1) >> 1) & 1u);
-      atomicExch(p.err, 1);
-    }
-  } else {
-    // epilogue: lane row = 32 * (warp - 4) + lane of each 128-column block
+  } else if (warp < 8) {
+    // ---- epilogue: lane row = 32 * (warp - 4) + lane of each 128-column block
     const int row = 32 * (warp - 4) + lane;
     uint64_t c_off[2] = {0, 0};
 #pragma unroll
@@ -406,29 +347,87 @@ __global__ void __launch_bounds__(kThreads, 1) k_dense_tc(const __grid_constant_
     }
     for (uint64_t r = 0; r < count; ++r) {
       const int b = (int)(r & 1);
-      const bool ok = wait(&mma_done[b], (uint32_t)(r >> 1) & 1u);
-      if (ok) {
-        tc_fence_after();
-        const uint64_t tb = tile_base(p, t_begin + r);
+      if (!wait_warp(&mma_done[b], (uint32_t)(r >> 1) & 1u)) break;
+      tc_fence_after();
+      const uint64_t tb = tile_base(p, t_begin + r);
 #pragma unroll
-        for (int h = 0; h < 2; ++h) {
-          float v[32];
-          // columns kColD + [32h, 32h + 32): block h (k = 4) or outputs 16h..16h+15 (k = 5)
-          tmem_ld32(tmem + lane_base + (uint32_t)(b * kTmemBufCols + kColD + 32 * h), v);
-          float2* dst = p.state + tb + (G == 2 ? c_off[h] : c_off[0]);
-          const int r0 = (G == 2) ? 0 : 16 * h;
-#pragma unroll
-          for (int q = 0; q < 16; ++q) dst[r_off[r0 + q]] = make_float2(v[2 * q], v[2 * q + 1]);
+      for (int h = 0; h < 2; ++h) {
+        float v[32];
+        // columns kColD + [32h, 32h + 32): block h (k = 4) or outputs 16h..16h+15 (k = 5)
+        tmem_ld32(tmem + lane_base + (uint32_t)(b * kTmemBufCols + kColD + 32 * h), v);
+        if (h == 1) {  // every accumulator of the buffer is in registers: release it
+          tc_fence_before();
+          __syncwarp();
+          if (lane == 0) arrive(&tmem_free[b]);
         }
-        tc_fence_before();
+        float2* dst = p.state + tb + (G == 2 ? c_off[h] : c_off[0]);
+        const int r0 = (G == 2) ? 0 : 16 * h;
+#pragma unroll
+        for (int q = 0; q < 16; ++q) dst[r_off[r0 + q]] = make_float2(v[2 * q], v[2 * q + 1]);
       }
-      if (!bar_and(2, kGroup, ok && !*abort_flag)) {
-        *abort_flag = 1;
-        break;
-      }
-      if (tid == kGroup)
-        asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(&tmem_free[b])) : "memory");
     }
+  } else if (warp == 8) {
+    // ---- loads: warp 8's lanes move one run each
+    const int nrun = 1 << (kTileBits - p.runbits);  // at most 32: runs are at least 2^7 amplitudes
+    const uint32_t run_bytes = (uint32_t)(8u << p.runbits);
+    uint64_t run_off = 0;
+    if (lane < nrun)
+      for (int bb = p.runbits; bb < kTileBits; ++bb)
+        if ((lane >> (bb - p.runbits)) & 1) run_off |= 1ull << p.tbit[bb];
+    for (; issued < count; ++issued) {
+      const int s = (int)(issued % kStages);
+      if (issued >= (uint64_t)kStages && !wait_warp(&empty[s], (uint32_t)(issued / kStages - 1) & 1u)) break;
+      if (lane == 0) mbar_expect_tx(&full[s], (uint32_t)kStageBytes);
+      __syncwarp();
+      const uint64_t tb = tile_base(p, t_begin + issued);
+      if (lane < nrun)
+        bulk_g2s(stage + s * kStageBytes + (size_t)lane * run_bytes, p.state + tb + run_off, run_bytes, &full[s]);
+    }
+  } else {
+    // ---- MMA issue: lane 0 of warp 9
+    if (lane == 0) {
+      const uint64_t dbh = smem_desc(smem_u32(b_hi)), dbl = smem_desc(smem_u32(b_lo));
+      for (uint64_t r = 0; r < count; ++r) {
+        const int b = (int)(r & 1);
+        if (!wait(&a_full[b], (uint32_t)(r >> 1) & 1u)) break;
+        if (r >= 2 && !wait(&tmem_free[b], (uint32_t)((r - 2) >> 1) & 1u)) break;  // D of buffer b is read
+        tc_fence_after();
+        const uint32_t buf = tmem + (uint32_t)(b * kTmemBufCols);
+#pragma unroll
+        for (int step = 0; step < Kp / 8; ++step) {
+          const int atom = step >> 2;
+          const uint32_t kin = (uint32_t)(step & 3) * 32u;
+          const uint64_t boff = ((uint32_t)(atom * Np * 128) + kin) >> 4;
+#pragma unroll
+          for (int g = 0; g < G; ++g) {
+            const uint32_t d = buf + (uint32_t)(kColD + g * Np);
+            const uint32_t ah = buf + (uint32_t)(g * Kp + 8 * step);
+            const uint32_t al = buf + (uint32_t)(kColALo + g * Kp + 8 * step);
+            mma_tf32_ts(d, ah, dbh + boff, idesc, step > 0 ? 1u : 0u);
+            mma_tf32_ts(d, al, dbh + boff, idesc, 1);
+            mma_tf32_ts(d, ah, dbl + boff, idesc, 1);
+          }
+        }
+        mma_commit(&mma_done[b]);
+        ++mmas;
+      }
+    }
+    __syncwarp();
+  }
+  __syncthreads();  // every role has left its loop
+  if (*abort_flag) {
+    // nothing of this CTA may still be in flight when it frees its memory: the last bulk
+    // copies issued (they land whether or not a transform consumed them) and the last MMAs
+    const uint64_t t0 = global_ns();
+    if (warp == 8 && lane == 0)
+      for (uint64_t q = issued > (uint64_t)kStages ? issued - kStages : 0; q < issued; ++q)
+        while (!mbar_test(&full[q % kStages], (uint32_t)(q / kStages) & 1u) && global_ns() - t0 < 2000000000ull) {
+        }
+    if (warp == 9 && lane == 0 && mmas)
+      while (!mbar_test(&mma_done[(mmas - 1) & 1], (uint32_t)((mmas - 1) >> 1) & 1u) &&
+             global_ns() - t0 < 2000000000ull) {
+      }
+    if (tid == 0) atomicExch(p.err, 1);
   }
   tc_fence_before();
   __syncthreads();
@@ -439,7 +438,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_dense_tc(const __grid_constant_
 }
 
 size_t dense_tc_smem_bytes() {
-  return 1024 + 2 * kBHalfBytes + kStages * kStageBytes + (kStages + 4) * 8 + 32 * 8 + 8 + 8;
+  return 1024 + 2 * kBHalfBytes + kStages * kStageBytes + (2 * kStages + 6) * 8 + 32 * 8 + 32 * 4 + 8 + 8;
 }
 
 }  // namespace
