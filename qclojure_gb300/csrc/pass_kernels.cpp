@@ -396,6 +396,51 @@ class PassGen {
   }
   int carry_ = 0;
 
+  // Conditional X gates on register bits are not applied to the registers: a runtime
+  // mask xm records them (register p holds the amplitude of logical register p ^ xm),
+  // and the next store to shared memory puts register p at the slot of p ^ xm, which is
+  // its slot XOR swz(deposit of xm at the register bit positions), the swizzle being
+  // linear over XOR. pend_: the register bits xm may have set; rpos_: their positions in
+  // the tile index under the current layout. An op that depends on a pending bit
+  // (targets it, is conditioned on it or selects registers by it) first applies those
+  // bits as conditional swaps (materialise).
+  uint32_t pend_ = 0;
+  int rpos_[4] = {0, 0, 0, 0};
+
+  void materialise(uint32_t bits) {
+    bits &= pend_;
+    if (!bits) return;
+    const std::string T = df_ ? "dfc" : "float2";
+    for (int bb = 0; bb < sh_.rbits; ++bb) {
+      if (!((bits >> bb) & 1)) continue;
+      o_ << "    if (xm & " << (1u << bb) << "u) {  // pending X on register bit " << bb << "\n";
+      for (int j = 0; j < ns_; ++j) {
+        if ((j >> bb) & 1) continue;
+        const int k = j | (1 << bb);
+        o_ << "      { const " << T << " y = " << r(j) << "; " << r(j) << " = " << r(k) << "; " << r(k) << " = y; }\n";
+        if (df_) since_[j] = since_[k] = std::max(since_[j], since_[k]);
+      }
+      o_ << "    }\n";
+    }
+    o_ << "    xm &= " << hex32(~bits & 0xFFu) << ";\n";
+    pend_ &= ~bits;
+  }
+  // register p goes to the slot of logical register p ^ xm
+  void store_regs(const std::string& fn) {
+    if (!pend_) {
+      for (int j = 0; j < ns_; ++j) o_ << "    " << fn << "(buf, q" << j << ", r" << j << ");\n";
+      return;
+    }
+    const int E = df_ ? 16 : 8;
+    o_ << "    { const int xo = swz<" << E << ">((int)(0u";
+    for (int bb = 0; bb < sh_.rbits; ++bb)
+      if ((pend_ >> bb) & 1) o_ << " | (((xm >> " << bb << ") & 1u) << " << rpos_[bb] << ")";
+    o_ << "));\n";
+    for (int j = 0; j < ns_; ++j) o_ << "      " << fn << "(buf, q" << j << " ^ xo, r" << j << ");\n";
+    o_ << "    }\n    xm = 0u;\n";
+    pend_ = 0;
+  }
+
   const char* pol() const { return df_ ? "DF" : "F32"; }
   std::string ld_raw() const { return df_ && !(io_ & kTileInPairs) ? "DF::ld_doubles" : std::string(pol()) + "::ld_work"; }
   std::string st_raw() const { return df_ && !(io_ & kTileOutPairs) ? "DF::st_doubles" : std::string(pol()) + "::st_work"; }
@@ -425,6 +470,13 @@ class PassGen {
   }
 
   std::string cmul(const TOp& t, int qr, int qi, const std::string& x) const {
+    const float rh = t.mf[qr], rl = t.mf[8 + qr], ih = t.mf[qi], il = t.mf[8 + qi];
+    const bool same = ih == rh && il == rl, opp = ih == -rh && il == -rl;
+    if (df_ && !tab_ && rh != 0.0f && (same || opp)) {
+      // (a + i a) or (a - i a): both parts of the constant the same pair up to sign
+      const bool neg = !same;
+      return "df_cmul_diag<" + b(lo_nz(t, qr)) + ", " + b(neg) + ">(" + h(t, qr) + ", " + l(t, qr) + ", " + x + ")";
+    }
     if (df_)
       return "df_cmul<" + b(lo_nz(t, qr)) + ", " + b(lo_nz(t, qi)) + ">(" + h(t, qr) + ", " + l(t, qr) +
              ", " + h(t, qi) + ", " + l(t, qi) + ", " + x + ")";
@@ -515,12 +567,72 @@ class PassGen {
 
   static std::string r(int j) { return "r" + std::to_string(j); }
 
+  // A unit rotation ([[1, b], [c, 1]] real, or [[1, i b], [i c, 1]]) on register bit rp
+  // while an X of that bit is pending in xm: threads with the X apply b and c exchanged.
+  void u2_unit_conj(const TOp& t, int rp, const std::string& c) {
+    const bool rx = t.cls == U2_RXLIKE;
+    const int qb = rx ? 3 : 2, qc = rx ? 5 : 4;
+    const bool same = !tab_ && t.mf[qb] == t.mf[qc] && (!df_ || t.mf[8 + qb] == t.mf[8 + qc]);
+    const bool lb = lo_nz(t, qb) || lo_nz(t, qc);
+    o_ << "    {  // U2 class " << t.cls << " on register bit " << rp << ", pending X" << (same ? " (symmetric)" : "")
+       << "\n";
+    std::string Bh = h(t, qb), Ch = h(t, qc), Bl = df_ ? l(t, qb) : "", Cl = df_ ? l(t, qc) : "";
+    if (!same) {
+      o_ << "      const bool sw = ((xm >> " << rp << ") & 1u) != 0u;\n";
+      o_ << "      const float Bh = sw ? " << Ch << " : " << Bh << ", Ch = sw ? " << Bh << " : " << Ch << ";\n";
+      if (df_) o_ << "      const float Bl = sw ? " << Cl << " : " << Bl << ", Cl = sw ? " << Bl << " : " << Cl << ";\n";
+      Bh = "Bh";
+      Ch = "Ch";
+      Bl = "Bl";
+      Cl = "Cl";
+    }
+    if (!c.empty()) o_ << "    if (" << c << ") {\n";
+    std::vector<int> done;
+    for (int q = 0; q < ns_ / 2; ++q) {
+      const int j0 = ((q >> rp) << (rp + 1)) | (q & ((1 << rp) - 1));
+      const int j1 = j0 | (1 << rp);
+      if (df_) {
+        if (rx)
+          o_ << "      df_rxunit<" << b(lb) << ", " << b(lb) << ">(" << Bh << ", " << Bl << ", " << Ch << ", " << Cl
+             << ", " << r(j0) << ", " << r(j1) << ");\n";
+        else
+          o_ << "      df_realunit<" << b(lb) << ", " << b(lb) << ", false>(" << Bh << ", " << Bl << ", " << Ch << ", "
+             << Cl << ", " << r(j0) << ", " << r(j1) << ");\n";
+      } else {
+        if (rx) o_ << "      f_rxunit(" << Bh << ", " << Ch << ", " << r(j0) << ", " << r(j1) << ");\n";
+        else o_ << "      f_realunit<false>(" << Bh << ", " << Ch << ", " << r(j0) << ", " << r(j1) << ");\n";
+      }
+      done.push_back(j0);
+      done.push_back(j1);
+    }
+    if (!c.empty()) o_ << "    }\n";
+    o_ << "    }\n";
+    for (int j : done) touched(j);
+  }
+
   void op(const TOp& t) {
     const uint32_t cr = t.rmask & (uint32_t)(ns_ - 1);
     switch (t.kind) {
       case OK_U2: {
         const int rp = t.t2;
         const std::string c = cond(t.gcmask, t.gcmask, t.tmask, t.tval);
+        if (t.cls == U2_X && cr == 0 && !c.empty()) {  // a conditional X on every pair: into xm
+          o_ << "    xm ^= (unsigned)(" << c << ") << " << rp << ";  // X on register bit " << rp << "\n";
+          pend_ |= 1u << rp;
+          break;
+        }
+        materialise(cr);
+        // On a pending X of its own bit: a swap is the same on either order of its pair;
+        // the unit rotations [[1, b], [c, 1]] and [[1, i b], [i c, 1]] become the same
+        // form with b and c exchanged (X U X), chosen per thread from xm; other classes
+        // apply the X first.
+        const bool unit_rot = unit_diagonal(t) && (t.cls == U2_RXLIKE || (t.cls == U2_REAL && t.m[6] > 0));
+        const bool conj = ((pend_ >> rp) & 1) && unit_rot;
+        if (t.cls != U2_X && !conj) materialise(1u << rp);
+        if (conj) {
+          u2_unit_conj(t, rp, c);
+          break;
+        }
         o_ << "    {  // U2 class " << t.cls << " on register bit " << rp << "\n";
         if (!c.empty()) o_ << "    if (" << c << ") {\n";
         std::vector<int> done;
@@ -539,6 +651,7 @@ class PassGen {
         for (int j : done) touched(j);
       } break;
       case OK_PHASE: {
+        materialise(cr);
         const std::string c = cond(t.gmask, t.gmask, t.tmask, t.tval);
         o_ << "    {  // phase class " << t.cls << "\n";
         if (!c.empty()) o_ << "    if (" << c << ") {\n";
@@ -563,6 +676,7 @@ class PassGen {
       } break;
       case OK_SWAP: {
         const int A = t.dbits[0], B = t.dbits[1];
+        materialise(cr | (1u << A) | (1u << B));
         const bool isw = (t.flags & 1) != 0;
         const std::string c = cond(t.gcmask, t.gcmask, t.tmask, t.tval);
         o_ << "    {  // swap of register bits " << A << ", " << B << (isw ? " (iSWAP)" : "") << "\n";
@@ -583,6 +697,7 @@ class PassGen {
         o_ << "    }\n";
       } break;
       case OK_BLOCKADE: {
+        materialise(cr);
         o_ << "    {  // blockade phase\n      const int cnt = __popcll(base & " << hex64(t.gmask) << ") + __popc(lt & "
            << hex32(t.tmask) << ");\n";
         for (int j = 0; j < ns_; ++j) {
@@ -595,6 +710,7 @@ class PassGen {
           if (1 - __builtin_popcount((unsigned)j & cr) >= 0) touched(j);
       } break;
       case OK_PARITY: {
+        materialise(cr);
         o_ << "    {  // parity phase\n      const bool par = ((__popcll(base & " << hex64(t.gmask) << ") + __popc(lt & "
            << hex32(t.tmask) << ")) & 1) != 0;\n";
         // even register parity takes (par ? p1 : p0), odd (par ? p0 : p1)
@@ -624,6 +740,7 @@ class PassGen {
         for (int j = 0; j < ns_; ++j) touched(j);
       } break;
       case OK_COLLAPSE: {
+        materialise(cr);
         const std::string c = cond(t.gmask, t.gval, t.tmask, t.tval);
         const uint32_t rv = t.rval & (uint32_t)(ns_ - 1);
         o_ << "    {  // collapse\n      const bool tc = " << (c.empty() ? "true" : c) << ";\n";
@@ -738,6 +855,11 @@ class PassGen {
 
   void phase_run(int begin, int end) {
     const int R = sh_.rbits;
+    {  // the run selects registers by its ops' register masks
+      uint32_t m = 0;
+      for (int i = begin; i < end; ++i) m |= ops_[i].rmask & (uint32_t)(ns_ - 1);
+      materialise(m);
+    }
     // cost of the op-by-op form: complex products
     int cost_ops = 0;
     for (int i = begin; i < end; ++i) {
@@ -850,6 +972,11 @@ class PassGen {
   int ntables_ = 0;
   void parity_run(int begin, int end) {
     const int E = end - begin;
+    {  // register parities: the ops' register masks (from the table: any register bit)
+      uint32_t m = tab_ ? (uint32_t)(ns_ - 1) : 0u;
+      for (int i = begin; i < end; ++i) m |= ops_[i].rmask & (uint32_t)(ns_ - 1);
+      materialise(m);
+    }
     o_ << "    {  // parity run of " << E << " ops\n      int";
     for (int j = 0; j < ns_; ++j) o_ << (j ? ", m" : " m") << j << " = 0";
     o_ << ";\n";
@@ -922,18 +1049,20 @@ class PassGen {
     for (int j = 0; j < ns_; ++j) o_ << (j ? ", r" : " r") << j;
     o_ << ";\n    int";
     for (int j = 0; j < ns_; ++j) o_ << (j ? ", q" : " q") << j;
-    o_ << ";\n    unsigned lt = 0;\n";
-    o_ << "    (void)lt;\n";
+    o_ << ";\n    unsigned lt = 0, xm = 0u;\n";
+    o_ << "    (void)lt; (void)xm;\n";
+    pend_ = 0;
     bool in_regs = false, raw = true;
     for (int i = 0; i < nops_; ++i) {
       const TOp& t = ops_[i];
       if (t.kind == OK_LAYOUT) {
         if (in_regs) {
           renorm_for_store();
-          for (int j = 0; j < ns_; ++j) o_ << "    " << pol() << "::st_work(buf, q" << j << ", r" << j << ");\n";
+          store_regs(std::string(pol()) + "::st_work");
           o_ << "    __syncthreads();\n";
           raw = false;
         }
+        for (int q = 0; q < sh_.rbits; ++q) rpos_[q] = t.dbits[q];
         // thread bits: zeros inserted at the register positions (ascending)
         o_ << "    lt = tid;\n";
         for (int q = 0; q < sh_.rbits; ++q) {
@@ -973,7 +1102,7 @@ class PassGen {
     }
     if (in_regs) {
       if (io_ & kTileOutPairs) renorm_for_store();  // st_doubles normalises on its own
-      for (int j = 0; j < ns_; ++j) o_ << "    " << st_raw() << "(buf, q" << j << ", r" << j << ");\n";
+      store_regs(st_raw());
     } else if (df_ && ((io_ & kTileInPairs) != 0) != ((io_ & kTileOutPairs) != 0)) {
       // no op loaded the tile: convert its storage form in place, each thread its own slots
       o_ << "    for (int l = (int)tid; l < (1 << K_BITS); l += (1 << K_BITS) >> R_BITS) {\n"

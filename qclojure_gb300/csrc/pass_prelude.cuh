@@ -137,6 +137,23 @@ __device__ __forceinline__ dfc df_cmul(float grh, float grl, float gih, float gi
   dot2<RL, IL>(grh, grl, x.ih, x.il, gih, gil, x.rh, x.rl, y.ih, y.il);
   return y;
 }
+// (a + i a) x (NEG = false) or (a - i a) x (NEG = true), a a constant pair: the sum and
+// the difference of x's parts first, then one product each (a T-gate phase)
+template <bool AL, bool NEG>
+__device__ __forceinline__ dfc df_cmul_diag(float ah, float al, const dfc& x) {
+  float dh, dl, sh, sl;
+  dfc y;
+  if (!NEG) {  // a (xr - xi) + i a (xr + xi)
+    add2(x.rh, x.rl, -x.ih, -x.il, dh, dl);
+    add2(x.rh, x.rl, x.ih, x.il, sh, sl);
+  } else {  // a (xr + xi) + i a (xi - xr)
+    add2(x.rh, x.rl, x.ih, x.il, dh, dl);
+    add2(x.ih, x.il, -x.rh, -x.rl, sh, sl);
+  }
+  tprod<AL>(ah, al, dh, dl, y.rh, y.rl);
+  tprod<AL>(ah, al, sh, sl, y.ih, y.il);
+  return y;
+}
 // a real scalar times x
 template <bool AL>
 __device__ __forceinline__ dfc df_scale(float ah, float al, const dfc& x) {
