@@ -480,6 +480,12 @@ int qg_kernel_launches(uint64_t* count);
 int qg_pass_kernels_build(const qg_circuit* circuit, int32_t precision, int32_t arithmetic, int32_t* kernels_out,
                           double* compile_ms_out, char* err_buf, int64_t err_len);
 int qg_pass_kernels_info(int32_t* available, uint64_t* cache_hits, uint64_t* cache_misses);
+/* Failure-path diagnostic (no counterpart in the reference): while on != 0, the
+   tensor-core dense-block kernel's MMA thread issues nothing, so the kernel's bounded
+   waits (about a second) run out, it frees its tensor memory and returns, and the run
+   fails with QG_ERR_DEVICE ("a bounded wait gave up"); the context stays usable.
+   Process-wide; for tests of the failure path only. */
+int qg_diag_dense_tc_stall(int32_t on);
 
 /* ---- autotuner (no counterpart in the reference; the reference's hook for gate
    optimisation is gate_optimization.clj:776-860, which this tiled executor replaces) --

@@ -31,6 +31,7 @@
 // memory and returns, and the host reports the error.
 #include <cuda_runtime.h>
 
+#include <atomic>
 #include <cstdint>
 #include <cstring>
 #include <vector>
@@ -57,6 +58,7 @@ struct DenseTcParams {
   float2* state;
   const float* w;        // B hi then B lo, already in the swizzled K-major layout (2 * bbytes)
   int* err;              // set to a nonzero code when a wait gives up
+  int stall;             // failure-path diagnostic: the MMA thread issues nothing
   uint64_t ntiles;
   int k;                 // 4 or 5
   int bbytes;            // bytes of one of B hi / B lo
@@ -384,8 +386,9 @@ __global__ void __launch_bounds__(kThreads, 1) k_dense_tc(const __grid_constant_
         bulk_g2s(stage + s * kStageBytes + (size_t)lane * run_bytes, p.state + tb + run_off, run_bytes, &full[s]);
     }
   } else {
-    // ---- MMA issue: lane 0 of warp 9
-    if (lane == 0) {
+    // ---- MMA issue: lane 0 of warp 9 (none under the failure-path diagnostic, so the
+    // epilogue's wait for tile 0 runs out)
+    if (lane == 0 && !p.stall) {
       const uint64_t dbh = smem_desc(smem_u32(b_hi)), dbl = smem_desc(smem_u32(b_lo));
       for (uint64_t r = 0; r < count; ++r) {
         const int b = (int)(r & 1);
@@ -444,6 +447,8 @@ size_t dense_tc_smem_bytes() {
 }  // namespace
 
 bool dense_tc_eligible(int n, int dk) { return dk >= 1 && dk <= 5 && n >= kTileBits; }
+
+std::atomic<int> g_dense_tc_stall{0};
 
 // The block's real form for the kernel: a 2^k x 2^k complex block (row-major, (re, im)
 // per entry; bit b of a row or column index is absolute bit pos[b]) widened to
@@ -529,6 +534,7 @@ cudaError_t launch_dense_tc(void* state, int n, int ke, const int* tbits, const 
   p.state = (float2*)state;
   p.w = d_w;
   p.err = d_err;
+  p.stall = g_dense_tc_stall.load() ? 1 : 0;
   p.k = ke;
   p.bbytes = (2 << ke) * (2 << ke) * 4;
   p.ntiles = 1ull << (n - kTileBits);

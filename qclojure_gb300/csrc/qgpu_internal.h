@@ -2,6 +2,7 @@
 // (kernels.cu) and the runtime (runtime.cpp) of libqgpu.so.
 #pragma once
 
+#include <atomic>
 #include <cstdint>
 #include <memory>
 #include <string>
@@ -356,6 +357,7 @@ cudaError_t noalloc_sample_scratch(int device, void** ptr, size_t* bytes);
 // inside the kernel gives up.
 constexpr int kDenseTcFlag = 1;  // GOp::flags of an OK_DENSE op run by launch_dense_tc
 bool dense_tc_eligible(int n, int dk);
+extern std::atomic<int> g_dense_tc_stall;  // qg_diag_dense_tc_stall
 int dense_tc_prepare(int n, int dk, const int* pos, const double* mat, std::vector<float>* w_out, int* tbits_out);
 cudaError_t launch_dense_tc(void* state, int n, int ke, const int* tbits, const float* d_w, int* d_err,
                             cudaStream_t st);

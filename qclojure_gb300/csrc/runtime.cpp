@@ -2490,6 +2490,11 @@ int qg_pass_kernels_build(const qg_circuit* circuit, int32_t precision, int32_t 
   return rc;
 }
 
+int qg_diag_dense_tc_stall(int32_t on) {
+  g_dense_tc_stall.store(on ? 1 : 0);
+  return QG_OK;
+}
+
 int qg_pass_kernels_info(int32_t* available, uint64_t* cache_hits, uint64_t* cache_misses) {
   if (available) *available = pass_kernels_unavailable() ? 0 : 1;
   size_t h = 0, m = 0;

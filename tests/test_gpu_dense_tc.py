@@ -87,3 +87,36 @@ def test_two_calls_and_small_states(oracle):
     small = workloads.layered_circuit(9, 4, seed=6)
     kinds = _check(oracle, small, 5, expect_tc=False)
     assert not (kinds == TC_PASS).any()
+
+
+def test_bounded_wait_gives_up_and_the_context_survives(oracle):
+    """Failure path without a GPU fault: with the diagnostic switch on, the kernel's MMA
+    thread issues nothing, so the epilogue's bounded wait for the first tile runs out
+    (about a second); the kernel drains its bulk copies, frees its tensor memory and
+    returns, the run fails with a device error naming the wait, and the same context
+    then applies the block correctly."""
+    from qclojure_gb300 import _abi as A
+    from qclojure_gb300.state import Context
+
+    lib = A.load_library()
+    n = 14
+    c = {"num-qubits": n, "operations": _on_qubits(n, [3, 9, 10, 11], 16, seed=77)}
+    ref = oracle.run(c)
+    with Context(fusion="dense", fusion_width=4) as ctx:
+        with ctx.state(n, "c64") as st:
+            st.set_basis(0)
+            _, kinds = st.profile(c, fusion="dense")
+            assert 1 <= (kinds == TC_PASS).sum() <= 2, kinds  # one block: about a second per stalled pass
+            st.set_basis(0)
+            assert lib.qg_diag_dense_tc_stall(1) == 0
+            try:
+                with pytest.raises(A.QgError, match="bounded wait") as ei:
+                    st.apply(c, fusion="dense")
+                assert ei.value.code == A.QG_ERR_DEVICE
+            finally:
+                lib.qg_diag_dense_tc_stall(0)
+            st.set_basis(0)
+            st.apply(c, fusion="dense")
+            got = st.download()
+    tvd = 0.5 * float(np.abs(np.abs(got) ** 2 - np.abs(ref) ** 2).sum())
+    assert float(np.max(np.abs(got - ref))) <= 2e-5 and tvd <= 1e-5
