@@ -503,7 +503,7 @@ int qg_diag_dense_tc_stall(int32_t on);
 typedef struct qg_tuning {
   int32_t tile_bits;    /* local qubits per tile: 10 to 13 */
   int32_t reg_bits;     /* amplitudes per thread = 2^reg_bits (3 or 4) */
-  int32_t buffers;      /* tile buffers in shared memory (1 or 2) */
+  int32_t buffers;      /* tile buffers in shared memory (1 to 3: tiles in flight + 1) */
   int32_t ctas_per_sm;  /* CTAs per SM the kernels are built for */
   double ms;            /* measured device time of the calibration circuit (qg_autotune) */
 } qg_tuning;

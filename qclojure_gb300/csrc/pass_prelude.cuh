@@ -368,7 +368,7 @@ __device__ __forceinline__ void f_rxlike(float a, float b, float c, float d, flo
 // The tile loop. P supplies: E (bytes per amplitude in HBM), K_BITS, KLOW,
 // R_BITS (each of the 2^(K_BITS - R_BITS) threads holds 2^R_BITS amplitudes),
 // BUFS (1: one tile buffer, the SM's other CTAs overlap their copies with this
-// one's arithmetic; 2: the next tile is prefetched into a second buffer), LM
+// one's arithmetic; 2 or 3: the next one or two tiles are prefetched), LM
 // (mask of the local bit positions), hioff(h) (HBM offset, in amplitudes, of the
 // h-th 2^KLOW-amplitude run of a tile), tile_base(t) (first amplitude of tile t)
 // and body(buf, base, cs) (the gate run on the tile in shared memory; it ends
@@ -406,29 +406,40 @@ __device__ __forceinline__ void run_pass(unsigned char* __restrict__ state, u64 
     }
     return;
   }
+  // a ring of BUFS buffers: the next BUFS - 1 tiles are in flight while one is worked
+  // on; one copy group is committed per tile (empty ones past the range), so waiting
+  // for all but the newest BUFS - 1 groups waits for the current tile
+  u64 pb = base, pt = w0;
 #pragma unroll
-  for (int i = 0; i < CPT; ++i) cp_async16(smem + soff[i], state + base * E + goff[i]);
-  cp_commit();
-  int it = 0;
-  for (u64 t = w0; t < w1; ++t, ++it) {
-    unsigned char* cur = smem + (it & 1) * (K * E);
-    const u64 nb = ((base | P::LM) + 1) & ~P::LM;
-    if (t + 1 < w1) {
-      unsigned char* nxt = smem + ((it + 1) & 1) * (K * E);
+  for (int q = 0; q < P::BUFS - 1; ++q) {
+    if (pt < w1) {
 #pragma unroll
-      for (int i = 0; i < CPT; ++i) cp_async16(nxt + soff[i], state + nb * E + goff[i]);
-      cp_commit();
-      cp_wait<1>();
-    } else {
-      cp_wait<0>();
+      for (int i = 0; i < CPT; ++i) cp_async16(smem + q * (K * E) + soff[i], state + pb * E + goff[i]);
+      pb = ((pb | P::LM) + 1) & ~P::LM;
+      ++pt;
     }
+    cp_commit();
+  }
+  int cb = 0, nbuf = P::BUFS - 1;  // buffer of the current tile, of the next prefetch
+  for (u64 t = w0; t < w1; ++t) {
+    unsigned char* cur = smem + cb * (K * E);
+    if (pt < w1) {
+#pragma unroll
+      for (int i = 0; i < CPT; ++i) cp_async16(smem + nbuf * (K * E) + soff[i], state + pb * E + goff[i]);
+      pb = ((pb | P::LM) + 1) & ~P::LM;
+      ++pt;
+    }
+    cp_commit();
+    cp_wait<P::BUFS - 1>();
     __syncthreads();
     P::body(cur, base, nullptr);
 #pragma unroll
     for (int i = 0; i < CPT; ++i)
       *reinterpret_cast<uint4*>(state + base * E + goff[i]) = *reinterpret_cast<const uint4*>(cur + soff[i]);
-    __syncthreads();  // this buffer is refilled two tiles later
-    base = nb;
+    __syncthreads();  // this buffer is refilled by the next prefetch
+    base = ((base | P::LM) + 1) & ~P::LM;
+    nbuf = cb;
+    cb = cb + 1 == P::BUFS ? 0 : cb + 1;
   }
 }
 
@@ -459,19 +470,30 @@ __device__ __forceinline__ void run_pass_range(unsigned char* const* __restrict_
     __syncthreads();  // the previous state's readers of cs are done
     for (int q = (int)threadIdx.x; q < ncoef; q += T) cs[q] = coefs[(u64)si * ncoef + q];
     u64 base = P::tile_base(t0);
+    // the ring of run_pass (one buffer: the next tile is loaded after the store)
+    u64 pb = base, pt = t0;
 #pragma unroll
-    for (int i = 0; i < CPT; ++i) cp_async16(smem + soff[i], state + base * E + goff[i]);
-    cp_commit();
-    int it = 0;
-    for (u64 t = t0; t < t1; ++t, ++it) {
-      unsigned char* cur = smem + (P::BUFS == 2 ? (it & 1) : 0) * (K * E);
-      const u64 nb = ((base | P::LM) + 1) & ~P::LM;
-      if (P::BUFS == 2 && t + 1 < t1) {
-        unsigned char* nxt = smem + ((it + 1) & 1) * (K * E);
+    for (int q = 0; q < (P::BUFS > 1 ? P::BUFS - 1 : 1); ++q) {
+      if (pt < t1) {
 #pragma unroll
-        for (int i = 0; i < CPT; ++i) cp_async16(nxt + soff[i], state + nb * E + goff[i]);
+        for (int i = 0; i < CPT; ++i) cp_async16(smem + q * (K * E) + soff[i], state + pb * E + goff[i]);
+        pb = ((pb | P::LM) + 1) & ~P::LM;
+        ++pt;
+      }
+      cp_commit();
+    }
+    int cb = 0, nbuf = P::BUFS > 1 ? P::BUFS - 1 : 0;
+    for (u64 t = t0; t < t1; ++t) {
+      unsigned char* cur = smem + cb * (K * E);
+      if (P::BUFS > 1) {
+        if (pt < t1) {
+#pragma unroll
+          for (int i = 0; i < CPT; ++i) cp_async16(smem + nbuf * (K * E) + soff[i], state + pb * E + goff[i]);
+          pb = ((pb | P::LM) + 1) & ~P::LM;
+          ++pt;
+        }
         cp_commit();
-        cp_wait<1>();
+        cp_wait<(P::BUFS > 1 ? P::BUFS - 1 : 0)>();
       } else {
         cp_wait<0>();
       }
@@ -481,12 +503,18 @@ __device__ __forceinline__ void run_pass_range(unsigned char* const* __restrict_
       for (int i = 0; i < CPT; ++i)
         *reinterpret_cast<uint4*>(state + base * E + goff[i]) = *reinterpret_cast<const uint4*>(cur + soff[i]);
       __syncthreads();  // the buffer is refilled by a later tile
-      if (P::BUFS == 1 && t + 1 < t1) {
+      if (P::BUFS == 1 && pt < t1) {
 #pragma unroll
-        for (int i = 0; i < CPT; ++i) cp_async16(smem + soff[i], state + nb * E + goff[i]);
+        for (int i = 0; i < CPT; ++i) cp_async16(smem + soff[i], state + pb * E + goff[i]);
+        pb = ((pb | P::LM) + 1) & ~P::LM;
+        ++pt;
         cp_commit();
       }
-      base = nb;
+      base = ((base | P::LM) + 1) & ~P::LM;
+      if (P::BUFS > 1) {
+        nbuf = cb;
+        cb = cb + 1 == P::BUFS ? 0 : cb + 1;
+      }
     }
     w += t1 - t0;
   }

@@ -2538,7 +2538,7 @@ static bool tuning_valid(const qg_tuning& t, int n, int prec) {
   const int E = prec == QG_C128 ? 16 : 8;
   if (t.tile_bits < 10 || t.tile_bits > kMaxTileBits || t.tile_bits > n) return false;
   if (t.reg_bits < 3 || t.reg_bits > 4 || t.tile_bits - t.reg_bits < 5 || t.tile_bits - t.reg_bits > 10) return false;
-  if (t.buffers < 1 || t.buffers > 2 || t.ctas_per_sm < 1 || t.ctas_per_sm > 8) return false;
+  if (t.buffers < 1 || t.buffers > 3 || t.ctas_per_sm < 1 || t.ctas_per_sm > 8) return false;
   const long smem = (long)t.buffers * (1L << t.tile_bits) * E;
   return smem <= 227L * 1024 && smem * t.ctas_per_sm <= 228L * 1024;
 }

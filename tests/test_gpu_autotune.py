@@ -42,7 +42,7 @@ def test_tuning_set_refuses_impossible_shapes():
     from qclojure_gb300.state import Context
 
     with Context(pass_kernels="always") as ctx:
-        for bad in ((14, 3, 2, 1), (12, 5, 2, 1), (13, 3, 2, 2), (12, 3, 3, 1), (9, 3, 2, 1)):
+        for bad in ((14, 3, 2, 1), (12, 5, 2, 1), (13, 3, 2, 2), (12, 3, 4, 1), (9, 3, 2, 1)):
             with pytest.raises(QgError) as ei:
                 ctx.set_tuning(20, "c128", *bad)
             assert ei.value.code == QG_ERR_INVALID_ARG
