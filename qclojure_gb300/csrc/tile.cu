@@ -63,10 +63,22 @@ struct PolExact {
   __device__ static V load_work(const unsigned char* sm, int pos) { return load_raw(sm, pos); }
   __device__ static void store_raw(unsigned char* sm, int pos, const V& v) { reinterpret_cast<V*>(sm)[pos] = v; }
   __device__ static void store_work(unsigned char* sm, int pos, const V& v) { store_raw(sm, pos, v); }
+  // FP64 keeps the reference's rounded products and sums (bit-identical to the oracle);
+  // complex64, whose contract is a probability tolerance, contracts a product and a
+  // sum into one FMA
+  static constexpr bool kFMA = sizeof(R) == 4;
+  __device__ static R mad(R a, R b, R c) {  // a b + c
+    if constexpr (kFMA) return fmaf(a, b, c);
+    else return addD(mulD(a, b), c);
+  }
+  __device__ static R msub(R a, R b, R c) {  // a b - c
+    if constexpr (kFMA) return fmaf(a, b, -c);
+    else return subD(mulD(a, b), c);
+  }
   __device__ static V cm(R gr, R gi, V x) {  // (gr x.re - gi x.im, gr x.im + gi x.re)
     V r;
-    r.x = subD(mulD(gr, x.x), mulD(gi, x.y));
-    r.y = addD(mulD(gr, x.y), mulD(gi, x.x));
+    r.x = msub(gr, x.x, mulD(gi, x.y));
+    r.y = mad(gr, x.y, mulD(gi, x.x));
     return r;
   }
   template <int CLS>
@@ -74,19 +86,26 @@ struct PolExact {
     const R* m = c.m;
     V y0, y1;
     if (CLS == U2_GENERAL) {
-      V a = cm(m[0], m[1], x0), b = cm(m[2], m[3], x1), d = cm(m[4], m[5], x0), e = cm(m[6], m[7], x1);
-      y0.x = addD(a.x, b.x); y0.y = addD(a.y, b.y);
-      y1.x = addD(d.x, e.x); y1.y = addD(d.y, e.y);
+      if constexpr (kFMA) {  // y = m0 x0 + m1 x1, four FMAs per component
+        y0.x = fmaf(m[0], x0.x, fmaf(-m[1], x0.y, fmaf(m[2], x1.x, -m[3] * x1.y)));
+        y0.y = fmaf(m[0], x0.y, fmaf(m[1], x0.x, fmaf(m[2], x1.y, m[3] * x1.x)));
+        y1.x = fmaf(m[4], x0.x, fmaf(-m[5], x0.y, fmaf(m[6], x1.x, -m[7] * x1.y)));
+        y1.y = fmaf(m[4], x0.y, fmaf(m[5], x0.x, fmaf(m[6], x1.y, m[7] * x1.x)));
+      } else {
+        V a = cm(m[0], m[1], x0), b = cm(m[2], m[3], x1), d = cm(m[4], m[5], x0), e = cm(m[6], m[7], x1);
+        y0.x = addD(a.x, b.x); y0.y = addD(a.y, b.y);
+        y1.x = addD(d.x, e.x); y1.y = addD(d.y, e.y);
+      }
     } else if (CLS == U2_REAL) {
-      y0.x = addD(mulD(m[0], x0.x), mulD(m[2], x1.x));
-      y0.y = addD(mulD(m[0], x0.y), mulD(m[2], x1.y));
-      y1.x = addD(mulD(m[4], x0.x), mulD(m[6], x1.x));
-      y1.y = addD(mulD(m[4], x0.y), mulD(m[6], x1.y));
+      y0.x = mad(m[0], x0.x, mulD(m[2], x1.x));
+      y0.y = mad(m[0], x0.y, mulD(m[2], x1.y));
+      y1.x = mad(m[4], x0.x, mulD(m[6], x1.x));
+      y1.y = mad(m[4], x0.y, mulD(m[6], x1.y));
     } else if (CLS == U2_RXLIKE) {
-      y0.x = subD(mulD(m[0], x0.x), mulD(m[3], x1.y));
-      y0.y = addD(mulD(m[0], x0.y), mulD(m[3], x1.x));
-      y1.x = subD(mulD(m[6], x1.x), mulD(m[5], x0.y));
-      y1.y = addD(mulD(m[5], x0.x), mulD(m[6], x1.y));
+      y0.x = msub(m[0], x0.x, mulD(m[3], x1.y));
+      y0.y = mad(m[0], x0.y, mulD(m[3], x1.x));
+      y1.x = msub(m[6], x1.x, mulD(m[5], x0.y));
+      y1.y = mad(m[5], x0.x, mulD(m[6], x1.y));
     } else if (CLS == U2_DIAG) {
       y0 = cm(m[0], m[1], x0);
       y1 = cm(m[6], m[7], x1);
