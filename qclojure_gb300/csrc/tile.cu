@@ -54,6 +54,8 @@ struct PolExact {
   static constexpr int kElem = sizeof(V);  // bytes per amplitude in HBM and shared memory
   static constexpr bool kDense = true;     // dense fused blocks supported
   static constexpr bool kDF = false;
+  // complex64 interprets two tiles per op dispatch (run_ops2); FP64 one
+  static constexpr bool kTwoTiles = sizeof(R) == 4;
   static constexpr int kCst = sizeof(R) == 8 ? 0 : 1;
   static constexpr bool kInPairs = false, kOutPairs = false;
   struct Cst {
@@ -158,6 +160,7 @@ struct PolDFT {
   // programs that hold them
   static constexpr bool kDense = DENSE;
   static constexpr bool kDF = true;
+  static constexpr bool kTwoTiles = false;
   static constexpr bool kInPairs = (IO & 1) != 0, kOutPairs = (IO & 2) != 0;
   static constexpr int kCst = 2;
   struct Cst {
@@ -680,6 +683,170 @@ __device__ void run_ops(unsigned char* buf, const KOp* __restrict__ sops, int no
 #undef QG_PHASE_CR
 #undef QG_PHASE_CASES
 
+// The interpreter on two tiles of one state at once, eight registers of each per
+// thread: every op record is read, dispatched and its constants loaded once for sixteen
+// amplitudes, which halves the per-op overhead per amplitude (the interpreter's cost:
+// its gate arithmetic is a small share). Conditions on the tile index are evaluated per
+// tile; everything else is shared. Used for complex64 (no pair formats).
+#define QG_U2_PAIR(CLS, RP)                                                        \
+  case KC_U2 + CLS * 4 + RP: {                                                     \
+    const typename P::Cst c_ = kcst<P>(op);                                        \
+    u2_regs<P, CLS, RP, false>(r0, c_, 0, true);                                   \
+    u2_regs<P, CLS, RP, false>(r1, c_, 0, true);                                   \
+  } break;                                                                         \
+  case KF_COND | (KC_U2 + CLS * 4 + RP): {                                         \
+    const typename P::Cst c_ = kcst<P>(op);                                        \
+    u2_regs<P, CLS, RP, true>(r0, c_, cr, tc0);                                    \
+    u2_regs<P, CLS, RP, true>(r1, c_, cr, tc1);                                    \
+  } break;
+#define QG_U2_CASES2(CLS) QG_U2_PAIR(CLS, 0) QG_U2_PAIR(CLS, 1) QG_U2_PAIR(CLS, 2)
+#define QG_PHASE_CR2(CLS, CR)                                                      \
+  case KC_PHASE + CLS * 8 + CR: {                                                  \
+    const typename P::Cst c_ = kcst<P>(op);                                        \
+    phase_regs<P, CLS, CR>(r0, c_);                                                \
+    phase_regs<P, CLS, CR>(r1, c_);                                                \
+  } break;                                                                         \
+  case KF_COND | (KC_PHASE + CLS * 8 + CR): {                                      \
+    const typename P::Cst c_ = kcst<P>(op);                                        \
+    if (tc0) phase_regs<P, CLS, CR>(r0, c_);                                       \
+    if (tc1) phase_regs<P, CLS, CR>(r1, c_);                                       \
+  } break;
+#define QG_PHASE_CASES2(CLS) \
+  QG_PHASE_CR2(CLS, 0) QG_PHASE_CR2(CLS, 1) QG_PHASE_CR2(CLS, 2) QG_PHASE_CR2(CLS, 3) \
+  QG_PHASE_CR2(CLS, 4) QG_PHASE_CR2(CLS, 5) QG_PHASE_CR2(CLS, 6) QG_PHASE_CR2(CLS, 7)
+
+template <class P>
+__device__ void run_ops2(unsigned char* buf0, unsigned char* buf1, const KOp* __restrict__ sops, int nops,
+                         const double* __restrict__ dense, uint64_t base0, uint64_t base1, const TileGeo& g) {
+  static_assert(!P::kDF && !P::kInPairs && !P::kOutPairs, "two-tile interpretation: one storage format");
+  using Reg = typename P::Reg;
+  constexpr int E = P::kElem;
+  Reg r0[kRegs], r1[kRegs];
+  int pos[kRegs];  // swizzled shared-memory slot of register j in the current layout (both tiles)
+  uint32_t lt = 0;
+  bool in_regs = false;
+  for (int o = 0; o < nops; ++o) {
+    const KOp& op = sops[o];
+    const int code = op.code;
+    if (code == KC_LAYOUT) {
+      if (in_regs) {
+#pragma unroll
+        for (int j = 0; j < kRegs; ++j) {
+          P::store_work(buf0, pos[j], r0[j]);
+          P::store_work(buf1, pos[j], r1[j]);
+        }
+        __syncthreads();
+      }
+      lt = threadIdx.x;
+      const uint32_t rb[3] = {op.tmask, op.tval, op.rmr};
+#pragma unroll
+      for (int q = 0; q < 3; ++q) lt = ((lt >> rb[q]) << (rb[q] + 1)) | (lt & ((1u << rb[q]) - 1));
+#pragma unroll
+      for (int j = 0; j < kRegs; ++j) pos[j] = swz<E>(lt | __float_as_uint(op.c[j]));
+#pragma unroll
+      for (int j = 0; j < kRegs; ++j) {
+        r0[j] = P::load_work(buf0, pos[j]);
+        r1[j] = P::load_work(buf1, pos[j]);
+      }
+      in_regs = true;
+      continue;
+    }
+    if (code == KC_DENSE) {
+      if (in_regs) {
+#pragma unroll
+        for (int j = 0; j < kRegs; ++j) {
+          P::store_work(buf0, pos[j], r0[j]);
+          P::store_work(buf1, pos[j], r1[j]);
+        }
+        in_regs = false;
+        __syncthreads();
+      }
+      if constexpr (P::kDense) {
+        dense_smem<P>(buf0, op, dense, g);
+        dense_smem<P>(buf1, op, dense, g);
+      }
+      continue;
+    }
+    bool tc0 = true, tc1 = true;
+    uint32_t cr = 0;
+    if (code & KF_COND) {
+      const bool tl = (lt & op.tmask) == op.tval;
+      tc0 = tl && (base0 & op.gmask) == op.gval;
+      tc1 = tl && (base1 & op.gmask) == op.gval;
+      cr = op.rmr & 0xFFu;
+    }
+    switch (code) {
+      QG_U2_CASES2(U2_GENERAL)
+      QG_U2_CASES2(U2_REAL)
+      QG_U2_CASES2(U2_RXLIKE)
+      QG_U2_CASES2(U2_DIAG)
+      QG_U2_CASES2(U2_ANTIDIAG)
+      QG_U2_CASES2(U2_X)
+      QG_U2_CASES2(U2_IMAG_ANTI)
+      QG_PHASE_CASES2(PH_GENERAL)
+      QG_PHASE_CASES2(PH_NEG)
+      QG_PHASE_CASES2(PH_I)
+      QG_PHASE_CASES2(PH_MINUS_I)
+      default: {
+        const int k = code & 0xFF;
+        if (k >= KC_SWAP && k < KC_SWAP + 6) {
+          const int pr = (k - KC_SWAP) % 3;
+          const bool isw = (k - KC_SWAP) >= 3;
+          if (pr == 0) {
+            if (tc0) swap_regs<P, 0, 1>(r0, cr, isw);
+            if (tc1) swap_regs<P, 0, 1>(r1, cr, isw);
+          } else if (pr == 1) {
+            if (tc0) swap_regs<P, 0, 2>(r0, cr, isw);
+            if (tc1) swap_regs<P, 0, 2>(r1, cr, isw);
+          } else {
+            if (tc0) swap_regs<P, 1, 2>(r0, cr, isw);
+            if (tc1) swap_regs<P, 1, 2>(r1, cr, isw);
+          }
+        } else if (k == KC_BLOCKADE) {
+          const typename P::Cst c = kcst<P>(op);
+          const int ct = __popc(lt & op.tmask);
+          const int cnt0 = __popcll(base0 & op.gmask) + ct, cnt1 = __popcll(base1 & op.gmask) + ct;
+#pragma unroll
+          for (int j = 0; j < kRegs; ++j) {
+            if (cnt0 <= 1 && cnt0 + __popc(j & cr) == 1) r0[j] = P::cmul_idx(c, 0, r0[j]);
+            if (cnt1 <= 1 && cnt1 + __popc(j & cr) == 1) r1[j] = P::cmul_idx(c, 0, r1[j]);
+          }
+        } else if (k == KC_PARITY) {
+          const typename P::Cst c = kcst<P>(op);
+          const int pt = __popc(lt & op.tmask);
+          const int par0 = (__popcll(base0 & op.gmask) + pt) & 1, par1 = (__popcll(base1 & op.gmask) + pt) & 1;
+#pragma unroll
+          for (int j = 0; j < kRegs; ++j) {
+            r0[j] = P::cmul_idx(c, par0 ^ (__popc(j & cr) & 1), r0[j]);
+            r1[j] = P::cmul_idx(c, par1 ^ (__popc(j & cr) & 1), r1[j]);
+          }
+        } else if (k == KC_COLLAPSE) {
+          const typename P::Cst c = kcst<P>(op);
+          const uint32_t rv = (op.rmr >> 8) & 0xFFu;
+#pragma unroll
+          for (int j = 0; j < kRegs; ++j) {
+            r0[j] = (tc0 && (j & cr) == rv) ? P::scale(c, r0[j]) : P::zero();
+            r1[j] = (tc1 && (j & cr) == rv) ? P::scale(c, r1[j]) : P::zero();
+          }
+        }
+      } break;
+    }
+  }
+  if (in_regs) {
+#pragma unroll
+    for (int j = 0; j < kRegs; ++j) {
+      P::store_raw(buf0, pos[j], r0[j]);
+      P::store_raw(buf1, pos[j], r1[j]);
+    }
+  }
+  __syncthreads();
+}
+
+#undef QG_U2_PAIR
+#undef QG_U2_CASES2
+#undef QG_PHASE_CR2
+#undef QG_PHASE_CASES2
+
 // States processed by one launch: all share the pass structure (PassDesc, op
 // kinds and count); op records may differ per state (ops_stride records apart).
 struct BatchArgs {
@@ -691,7 +858,7 @@ struct BatchArgs {
 
 template <class P>
 __global__ void __launch_bounds__(512, 1) k_tile2(const PassDesc pd, const BatchArgs ba, int nops,
-                                                  const double* __restrict__ dense, uint64_t ntiles) {
+                                                  const double* __restrict__ dense, uint64_t ntiles, int pairs) {
   constexpr int E = P::kElem;
   extern __shared__ __align__(128) unsigned char smem[];
   TileGeo g;
@@ -701,7 +868,8 @@ __global__ void __launch_bounds__(512, 1) k_tile2(const PassDesc pd, const Batch
   g.T = blockDim.x;
   const size_t tile_bytes = (size_t)g.K * E;
   const int nhi = 1 << (g.k - g.klow);
-  KOp* sops = reinterpret_cast<KOp*>(smem + 2 * tile_bytes);  // 16-byte aligned: tile_bytes % 16 == 0
+  // pairs: four tile buffers (two pairs: one interpreted, one in flight), else two
+  KOp* sops = reinterpret_cast<KOp*>(smem + (pairs ? 4 : 2) * tile_bytes);  // 16-byte aligned: tile_bytes % 16 == 0
   uint64_t* hioff = reinterpret_cast<uint64_t*>(sops + nops);
   for (int h = threadIdx.x; h < nhi; h += g.T) {
     uint64_t off = 0;
@@ -735,6 +903,47 @@ __global__ void __launch_bounds__(512, 1) k_tile2(const PassDesc pd, const Batch
     staged = si;
     __syncthreads();
     uint64_t base = tile_base(pd, t0);
+    if constexpr (P::kTwoTiles) {
+      if (pairs) {
+        // tiles two at a time (one op dispatch for both); the next pair loads into the
+        // other two buffers meanwhile; an odd last tile runs alone
+        auto next = [&](uint64_t b) { return ((b | lm) + 1) & ~lm; };
+        auto buf = [&](int q) { return smem + q * tile_bytes; };
+        cp.load(buf(0), state + base * E);
+        if (t0 + 1 < t1) cp.load(buf(1), state + next(base) * E);
+        cp_commit();
+        int slot = 0;
+        for (uint64_t tile = t0; tile < t1;) {
+          const int cnt = (t1 - tile >= 2) ? 2 : 1;
+          const uint64_t b0 = base, b1 = next(base);
+          const uint64_t nb = cnt == 2 ? next(b1) : b1;
+          const uint64_t ntile = tile + cnt;
+          if (ntile < t1) {
+            cp.load(buf(2 * (slot ^ 1)), state + nb * E);
+            if (ntile + 1 < t1) cp.load(buf(2 * (slot ^ 1) + 1), state + next(nb) * E);
+            cp_commit();
+            cp_wait<1>();
+          } else {
+            cp_wait<0>();
+          }
+          __syncthreads();
+          if (cnt == 2) {
+            run_ops2<P>(buf(2 * slot), buf(2 * slot + 1), sops, nops, dense, b0, b1, g);
+            cp.store(buf(2 * slot), state + b0 * E);
+            cp.store(buf(2 * slot + 1), state + b1 * E);
+          } else {
+            run_ops<P>(buf(2 * slot), sops, nops, dense, b0, g);
+            cp.store(buf(2 * slot), state + b0 * E);
+          }
+          __syncthreads();  // these buffers are refilled by the pair after next
+          base = nb;
+          tile = ntile;
+          slot ^= 1;
+        }
+        w += t1 - t0;
+        continue;
+      }
+    }
     cp.load(smem, state + base * E);
     cp_commit();
     int i = 0;
@@ -1020,7 +1229,10 @@ cudaError_t launch_t(int n, const PassDesc& pd, const BatchArgs& ba, const doubl
   if (threads < 1 || threads > 512 || (K * E) % 16 != 0 || K * E < 16 * threads || nops > kMaxKOps ||
       ba.nstates < 1)
     return cudaErrorInvalidValue;
-  const size_t smem = 2 * (size_t)K * E + sizeof(KOp) * (size_t)nops + sizeof(uint64_t) * (1u << (pd.k - pd.klow));
+  // complex64 interprets tile pairs when four buffers fit where two 64 KiB ones do
+  const int pairs = (P::kTwoTiles && 4 * (size_t)K * E <= 2 * (size_t(64) << 10)) ? 1 : 0;
+  const size_t smem = (pairs ? 4 : 2) * (size_t)K * E + sizeof(KOp) * (size_t)nops +
+                      sizeof(uint64_t) * (1u << (pd.k - pd.klow));
   const uint64_t ntiles = 1ULL << (n - pd.k);
   const uint64_t work = ntiles * (uint64_t)ba.nstates;
   int per_sm = (int)((220 * 1024) / smem);
@@ -1036,7 +1248,7 @@ cudaError_t launch_t(int n, const PassDesc& pd, const BatchArgs& ba, const doubl
   if (smem > kSmemLimit) return cudaErrorInvalidValue;
   cudaError_t e = cudaFuncSetAttribute(k_tile2<P>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmemLimit);
   if (e != cudaSuccess) return e;
-  k_tile2<P><<<(unsigned)grid, threads, smem, st>>>(pd, ba, nops, d_dense, ntiles);
+  k_tile2<P><<<(unsigned)grid, threads, smem, st>>>(pd, ba, nops, d_dense, ntiles, pairs);
   count_launch(1);
   return cudaGetLastError();
 }

@@ -163,6 +163,24 @@ def test_layered_c64(states, oracle, n, fusion):
     assert 0.5 * np.sum(np.abs(p - oracle.probabilities(ref))) <= 1e-5  # TVD
 
 
+@pytest.mark.parametrize("n", [20, 21, 22])
+def test_layered_c64_interpreted_tile_pairs(oracle, n):
+    """Interpreted complex64 passes take two tiles per op dispatch; at these sizes a CTA
+    holds several tiles of the state, odd counts included (its last tile runs alone), and
+    the QFT's controlled phases test conditions on tile-index bits per tile."""
+    from qclojure_gb300 import workloads
+    from qclojure_gb300.state import Context
+
+    c = workloads.large_circuit(n, 4, seed=30 + n)
+    ref = oracle.run(c)
+    with Context(pass_kernels="off") as ctx:
+        with ctx.state(n, "c64") as st:
+            st.apply(c)
+            got = st.download()
+    assert np.max(np.abs(got - ref)) <= 2e-5
+    assert 0.5 * np.sum(np.abs(np.abs(got) ** 2 - np.abs(ref) ** 2)) <= 1e-5  # TVD
+
+
 def test_initial_state_upload(states, oracle):
     from qclojure_gb300 import workloads
 
