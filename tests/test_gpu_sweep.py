@@ -150,3 +150,30 @@ def test_same_structure_sweep_specialised(gpu_ctx, oracle, precision, tol):
             ref = _energy(oracle, c)
             assert abs(e - ref) <= tol * max(1.0, abs(ref)), (e, ref)
         assert np.max(np.abs(en - en2)) > 1e-6
+
+
+@pytest.mark.parametrize("precision,arith,tol", [("c128", "double-float", 1e-12), ("c64", "exact", 2e-5)])
+def test_sweep_cnot_rotation_layers(gpu_ctx, oracle, precision, arith, tol):
+    """Table-form kernels on layers of RX / RY / RZ and CNOT matchings, one structure with
+    different angles per state: a CNOT whose control is a thread bit stays pending in a
+    per-thread register mask, and the next unit rotation of its target takes its
+    off-diagonals from the table exchanged; every state matches the oracle."""
+    import copy
+    import math
+
+    from qclojure_gb300 import workloads
+    from qclojure_gb300.sweep import Sweep
+
+    base = workloads.layered_circuit(14, 6, seed=3, gates=("rx", "ry", "rz"))
+    rng = np.random.default_rng(4)
+    circs = []
+    for _ in range(6):
+        c = copy.deepcopy(base)
+        for op in c["operations"]:
+            if "angle" in op["operation-params"]:
+                op["operation-params"]["angle"] = float(rng.uniform(0, 2 * math.pi))
+        circs.append(c)
+    with Sweep(gpu_ctx, circs, precision=precision, arithmetic=arith) as sw:
+        sw.run()
+        for k, c in enumerate(circs):
+            assert np.max(np.abs(sw.state(k) - oracle.run(c))) <= tol, k
