@@ -965,9 +965,13 @@ class PassGen {
   // register j counts the ops that see odd parity, m_j, and is multiplied by
   // p0^(E-m_j) p1^m_j from a table. With literal masks the register parities are
   // resolved at generation time; with a coefficient table (sweep groups) the
-  // masks come from the op's row (tile bits in floats 12-13, thread bits in 14,
-  // register bits in 15, as raw bits) and the table's entries from the run's rows
-  // (entry m < E in floats 0-3 of row first + m, entry E in floats 4-7 of row first).
+  // masks come from the op's row (tile bits in floats 12-13, thread bits in 14, and in
+  // 15 the register-parity mask: bit j = parity of register j's bits under the op's
+  // register mask, as raw bits) and the table's entries from the run's rows (entry
+  // m < E in floats 0-3 of row first + m, entry E in floats 4-7 of row first). There
+  // the counts are kept bit-sliced: per op, the set of registers that see odd parity is
+  // one XOR of that mask, added into bit planes c_p (bit j of c_p: bit p of m_j) with
+  // two logic operations per plane, and each m_j is read out of the planes once.
   std::ostringstream pre_;  // namespace-scope declarations (literal phase tables)
   int ntables_ = 0;
   void parity_run(int begin, int end) {
@@ -977,22 +981,38 @@ class PassGen {
       for (int i = begin; i < end; ++i) m |= ops_[i].rmask & (uint32_t)(ns_ - 1);
       materialise(m);
     }
-    o_ << "    {  // parity run of " << E << " ops\n      int";
-    for (int j = 0; j < ns_; ++j) o_ << (j ? ", m" : " m") << j << " = 0";
-    o_ << ";\n";
-    for (int e = begin; e < end; ++e) {
-      const TOp& t = ops_[e];
-      if (tab_) {
-        const int row = 16 * t.pad1;
+    o_ << "    {  // parity run of " << E << " ops\n";
+    if (tab_) {
+      int planes = 0;
+      while ((1 << planes) <= E) ++planes;  // counts 0..E
+      o_ << "      unsigned";
+      for (int p = 0; p < planes; ++p) o_ << (p ? ", c" : " c") << p << " = 0u";
+      o_ << ";\n";
+      for (int e = begin; e < end; ++e) {
+        const int row = 16 * ops_[e].pad1;
         o_ << "      { const qgp::u64 G = (qgp::u64)__float_as_uint(cs[" << row + 12
            << "]) | ((qgp::u64)__float_as_uint(cs[" << row + 13 << "]) << 32);\n";
-        o_ << "        const unsigned T = __float_as_uint(cs[" << row + 14 << "]), R = __float_as_uint(cs[" << row + 15
+        o_ << "        const unsigned T = __float_as_uint(cs[" << row + 14 << "]), P = __float_as_uint(cs[" << row + 15
            << "]);\n";
-        o_ << "        const int o = (__popcll(base & G) + __popc(lt & T)) & 1;\n";
-        for (int j = 0; j < ns_; ++j) o_ << "        m" << j << " += o ^ (__popc(" << j << "u & R) & 1);\n";
+        o_ << "        unsigned v = P ^ (0u - (unsigned)((__popcll(base & G) + __popc(lt & T)) & 1)), w;\n";
+        for (int p = 0; p < planes; ++p) {
+          if (p + 1 < planes) o_ << "        w = c" << p << " & v; c" << p << " ^= v; v = w;\n";
+          else o_ << "        c" << p << " ^= v;\n";
+        }
         o_ << "      }\n";
-        continue;
       }
+      for (int j = 0; j < ns_; ++j) {
+        o_ << "      const int m" << j << " = (int)(";
+        for (int p = 0; p < planes; ++p) o_ << (p ? " | " : "") << "(((c" << p << " >> " << j << ") & 1u) << " << p << ")";
+        o_ << ");\n";
+      }
+    } else {
+      o_ << "      int";
+      for (int j = 0; j < ns_; ++j) o_ << (j ? ", m" : " m") << j << " = 0";
+      o_ << ";\n";
+    }
+    for (int e = begin; e < end && !tab_; ++e) {
+      const TOp& t = ops_[e];
       std::string oe;
       if (t.gmask) oe += "__popcll(base & " + hex64(t.gmask) + ")";
       if (t.tmask) oe += std::string(oe.empty() ? "" : " + ") + "__popc(lt & " + hex32(t.tmask) + ")";
@@ -1656,7 +1676,8 @@ cudaError_t launch_pass_kernel_batch(const PassKernels& pk, size_t step, int n, 
 // Coefficient rows of one pass for the table form: 16 floats per op, in the
 // pass's op order (double-float: hi[8], lo[8]; complex64: the 8 entries as
 // floats). Parity ops instead hold their masks under the kernel's layout (tile
-// bits in floats 12-13, thread bits in 14, register bits in 15, as raw bits) and,
+// bits in floats 12-13, thread bits in 14, and in 15 the register-parity mask, bit j
+// the parity of register j's bits under the op's register mask; as raw bits) and,
 // per run, the table of combined phases (entry m < E in floats 0-3 of the run's
 // row m, entry E in floats 4-7 of its first row; complex64: 2 floats each).
 void pass_coefficients(const Program& prog, size_t step, int prec, float* out) {
@@ -1679,6 +1700,7 @@ void pass_coefficients(const Program& prog, size_t step, int prec, float* out) {
   std::vector<TOp> tagged(ops, ops + nops);
   for (int i = 0; i < nops; ++i) tagged[i].pad1 = i;
   const std::vector<TOp> plan = plan_layouts(tagged.data(), nops, pd.k, shape_of(prog, prec).rbits, true);
+  const int ns = 1 << shape_of(prog, prec).rbits;  // registers per thread
   auto put = [&](float* at, std::complex<double> v) {
     if (prec == QG_C128) {
       const float rh = (float)v.real(), ih = (float)v.imag();
@@ -1700,11 +1722,14 @@ void pass_coefficients(const Program& prog, size_t step, int prec, float* out) {
     for (int e = 0; e < E; ++e) {
       const TOp& t = plan[i + e];
       float* row = out + 16 * t.pad1;
-      const uint32_t g0 = (uint32_t)t.gmask, g1 = (uint32_t)(t.gmask >> 32), tm = t.tmask, rm = t.rmask;
+      // register-parity mask: bit j = parity of register j's bits under the op's mask
+      uint32_t par = 0;
+      for (int j = 0; j < ns; ++j) par |= (uint32_t)(__builtin_popcount((unsigned)j & t.rmask) & 1) << j;
+      const uint32_t g0 = (uint32_t)t.gmask, g1 = (uint32_t)(t.gmask >> 32), tm = t.tmask;
       std::memcpy(row + 12, &g0, 4);
       std::memcpy(row + 13, &g1, 4);
       std::memcpy(row + 14, &tm, 4);
-      std::memcpy(row + 15, &rm, 4);
+      std::memcpy(row + 15, &par, 4);
       put(row, tab[e]);
     }
     put(out + 16 * plan[i].pad1 + 4, tab[E]);
