@@ -15,6 +15,7 @@
 #include <cstdio>
 
 #include "qgpu_internal.h"
+#include "quant.cuh"
 
 namespace qg {
 
@@ -304,8 +305,14 @@ __device__ __forceinline__ void block_reduce_store(DD v, double* d_part, int slo
 
 template <typename R>
 __device__ __forceinline__ double p_of(typename C2<R>::T a) {
-  double re = (double)a.x, im = (double)a.y;
-  return __dadd_rn(__dmul_rn(re, re), __dmul_rn(im, im));
+  if constexpr (sizeof(R) == 4) {
+    // the squares of floats are exact doubles, built on the integer pipes (quant.cuh):
+    // only the rounded sum is an FP64 instruction
+    return __dadd_rn(qg_sq_float(a.x), qg_sq_float(a.y));
+  } else {
+    const double re = a.x, im = a.y;
+    return __dadd_rn(__dmul_rn(re, re), __dmul_rn(im, im));
+  }
 }
 
 template <typename R>
@@ -537,32 +544,73 @@ SampleGeom sample_geom(int n) {
   return g;
 }
 
-__device__ __forceinline__ unsigned long long quant(double p) {
-  double v = p * 4611686018427387904.0;
-  return v > 0 ? (unsigned long long)v : 0ULL;
-}
+// floor(p 2^62) on the integer pipes (quant.cuh): the FP64 product and conversion's value
+__device__ __forceinline__ unsigned long long quant(double p) { return qg_quant62(p); }
 
-// one CTA (256 threads = 8 warps) per sample block; each warp handles cpb/8 chunks.
-// Only integer sums are formed here: the FP64 total of the normalisation check
-// is derived from them (k_samp_scan). A compensated FP64 reduction per chunk
-// ran on the FP64 pipe (about 1/58 of the FP32 rate on this part) and bound
-// the whole sampler by it.
+// one CTA (256 threads = 8 warps) per sample block. Only integer sums are formed here:
+// the FP64 total of the normalisation check is derived from them (k_samp_scan). A
+// compensated FP64 reduction per chunk ran on the FP64 pipe (about 1/58 of the FP32
+// rate on this part) and bound the whole sampler by it.
+// Full blocks (256 chunks of 32 amplitudes: states of 13 qubits and more, 16-byte aligned,
+// as every state the runtime allocates): warp w takes
+// the block's chunks 32w .. 32w + 31 and reads them with 16-byte loads, eight per lane in
+// flight (one amplitude per lane and load for complex128, two for complex64), so a
+// chunk's 32 amplitudes are 32 or 16 consecutive lanes, summed by a butterfly within
+// them. Integer sums are associative: every chunk sum equals the lane-per-amplitude
+// form's.
 template <typename R>
 __global__ void __launch_bounds__(256) k_samp_sums(const typename C2<R>::T* __restrict__ s, SampleGeom g,
                                                    unsigned long long* __restrict__ csum,
                                                    unsigned long long* __restrict__ bsum) {
+  using T = typename C2<R>::T;
+  constexpr int A = 16 / (int)sizeof(T);  // amplitudes per 16-byte load
+  constexpr int CL = 32 / A;              // lanes per chunk
+  constexpr int LOADS = 32 / A;           // loads per lane for the warp's 32 chunks
+  constexpr int U = 8;                    // loads in flight per lane
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   __shared__ unsigned long long wq[8];
   for (uint64_t b = blockIdx.x; b < g.nb; b += gridDim.x) {
     unsigned long long bq = 0;
-    for (int c = warp; c < g.cpb; c += 8) {
-      uint64_t chunk = b * g.cpb + c;
-      unsigned long long q = 0;
-      if (lane < g.ch) q = quant(p_of<R>(s[chunk * g.ch + lane]));
-      for (int o = 16; o > 0; o >>= 1) q += __shfl_down_sync(0xffffffffu, q, o);
-      if (lane == 0) {
-        csum[chunk] = q;
-        bq += q;
+    if (g.ch == 32 && g.cpb == 256 && (reinterpret_cast<uintptr_t>(s) & 15u) == 0) {
+      const uint64_t c0 = b * 256 + (uint64_t)warp * 32;  // the warp's first chunk
+      const uint4* src = reinterpret_cast<const uint4*>(s + c0 * 32);
+#pragma unroll
+      for (int i0 = 0; i0 < LOADS; i0 += U) {
+        uint4 v[U];
+#pragma unroll
+        for (int u = 0; u < U; ++u) v[u] = __ldg(src + (i0 + u) * 32 + lane);
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+          unsigned long long q;
+          if constexpr (A == 2) {
+            const float2 x0 = make_float2(__uint_as_float(v[u].x), __uint_as_float(v[u].y));
+            const float2 x1 = make_float2(__uint_as_float(v[u].z), __uint_as_float(v[u].w));
+            q = quant(p_of<R>(x0)) + quant(p_of<R>(x1));
+          } else {
+            const double2 x = make_double2(__hiloint2double((int)v[u].y, (int)v[u].x),
+                                           __hiloint2double((int)v[u].w, (int)v[u].z));
+            q = quant(p_of<R>(x));
+          }
+#pragma unroll
+          for (int o = CL / 2; o > 0; o >>= 1) q += __shfl_xor_sync(0xffffffffu, q, o);
+          if ((lane & (CL - 1)) == 0) {
+            csum[c0 + (uint64_t)((i0 + u) * A + lane / CL)] = q;
+            bq += q;
+          }
+        }
+      }
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) bq += __shfl_xor_sync(0xffffffffu, bq, o);
+    } else {
+      for (int c = warp; c < g.cpb; c += 8) {
+        uint64_t chunk = b * g.cpb + c;
+        unsigned long long q = 0;
+        if (lane < g.ch) q = quant(p_of<R>(s[chunk * g.ch + lane]));
+        for (int o = 16; o > 0; o >>= 1) q += __shfl_down_sync(0xffffffffu, q, o);
+        if (lane == 0) {
+          csum[chunk] = q;
+          bq += q;
+        }
       }
     }
     if (lane == 0) wq[warp] = bq;
