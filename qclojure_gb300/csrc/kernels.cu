@@ -552,12 +552,10 @@ __device__ __forceinline__ unsigned long long quant(double p) { return qg_quant6
 // compensated FP64 reduction per chunk ran on the FP64 pipe (about 1/58 of the FP32
 // rate on this part) and bound the whole sampler by it.
 // Full blocks (256 chunks of 32 amplitudes: states of 13 qubits and more, 16-byte aligned,
-// as every state the runtime allocates): warp w takes
-// the block's chunks 32w .. 32w + 31 and reads them with 16-byte loads, eight per lane in
-// flight (one amplitude per lane and load for complex128, two for complex64), so a
-// chunk's 32 amplitudes are 32 or 16 consecutive lanes, summed by a butterfly within
-// them. Integer sums are associative: every chunk sum equals the lane-per-amplitude
-// form's.
+// as every state the runtime allocates): warp w takes the block's chunks 32w .. 32w + 31
+// and reads them with 16-byte loads, eight per lane in flight (one amplitude per lane and
+// load for complex128, two for complex64). Integer sums are associative: every chunk sum
+// equals the lane-per-amplitude form's.
 template <typename R>
 __global__ void __launch_bounds__(256) k_samp_sums(const typename C2<R>::T* __restrict__ s, SampleGeom g,
                                                    unsigned long long* __restrict__ csum,
@@ -574,28 +572,53 @@ __global__ void __launch_bounds__(256) k_samp_sums(const typename C2<R>::T* __re
     if (g.ch == 32 && g.cpb == 256 && (reinterpret_cast<uintptr_t>(s) & 15u) == 0) {
       const uint64_t c0 = b * 256 + (uint64_t)warp * 32;  // the warp's first chunk
       const uint4* src = reinterpret_cast<const uint4*>(s + c0 * 32);
+      if constexpr (A == 2) {
+        // complex64: load u gives lane L amplitudes 64u + 2L, +1 (chunk 2u + L / 16), so
+        // each half-warp holds one partial per chunk of its parity; recursive halving
+        // (each step a lane sends the half of its partials it does not keep) leaves lane
+        // l of half h the sum of chunk 2l + h after 15 exchanges for all 32 chunks
+        unsigned long long w[LOADS];
 #pragma unroll
-      for (int i0 = 0; i0 < LOADS; i0 += U) {
-        uint4 v[U];
+        for (int i0 = 0; i0 < LOADS; i0 += U) {
+          uint4 v[U];
 #pragma unroll
-        for (int u = 0; u < U; ++u) v[u] = __ldg(src + (i0 + u) * 32 + lane);
+          for (int u = 0; u < U; ++u) v[u] = __ldg(src + (i0 + u) * 32 + lane);
 #pragma unroll
-        for (int u = 0; u < U; ++u) {
-          unsigned long long q;
-          if constexpr (A == 2) {
+          for (int u = 0; u < U; ++u) {
             const float2 x0 = make_float2(__uint_as_float(v[u].x), __uint_as_float(v[u].y));
             const float2 x1 = make_float2(__uint_as_float(v[u].z), __uint_as_float(v[u].w));
-            q = quant(p_of<R>(x0)) + quant(p_of<R>(x1));
-          } else {
+            w[i0 + u] = quant(p_of<R>(x0)) + quant(p_of<R>(x1));
+          }
+        }
+#pragma unroll
+        for (int o = 8, K = LOADS; o >= 1; o >>= 1, K >>= 1) {
+          const bool up = (lane & o) != 0;
+#pragma unroll
+          for (int i = 0; i < K / 2; ++i) {
+            const unsigned long long send = up ? w[i] : w[i + K / 2];
+            const unsigned long long keep = up ? w[i + K / 2] : w[i];
+            w[i] = keep + __shfl_xor_sync(0xffffffffu, send, o);
+          }
+        }
+        csum[c0 + 2 * (uint64_t)(lane & 15) + (uint64_t)(lane >> 4)] = w[0];
+        bq = w[0];
+      } else {
+#pragma unroll
+        for (int i0 = 0; i0 < LOADS; i0 += U) {
+          uint4 v[U];
+#pragma unroll
+          for (int u = 0; u < U; ++u) v[u] = __ldg(src + (i0 + u) * 32 + lane);
+#pragma unroll
+          for (int u = 0; u < U; ++u) {
             const double2 x = make_double2(__hiloint2double((int)v[u].y, (int)v[u].x),
                                            __hiloint2double((int)v[u].w, (int)v[u].z));
-            q = quant(p_of<R>(x));
-          }
+            unsigned long long q = quant(p_of<R>(x));
 #pragma unroll
-          for (int o = CL / 2; o > 0; o >>= 1) q += __shfl_xor_sync(0xffffffffu, q, o);
-          if ((lane & (CL - 1)) == 0) {
-            csum[c0 + (uint64_t)((i0 + u) * A + lane / CL)] = q;
-            bq += q;
+            for (int o = 16; o > 0; o >>= 1) q += __shfl_xor_sync(0xffffffffu, q, o);
+            if (lane == 0) {
+              csum[c0 + (uint64_t)(i0 + u)] = q;
+              bq += q;
+            }
           }
         }
       }

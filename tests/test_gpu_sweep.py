@@ -177,3 +177,23 @@ def test_sweep_cnot_rotation_layers(gpu_ctx, oracle, precision, arith, tol):
         sw.run()
         for k, c in enumerate(circs):
             assert np.max(np.abs(sw.state(k) - oracle.run(c))) <= tol, k
+
+
+def test_interpreted_c64_sweep_tile_pairs(oracle):
+    """An interpreted complex64 sweep: one launch per pass over every state of a group,
+    each CTA taking a range of (state, tile) items and interpreting tiles of one state two
+    at a time (odd remainders alone). States of 20 qubits give several tiles per CTA;
+    every state matches the oracle. (A sweep schedules in circuit order, a single
+    complex64 run reorders commuting gates, so the two round differently.)"""
+    from qclojure_gb300.state import Context
+    from qclojure_gb300.sweep import Sweep
+
+    circs = _qaoa_set(5, seed=9, ns=(20,))
+    with Context(pass_kernels="off") as ctx:
+        with Sweep(ctx, circs, precision="c64", arithmetic="exact") as sw:
+            sw.run()
+            for k, c in enumerate(circs):
+                ref = oracle.run(c)
+                got = sw.state(k)
+                assert np.max(np.abs(got - ref)) <= 2e-5
+                assert 0.5 * np.sum(np.abs(np.abs(got) ** 2 - np.abs(ref) ** 2)) <= 1e-5  # TVD
