@@ -631,7 +631,7 @@ def main():
                      "peak_source": peak_src, "pass_bytes": pass_bytes, "mean_pass_ms": mean_pass,
                      "passes": len(dom),
                      "note": ("passes are bound by FP32 instruction issue, not HBM: ncu on the same kernel "
-                              "and shape (26 qubits) shows 58-68% issue active and 29-32% DRAM throughput "
+                              "and shape (26 qubits) shows 59-68% issue active and 31-32% DRAM throughput "
                               "for double-float complex128")
                      if dom_kind == 3 and args.precision == "c128" else None},
         "gpu_launches": int(l1.value - l0.value),
