@@ -112,7 +112,7 @@ inline bool hi_lo_nonzero(const TOp& t, int q) { return t.mf[8 + q] != 0.0f; }
 // blockade masks are data (they differ between members, for instance between
 // QAOA graphs), so the layout must not depend on them: ops keep their order
 // (no sinking, no look-ahead) and the free register bits ignore those masks.
-std::vector<TOp> plan_layouts(const TOp* ops, int nops, int k, int R, bool table = false) {
+std::vector<TOp> plan_layouts(const TOp* ops, int nops, int k, int R, bool table = false, bool pair0 = false) {
   auto required = [](const TOp& t) -> uint32_t {
     if (t.kind == OK_U2) return 1u << t.t;
     if (t.kind == OK_SWAP) return (1u << t.t) | (1u << t.t2);
@@ -187,6 +187,10 @@ std::vector<TOp> plan_layouts(const TOp* ops, int nops, int k, int R, bool table
       int best = -1;
       for (int b = k - 1; b >= 0; --b)
         if (!(rb & (1u << b)) && (best < 0 || uses[b] > uses[best])) best = b;
+      // pair0 (complex64): a free register slot that no condition asks for takes tile
+      // bit 0, so registers j and j + 1 share one 16-byte slot pair in shared memory and
+      // a layout change moves them with one access
+      if (pair0 && uses[best] == 0 && !(rb & 1u)) best = 0;
       rb |= 1u << best;
     }
     int pos[5], np = 0;
@@ -305,7 +309,7 @@ class PassGen {
       if (ops[i].kind == OK_DENSE) unsupported_ = true;
       if (table && (ops[i].kind == OK_BLOCKADE || ops[i].kind == OK_COLLAPSE)) unsupported_ = true;
     }
-    if (!unsupported_) plan_ = plan_layouts(tagged.data(), nops, pd.k, sh_.rbits, table);
+    if (!unsupported_) plan_ = plan_layouts(tagged.data(), nops, pd.k, sh_.rbits, table, !df_);
     // pairs handed over by the previous pass may carry unnormalised operations
     if (io & kTileInPairs) carry_ = kRenormEvery / 2 - 1;
     ops_ = plan_.data();
@@ -426,7 +430,26 @@ class PassGen {
     pend_ &= ~bits;
   }
   // register p goes to the slot of logical register p ^ xm
+  // complex64 with tile bit 0 as register bit 0: registers j, j + 1 (j even) fill one
+  // 16-byte slot pair (the swizzle keeps bit 0)
+  bool paired() const { return !df_ && rpos_[0] == 0; }
   void store_regs(const std::string& fn) {
+    if (paired() && !(pend_ & 1u)) {  // a pending X of register bit 0 would swap the halves
+      std::string xo = "";
+      if (pend_) {
+        const int E = 8;
+        o_ << "    { const int xo = swz<" << E << ">((int)(0u";
+        for (int bb = 0; bb < sh_.rbits; ++bb)
+          if ((pend_ >> bb) & 1) o_ << " | (((xm >> " << bb << ") & 1u) << " << rpos_[bb] << ")";
+        o_ << "));\n";
+        xo = " ^ xo";
+      }
+      for (int j = 0; j < ns_; j += 2)
+        o_ << "    F32::st_pair(buf, q" << j << xo << ", r" << j << ", r" << j + 1 << ");\n";
+      if (pend_) o_ << "    }\n    xm = 0u;\n";
+      pend_ = 0;
+      return;
+    }
     if (!pend_) {
       for (int j = 0; j < ns_; ++j) o_ << "    " << fn << "(buf, q" << j << ", r" << j << ");\n";
       return;
@@ -1096,7 +1119,12 @@ class PassGen {
           o_ << "    q" << j << " = swz<" << E << ">((int)(lt | " << hex32(lj) << "));\n";
         }
         const std::string ld = raw ? ld_raw() : std::string(pol()) + "::ld_work";
-        for (int j = 0; j < ns_; ++j) o_ << "    r" << j << " = " << ld << "(buf, q" << j << ");\n";
+        if (paired()) {  // complex64: raw and working forms are the same
+          for (int j = 0; j < ns_; j += 2)
+            o_ << "    F32::ld_pair(buf, q" << j << ", r" << j << ", r" << j + 1 << ");\n";
+        } else {
+          for (int j = 0; j < ns_; ++j) o_ << "    r" << j << " = " << ld << "(buf, q" << j << ");\n";
+        }
         for (int j = 0; j < ns_; ++j) since_[j] = carry_;
         in_regs = true;
         continue;
@@ -1699,7 +1727,8 @@ void pass_coefficients(const Program& prog, size_t step, int prec, float* out) {
   if (!parity) return;
   std::vector<TOp> tagged(ops, ops + nops);
   for (int i = 0; i < nops; ++i) tagged[i].pad1 = i;
-  const std::vector<TOp> plan = plan_layouts(tagged.data(), nops, pd.k, shape_of(prog, prec).rbits, true);
+  const std::vector<TOp> plan =
+      plan_layouts(tagged.data(), nops, pd.k, shape_of(prog, prec).rbits, true, prec == QG_C64);
   const int ns = 1 << shape_of(prog, prec).rbits;  // registers per thread
   auto put = [&](float* at, std::complex<double> v) {
     if (prec == QG_C128) {

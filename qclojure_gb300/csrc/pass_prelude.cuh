@@ -294,6 +294,15 @@ struct F32 {
   static __device__ __forceinline__ void st_work(unsigned char* b, int pos, const V& v) {
     reinterpret_cast<float2*>(b)[pos] = v;
   }
+  // two registers in the 16-byte slot pair (pos, pos + 1), pos even
+  static __device__ __forceinline__ void ld_pair(const unsigned char* b, int pos, V& a, V& c) {
+    const float4 v = *reinterpret_cast<const float4*>(b + pos * 8);
+    a = make_float2(v.x, v.y);
+    c = make_float2(v.z, v.w);
+  }
+  static __device__ __forceinline__ void st_pair(unsigned char* b, int pos, const V& a, const V& c) {
+    *reinterpret_cast<float4*>(b + pos * 8) = make_float4(a.x, a.y, c.x, c.y);
+  }
   static __device__ __forceinline__ V zero() { return make_float2(0.f, 0.f); }
   static __device__ __forceinline__ V neg(const V& x) { return make_float2(-x.x, -x.y); }
   static __device__ __forceinline__ V mul_i(const V& x) { return make_float2(-x.y, x.x); }
