@@ -486,6 +486,12 @@ int qg_pass_kernels_info(int32_t* available, uint64_t* cache_hits, uint64_t* cac
    fails with QG_ERR_DEVICE ("a bounded wait gave up"); the context stays usable.
    Process-wide; for tests of the failure path only. */
 int qg_diag_dense_tc_stall(int32_t on);
+/* Sampler diagnostic (no counterpart in the reference): the quantised probability sums
+   measure-state's draws use (state.clj:869-913 with floor(p 2^62) integer prefix sums),
+   one per chunk of min(2^n, 32) amplitudes in chunk_sums[0 .. count) (count must be
+   2^n / min(2^n, 32)), and their total in *total. Runs the sampler's first two kernels
+   only; for parity tests of the quantisation. */
+int qg_diag_sample_sums(void* state, uint64_t* chunk_sums, uint64_t count, uint64_t* total);
 
 /* ---- autotuner (no counterpart in the reference; the reference's hook for gate
    optimisation is gate_optimization.clj:776-860, which this tiled executor replaces) --

@@ -51,6 +51,8 @@ def lib():
                                          C.POINTER(C.c_uint64)]
         L.or_refalgo_circuit.restype = C.c_int
         L.or_sample_one.restype = C.c_uint64
+        L.or_chunk_sums.argtypes = [DP, C.c_int, C.POINTER(C.c_uint64)]
+        L.or_chunk_sums.restype = C.c_uint64
         _lib = L
     return _lib
 
@@ -91,6 +93,15 @@ def sample(s: np.ndarray, shots: int, seed: int) -> np.ndarray:
     if rc:
         raise ValueError("State is not properly normalized")
     return out[:shots]
+
+
+def chunk_sums(s: np.ndarray) -> tuple[np.ndarray, int]:
+    """The sampler's quantised sums per chunk of min(2^n, 32) amplitudes, and their total."""
+    n = int(np.log2(s.size))
+    out = np.empty(max(1, s.size // 32), np.uint64)
+    T = lib().or_chunk_sums(_dp(np.ascontiguousarray(s, dtype=np.complex128)), n,
+                            out.ctypes.data_as(C.POINTER(C.c_uint64)))
+    return out, int(T)
 
 
 def pauli_expectation(s: np.ndarray, pauli: str) -> float:

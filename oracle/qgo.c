@@ -210,6 +210,20 @@ uint64_t or_quantize(double p) {
   return (uint64_t)v;
 }
 
+/* The sampler's quantised chunk sums: csum[c] = sum of floor(p_i 2^62) over the chunk's
+   min(2^n, 32) amplitudes, p_i = re^2 + im^2 in FP64 as in measure-state
+   (state.clj:869-913); returns their total, the T a draw is scaled by. */
+uint64_t or_chunk_sums(const double* s, int n, uint64_t* csum) {
+  uint64_t N = 1ULL << n, ch = N < 32 ? N : 32, T = 0;
+  for (uint64_t c = 0; c < N / ch; ++c) {
+    uint64_t q = 0;
+    for (uint64_t i = c * ch; i < (c + 1) * ch; ++i) q += or_quantize(s[2 * i] * s[2 * i] + s[2 * i + 1] * s[2 * i + 1]);
+    csum[c] = q;
+    T += q;
+  }
+  return T;
+}
+
 /* ---- measure-specific-qubits (state.clj:915-1014) ------------------------ */
 int or_measure(double* s, int n, const int* qubits, int m, uint64_t seed, uint64_t draw_index,
                uint64_t* outcome_out, double* prob_out) {

@@ -237,6 +237,7 @@ SIGNATURES = {
     "qg_pass_kernels_build": ([C.POINTER(QgCircuit), I32, I32, I32P, DP, C.c_char_p, I64], C.c_int),
     "qg_pass_kernels_info": ([I32P, U64P, U64P], C.c_int),
     "qg_diag_dense_tc_stall": ([I32], C.c_int),
+    "qg_diag_sample_sums": ([P, U64P, U64, U64P], C.c_int),
     "qg_job_loop_info": ([P, C.POINTER(QgLoopInfo)], C.c_int),
     "qg_autotune": ([P, I32, I32, C.POINTER(QgCircuit), C.POINTER(QgTuning), C.POINTER(QgTuning), I32, I32P],
                     C.c_int),

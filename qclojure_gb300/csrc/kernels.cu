@@ -555,7 +555,14 @@ __device__ __forceinline__ unsigned long long quant(double p) { return qg_quant6
 // as every state the runtime allocates): warp w takes the block's chunks 32w .. 32w + 31
 // and reads them with 16-byte loads, eight per lane in flight (one amplitude per lane and
 // load for complex128, two for complex64). Integer sums are associative: every chunk sum
-// equals the lane-per-amplitude form's.
+// equals the lane-per-amplitude form's. The quantised probabilities come from the
+// fixed-point fast path (qg_quant62_sq_fast, no FP64 instruction) wherever its guard
+// allows, and from the FP64 expression (one vote per group of eight loads) where it
+// fails; both give the same integers. Parts of 2^-10 or more fail it, and since the
+// probabilities sum to one, at most 2^20 amplitudes of a state have them. complex128
+// votes on the group's largest part first and sends such groups to the FP64 expression
+// whole; for complex64 that check cost more than it saved (28 qubits: 530 against
+// 585 us per launch, even for a GHZ state).
 template <typename R>
 __global__ void __launch_bounds__(256) k_samp_sums(const typename C2<R>::T* __restrict__ s, SampleGeom g,
                                                    unsigned long long* __restrict__ csum,
@@ -583,11 +590,23 @@ __global__ void __launch_bounds__(256) k_samp_sums(const typename C2<R>::T* __re
           uint4 v[U];
 #pragma unroll
           for (int u = 0; u < U; ++u) v[u] = __ldg(src + (i0 + u) * 32 + lane);
+          unsigned slow = 0;
 #pragma unroll
           for (int u = 0; u < U; ++u) {
-            const float2 x0 = make_float2(__uint_as_float(v[u].x), __uint_as_float(v[u].y));
-            const float2 x1 = make_float2(__uint_as_float(v[u].z), __uint_as_float(v[u].w));
-            w[i0 + u] = quant(p_of<R>(x0)) + quant(p_of<R>(x1));
+            uint64_t q0, q1;
+            const bool f0 = qg_quant62_sq_fast(__uint_as_float(v[u].x), __uint_as_float(v[u].y), &q0);
+            const bool f1 = qg_quant62_sq_fast(__uint_as_float(v[u].z), __uint_as_float(v[u].w), &q1);
+            w[i0 + u] = q0 + q1;
+            slow |= (unsigned)!(f0 && f1) << u;
+          }
+          if (__any_sync(0xffffffffu, slow)) {  // the FP64 expression
+#pragma unroll
+            for (int u = 0; u < U; ++u)
+              if (slow & (1u << u)) {
+                const float2 x0 = make_float2(__uint_as_float(v[u].x), __uint_as_float(v[u].y));
+                const float2 x1 = make_float2(__uint_as_float(v[u].z), __uint_as_float(v[u].w));
+                w[i0 + u] = quant(p_of<R>(x0)) + quant(p_of<R>(x1));
+              }
           }
         }
 #pragma unroll
@@ -608,11 +627,33 @@ __global__ void __launch_bounds__(256) k_samp_sums(const typename C2<R>::T* __re
           uint4 v[U];
 #pragma unroll
           for (int u = 0; u < U; ++u) v[u] = __ldg(src + (i0 + u) * 32 + lane);
+          uint64_t qs[U];
+          bool big = false;
+#pragma unroll
+          for (int u = 0; u < U; ++u)  // high words: sign, exponent, top of the significand
+            big |= max(v[u].y & 0x7FFFFFFFu, v[u].w & 0x7FFFFFFFu) >= (1013u << 20);
+          unsigned slow = (1u << U) - 1;
+          if (!__any_sync(0xffffffffu, big)) {
+            slow = 0;
+#pragma unroll
+            for (int u = 0; u < U; ++u) {
+              const bool f = qg_quant62_sq_fast(__hiloint2double((int)v[u].y, (int)v[u].x),
+                                                __hiloint2double((int)v[u].w, (int)v[u].z), &qs[u]);
+              slow |= (unsigned)!f << u;
+            }
+          }
+          if (__any_sync(0xffffffffu, slow)) {  // the FP64 expression
+#pragma unroll
+            for (int u = 0; u < U; ++u)
+              if (slow & (1u << u)) {
+                const double2 x = make_double2(__hiloint2double((int)v[u].y, (int)v[u].x),
+                                               __hiloint2double((int)v[u].w, (int)v[u].z));
+                qs[u] = quant(p_of<R>(x));
+              }
+          }
 #pragma unroll
           for (int u = 0; u < U; ++u) {
-            const double2 x = make_double2(__hiloint2double((int)v[u].y, (int)v[u].x),
-                                           __hiloint2double((int)v[u].w, (int)v[u].z));
-            unsigned long long q = quant(p_of<R>(x));
+            unsigned long long q = qs[u];
 #pragma unroll
             for (int o = 16; o > 0; o >>= 1) q += __shfl_xor_sync(0xffffffffu, q, o);
             if (lane == 0) {

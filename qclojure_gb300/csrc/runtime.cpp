@@ -2507,6 +2507,38 @@ int qg_diag_dense_tc_stall(int32_t on) {
   return QG_OK;
 }
 
+// The sampler's scratch holds the chunk sums first, then the block sums, then the block
+// prefixes with the total T after them (sampler_scratch_bytes_at).
+static int st_sample_sums(State* s, uint64_t* h_csum, uint64_t count, uint64_t* h_total, std::string* err) {
+  const uint64_t N = 1ULL << s->n, ch = N < 32 ? N : 32, nch = N / ch, cpb = nch < 256 ? nch : 256,
+                 nb = nch / cpb;
+  if (count != nch) {
+    *err = "qg_diag_sample_sums: count must be " + std::to_string(nch);
+    return QG_ERR_INVALID_ARG;
+  }
+  void* d_scratch = nullptr;
+  double* d_total = nullptr;
+  CK(cudaMallocAsync(&d_scratch, sampler_scratch_bytes(s->n, 0), s->stream), "alloc sampler");
+  CK(cudaMallocAsync((void**)&d_total, sizeof(double) * 2, s->stream), "alloc total");
+  CK(launch_sample(s->d, s->prec, s->n, 0, 0, d_scratch, nullptr, d_total, s->stream), "sample sums");
+  const uint64_t* d_q = (const uint64_t*)d_scratch;
+  CK(cudaMemcpyAsync(h_csum, d_q, sizeof(uint64_t) * nch, cudaMemcpyDeviceToHost, s->stream), "D2H chunk sums");
+  CK(cudaMemcpyAsync(h_total, d_q + nch + nb + nb, sizeof(uint64_t), cudaMemcpyDeviceToHost, s->stream),
+     "D2H total");
+  CK(cudaStreamSynchronize(s->stream), "sync");
+  cudaFreeAsync(d_scratch, s->stream);
+  cudaFreeAsync(d_total, s->stream);
+  return QG_OK;
+}
+
+int qg_diag_sample_sums(void* state, uint64_t* chunk_sums, uint64_t count, uint64_t* total) {
+  if (!state || !chunk_sums || !total) return QG_ERR_INVALID_ARG;
+  State* s = (State*)state;
+  cudaSetDevice(s->ctx->device);
+  std::string err;
+  return state_err(s, st_sample_sums(s, chunk_sums, count, total, &err), err);
+}
+
 int qg_pass_kernels_info(int32_t* available, uint64_t* cache_hits, uint64_t* cache_misses) {
   if (available) *available = pass_kernels_unavailable() ? 0 : 1;
   size_t h = 0, m = 0;

@@ -155,6 +155,16 @@ class DeviceState:
         self._ck(self.lib.qg_state_sample(self.h, C.c_uint64(shots), C.c_uint64(seed), out.ctypes.data_as(A.U64P)))
         return out[:shots]
 
+    def sample_sums(self) -> tuple[np.ndarray, int]:
+        """The sampler's quantised probability sums (floor(p 2^62) per amplitude) per chunk
+        of min(2^n, 32) amplitudes, and their total."""
+        count = max(1, (1 << self.n) // 32)
+        out = np.empty(count, np.uint64)
+        total = C.c_uint64()
+        self._ck(self.lib.qg_diag_sample_sums(self.h, out.ctypes.data_as(A.U64P), C.c_uint64(count),
+                                              C.byref(total)))
+        return out, int(total.value)
+
     def sample_noalloc(self, shots: int, seed: int, device_outcomes: int) -> None:
         """Write `shots` outcomes (uint64) to caller-owned device memory at address
         `device_outcomes`; no device allocation (states of at most 24 qubits)."""
