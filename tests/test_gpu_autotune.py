@@ -37,6 +37,24 @@ def test_autotune_picks_no_slower_shape_and_stays_exact(oracle, precision, tol):
             assert np.max(np.abs(got - oracle.run(c))) <= tol, t
 
 
+@pytest.mark.parametrize("shape", [(12, 4, 2, 1), (11, 4, 2, 2), (12, 4, 1, 1), (10, 3, 3, 4)])
+def test_every_accepted_double_float_shape_is_exact(oracle, shape):
+    """Shapes qg_tuning_set accepts beyond the autotuner's candidates (16 amplitudes per
+    thread in double-float, three tile buffers) compute the state within 1e-12."""
+    from qclojure_gb300 import workloads
+    from qclojure_gb300.state import Context
+
+    n = 16
+    c = workloads.layered_circuit(n, 10, seed=9)
+    c = {"num-qubits": n, "operations": c["operations"] + workloads.qft_ops(n)}
+    with Context(pass_kernels="always", arithmetic="double-float") as ctx:
+        ctx.set_tuning(n, "c128", *shape)
+        with ctx.state(n, "c128") as st:
+            st.apply(c)
+            got = st.download()
+    assert np.max(np.abs(got - oracle.run(c))) <= 1e-12
+
+
 def test_tuning_set_refuses_impossible_shapes():
     from qclojure_gb300._abi import QG_ERR_INVALID_ARG, QgError
     from qclojure_gb300.state import Context
