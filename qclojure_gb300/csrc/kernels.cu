@@ -562,9 +562,10 @@ __device__ __forceinline__ unsigned long long quant(double p) { return qg_quant6
 // probabilities sum to one, at most 2^20 amplitudes of a state have them. complex128
 // votes on the group's largest part first and sends such groups to the FP64 expression
 // whole; for complex64 that check cost more than it saved (28 qubits: 530 against
-// 585 us per launch, even for a GHZ state).
+// 585 us per launch, even for a GHZ state). Three CTAs per SM: 80 registers (ptxas
+// otherwise picks 64 for complex128 and spills).
 template <typename R>
-__global__ void __launch_bounds__(256) k_samp_sums(const typename C2<R>::T* __restrict__ s, SampleGeom g,
+__global__ void __launch_bounds__(256, 3) k_samp_sums(const typename C2<R>::T* __restrict__ s, SampleGeom g,
                                                    unsigned long long* __restrict__ csum,
                                                    unsigned long long* __restrict__ bsum) {
   using T = typename C2<R>::T;
@@ -651,15 +652,25 @@ __global__ void __launch_bounds__(256) k_samp_sums(const typename C2<R>::T* __re
                 qs[u] = quant(p_of<R>(x));
               }
           }
+          // load u holds chunk i0 + u across the warp: recursive halving over lane bits 4,
+          // 3, 2 (7 exchanges) leaves lane l a partial of chunk i0 + ((l >> 2) & 7), and two
+          // butterfly steps over bits 1, 0 complete it (5 exchanges per chunk before)
 #pragma unroll
-          for (int u = 0; u < U; ++u) {
-            unsigned long long q = qs[u];
+          for (int o = 16, K = U; o >= 4; o >>= 1, K >>= 1) {
+            const bool up = (lane & o) != 0;
 #pragma unroll
-            for (int o = 16; o > 0; o >>= 1) q += __shfl_xor_sync(0xffffffffu, q, o);
-            if (lane == 0) {
-              csum[c0 + (uint64_t)(i0 + u)] = q;
-              bq += q;
+            for (int i = 0; i < K / 2; ++i) {
+              const uint64_t send = up ? qs[i] : qs[i + K / 2];
+              const uint64_t keep = up ? qs[i + K / 2] : qs[i];
+              qs[i] = keep + __shfl_xor_sync(0xffffffffu, send, o);
             }
+          }
+          unsigned long long q = qs[0];
+          q += __shfl_xor_sync(0xffffffffu, q, 2);
+          q += __shfl_xor_sync(0xffffffffu, q, 1);
+          if ((lane & 3) == 0) {
+            csum[c0 + (uint64_t)(i0 + ((lane >> 2) & 7))] = q;
+            bq += q;
           }
         }
       }
