@@ -35,6 +35,7 @@
 #include <thread>
 #include <unordered_map>
 
+#include "csa.h"
 #include "qgpu_internal.h"
 
 namespace qg {
@@ -1008,22 +1009,30 @@ class PassGen {
     if (tab_) {
       int planes = 0;
       while ((1 << planes) <= E) ++planes;  // counts 0..E
-      o_ << "      unsigned";
-      for (int p = 0; p < planes; ++p) o_ << (p ? ", c" : " c") << p << " = 0u";
-      o_ << ";\n";
-      for (int e = begin; e < end; ++e) {
-        const int row = 16 * ops_[e].pad1;
-        o_ << "      { const qgp::u64 G = (qgp::u64)__float_as_uint(cs[" << row + 12
-           << "]) | ((qgp::u64)__float_as_uint(cs[" << row + 13 << "]) << 32);\n";
-        o_ << "        const unsigned T = __float_as_uint(cs[" << row + 14 << "]), P = __float_as_uint(cs[" << row + 15
-           << "]);\n";
-        o_ << "        unsigned v = P ^ (0u - (unsigned)((__popcll(base & G) + __popc(lt & T)) & 1)), w;\n";
-        for (int p = 0; p < planes; ++p) {
-          if (p + 1 < planes) o_ << "        w = c" << p << " & v; c" << p << " ^= v; v = w;\n";
-          else o_ << "        c" << p << " ^= v;\n";
+      // op e's word (bit j: its parity for register j) into a carry-save counter (csa.h)
+      const CsaPlan plan = csa_plan(E, planes);
+      for (const CsaOp& c : plan.ops) {
+        if (c.kind == CsaOp::IN) {
+          const int row = 16 * ops_[begin + c.a].pad1;
+          o_ << "      unsigned k" << c.s << ";\n";
+          o_ << "      { const qgp::u64 G = (qgp::u64)__float_as_uint(cs[" << row + 12
+             << "]) | ((qgp::u64)__float_as_uint(cs[" << row + 13 << "]) << 32);\n";
+          o_ << "        const unsigned T = __float_as_uint(cs[" << row + 14 << "]), P = __float_as_uint(cs["
+             << row + 15 << "]);\n";
+          o_ << "        k" << c.s << " = P ^ (0u - (unsigned)((__popcll(base & G) + __popc(lt & T)) & 1)); }\n";
+        } else if (c.kind == CsaOp::FULL) {
+          o_ << "      const unsigned k" << c.s << " = k" << c.a << " ^ k" << c.b << " ^ k" << c.c << ";\n";
+          if (c.cy >= 0)
+            o_ << "      const unsigned k" << c.cy << " = (k" << c.a << " & k" << c.b << ") | (k" << c.c << " & (k"
+               << c.a << " ^ k" << c.b << "));\n";
+        } else {
+          o_ << "      const unsigned k" << c.s << " = k" << c.a << " ^ k" << c.b << ";\n";
+          if (c.cy >= 0) o_ << "      const unsigned k" << c.cy << " = k" << c.a << " & k" << c.b << ";\n";
         }
-        o_ << "      }\n";
       }
+      for (int p = 0; p < planes; ++p)
+        o_ << "      const unsigned c" << p << " = "
+           << (plan.planes[p] >= 0 ? "k" + std::to_string(plan.planes[p]) : std::string("0u")) << ";\n";
       for (int j = 0; j < ns_; ++j) {
         o_ << "      const int m" << j << " = (int)(";
         for (int p = 0; p < planes; ++p) o_ << (p ? " | " : "") << "(((c" << p << " >> " << j << ") & 1u) << " << p << ")";

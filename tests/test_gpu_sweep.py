@@ -197,3 +197,20 @@ def test_interpreted_c64_sweep_tile_pairs(oracle):
                 got = sw.state(k)
                 assert np.max(np.abs(got - ref)) <= 2e-5
                 assert 0.5 * np.sum(np.abs(np.abs(got) ** 2 - np.abs(ref) ** 2)) <= 1e-5  # TVD
+
+
+@pytest.mark.parametrize("precision,arith,tol", [("c128", "double-float", 1e-12), ("c64", "exact", 2e-5)])
+def test_qaoa_sweep_large_parity_runs(gpu_ctx, oracle, precision, arith, tol):
+    """QAOA circuits of 22 and 24 qubits (33 and 36 RZZ edges per cost layer): the
+    table-form parity runs count up to 36 edges per register in six bit planes through
+    the carry-save counter; energies and states match the oracle."""
+    from qclojure_gb300.sweep import Sweep
+
+    circs = _qaoa_set(3, seed=31, ns=(22, 24))
+    with Sweep(gpu_ctx, circs, precision=precision, arithmetic=arith) as sw:
+        en, _ = sw.run([c["hamiltonian"] for c in circs])
+        for k, c in enumerate(circs):
+            ref = oracle.run(c)
+            e_ref = oracle.hamiltonian_expectation(ref, c["hamiltonian"])
+            assert abs(en[k] - e_ref) <= (1e-10 if precision == "c128" else 1e-4) * max(1.0, abs(e_ref))
+            assert np.max(np.abs(sw.state(k) - ref)) <= tol, k
