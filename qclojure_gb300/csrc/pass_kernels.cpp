@@ -1033,10 +1033,28 @@ class PassGen {
       for (int p = 0; p < planes; ++p)
         o_ << "      const unsigned c" << p << " = "
            << (plan.planes[p] >= 0 ? "k" + std::to_string(plan.planes[p]) : std::string("0u")) << ";\n";
-      for (int j = 0; j < ns_; ++j) {
-        o_ << "      const int m" << j << " = (int)(";
-        for (int p = 0; p < planes; ++p) o_ << (p ? " | " : "") << "(((c" << p << " >> " << j << ") & 1u) << " << p << ")";
-        o_ << ");\n";
+      if (planes <= 8) {
+        // counts as bytes: nibble k of plane p spread to bit p of four bytes with one
+        // multiply (bit i times 2^(7i + p) lands on bit 8i + p; the four terms never
+        // overlap), then each register's byte taken out
+        const int words = ns_ / 4;
+        for (int k = 0; k < words; ++k) {
+          o_ << "      const unsigned b" << k << " = ";
+          for (int p = 0; p < planes; ++p)
+            o_ << (p ? "\n        | " : "") << "((((c" << p << " >> " << 4 * k << ") & 0xFu) * " << hex32(0x00204081u << p)
+               << ") & " << hex32(0x01010101u << p) << ")";
+          o_ << ";\n";
+        }
+        for (int j = 0; j < ns_; ++j)
+          o_ << "      const int m" << j << " = (int)__byte_perm(b" << j / 4 << ", 0u, " << hex32(0x4440u | (unsigned)(j % 4))
+             << ");\n";
+      } else {
+        for (int j = 0; j < ns_; ++j) {
+          o_ << "      const int m" << j << " = (int)(";
+          for (int p = 0; p < planes; ++p)
+            o_ << (p ? " | " : "") << "(((c" << p << " >> " << j << ") & 1u) << " << p << ")";
+          o_ << ");\n";
+        }
       }
     } else {
       o_ << "      int";
