@@ -114,12 +114,11 @@ QG_QHD uint64_t qg_umulhi(uint64_t a, uint64_t b) {
 // x^2 2^82 = (m 2^7)^2 2^(2 ef - 232). Zeros and subnormals shift out entirely.
 QG_QHD uint64_t qg_sq_fix(float x, bool* big) {
   const uint32_t u = qg_bits_of(x) & 0x7FFFFFFFu;
-  const int ef = (int)(u >> 23);
-  *big = ef > 116;
+  *big = u >= (117u << 23);
   const uint32_t m7 = ((u << 7) & 0x3FFFFF80u) | 0x40000000u;
   const uint64_t M = (uint64_t)m7 * m7;
-  const unsigned r = 232u - 2u * (unsigned)ef;  // wraps above 63 when *big: any value then
-  return M >> (r < 63u ? r : 63u);               // M < 2^62: a shift by 63 leaves 0
+  const unsigned r = 232u - 2u * (u >> 23);  // wraps above 63 when *big: any value then
+  return M >> (r < 63u ? r : 63u);           // M < 2^62: a shift by 63 leaves 0
 }
 
 // floor(x^2 2^82) for a double with |x| < 2^-10 (*big set otherwise), truncated from
@@ -142,12 +141,12 @@ QG_QHD uint64_t qg_sq_fix(double x, bool* big) {
 template <bool EXACT_SQUARES>
 QG_QHD bool qg_quant62_fix(uint64_t xf, uint64_t yf, uint64_t* q) {
   const uint64_t s = xf + yf;                                  // each below 2^62 on the fast path
-  const uint32_t t = (uint32_t)(s >> 52) + 4u;                 // 2 hb
+  const uint32_t t = (uint32_t)(s >> 52);                      // 2 hb - 4
   const uint32_t fr = (uint32_t)s & ((1u << kQgFix) - 1u);
   *q = s >> kQgFix;
-  const bool upper = fr + t <= (1u << kQgFix) - 2u;
+  const bool upper = fr + t <= (1u << kQgFix) - 6u;
   if (EXACT_SQUARES) return upper;
-  return upper && (fr >= t || *q == 0);
+  return upper && (fr >= t + 4u || *q == 0);
 }
 
 // True when a part is at least 2^-10 in magnitude (outside the fast path's range): a
