@@ -475,8 +475,12 @@ int qg_kernel_launches(uint64_t* count);
    generates and compiles the kernels of a circuit's tiled passes for sm_103a without
    loading them (no device needed): QG_OK with the kernel count and compile time,
    QG_ERR_DEVICE with the compiler's message in err_buf when a compile fails,
-   QG_ERR_UNSUPPORTED when NVRTC is not available. qg_pass_kernels_info reports whether
-   NVRTC is available and the compiled-program cache's hits and misses. */
+   QG_ERR_UNSUPPORTED when NVRTC is not available. With QG_PASS_BUILD_TABLE OR'ed into
+   `arithmetic` it builds the table-form kernels a parameter sweep compiles for the
+   circuit's structure instead (gates in circuit order, matrix entries and parity masks
+   read from a per-state table). qg_pass_kernels_info reports whether NVRTC is available
+   and the compiled-program cache's hits and misses. */
+#define QG_PASS_BUILD_TABLE 0x100
 int qg_pass_kernels_build(const qg_circuit* circuit, int32_t precision, int32_t arithmetic, int32_t* kernels_out,
                           double* compile_ms_out, char* err_buf, int64_t err_len);
 int qg_pass_kernels_info(int32_t* available, uint64_t* cache_hits, uint64_t* cache_misses);

@@ -50,6 +50,7 @@ CANCEL_OUTCOME = {0: "cancelled", 1: "cannot-cancel", 2: "not-found"}
 QG_C128, QG_C64 = 0, 1
 QG_FUSE_PLAIN, QG_FUSE_TILED, QG_FUSE_DENSE = 0, 1, 2
 QG_ARITH_EXACT, QG_ARITH_DOUBLE_FLOAT = 0, 1
+QG_PASS_BUILD_TABLE = 0x100
 QG_PASS_KERNELS_AUTO, QG_PASS_KERNELS_OFF, QG_PASS_KERNELS_ALWAYS = 0, 1, 2
 PASS_KERNELS = {"auto": 0, "off": 1, "always": 2}
 

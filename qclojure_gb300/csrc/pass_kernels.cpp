@@ -1376,12 +1376,13 @@ bool compile_units(std::vector<Unit>& units, std::string* why) {
 
 }  // namespace
 
-int pass_kernels_build_only(const Program& prog, int prec, int* kernels, double* compile_ms, std::string* why) {
+int pass_kernels_build_only(const Program& prog, int prec, int* kernels, double* compile_ms, std::string* why,
+                            bool table) {
   std::vector<Unit> units;
   std::string key;
   *kernels = 0;
   *compile_ms = 0;
-  if (!generate_units(prog, prec, &units, &key, why)) return 0;
+  if (!generate_units(prog, prec, &units, &key, why, table)) return 0;
   const auto t0 = std::chrono::steady_clock::now();
   if (!compile_units(units, why)) return -1;
   *compile_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();

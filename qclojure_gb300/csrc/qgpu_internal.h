@@ -269,7 +269,8 @@ cudaError_t launch_pass_kernel(const PassKernels& pk, size_t step, int n, const 
 const char* pass_kernels_unavailable();
 // Generate and compile without loading (no device needed): 1 compiled, 0 nothing
 // to specialise, -1 a compile error (in why).
-int pass_kernels_build_only(const Program& prog, int prec, int* kernels, double* compile_ms, std::string* why);
+int pass_kernels_build_only(const Program& prog, int prec, int* kernels, double* compile_ms, std::string* why,
+                            bool table = false);
 std::string pass_kernels_source(const Program& prog, int prec);
 void pass_kernel_cache_stats(size_t* hits, size_t* misses);
 // batched sweep kernels (sweep.cu)

@@ -2483,12 +2483,15 @@ int qg_pass_kernels_build(const qg_circuit* circuit, int32_t precision, int32_t 
   if (!circuit || (precision != QG_C128 && precision != QG_C64)) return QG_ERR_INVALID_ARG;
   std::string err;
   Program prog;
-  const int arith = arithmetic == QG_ARITH_DOUBLE_FLOAT ? QG_ARITH_DOUBLE_FLOAT : QG_ARITH_EXACT;
-  int rc = compile_program(circuit, precision, QG_FUSE_TILED, 4, arith, &prog, &err);
+  const bool table = (arithmetic & QG_PASS_BUILD_TABLE) != 0;
+  const int arith =
+      (arithmetic & ~QG_PASS_BUILD_TABLE) == QG_ARITH_DOUBLE_FLOAT ? QG_ARITH_DOUBLE_FLOAT : QG_ARITH_EXACT;
+  // a sweep keeps every circuit's gates in order (its states share one pass structure)
+  int rc = compile_program(circuit, precision, QG_FUSE_TILED, 4, arith, &prog, &err, !table);
   if (rc == QG_OK) {
     int kernels = 0;
     double ms = 0;
-    const int r = pass_kernels_build_only(prog, precision, &kernels, &ms, &err);
+    const int r = pass_kernels_build_only(prog, precision, &kernels, &ms, &err, table);
     if (kernels_out) *kernels_out = kernels;
     if (compile_ms_out) *compile_ms_out = ms;
     if (r < 0) rc = QG_ERR_DEVICE;

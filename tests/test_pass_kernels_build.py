@@ -63,3 +63,27 @@ def test_qaoa_parity_runs_compile(lib, precision, arithmetic):
     rc, kernels, err = _build(lib, workloads.qaoa_maxcut(16, 3, seed=4), precision, arithmetic)
     assert rc == 0, err
     assert kernels > 0
+
+
+@pytest.mark.parametrize("precision,arithmetic", [(0, 1), (1, 0)], ids=["c128-double-float", "c64"])
+def test_table_form_sweep_kernels_compile(lib, precision, arithmetic):
+    """The table-form kernels a parameter sweep compiles (QG_PASS_BUILD_TABLE): QAOA cost
+    layers of 36 edges (counts in six bit planes, read out as bytes) and one run of 300
+    RZZ of a single angle (nine planes: the read-out bit by bit)."""
+    import numpy as np
+
+    from qclojure_gb300 import _abi as A
+    from qclojure_gb300 import workloads
+
+    rc, kernels, err = _build(lib, workloads.qaoa_maxcut(24, 3, seed=4), precision, arithmetic | A.QG_PASS_BUILD_TABLE)
+    assert rc == 0, err
+    assert kernels > 0
+    rng = np.random.default_rng(3)
+    ops = [{"operation-type": "h", "operation-params": {"target": q}} for q in range(14)]
+    for _ in range(300):
+        a, b = (int(x) for x in rng.choice(14, 2, replace=False))
+        ops.append({"operation-type": "rzz", "operation-params": {"qubit1": a, "qubit2": b, "angle": 0.375}})
+    rc, kernels, err = _build(lib, {"num-qubits": 14, "operations": ops}, precision,
+                              arithmetic | A.QG_PASS_BUILD_TABLE)
+    assert rc == 0, err
+    assert kernels > 0
